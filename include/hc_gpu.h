@@ -1,0 +1,228 @@
+/* libhc_gpu: GB300 (sm_103a) implementation of HAIL-CAESAR's per-timestep
+ * raster path, behind a plain C ABI.
+ *
+ * The reference has no plugin API: its hot path is the set of argument-free
+ * member functions of LSDCatchmentModel that src/main.cpp:139-204 calls once
+ * per iteration, all communicating through private TNT arrays.  Each entry
+ * point below names the member function it replaces (file:line in the
+ * reference, src/catchmentmodel/LSDCatchmentModel.cpp unless stated).  The
+ * model state lives in device memory owned by an hc_ctx; hc_upload/
+ * hc_download move whole fields in the reference's own (TNT, padded,
+ * row-major) layout, so the host side keeps its arrays unchanged.
+ *
+ * Every call returns an hc_status; the library never exits the process.
+ * One host thread per context; all work is ordered on the context's stream.
+ */
+#ifndef HC_GPU_H
+#define HC_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HC_G_MAX 10      /* LSDCatchmentModel.hpp:444 (grain fractions + 1) */
+#define HC_NSTRATA 10    /* strata layers, LSDCatchmentModel.cpp:1759 */
+#define HC_MAX_RF 16     /* largest rfnum (hydroindex rain zones) supported */
+#define HC_MAX_POINTS 3  /* reach input points, LSDCatchmentModel.cpp:1742-1800 */
+
+typedef enum hc_status {
+  HC_OK = 0,
+  HC_ERR_ARG = 1,        /* bad argument: null pointer, size, unknown field */
+  HC_ERR_CUDA = 2,       /* a CUDA call failed; see hc_last_error */
+  HC_ERR_NONFINITE = 3,  /* a NaN/Inf water depth was detected */
+  HC_ERR_TIMEOUT = 4,    /* a device wait gave up (bounded spin) */
+  HC_ERR_NOMEM = 5,      /* device allocation failed or exceeds the cap */
+  HC_ERR_STATE = 6,      /* call out of order (e.g. run before prepare) */
+  HC_ERR_UNSUPPORTED = 7 /* option outside what the library implements */
+} hc_status;
+
+/* Every scalar the path reads.  Defaults (hc_params_default) are the
+ * reference's member initialisers, LSDCatchmentModel.hpp:437-568, and the
+ * driver constants of main.cpp:127-132. */
+typedef struct hc_params {
+  int32_t imax, jmax;     /* rows (DEM nrows) and columns (DEM ncols) */
+  double DX;              /* cell size, m */
+  /* flow routing */
+  double courant_number;
+  double froude_limit;
+  double mannings;
+  double hflow_threshold;
+  double edgeslope;
+  double water_depth_erosion_threshold; /* fixed 0.01 in the reference */
+  double in_out_difference_allowed;
+  int32_t max_time_step;  /* s */
+  int32_t spatially_var_mannings;
+  double ERODEFACTOR;     /* key erosion_limit */
+  int32_t maxcycle;       /* hours (key max_run_duration) */
+  /* rainfall / TOPMODEL (uniform or hydroindex-zoned rain) */
+  double rain_data_time_step; /* minutes */
+  int32_t rfnum;
+  double M;
+  double rain_factor;
+  double baseflow;
+  double MIN_Q, MIN_Q_MAXVAL;
+  /* reach inputs */
+  int32_t reach_mode;
+  int32_t number_of_points;
+  int32_t inpoints[HC_MAX_POINTS][2];
+  int32_t reach_input_data_timestep; /* minutes */
+  int32_t div_inputs;
+  /* sediment */
+  int32_t hydro_only;
+  int32_t wilcock, einstein;
+  double active;
+  double max_vel;
+  double Csuspmax;
+  double bedrock_erosion_threshold;
+  double bedrock_erosion_rate;
+  double vegTauCrit;
+  double veg_lat_restriction;
+  double lateral_constant;
+  double chann_lateral_erosion;
+  double failureangle;
+  double CREEP_RATE;
+  double d[HC_G_MAX];          /* d[1..9] grain sizes, m */
+  double dprop[HC_G_MAX + 1];  /* dprop[0..10] */
+  double fallVelocity[HC_G_MAX + 1];
+  int32_t isSuspended[HC_G_MAX + 1];
+  int32_t vegetation_on;
+  /* lateral3 */
+  double edge_smoothing_passes;
+  double downstream_shift;
+  double lateral_cross_channel_smoothing;
+  /* driver intervals, main.cpp:127-132 */
+  int32_t scan_area_interval_iter;
+  int32_t in_channel_landslide_iter_interval;
+  int32_t creep_time_interval;
+  int32_t global_landsliding_interval;
+  double creep_coeff;
+  int32_t LIMIT;
+} hc_params;
+
+/* Scalar state of the model object (members of LSDCatchmentModel that the
+ * per-step path reads or writes).  Kept on the device during a run. */
+typedef struct hc_scalars {
+  double cycle, previous, time_step, maxdepth;
+  double waterinput, waterOut, input_output_difference, temptot;
+  double counter, erode_call, erode_mult, lateralcounter;
+  double time_1, baseflow, grain_array_tot;
+  double sediQ, globalsediq, tempbmax;
+  double creep_time, creep_time2;
+  double sum_grain[HC_G_MAX + 1];
+  double j[HC_MAX_RF + 1], jo[HC_MAX_RF + 1], j_mean[HC_MAX_RF + 1];
+  double old_j_mean[HC_MAX_RF + 1], new_j_mean[HC_MAX_RF + 1];
+  double nActualGridCells[HC_MAX_RF + 1];
+  double catchment_input_counter[HC_MAX_RF + 1];
+  double totalinputpoints;
+  double flow_timestep;   /* flow dt of the current iteration */
+  double stop_flag;       /* nonzero: host-side work needed before resuming */
+} hc_scalars;
+
+/* Per-iteration record of hc_run (same fields as oracle/ref_harness). */
+typedef struct hc_step_record {
+  double counter, cycle, time_step, maxdepth, waterOut, waterinput,
+      erode_mult, sediQ, globalsediq, baseflow;
+} hc_step_record;
+
+/* Fields that hc_upload / hc_download move, in the reference's layouts. */
+typedef enum hc_field {
+  HC_F_ELEV = 0,         /* double (imax+2)(jmax+2) */
+  HC_F_WATER_DEPTH,      /* double (imax+2)(jmax+2) */
+  HC_F_QX, HC_F_QY, HC_F_QXS, HC_F_QYS, /* double (imax+2)(jmax+2) */
+  HC_F_VSUSPTOT,         /* double (imax+2)(jmax+2) */
+  HC_F_VEL, HC_F_TAU,    /* double (imax+2)(jmax+2) */
+  HC_F_BEDROCK,          /* double (imax+2)(jmax+2) */
+  HC_F_MANNINGS,         /* double (imax+2)(jmax+2) spat_var_mannings */
+  HC_F_AREA,             /* double (imax+2)(jmax+2) drainage area */
+  HC_F_SS,               /* double (imax+2)(jmax+2) */
+  HC_F_VEL_DIR,          /* double (imax+2)(jmax+2)*9 */
+  HC_F_SR, HC_F_SL, HC_F_SU, HC_F_SD, /* double (imax+2)(jmax+2)*10 */
+  HC_F_INDEX,            /* int32 (imax+2)(jmax+2), -9999 = no grain record */
+  HC_F_GRAIN,            /* double (imax+2)(jmax+2)/LIMIT * 11, by index */
+  HC_F_STRATA,           /* double (imax+2)(jmax+2)/LIMIT * 10 * 11 */
+  HC_F_DOWN_SCAN,        /* int32 (jmax+2)(imax+2) wet-row lists */
+  HC_F_EDGE,             /* double (imax+1)(jmax+1) */
+  HC_F_VEG,              /* double (imax+1)(jmax+1)*4 */
+  HC_F_RFAREA,           /* int32 (imax+2)(jmax+2) */
+  HC_F_INPUTPOINTS,      /* uint8 (imax+2)(jmax+2) reach input mask */
+  HC_F_COUNT
+} hc_field;
+
+typedef struct hc_ctx hc_ctx;
+
+/* Run flags (hc_run and the oracle's hco_iterate). */
+#define HC_RUN_LATERAL 1  /* call lateral3 after erosion (main.cpp:178) */
+#define HC_RUN_NOHILL 2   /* skip creep and global landsliding */
+
+/* Fills p with the reference defaults for an imax x jmax grid of cell DX. */
+void hc_params_default(hc_params* p, int32_t imax, int32_t jmax, double DX);
+
+/* Element count and element size of a field for the given parameters. */
+int64_t hc_field_count(const hc_params* p, hc_field f);
+int32_t hc_field_elsize(hc_field f);
+
+/* Allocates the device mirror of the model state and zeroes it like
+ * initialise_arrays + zero_values (:1617-1843, :2891-2982).  max_bytes caps
+ * the device allocation (0 = no cap). */
+hc_status hc_create(const hc_params* p, size_t max_bytes, hc_ctx** out);
+hc_status hc_destroy(hc_ctx* ctx);
+const char* hc_last_error(const hc_ctx* ctx);
+
+/* Copies a whole field host->device / device->host (synchronous w.r.t.
+ * the host buffer).  nbytes must equal count*elsize. */
+hc_status hc_upload(hc_ctx* ctx, hc_field f, const void* host, size_t nbytes);
+hc_status hc_download(hc_ctx* ctx, hc_field f, void* host, size_t nbytes);
+
+/* Rain table (rows x cols float, mm/h, read_rainfalldata :532-556) and reach
+ * table of input point p (rows x cols float, read_reachfile :558-606). */
+hc_status hc_set_rain(hc_ctx* ctx, const float* rain, int32_t rows, int32_t cols);
+hc_status hc_set_reach(hc_ctx* ctx, int32_t point, const float* data,
+                       int32_t rows, int32_t cols);
+
+hc_status hc_get_scalars(hc_ctx* ctx, hc_scalars* s);
+hc_status hc_set_scalars(hc_ctx* ctx, const hc_scalars* s);
+
+/* Set-up that main.cpp:102-122 does once: count_catchment_gridcells (:2813),
+ * set_time_counters (:1862), initialise_rainfall_runoff (:2041),
+ * initialise_drainage_area (:2055).  Call after the fields are uploaded. */
+hc_status hc_prepare(hc_ctx* ctx);
+
+/* ---- member-level entry points (one reference member each) ---- */
+/* set_maximum_timestep :1890-1910 (with set_inputoutput_diff :1879) */
+hc_status hc_set_maximum_timestep(hc_ctx* ctx);
+/* flow_route :3063-3247, dt = get_flow_timestep :1913-1923 */
+hc_status hc_flow_route(hc_ctx* ctx);
+/* depth_update :3259-3299; maxdepth lands in the scalars */
+hc_status hc_depth_update(hc_ctx* ctx);
+/* scan_area :3821-3849 */
+hc_status hc_scan_area(hc_ctx* ctx);
+/* water_flux_out :3005-3047 */
+hc_status hc_water_flux_out(hc_ctx* ctx);
+/* erode(mult) :4211-4845; returns tempbmax */
+hc_status hc_erode(hc_ctx* ctx, double mult, double* tempbmax);
+/* lateral_channel_erode :4850-5291 */
+hc_status hc_lateral_channel_erode(hc_ctx* ctx);
+/* in_channel_landsliding :5429-5527 */
+hc_status hc_in_channel_landsliding(hc_ctx* ctx);
+
+/* ---- whole iterations ----
+ * Runs up to n iterations of main.cpp:139-204 on the device (the same
+ * member sequence as above, with the scalar logic of set_loop_cycle,
+ * set_inputoutput_diff, set_maximum_timestep, increment_counters,
+ * reach_water_and_sediment_input, catchment_waterinputs, call_erosion,
+ * call_lateral and call_channel_landsliding kept on the device), stopping
+ * early when cycle/60 >= maxcycle.  rec (may be NULL) receives one record per
+ * iteration.  *done = iterations run. */
+hc_status hc_run(hc_ctx* ctx, int64_t n, int32_t flags, hc_step_record* rec,
+                 int64_t* done);
+
+/* Stream the context issues its work on (a cudaStream_t). */
+void* hc_stream(hc_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
