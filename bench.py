@@ -1,0 +1,308 @@
+"""Benchmark: cell-steps/s of HAIL-CAESAR's per-timestep raster path on GB300.
+
+One step = one iteration of the reference's main loop (src/main.cpp:139-204):
+inputs, flow_route, depth_update, the Courant dt, scan_area, erosion/deposition
+with grain sorting, lateral3, water_flux_out and slide_3, on one batch of
+synthetic input already resident in HBM.
+
+Workloads (seeded synthetic inputs with the benchmark configurations' shapes):
+  catchment2000  (default) catchment mode, 2000 x 2000 cells at 20 m, fractal
+                 DEM with 300 m relief pit-filled to one outlet edge,
+                 gamma rain + 60 mm/h storm, per-cell Manning's n, Einstein
+                 transport, lateral3 and slide_3 on; timed after a spin-up
+                 to storm onset (12 simulated hours)
+  flow8192       flow-only 8192 x 8192 at 5 m, 30 mm/h rain, erosion off
+  reach          reach mode 300 x 100 at 10 m, Wilcock-Crowe
+
+--impl gb300 (default) times libhc_gpu; --impl reference times the CPU
+implementation of the path (the oracle port, OpenMP over the reference's own
+column loops) on the host cores, from the same spun-up state definition.
+
+Replicas only: under torchrun each rank runs its own model on its own GPU;
+no data moves between ranks; value = all ranks' cell-steps / max rank time.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "hail-caesar_gb300")
+for p in (ROOT, PKG):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+import synth  # noqa: E402
+from hc_abi import HC_RUN_LATERAL  # noqa: E402
+
+METRIC = "cell-steps/s on 1 GB300 (plain vs batched ensemble); adjoint/forward cost"
+UNIT = "cell-steps/s"
+
+
+def make_workload(name):
+    """(case, spin-up simulated minutes, description)."""
+    if name == "catchment2000":
+        case = synth.catchment_case(n=2000, DX=20.0, hours=72, lateral=True)
+        return case, 12 * 60.0, "catchment 2000x2000 @20 m, erosion + lateral3 + slide_3, after 12 h"
+    if name == "flow8192":
+        case = synth.flow_case(n=8192, DX=5.0, hours=2)
+        return case, 30.0, "flow-only 8192x8192 @5 m, 30 mm/h, after 30 min"
+    if name == "reach":
+        case = synth.reach_case(imax=300, jmax=100, DX=10.0, hours=24)
+        return case, 6 * 60.0, "reach 300x100 @10 m, Wilcock, after 6 h (hydrograph peak)"
+    raise SystemExit("unknown workload " + name)
+
+
+# ---------------------------------------------------------------- helpers
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) == 7:
+                self.rows.append(parts)
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        time.sleep(0.2)
+        rows = self.rows
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[0]) for r in rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[3 + k] == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(rows)}
+
+
+def measured_peak_hbm():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def spin_up(model, minutes, flags):
+    """Runs the model until the simulated clock passes `minutes`."""
+    while True:
+        model.run(2000, flags, records=False)
+        s = model.scalars()
+        if s.cycle >= minutes or s.cycle / 60 >= model.p.maxcycle:
+            return s
+
+
+# per-cell algorithmic bytes of flow_route: elevation, depth, qx, qy read and
+# qx, qy written (48 B); + Manning's n (8 B) when spatially variable;
+# + suspended load (Vsusptot read, qxs, qys written: 24 B) and the two
+# vel_dir entries erosion consumes (16 B) when erosion is on.
+def flow_bytes_per_cell(p):
+    b = 48
+    if p.spatially_var_mannings:
+        b += 8
+    if not p.hydro_only:
+        b += 24 + 16
+    return b
+
+
+# ---------------------------------------------------------------- GPU arm
+def run_gpu(args, rank, world, dist):
+    import torch
+    import hc
+    torch.cuda.set_device(rank % max(1, torch.cuda.device_count()))
+    case, spin_min, desc = make_workload(args.workload)
+    flags = case.flags
+    model = hc.Model(case)
+    spin_up(model, spin_min, flags)
+    stream = torch.cuda.ExternalStream(model.stream())
+    model.run(args.warmup, flags, records=False)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(torch.cuda.current_device()) if rank == 0 else None
+    if clocks:
+        clocks.start()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    l0 = model.counters()[0]
+    e0.record(stream)
+    done = model.run(args.steps, flags, records=False)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    launches = model.counters()[0] - l0
+    clk = clocks.stop() if clocks else None
+    if dist:
+        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        n = torch.tensor([done], dtype=torch.float64, device="cuda")
+        dist.all_reduce(n, op=dist.ReduceOp.SUM)
+        total_steps = float(n.item())
+    else:
+        total_steps = done
+    cells = case.cells
+    value = cells * total_steps / (ms / 1e3)
+    out = {"ms": ms, "done": done, "value": value, "clocks": clk, "cells": cells, "desc": desc,
+           "launches": launches}
+    if rank != 0:
+        return out, model, case
+    # end-to-end through the public API: one hc_run call per step with the
+    # step's record read back to host memory (the drop-in call pattern)
+    e2e_steps = max(3, min(args.steps, 50))
+    _, h0, d0 = model.counters()
+    t0 = time.perf_counter()
+    e0.record(stream)
+    for _ in range(e2e_steps):
+        model.run(1, flags, records=True)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    _, h1, d1 = model.counters()
+    # host wall clock: each call synchronises, so the host clock bounds the
+    # device time and includes the per-call host work
+    out["e2e"] = {"value": cells * e2e_steps / e2e_s, "unit": UNIT,
+                  "h2d_bytes_per_step": (h1 - h0) // e2e_steps,
+                  "d2h_bytes_per_step": (d1 - d0) // e2e_steps,
+                  "steps": e2e_steps, "api": "hc_run(ctx, 1, flags, host_records) per step"}
+    # per-phase breakdown of a few iterations (phase by phase, no graph)
+    prof = [model.profile_iteration(flags) for _ in range(5)]
+    out["phases_ms"] = {k: float(np.median([p_[k] for p_ in prof])) for k in prof[0]}
+    # dominant kernel, timed alone with events on the library's stream
+    reps = 20
+    ms_flow, wet = model.bench_kernel("flow_route", reps)
+    peak, kind = measured_peak_hbm()
+    per_cell = flow_bytes_per_cell(case.params)
+    ach = wet * per_cell / (ms_flow / 1e3) / 1e9
+    out["roofline"] = {"bound": "hbm", "kernel": "k_flow_route", "achieved": ach, "peak": peak,
+                       "unit": "GB/s", "frac": ach / peak, "traffic": None,
+                       "peak_kind": kind, "bytes_per_wet_cell": per_cell, "wet_cells": wet,
+                       "launch_ms": ms_flow}
+    return out, model, case
+
+
+def cpu_sample(model, case, flags, budget_s=15.0):
+    """The oracle port (OpenMP build) timed on the host from the GPU state."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    oracle.build()
+    o = oracle.Oracle(case, omp=True)
+    o.load_from(model)
+    cores = os.cpu_count()
+    n = 0
+    t0 = time.perf_counter()
+    while time.perf_counter() - t0 < budget_s:
+        o.iterate(1, flags)
+        n += 1
+    dt = time.perf_counter() - t0
+    return {"value": case.cells * n / dt, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": "%d steps from the GPU's timed state, %.1f s" % (n, dt)}
+
+
+# ---------------------------------------------------------------- reference arm
+def run_reference(args):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    oracle.build()
+    case, spin_min, desc = make_workload(args.workload)
+    flags = case.flags
+    o = oracle.Oracle(case, omp=True)
+    while True:
+        o.iterate(2000, flags)
+        if o.scalar("cycle") >= spin_min:
+            break
+    o.iterate(args.warmup, flags)
+    t0 = time.perf_counter()
+    o.iterate(args.steps, flags)
+    dt = time.perf_counter() - t0
+    v = case.cells * args.steps / dt
+    cores = os.cpu_count()
+    return {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": args.workload, "description": desc,
+                                            "cells": case.cells},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": "%d steps after spin-up, OpenMP port" % args.steps},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="catchment2000",
+                    choices=["catchment2000", "flow8192", "reach"])
+    ap.add_argument("--cpu-budget", type=float, default=15.0)
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps(run_reference(args)))
+        return
+    dist = None
+    if world > 1:
+        import torch.distributed as tdist
+        tdist.init_process_group("nccl")
+        dist = tdist
+    out, model, case = run_gpu(args, rank, world, dist)
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": out["value"], "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": out["ms"] / out["done"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded generators, hail-caesar_gb300/synth.py)",
+            "config": {"workload": args.workload, "description": out["desc"],
+                       "cells": out["cells"], "parallelism": "replicas x%d" % world,
+                       "l2": "inputs larger than L2 (model state several GB)"},
+            "clocks": out["clocks"], "e2e": out["e2e"], "roofline": out["roofline"],
+            "gpu_launches": out["launches"], "phases_ms": out["phases_ms"],
+        }
+        if world == 1:
+            line["cpu_baseline"] = cpu_sample(model, case, case.flags, args.cpu_budget)
+        print(json.dumps(line))
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,1081 @@
+// The C ABI of libhc_gpu (include/hc_gpu.h): context life cycle, field
+// transfers in the reference's layouts, the member-level entry points, and
+// hc_run, which executes whole iterations of the reference's main loop from a
+// CUDA graph with the driver's scalar logic on the device.
+
+#include "hc_internal.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+size_t lateral_scratch_bytes(int imax, int jmax);
+
+// ------------------------------------------------------------------ errors
+hc_status hc_fail(hc_ctx* c, hc_status st, const char* fmt, ...) {
+  if (c) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(c->err, sizeof c->err, fmt, ap);
+    va_end(ap);
+  }
+  return st;
+}
+
+hc_status hc_cuda(hc_ctx* c, cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return HC_OK;
+  return hc_fail(c, HC_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define HC_TRY(expr)                         \
+  do {                                       \
+    hc_status st_ = (expr);                  \
+    if (st_ != HC_OK) return st_;            \
+  } while (0)
+#define HC_CU(expr, what) HC_TRY(hc_cuda(c, (expr), what))
+
+namespace {
+
+struct Extra {
+  double* lateral;  // lateral3 scratch
+  float* h_rain; int h_rain_rows, h_rain_cols;
+  std::vector<hc_step_record> dummy;
+};
+
+// per-context side allocations not in hc_view
+std::vector<std::pair<hc_ctx*, Extra>>& extras() {
+  static std::vector<std::pair<hc_ctx*, Extra>> e;
+  return e;
+}
+Extra& extra(hc_ctx* c) {
+  for (auto& p : extras())
+    if (p.first == c) return p.second;
+  extras().push_back({c, Extra{}});
+  return extras().back().second;
+}
+void drop_extra(hc_ctx* c) {
+  auto& e = extras();
+  for (size_t k = 0; k < e.size(); k++)
+    if (e[k].first == c) {
+      e.erase(e.begin() + k);
+      return;
+    }
+}
+
+__global__ void k_fill_d(double* a, size_t n, double v) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x)
+    a[i] = v;
+}
+__global__ void k_fill_i(int32_t* a, size_t n, int32_t v) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x)
+    a[i] = v;
+}
+__global__ void k_fill_u64(unsigned long long* a, size_t n, unsigned long long v) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x)
+    a[i] = v;
+}
+
+__global__ void k_set_max_ts(const hc_view c, hc_dev* d) {
+  hc_scalars& s = d->s;
+  const hc_params& p = c.p;
+  s.input_output_difference = fabs(s.waterinput - s.waterOut);
+  auto cfl = [&]() { return p.courant_number * (p.DX / sqrt(9.81 * (s.maxdepth))); };
+  if (s.maxdepth <= 0.1) s.maxdepth = 0.1;
+  if (s.time_step < cfl()) s.time_step = cfl();
+  if (s.input_output_difference > p.in_out_difference_allowed && s.time_step > (cfl()))
+    s.time_step = cfl();
+}
+
+template <class T>
+hc_status dalloc(hc_ctx* c, T** p, size_t count) {
+  size_t bytes = count * sizeof(T);
+  if (bytes == 0) bytes = sizeof(T);
+  if (c->max_bytes && c->bytes + bytes > c->max_bytes)
+    return hc_fail(c, HC_ERR_NOMEM, "device allocation cap of %zu bytes exceeded", c->max_bytes);
+  cudaError_t e = cudaMalloc((void**)p, bytes);
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    cudaGetLastError();
+    return hc_fail(c, HC_ERR_NOMEM, "cudaMalloc(%zu): %s", bytes, cudaGetErrorString(e));
+  }
+  c->bytes += bytes;
+  return HC_OK;
+}
+
+void fill_d(hc_ctx* c, double* a, size_t n, double v) {
+  if (!a || !n) return;
+  k_fill_d<<<(unsigned)std::min<size_t>((n + 255) / 256, 4096), 256, 0, c->s>>>(a, n, v);
+}
+void fill_i(hc_ctx* c, int32_t* a, size_t n, int32_t v) {
+  if (!a || !n) return;
+  k_fill_i<<<(unsigned)std::min<size_t>((n + 255) / 256, 4096), 256, 0, c->s>>>(a, n, v);
+}
+
+}  // namespace
+
+double* lateral_buffer(hc_ctx* c) { return extra(c).lateral; }
+
+// ------------------------------------------------------------------ params
+extern "C" void hc_params_default(hc_params* p, int32_t imax, int32_t jmax, double DX) {
+  std::memset(p, 0, sizeof *p);
+  p->imax = imax;
+  p->jmax = jmax;
+  p->DX = DX;
+  p->courant_number = 0.7;
+  p->froude_limit = 0.8;
+  p->mannings = 0.04;
+  p->hflow_threshold = 0.00001;
+  p->edgeslope = 0.001;
+  p->water_depth_erosion_threshold = 0.01;
+  p->in_out_difference_allowed = 0;
+  p->max_time_step = 0;
+  p->ERODEFACTOR = 0.05;
+  p->maxcycle = 1000;
+  p->rain_data_time_step = 60;
+  p->rfnum = 1;
+  p->M = 0.005;
+  p->rain_factor = 1;
+  p->baseflow = 0.00000005;
+  p->MIN_Q = 0.01;
+  p->MIN_Q_MAXVAL = 1000.0;
+  p->reach_input_data_timestep = 60;
+  p->div_inputs = 1;
+  p->active = 0.2;
+  p->max_vel = 5;
+  p->Csuspmax = 0.05;
+  p->vegTauCrit = 100;
+  p->veg_lat_restriction = 0.1;
+  p->lateral_constant = 0.0000002;
+  p->chann_lateral_erosion = 20.0;
+  p->failureangle = 45;
+  p->CREEP_RATE = 0.0025;
+  const double d[10] = {0.0, 0.000065, 0.001, 0.002, 0.004, 0.008, 0.016, 0.032, 0.064, 0.128};
+  const double dp[11] = {0.0, 0.05, 0.05, 0.15, 0.225, 0.25, 0.1, 0.075, 0.05, 0.05, 0.0};
+  const double fv[11] = {0.0, 0.033, 0.109, 0.164, 0.237, 0.338, 0.479, 0.678, 0.959, 1.357, 0.0};
+  for (int n = 0; n < 10; n++) p->d[n] = d[n];
+  for (int n = 0; n < 11; n++) {
+    p->dprop[n] = dp[n];
+    p->fallVelocity[n] = fv[n];
+    p->isSuspended[n] = (n == 1);
+  }
+  p->edge_smoothing_passes = 100.0;
+  p->downstream_shift = 5.0;
+  p->lateral_cross_channel_smoothing = 0.0001;
+  p->scan_area_interval_iter = 5;
+  p->in_channel_landslide_iter_interval = 10;
+  p->creep_time_interval = 14400;
+  p->global_landsliding_interval = 1440;
+  p->creep_coeff = 0.028;
+  p->LIMIT = 1;
+}
+
+extern "C" int64_t hc_field_count(const hc_params* p, hc_field f) {
+  if (!p) return -1;
+  const int64_t N2 = (int64_t)(p->imax + 2) * (p->jmax + 2);
+  const int64_t E2 = (int64_t)(p->imax + 1) * (p->jmax + 1);
+  const int64_t nrec = N2 / std::max(1, p->LIMIT);
+  switch (f) {
+    case HC_F_VEL_DIR: return N2 * 9;
+    case HC_F_SR: case HC_F_SL: case HC_F_SU: case HC_F_SD: return N2 * 10;
+    case HC_F_GRAIN: return nrec * 11;
+    case HC_F_STRATA: return nrec * 10 * 11;
+    case HC_F_EDGE: return E2;
+    case HC_F_VEG: return E2 * 4;
+    default:
+      if (f >= 0 && f < HC_F_COUNT) return N2;
+      return -1;
+  }
+}
+
+extern "C" int32_t hc_field_elsize(hc_field f) {
+  switch (f) {
+    case HC_F_INDEX: case HC_F_DOWN_SCAN: case HC_F_RFAREA: return 4;
+    case HC_F_INPUTPOINTS: return 1;
+    default: return (f >= 0 && f < HC_F_COUNT) ? 8 : -1;
+  }
+}
+
+extern "C" const char* hc_last_error(const hc_ctx* c) { return c ? c->err : "null context"; }
+extern "C" void* hc_stream(hc_ctx* c) { return c ? (void*)c->s : nullptr; }
+
+// ------------------------------------------------------------------ create
+static hc_status free_all(hc_ctx* c);
+
+extern "C" hc_status hc_create(const hc_params* p, size_t max_bytes, hc_ctx** out) {
+  if (!p || !out) return HC_ERR_ARG;
+  *out = nullptr;
+  if (p->imax < 3 || p->jmax < 3 || !(p->DX > 0)) return HC_ERR_ARG;
+  if (p->rfnum < 1 || p->rfnum > HC_MAX_RF) return HC_ERR_ARG;
+  if (p->number_of_points < 0 || p->number_of_points > HC_MAX_POINTS) return HC_ERR_ARG;
+  if (p->LIMIT < 1 || p->scan_area_interval_iter < 1 || p->in_channel_landslide_iter_interval < 1)
+    return HC_ERR_ARG;
+  if (p->vegetation_on) return HC_ERR_UNSUPPORTED;
+  if ((double)(p->imax + 2) * (p->jmax + 2) * 5 > 2147483647.0) return HC_ERR_UNSUPPORTED;
+  hc_ctx* c = new hc_ctx();
+  std::memset((void*)c, 0, sizeof *c);
+  c->max_bytes = max_bytes;
+  hc_view& v = c->v;
+  v.p = *p;
+  v.rDX = 1.0 / p->DX;
+  v.imax = p->imax;
+  v.jmax = p->jmax;
+  v.W = (size_t)p->jmax + 2;
+  v.N2 = (size_t)(p->imax + 2) * v.W;
+  v.E2 = (size_t)(p->imax + 1) * (p->jmax + 1);
+  const size_t N2 = v.N2, E2 = v.E2;
+  const bool sed = !p->hydro_only;
+  cudaGetDevice(&c->device);
+  if (cudaStreamCreateWithFlags(&c->s, cudaStreamNonBlocking) != cudaSuccess) {
+    cudaGetLastError();
+    delete c;
+    return HC_ERR_CUDA;
+  }
+  hc_status st = HC_OK;
+#define A(ptr, n)                                    \
+  if (st == HC_OK) st = dalloc(c, &(ptr), (n));
+  A(v.elev, N2) A(v.h, N2) A(v.qx, N2) A(v.qy, N2) A(v.qxs, N2) A(v.qys, N2) A(v.vs, N2)
+  A(v.vel, N2) A(v.tau, N2) A(v.bed, N2) A(v.man, N2) A(v.area, N2) A(v.ss, N2)
+  A(v.vd, 4 * N2) A(v.index, N2) A(v.mask, N2) A(v.rfarea, N2)
+  A(v.edge, E2) A(v.edge2, E2) A(v.veg, 4 * E2)
+  A(v.cin_x, (size_t)p->imax * p->jmax + 2) A(v.cin_y, (size_t)p->imax * p->jmax + 2)
+  if (sed) {
+    A(v.sflux, 40 * N2) A(v.grain, 11 * N2) A(v.strata, 90 * N2) A(v.alloc_key, N2)
+    A(v.erodetot, N2) A(v.erodetot3, N2)
+  } else {
+    A(v.erodetot, N2)
+  }
+  char* red = nullptr;
+  A(red, erode_scratch_bytes(N2, p->imax, p->jmax))
+  v.red = (double*)red;
+  A(v.touched, slide_scratch_bytes(N2))
+  double* lat = nullptr;
+  if (sed && p->imax == p->jmax) A(lat, lateral_scratch_bytes(p->imax, p->jmax) / 8 + 1)
+  A(c->dev, 1)
+#undef A
+  if (st != HC_OK) {
+    free_all(c);
+    return st;
+  }
+  extra(c).lateral = lat;
+  v.cin_cap = p->imax * p->jmax;
+  if (cudaMallocHost((void**)&c->hdev, sizeof(hc_dev)) != cudaSuccess) {
+    cudaGetLastError();
+    free_all(c);
+    return HC_ERR_NOMEM;
+  }
+  c->h_cin_x = (int32_t*)calloc((size_t)p->imax * p->jmax + 2, 4);
+  c->h_cin_y = (int32_t*)calloc((size_t)p->imax * p->jmax + 2, 4);
+  // zero_values :2891-2982
+  cudaStream_t s = c->s;
+  for (double* a : {v.h, v.qx, v.qy, v.qxs, v.qys, v.vs, v.vel, v.tau, v.man, v.area, v.ss})
+    cudaMemsetAsync(a, 0, N2 * 8, s);
+  fill_d(c, v.elev, N2, -9999);
+  fill_d(c, v.bed, N2, -9999);
+  cudaMemsetAsync(v.vd, 0, 4 * N2 * 8, s);
+  fill_i(c, v.index, N2, -9999);
+  cudaMemsetAsync(v.mask, 0, N2, s);
+  fill_i(c, v.rfarea, N2, 1);
+  cudaMemsetAsync(v.edge, 0, E2 * 8, s);
+  cudaMemsetAsync(v.edge2, 0, E2 * 8, s);
+  cudaMemsetAsync(v.veg, 0, 4 * E2 * 8, s);
+  cudaMemsetAsync(v.cin_x, 0, ((size_t)p->imax * p->jmax + 2) * 4, s);
+  cudaMemsetAsync(v.cin_y, 0, ((size_t)p->imax * p->jmax + 2) * 4, s);
+  cudaMemsetAsync(v.erodetot, 0, N2 * 8, s);
+  if (sed) {
+    cudaMemsetAsync(v.sflux, 0, 40 * N2 * 8, s);
+    cudaMemsetAsync(v.grain, 0, 11 * N2 * 8, s);
+    cudaMemsetAsync(v.strata, 0, 90 * N2 * 8, s);
+    cudaMemsetAsync(v.erodetot3, 0, N2 * 8, s);
+    k_fill_u64<<<4096, 256, 0, s>>>(v.alloc_key, N2, ~0ull);
+  }
+  cudaMemsetAsync(v.red, 0, erode_scratch_bytes(N2, p->imax, p->jmax), s);
+  cudaMemsetAsync(v.touched, 0, slide_scratch_bytes(N2), s);
+  // scalar members at their initialisers (LSDCatchmentModel.hpp)
+  hc_dev* hd = c->hdev;
+  std::memset(hd, 0, sizeof *hd);
+  hc_scalars& sc = hd->s;
+  sc.cycle = 0;
+  sc.time_step = 1;
+  sc.maxdepth = 10;
+  sc.erode_call = 0;
+  sc.erode_mult = 1;
+  sc.lateralcounter = 1;
+  sc.time_1 = 1;
+  sc.baseflow = p->baseflow;
+  sc.grain_array_tot = 1;
+  sc.creep_time = 1;
+  sc.creep_time2 = 1;
+  for (int n = 0; n <= HC_MAX_RF; n++) sc.j[n] = sc.jo[n] = 0.000000001;
+  hd->grain_tot = 1;
+  cudaMemcpyAsync(c->dev, hd, sizeof(hc_dev), cudaMemcpyHostToDevice, s);
+  cudaError_t e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) {
+    free_all(c);
+    return HC_ERR_CUDA;
+  }
+  *out = c;
+  return HC_OK;
+}
+
+static hc_status free_all(hc_ctx* c) {
+  hc_view& v = c->v;
+  void* ptrs[] = {v.elev, v.h, v.qx, v.qy, v.qxs, v.qys, v.vs, v.vel, v.tau, v.bed, v.man,
+                  v.area, v.ss, v.vd, v.sflux, v.grain, v.strata, v.index, v.mask, v.rfarea,
+                  v.edge, v.edge2, v.veg, v.cin_x, v.cin_y, v.erodetot, v.erodetot3,
+                  v.alloc_key, v.red, v.touched, v.topm, v.rain, v.rec, c->dev,
+                  v.reach[0], v.reach[1], v.reach[2], extra(c).lateral};
+  for (void* q : ptrs)
+    if (q) cudaFree(q);
+  if (c->hdev) cudaFreeHost(c->hdev);
+  if (c->h_elev) cudaFreeHost(c->h_elev);
+  free(c->h_cin_x);
+  free(c->h_cin_y);
+  free(extra(c).h_rain);
+  if (c->graph) cudaGraphExecDestroy(c->graph);
+  if (c->s) cudaStreamDestroy(c->s);
+  drop_extra(c);
+  delete c;
+  return HC_OK;
+}
+
+extern "C" hc_status hc_destroy(hc_ctx* c) {
+  if (!c) return HC_ERR_ARG;
+  cudaStreamSynchronize(c->s);
+  return free_all(c);
+}
+
+// ------------------------------------------------------------------ transfers
+static double* plain_field(hc_ctx* c, hc_field f) {
+  hc_view& v = c->v;
+  switch (f) {
+    case HC_F_ELEV: return v.elev;
+    case HC_F_WATER_DEPTH: return v.h;
+    case HC_F_QX: return v.qx;
+    case HC_F_QY: return v.qy;
+    case HC_F_QXS: return v.qxs;
+    case HC_F_QYS: return v.qys;
+    case HC_F_VSUSPTOT: return v.vs;
+    case HC_F_VEL: return v.vel;
+    case HC_F_TAU: return v.tau;
+    case HC_F_BEDROCK: return v.bed;
+    case HC_F_MANNINGS: return v.man;
+    case HC_F_AREA: return v.area;
+    case HC_F_SS: return v.ss;
+    case HC_F_EDGE: return v.edge;
+    case HC_F_VEG: return v.veg;
+    default: return nullptr;
+  }
+}
+
+static int sflux_dir(hc_field f) {
+  switch (f) {
+    case HC_F_SU: return 0;
+    case HC_F_SR: return 1;
+    case HC_F_SD: return 2;
+    case HC_F_SL: return 3;
+    default: return -1;
+  }
+}
+
+static hc_status check_size(hc_ctx* c, hc_field f, size_t nbytes) {
+  const int64_t n = hc_field_count(&c->v.p, f);
+  const int32_t es = hc_field_elsize(f);
+  if (n < 0 || es < 0) return hc_fail(c, HC_ERR_ARG, "unknown field %d", (int)f);
+  if ((size_t)n * es != nbytes)
+    return hc_fail(c, HC_ERR_ARG, "field %d: %zu bytes given, %lld expected", (int)f, nbytes,
+                   (long long)n * es);
+  if (c->v.p.hydro_only && (f == HC_F_GRAIN || f == HC_F_STRATA || sflux_dir(f) >= 0))
+    return hc_fail(c, HC_ERR_STATE, "field %d is not kept in hydro-only mode", (int)f);
+  return HC_OK;
+}
+
+extern "C" hc_status hc_upload(hc_ctx* c, hc_field f, const void* host, size_t nbytes) {
+  if (!c || !host) return HC_ERR_ARG;
+  HC_TRY(check_size(c, f, nbytes));
+  c->h2d_bytes += nbytes;
+  hc_view& v = c->v;
+  const size_t N2 = v.N2;
+  cudaStream_t s = c->s;
+  if (double* d = plain_field(c, f)) {
+    HC_CU(cudaMemcpyAsync(d, host, nbytes, cudaMemcpyHostToDevice, s), "upload");
+    HC_CU(cudaStreamSynchronize(s), "upload");
+    return HC_OK;
+  }
+  switch (f) {
+    case HC_F_INDEX:
+      HC_CU(cudaMemcpyAsync(v.index, host, nbytes, cudaMemcpyHostToDevice, s), "upload");
+      break;
+    case HC_F_RFAREA:
+      HC_CU(cudaMemcpyAsync(v.rfarea, host, nbytes, cudaMemcpyHostToDevice, s), "upload");
+      break;
+    case HC_F_INPUTPOINTS:
+      // The reference clears inputpointsarray in zero_values after marking
+      // the reach cells (:2905), so the mask never affects a run; accepted
+      // and ignored.
+      break;
+    case HC_F_VEL_DIR: {
+      std::vector<double> planes(4 * N2);
+      const double* h = (const double*)host;
+      for (size_t cell = 0; cell < N2; cell++)
+        for (int k = 0; k < 4; k++) planes[(size_t)k * N2 + cell] = h[cell * 9 + 1 + 2 * k];
+      HC_CU(cudaMemcpy(v.vd, planes.data(), 4 * N2 * 8, cudaMemcpyHostToDevice), "upload");
+      break;
+    }
+    case HC_F_SR: case HC_F_SL: case HC_F_SU: case HC_F_SD: {
+      const int dir = sflux_dir(f);
+      std::vector<double> planes(10 * N2);
+      const double* h = (const double*)host;
+      for (size_t cell = 0; cell < N2; cell++)
+        for (int n = 0; n < 10; n++) planes[(size_t)n * N2 + cell] = h[cell * 10 + n];
+      HC_CU(cudaMemcpy(v.sflux + (size_t)dir * 10 * N2, planes.data(), 10 * N2 * 8,
+                       cudaMemcpyHostToDevice), "upload");
+      break;
+    }
+    case HC_F_GRAIN: case HC_F_STRATA: {
+      // rows addressed by index[][]: scatter into the cells' slots
+      std::vector<int32_t> idx(N2);
+      HC_CU(cudaMemcpy(idx.data(), v.index, N2 * 4, cudaMemcpyDeviceToHost), "upload");
+      const int64_t nrec = (int64_t)N2 / std::max(1, v.p.LIMIT);
+      const double* h = (const double*)host;
+      if (f == HC_F_GRAIN) {
+        std::vector<double> planes(11 * N2, 0.0);
+        for (size_t cell = 0; cell < N2; cell++) {
+          const int r = idx[cell];
+          if (r < 0 || r >= nrec) continue;
+          for (int n = 0; n < 11; n++) planes[(size_t)n * N2 + cell] = h[(size_t)r * 11 + n];
+        }
+        HC_CU(cudaMemcpy(v.grain, planes.data(), 11 * N2 * 8, cudaMemcpyHostToDevice), "upload");
+      } else {
+        std::vector<double> planes(90 * N2, 0.0);
+        for (size_t cell = 0; cell < N2; cell++) {
+          const int r = idx[cell];
+          if (r < 0 || r >= nrec) continue;
+          for (int z = 0; z < 10; z++)
+            for (int n = 0; n < 9; n++)
+              planes[((size_t)z * 9 + n) * N2 + cell] = h[((size_t)r * 10 + z) * 11 + n];
+        }
+        HC_CU(cudaMemcpy(v.strata, planes.data(), 90 * N2 * 8, cudaMemcpyHostToDevice), "upload");
+      }
+      break;
+    }
+    case HC_F_DOWN_SCAN: {
+      // lists of wet rows per column -> per-cell mask
+      const int32_t* ds = (const int32_t*)host;
+      std::vector<uint8_t> m(N2, 0);
+      const int I = v.imax, J = v.jmax;
+      for (int j = 1; j <= J; j++) {
+        int k = 1;
+        while (k <= I + 1 && ds[(size_t)j * (I + 2) + k] > 0) {
+          int i = ds[(size_t)j * (I + 2) + k];
+          if (i >= 1 && i <= I) m[(size_t)i * v.W + j] = 1;
+          k++;
+        }
+      }
+      HC_CU(cudaMemcpy(v.mask, m.data(), N2, cudaMemcpyHostToDevice), "upload");
+      break;
+    }
+    default:
+      return hc_fail(c, HC_ERR_ARG, "field %d cannot be uploaded", (int)f);
+  }
+  HC_CU(cudaStreamSynchronize(s), "upload");
+  return HC_OK;
+}
+
+extern "C" hc_status hc_download(hc_ctx* c, hc_field f, void* host, size_t nbytes) {
+  if (!c || !host) return HC_ERR_ARG;
+  HC_TRY(check_size(c, f, nbytes));
+  c->d2h_bytes += nbytes;
+  hc_view& v = c->v;
+  const size_t N2 = v.N2;
+  cudaStream_t s = c->s;
+  HC_CU(cudaStreamSynchronize(s), "download");
+  if (double* d = plain_field(c, f)) {
+    HC_CU(cudaMemcpy(host, d, nbytes, cudaMemcpyDeviceToHost), "download");
+    return HC_OK;
+  }
+  switch (f) {
+    case HC_F_INDEX:
+      HC_CU(cudaMemcpy(host, v.index, nbytes, cudaMemcpyDeviceToHost), "download");
+      break;
+    case HC_F_RFAREA:
+      HC_CU(cudaMemcpy(host, v.rfarea, nbytes, cudaMemcpyDeviceToHost), "download");
+      break;
+    case HC_F_INPUTPOINTS:
+      std::memset(host, 0, nbytes);
+      break;
+    case HC_F_VEL_DIR: {
+      std::vector<double> planes(4 * N2);
+      HC_CU(cudaMemcpy(planes.data(), v.vd, 4 * N2 * 8, cudaMemcpyDeviceToHost), "download");
+      double* h = (double*)host;
+      std::memset(h, 0, nbytes);
+      for (size_t cell = 0; cell < N2; cell++)
+        for (int k = 0; k < 4; k++) h[cell * 9 + 1 + 2 * k] = planes[(size_t)k * N2 + cell];
+      break;
+    }
+    case HC_F_SR: case HC_F_SL: case HC_F_SU: case HC_F_SD: {
+      const int dir = sflux_dir(f);
+      std::vector<double> planes(10 * N2);
+      HC_CU(cudaMemcpy(planes.data(), v.sflux + (size_t)dir * 10 * N2, 10 * N2 * 8,
+                       cudaMemcpyDeviceToHost), "download");
+      double* h = (double*)host;
+      for (size_t cell = 0; cell < N2; cell++)
+        for (int n = 0; n < 10; n++) h[cell * 10 + n] = planes[(size_t)n * N2 + cell];
+      break;
+    }
+    case HC_F_GRAIN: case HC_F_STRATA: {
+      std::vector<int32_t> idx(N2);
+      HC_CU(cudaMemcpy(idx.data(), v.index, N2 * 4, cudaMemcpyDeviceToHost), "download");
+      const int64_t nrec = (int64_t)N2 / std::max(1, v.p.LIMIT);
+      double* h = (double*)host;
+      std::memset(h, 0, nbytes);
+      if (f == HC_F_GRAIN) {
+        std::vector<double> planes(11 * N2);
+        HC_CU(cudaMemcpy(planes.data(), v.grain, 11 * N2 * 8, cudaMemcpyDeviceToHost), "download");
+        for (size_t cell = 0; cell < N2; cell++) {
+          const int r = idx[cell];
+          if (r < 0 || r >= nrec) continue;
+          for (int n = 0; n < 11; n++) h[(size_t)r * 11 + n] = planes[(size_t)n * N2 + cell];
+        }
+      } else {
+        std::vector<double> planes(90 * N2);
+        HC_CU(cudaMemcpy(planes.data(), v.strata, 90 * N2 * 8, cudaMemcpyDeviceToHost), "download");
+        for (size_t cell = 0; cell < N2; cell++) {
+          const int r = idx[cell];
+          if (r < 0 || r >= nrec) continue;
+          for (int z = 0; z < 10; z++)
+            for (int n = 0; n < 9; n++)
+              h[((size_t)r * 10 + z) * 11 + n] = planes[((size_t)z * 9 + n) * N2 + cell];
+        }
+      }
+      break;
+    }
+    case HC_F_DOWN_SCAN: {
+      std::vector<uint8_t> m(N2);
+      HC_CU(cudaMemcpy(m.data(), v.mask, N2, cudaMemcpyDeviceToHost), "download");
+      int32_t* ds = (int32_t*)host;
+      std::memset(ds, 0, nbytes);
+      const int I = v.imax, J = v.jmax;
+      for (int j = 1; j <= J; j++) {
+        int k = 1;
+        for (int i = 1; i <= I; i++)
+          if (m[(size_t)i * v.W + j]) ds[(size_t)j * (I + 2) + (k++)] = i;
+      }
+      break;
+    }
+    default:
+      return hc_fail(c, HC_ERR_ARG, "field %d cannot be downloaded", (int)f);
+  }
+  return HC_OK;
+}
+
+// ------------------------------------------------------------------ series
+extern "C" hc_status hc_set_rain(hc_ctx* c, const float* rain, int32_t rows, int32_t cols) {
+  if (!c || !rain || rows <= 0 || cols <= 0) return HC_ERR_ARG;
+  Extra& x = extra(c);
+  free(x.h_rain);
+  x.h_rain = (float*)malloc((size_t)rows * cols * 4);
+  std::memcpy(x.h_rain, rain, (size_t)rows * cols * 4);
+  x.h_rain_rows = rows;
+  x.h_rain_cols = cols;
+  hc_view& v = c->v;
+  if (v.rain) cudaFree(v.rain);
+  v.rain = nullptr;
+  HC_TRY(dalloc(c, &v.rain, (size_t)rows * cols));
+  HC_CU(cudaMemcpy(v.rain, rain, (size_t)rows * cols * 4, cudaMemcpyHostToDevice), "rain");
+  v.rain_rows = rows;
+  v.rain_cols = cols;
+  c->prepared = false;
+  return HC_OK;
+}
+
+extern "C" hc_status hc_set_reach(hc_ctx* c, int32_t point, const float* data, int32_t rows,
+                                  int32_t cols) {
+  if (!c || !data || point < 0 || point >= HC_MAX_POINTS || rows <= 0 || cols < 14)
+    return HC_ERR_ARG;
+  hc_view& v = c->v;
+  if (v.reach[point]) cudaFree(v.reach[point]);
+  v.reach[point] = nullptr;
+  HC_TRY(dalloc(c, &v.reach[point], (size_t)rows * cols));
+  HC_CU(cudaMemcpy(v.reach[point], data, (size_t)rows * cols * 4, cudaMemcpyHostToDevice), "reach");
+  v.reach_rows[point] = rows;
+  v.reach_cols[point] = cols;
+  c->graph_iters = 0;
+  return HC_OK;
+}
+
+// ------------------------------------------------------------------ scalars
+static hc_status pull(hc_ctx* c) {
+  c->d2h_bytes += sizeof(hc_dev);
+  HC_CU(cudaMemcpyAsync(c->hdev, c->dev, sizeof(hc_dev), cudaMemcpyDeviceToHost, c->s), "pull");
+  HC_CU(cudaStreamSynchronize(c->s), "pull");
+  return HC_OK;
+}
+static hc_status push(hc_ctx* c) {
+  c->h2d_bytes += sizeof(hc_dev);
+  HC_CU(cudaMemcpyAsync(c->dev, c->hdev, sizeof(hc_dev), cudaMemcpyHostToDevice, c->s), "push");
+  HC_CU(cudaStreamSynchronize(c->s), "push");
+  return HC_OK;
+}
+
+extern "C" hc_status hc_get_scalars(hc_ctx* c, hc_scalars* s) {
+  if (!c || !s) return HC_ERR_ARG;
+  HC_TRY(pull(c));
+  c->hdev->s.grain_array_tot = c->hdev->grain_tot;
+  *s = c->hdev->s;
+  return HC_OK;
+}
+
+extern "C" hc_status hc_set_scalars(hc_ctx* c, const hc_scalars* s) {
+  if (!c || !s) return HC_ERR_ARG;
+  HC_TRY(pull(c));
+  c->hdev->s = *s;
+  c->hdev->grain_tot = (int)s->grain_array_tot;
+  return push(c);
+}
+
+// ------------------------------------------------------------------ prepare
+static hc_status recompute_points(hc_ctx* c) {
+  hc_view& v = c->v;
+  const size_t N2 = v.N2;
+  std::vector<double> elev(N2), area(N2);
+  std::vector<int32_t> rf(N2);
+  HC_CU(cudaStreamSynchronize(c->s), "points");
+  HC_CU(cudaMemcpy(elev.data(), v.elev, N2 * 8, cudaMemcpyDeviceToHost), "points");
+  HC_CU(cudaMemcpy(rf.data(), v.rfarea, N2 * 4, cudaMemcpyDeviceToHost), "points");
+  HC_TRY(pull(c));
+  hc_scalars& s = c->hdev->s;
+  int total = 0;
+  host_drainage_and_points(&v.p, elev.data(), rf.data(), s.baseflow, area.data(), c->h_cin_x,
+                           c->h_cin_y, &total, s.catchment_input_counter);
+  s.totalinputpoints = total;
+  const size_t ncin = (size_t)v.imax * v.jmax + 2;
+  HC_CU(cudaMemcpy(v.area, area.data(), N2 * 8, cudaMemcpyHostToDevice), "points");
+  HC_CU(cudaMemcpy(v.cin_x, c->h_cin_x, ncin * 4, cudaMemcpyHostToDevice), "points");
+  HC_CU(cudaMemcpy(v.cin_y, c->h_cin_y, ncin * 4, cudaMemcpyHostToDevice), "points");
+  return push(c);
+}
+
+extern "C" hc_status hc_prepare(hc_ctx* c) {
+  if (!c) return HC_ERR_ARG;
+  hc_view& v = c->v;
+  const hc_params& p = v.p;
+  Extra& x = extra(c);
+  if (!x.h_rain) return hc_fail(c, HC_ERR_STATE, "hc_set_rain must come before hc_prepare");
+  for (int n = 0; n < p.number_of_points && p.reach_mode; n++)
+    if (!v.reach[n]) return hc_fail(c, HC_ERR_STATE, "reach table %d missing", n);
+  const size_t N2 = v.N2;
+  std::vector<double> elev(N2);
+  std::vector<int32_t> rf(N2);
+  HC_CU(cudaStreamSynchronize(c->s), "prepare");
+  HC_CU(cudaMemcpy(elev.data(), v.elev, N2 * 8, cudaMemcpyDeviceToHost), "prepare");
+  HC_CU(cudaMemcpy(rf.data(), v.rfarea, N2 * 4, cudaMemcpyDeviceToHost), "prepare");
+  HC_TRY(pull(c));
+  hc_scalars& s = c->hdev->s;
+  for (int n = 0; n <= HC_MAX_RF; n++) s.nActualGridCells[n] = 0;
+  for (int i = 1; i < p.imax; i++)  // count_catchment_gridcells :2813 (i < imax, j < jmax)
+    for (int j = 1; j < p.jmax; j++)
+      if (elev[(size_t)i * v.W + j] > -9999) {
+        const int r = rf[(size_t)i * v.W + j];
+        if (r < 0 || r > p.rfnum) return hc_fail(c, HC_ERR_ARG, "rfarea value %d out of range", r);
+        s.nActualGridCells[r] += 1;
+      }
+  s.creep_time = s.creep_time2 = s.time_1 = s.cycle;  // set_time_counters :1862
+  // TOPMODEL rows: initialise_rainfall_runoff's call, then one per minute
+  const int rows = p.maxcycle * 60 + std::max(0, p.max_time_step / 60) + 2000;
+  std::vector<double> table((size_t)rows * 2 * (p.rfnum + 1));
+  host_topmodel_table(&p, x.h_rain, x.h_rain_rows, x.h_rain_cols, rows, table.data());
+  if (v.topm) cudaFree(v.topm);
+  v.topm = nullptr;
+  HC_TRY(dalloc(c, &v.topm, table.size()));
+  HC_CU(cudaMemcpy(v.topm, table.data(), table.size() * 8, cudaMemcpyHostToDevice), "prepare");
+  v.topm_rows = rows;
+  for (int n = 1; n <= p.rfnum; n++) {
+    s.old_j_mean[n] = table[n];
+    s.new_j_mean[n] = table[(p.rfnum + 1) + n];
+  }
+  for (int n = 1; n <= 9; n++) v.dlog[n] = std::log(p.d[n]);
+  HC_TRY(push(c));
+  HC_TRY(recompute_points(c));
+  c->prepared = true;
+  c->graph_iters = 0;  // parameters of the view changed: rebuild the graph
+  return HC_OK;
+}
+
+// ------------------------------------------------------------------ members
+extern "C" hc_status hc_set_maximum_timestep(hc_ctx* c) {
+  if (!c) return HC_ERR_ARG;
+  k_set_max_ts<<<1, 1, 0, c->s>>>(c->v, c->dev);
+  HC_CU(cudaStreamSynchronize(c->s), "set_maximum_timestep");
+  return HC_OK;
+}
+
+extern "C" hc_status hc_flow_route(hc_ctx* c) {
+  if (!c) return HC_ERR_ARG;
+  launch_flow_dt(c);
+  launch_flow_route(c, 0);
+  HC_CU(cudaStreamSynchronize(c->s), "flow_route");
+  return HC_OK;
+}
+
+extern "C" hc_status hc_depth_update(hc_ctx* c) {
+  if (!c) return HC_ERR_ARG;
+  launch_flow_dt(c);
+  launch_depth_update(c, 0);
+  HC_CU(cudaStreamSynchronize(c->s), "depth_update");
+  return HC_OK;
+}
+
+extern "C" hc_status hc_scan_area(hc_ctx* c) {
+  if (!c) return HC_ERR_ARG;
+  launch_scan_area(c, 0);
+  HC_CU(cudaStreamSynchronize(c->s), "scan_area");
+  return HC_OK;
+}
+
+extern "C" hc_status hc_water_flux_out(hc_ctx* c) {
+  if (!c) return HC_ERR_ARG;
+  launch_flux_out(c, 0, 0);
+  HC_CU(cudaStreamSynchronize(c->s), "water_flux_out");
+  return HC_OK;
+}
+
+extern "C" hc_status hc_erode(hc_ctx* c, double mult, double* tempbmax) {
+  if (!c) return HC_ERR_ARG;
+  if (c->v.p.hydro_only) return hc_fail(c, HC_ERR_STATE, "erosion arrays absent (hydro_only)");
+  if (!c->prepared) {
+    for (int n = 1; n <= 9; n++) c->v.dlog[n] = std::log(c->v.p.d[n]);
+  }
+  launch_erode_begin(c, 0, mult < 0 ? 0 : mult);
+  for (int guard = 0;; guard++) {
+    launch_erode_pass(c, 0);
+    HC_TRY(pull(c));
+    if (c->hdev->pause & HC_PAUSE_ERROR)
+      return hc_fail(c, HC_ERR_STATE, "device error %d", c->hdev->err_code);
+    if (!c->hdev->erode_retry) break;
+    if (guard > 100000) return hc_fail(c, HC_ERR_TIMEOUT, "erosion retry loop did not end");
+  }
+  launch_erode_finish(c, 0);
+  HC_TRY(pull(c));
+  if (tempbmax) *tempbmax = c->hdev->s.tempbmax;
+  return HC_OK;
+}
+
+extern "C" hc_status hc_lateral_channel_erode(hc_ctx* c) {
+  if (!c) return HC_ERR_ARG;
+  if (c->v.p.hydro_only) return hc_fail(c, HC_ERR_STATE, "erosion arrays absent (hydro_only)");
+  return run_lateral(c);
+}
+
+extern "C" hc_status hc_in_channel_landsliding(hc_ctx* c) {
+  if (!c) return HC_ERR_ARG;
+  if (c->v.p.hydro_only) return hc_fail(c, HC_ERR_STATE, "erosion arrays absent (hydro_only)");
+  launch_slide3(c, 0);
+  HC_TRY(pull(c));
+  if (c->hdev->pause & HC_PAUSE_ERROR)
+    return hc_fail(c, HC_ERR_STATE, "device error %d", c->hdev->err_code);
+  return HC_OK;
+}
+
+// ------------------------------------------------------------------ hc_run
+static void launch_iteration(hc_ctx* c, int flags) {
+  launch_control(c);
+  launch_inputs(c);
+  launch_flow_route(c, 1);
+  launch_depth_update(c, 1);
+  launch_scan_area(c, 1);
+  if (!c->v.p.hydro_only) {
+    launch_erode_begin(c, 1, -1);
+    for (int k = 0; k < HC_ERODE_PASSES; k++) launch_erode_pass(c, HC_ERODE_PASSES);
+    launch_erode_finish(c, 1);
+    if (flags & HC_RUN_LATERAL) launch_lateral_check(c);
+  }
+  launch_flux_out(c, 1, 1);
+  if (!c->v.p.hydro_only) launch_slide3(c, 1);
+}
+
+static int graph_chunk() {
+  const char* e = getenv("HC_GRAPH_ITERS");
+  int k = e ? atoi(e) : 32;
+  return std::max(1, std::min(k, 4096));
+}
+
+static hc_status build_graph(hc_ctx* c, int flags) {
+  if (c->graph) cudaGraphExecDestroy(c->graph);
+  c->graph = nullptr;
+  const int K = graph_chunk();
+  cudaGraph_t g;
+  HC_CU(cudaStreamBeginCapture(c->s, cudaStreamCaptureModeThreadLocal), "capture");
+  c->capturing = true;
+  for (int k = 0; k < K; k++) launch_iteration(c, flags);
+  c->capturing = false;
+  HC_CU(cudaStreamEndCapture(c->s, &g), "capture");
+  size_t nn = 0;
+  cudaGraphGetNodes(g, nullptr, &nn);
+  std::vector<cudaGraphNode_t> nodes(nn);
+  cudaGraphGetNodes(g, nodes.data(), &nn);
+  c->graph_kernels = 0;
+  for (auto nd : nodes) {
+    cudaGraphNodeType t;
+    cudaGraphNodeGetType(nd, &t);
+    if (t == cudaGraphNodeTypeKernel) c->graph_kernels++;
+  }
+  cudaError_t e = cudaGraphInstantiate(&c->graph, g, 0);
+  cudaGraphDestroy(g);
+  HC_CU(e, "graph instantiate");
+  c->graph_iters = K;
+  c->graph_flags = flags;
+  return HC_OK;
+}
+
+// Finishes an iteration that stopped before water_flux_out (erosion retry
+// beyond the captured passes, or lateral3 due).
+static hc_status finish_iteration(hc_ctx* c, int flags) {
+  hc_dev* hd = c->hdev;
+  // the skipped iterations after the pause cleared it_active; this one resumes
+  hd->it_active = 1;
+  HC_TRY(push(c));
+  if (hd->pause & HC_PAUSE_ERODE) {
+    for (int guard = 0; hd->erode_retry; guard++) {
+      launch_erode_pass(c, 0);
+      HC_TRY(pull(c));
+      if (guard > 100000) return hc_fail(c, HC_ERR_TIMEOUT, "erosion retry loop did not end");
+    }
+    hd->pause &= ~HC_PAUSE_ERODE;
+    hd->rest_active = 1;
+    HC_TRY(push(c));
+    launch_erode_finish(c, 1);
+    if (flags & HC_RUN_LATERAL) launch_lateral_check(c);
+    HC_TRY(pull(c));
+  }
+  if (hd->pause & HC_PAUSE_LATERAL) {
+    HC_TRY(run_lateral(c));
+    HC_TRY(pull(c));
+    hd->s.lateralcounter = hd->s.counter + (50 * hd->s.erode_mult);  // call_lateral :2302
+    hd->do_lateral = 0;
+    hd->pause &= ~HC_PAUSE_LATERAL;
+    hd->rest_active = 1;
+    HC_TRY(push(c));
+  }
+  launch_flux_out(c, 1, 1);
+  if (!c->v.p.hydro_only) launch_slide3(c, 1);
+  return pull(c);
+}
+
+static hc_status host_steps(hc_ctx* c, int flags) {
+  hc_dev* hd = c->hdev;
+  const hc_params& p = c->v.p;
+  if (hd->pause & HC_PAUSE_HOSTSTEP) {
+    hd->pause &= ~HC_PAUSE_HOSTSTEP;
+    if (!p.hydro_only && !(flags & HC_RUN_NOHILL)) {
+      if (hd->s.cycle > hd->s.creep_time) {  // slope_creep :1976
+        hd->s.creep_time += p.creep_time_interval;
+        HC_TRY(push(c));
+        HC_TRY(run_creep(c, p.creep_coeff));
+        HC_TRY(pull(c));
+      }
+      if (hd->s.cycle > hd->s.creep_time2) {  // call_global_landsliding :1986
+        hd->s.creep_time2 += p.global_landsliding_interval;
+        HC_TRY(push(c));
+        HC_TRY(run_global_landsliding(c));
+        HC_TRY(pull(c));
+      }
+    }
+    HC_TRY(push(c));
+  }
+  if (hd->pause & HC_PAUSE_DRAINAGE) {
+    hd->pause &= ~HC_PAUSE_DRAINAGE;
+    HC_TRY(push(c));
+    HC_TRY(recompute_points(c));
+  }
+  return HC_OK;
+}
+
+extern "C" hc_status hc_run(hc_ctx* c, int64_t n, int32_t flags, hc_step_record* rec,
+                            int64_t* done) {
+  if (!c || n < 0) return HC_ERR_ARG;
+  if (done) *done = 0;
+  if (!c->prepared) return hc_fail(c, HC_ERR_STATE, "hc_prepare must come before hc_run");
+  if ((flags & HC_RUN_LATERAL) && c->v.imax != c->v.jmax && !c->v.p.hydro_only)
+    return hc_fail(c, HC_ERR_UNSUPPORTED, "lateral3 needs a square grid");
+  hc_view& v = c->v;
+  if (rec && v.rec_cap < n) {
+    if (v.rec) cudaFree(v.rec);
+    v.rec = nullptr;
+    v.rec_cap = 0;
+    HC_TRY(dalloc(c, &v.rec, (size_t)n));
+    v.rec_cap = n;
+    c->graph_iters = 0;  // the view changed
+  }
+  HC_TRY(pull(c));
+  hc_dev* hd = c->hdev;
+  if (hd->pause & HC_PAUSE_FINISHED) return HC_OK;
+  hd->pause = 0;
+  hd->budget = n;
+  hd->rec_index = 0;
+  hd->flags = flags;
+  HC_TRY(push(c));
+  if (!c->graph_iters || c->graph_flags != flags) HC_TRY(build_graph(c, flags));
+  int64_t ran = 0;
+  while (true) {
+    HC_CU(cudaGraphLaunch(c->graph, c->s), "graph launch");
+    c->launches += c->graph_kernels;
+    HC_TRY(pull(c));
+    if (hd->pause & HC_PAUSE_ERROR)
+      return hc_fail(c, HC_ERR_STATE, "device error %d", hd->err_code);
+    if (hd->pause & (HC_PAUSE_ERODE | HC_PAUSE_LATERAL)) HC_TRY(finish_iteration(c, flags));
+    HC_TRY(host_steps(c, flags));
+    ran = n - hd->budget;
+    if ((hd->pause & HC_PAUSE_FINISHED) || hd->budget <= 0) break;
+    if (hd->pause & ~(HC_PAUSE_BUDGET)) {
+      HC_TRY(pull(c));
+      if (hd->pause & HC_PAUSE_ERROR)
+        return hc_fail(c, HC_ERR_STATE, "device error %d", hd->err_code);
+    }
+    hd->pause &= HC_PAUSE_FINISHED;
+    HC_TRY(push(c));
+  }
+  if (rec && ran > 0) {
+    const int64_t nrec = std::min<int64_t>(hd->rec_index, n);
+    c->d2h_bytes += nrec * (int64_t)sizeof(hc_step_record);
+    HC_CU(cudaMemcpy(rec, v.rec, (size_t)nrec * sizeof(hc_step_record), cudaMemcpyDeviceToHost),
+          "records");
+  }
+  if (done) *done = ran;
+  hd->pause &= HC_PAUSE_FINISHED;
+  HC_TRY(push(c));
+  return HC_OK;
+}
+
+// ------------------------------------------------------------------ measurement
+__global__ void k_count_mask(const hc_view c, unsigned long long* n) {
+  unsigned long long local = 0;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < c.N2;
+       i += (size_t)gridDim.x * blockDim.x)
+    local += c.mask[i];
+  for (int o = 16; o > 0; o >>= 1) local += __shfl_xor_sync(0xffffffffu, local, o);
+  if ((threadIdx.x & 31) == 0 && local) atomicAdd(n, local);
+}
+
+extern "C" hc_status hc_bench_kernel(hc_ctx* c, const char* kernel, int32_t reps, double* avg_ms,
+                                     int64_t* wet) {
+  if (!c || !kernel || reps <= 0 || !avg_ms) return HC_ERR_ARG;
+  const std::string k(kernel);
+  unsigned long long* cnt = (unsigned long long*)((char*)c->v.red + 112);
+  HC_CU(cudaMemsetAsync(cnt, 0, 8, c->s), "bench");
+  k_count_mask<<<1024, 256, 0, c->s>>>(c->v, cnt);
+  unsigned long long h = 0;
+  HC_CU(cudaMemcpyAsync(&h, cnt, 8, cudaMemcpyDeviceToHost, c->s), "bench");
+  launch_flow_dt(c);
+  cudaEvent_t e0, e1;
+  HC_CU(cudaEventCreate(&e0), "bench");
+  HC_CU(cudaEventCreate(&e1), "bench");
+  HC_CU(cudaEventRecord(e0, c->s), "bench");
+  for (int r = 0; r < reps; r++) {
+    if (k == "flow_route") launch_flow_route(c, 0);
+    else if (k == "depth_update") launch_depth_update(c, 0);
+    else if (k == "scan_area") launch_scan_area(c, 0);
+    else if (k == "entrain" && !c->v.p.hydro_only) {
+      // one entrainment pass (retry flag forced on)
+      launch_erode_begin(c, 0, 1.0);
+      launch_erode_pass(c, 1);
+    } else {
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      return hc_fail(c, HC_ERR_ARG, "unknown kernel %s", kernel);
+    }
+  }
+  HC_CU(cudaEventRecord(e1, c->s), "bench");
+  HC_CU(cudaEventSynchronize(e1), "bench");
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  *avg_ms = ms / reps;
+  if (wet) *wet = (int64_t)h;
+  return HC_OK;
+}
+
+extern "C" hc_status hc_get_counters(hc_ctx* c, int64_t* launches, int64_t* h2d_bytes,
+                                     int64_t* d2h_bytes) {
+  if (!c) return HC_ERR_ARG;
+  if (launches) *launches = c->launches;
+  if (h2d_bytes) *h2d_bytes = c->h2d_bytes;
+  if (d2h_bytes) *d2h_bytes = c->d2h_bytes;
+  return HC_OK;
+}
+
+// One iteration of hc_run's sequence, launched phase by phase (no graph) with
+// a CUDA event after each phase; ms[k] receives the time of phase k:
+// 0 control+inputs, 1 flow_route, 2 depth_update, 3 scan_area,
+// 4 entrainment passes, 5 apply + lateral passes + edge output,
+// 6 lateral3 (when due), 7 water_flux_out, 8 slide_3.
+extern "C" hc_status hc_profile_iteration(hc_ctx* c, int32_t flags, double* ms) {
+  if (!c || !ms) return HC_ERR_ARG;
+  if (!c->prepared) return hc_fail(c, HC_ERR_STATE, "hc_prepare must come before profiling");
+  HC_TRY(pull(c));
+  hc_dev* hd = c->hdev;
+  hd->pause = 0;
+  hd->budget = 1;
+  hd->flags = flags;
+  HC_TRY(push(c));
+  cudaEvent_t ev[10];
+  for (int k = 0; k < 10; k++) HC_CU(cudaEventCreate(&ev[k]), "profile");
+  cudaEventRecord(ev[0], c->s);
+  launch_control(c);
+  launch_inputs(c);
+  cudaEventRecord(ev[1], c->s);
+  launch_flow_route(c, 1);
+  cudaEventRecord(ev[2], c->s);
+  launch_depth_update(c, 1);
+  cudaEventRecord(ev[3], c->s);
+  launch_scan_area(c, 1);
+  cudaEventRecord(ev[4], c->s);
+  const bool sed = !c->v.p.hydro_only;
+  if (sed) {
+    launch_erode_begin(c, 1, -1);
+    HC_TRY(pull(c));
+    for (int guard = 0; hd->erode_retry && hd->it_active && guard < 100000; guard++) {
+      launch_erode_pass(c, 0);
+      HC_TRY(pull(c));
+    }
+  }
+  cudaEventRecord(ev[5], c->s);
+  if (sed) {
+    launch_erode_finish(c, 1);
+    if (flags & HC_RUN_LATERAL) launch_lateral_check(c);
+  }
+  cudaEventRecord(ev[6], c->s);
+  HC_TRY(pull(c));
+  if (hd->pause & HC_PAUSE_LATERAL) {
+    HC_TRY(run_lateral(c));
+    HC_TRY(pull(c));
+    hd->s.lateralcounter = hd->s.counter + (50 * hd->s.erode_mult);
+    hd->pause &= ~HC_PAUSE_LATERAL;
+    hd->rest_active = 1;
+    HC_TRY(push(c));
+  }
+  cudaEventRecord(ev[7], c->s);
+  launch_flux_out(c, 1, 0);
+  cudaEventRecord(ev[8], c->s);
+  if (sed) launch_slide3(c, 1);
+  cudaEventRecord(ev[9], c->s);
+  HC_CU(cudaEventSynchronize(ev[9]), "profile");
+  for (int k = 0; k < 9; k++) {
+    float t = 0;
+    cudaEventElapsedTime(&t, ev[k], ev[k + 1]);
+    ms[k] = t;
+  }
+  for (int k = 0; k < 10; k++) cudaEventDestroy(ev[k]);
+  HC_TRY(pull(c));
+  HC_TRY(host_steps(c, flags));
+  hd->pause &= HC_PAUSE_FINISHED;
+  return push(c);
+}

@@ -1,0 +1,741 @@
+// erode(mult) :4211-4845 ("erodedepo"), with call_erosion :2277-2294.
+//
+// Structure on the device:
+//   k_erode_begin    time_step *= 1.5 (:4219), open the retry loop
+//   k_entrain        the entrainment pass (:4236-4548), one thread per cell;
+//                    its last block evaluates the retry test (:4550-4565)
+//   k_alloc_*        grain records requested during the pass get the
+//                    reference's row numbers in the reference's serial order
+//   k_apply_cols     the gather-apply pass with the in-line +/-x lateral
+//                    erosion (:4570-4682): one walker per column, because a
+//                    cell's lateral step changes its x-neighbours before the
+//                    next cell of the same column is processed
+//   k_apply_rows     the +/-y lateral pass (:4684-4747): one walker per row
+//   k_edge_out       sediment leaving the four edges (:4750-4841)
+//   k_erode_post     erode_mult / erode_call of call_erosion
+//
+// Allocation order.  The reference numbers grain records (addGS) in the order
+// its serial loop asks for them: during the entrainment pass a cell asks for
+// itself (before its transport) and for wet neighbours it sends bedload to
+// (directions 1,3,5,7, after its transport).  Each request here is keyed by
+// (loop position of the asking cell) * 5 + (0 self, 1..4 neighbour); a
+// cell's record is numbered by the smallest key that asked for it, which is
+// exactly the request that allocated it in the serial loop.  Record contents
+// do not depend on the number (elevation and bedrock are not changed by the
+// pass before a record is made), so the pass itself runs in parallel.
+
+#include "hc_grain.cuh"
+
+#include <math.h>
+
+namespace {
+
+constexpr double kG = 9.81;
+__constant__ int kDXc[9] = {0, 0, 1, 1, 1, 0, -1, -1, -1};
+__constant__ int kDYc[9] = {0, -1, -1, 0, 1, 1, 1, 0, -1};
+
+// plane of the outgoing-flux arrays: dir 0 su (p=1), 1 sr (p=3), 2 sd (p=5), 3 sl (p=7)
+__device__ __forceinline__ double& SF(const hc_view& c, int dir, int n, size_t cell) {
+  return c.sflux[((size_t)dir * 10 + n) * c.N2 + cell];
+}
+__device__ __forceinline__ size_t EX(const hc_view& c, int x, int y) {
+  return (size_t)x * (c.jmax + 1) + y;
+}
+
+__global__ void k_erode_begin(const hc_view c, hc_dev* d, int gated, double mult_override) {
+  if (gated) {
+    if (!(d->it_active && d->do_erode)) return;
+  } else {
+    d->do_erode = 1;
+    d->it_active = 1;
+    d->rest_active = 1;
+  }
+  d->s.time_step = d->s.time_step * 1.5;
+  d->mult = (mult_override >= 0) ? mult_override : d->s.erode_mult;
+  d->erode_retry = 1;
+  d->erode_passes = 0;
+  d->tempbmax_bits = 0;
+}
+
+// ---------------------------------------------------------------------------
+// entrainment pass
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) k_entrain(const hc_view c, hc_dev* d, int max_passes) {
+  __shared__ double wmax[4];
+  __shared__ bool last;
+  if (!(d->it_active && d->erode_retry)) return;
+  const hc_params& p = c.p;
+  const int jy = 1 + blockIdx.x * blockDim.x + threadIdx.x;  // column y
+  const int ix = 1 + blockIdx.y * blockDim.y + threadIdx.y;  // row x
+  const size_t W = c.W, N2 = c.N2;
+  const double thr = p.water_depth_erosion_threshold;
+  const double mult = d->mult;
+  double tb = 0;
+  if (ix <= c.imax && jy <= c.jmax - 1) {
+    const size_t cell = (size_t)ix * W + jy;
+    if (c.mask[cell]) {
+      c.vel[cell] = 0;
+      c.tau[cell] = 0;
+      for (int n = 0; n < HC_G; n++) {
+        SF(c, 0, n, cell) = 0;
+        SF(c, 1, n, cell) = 0;
+        SF(c, 2, n, cell) = 0;
+        SF(c, 3, n, cell) = 0;
+      }
+      c.ss[cell] = 0;
+      const double h = c.h[cell];
+      if (h > thr) {
+        const double DX = p.DX, rho = 1000.0;
+        const double e0 = c.elev[cell];
+        const unsigned long long pos = (unsigned long long)jy * (c.imax + 2) + ix;
+        double n_man = p.spatially_var_mannings ? c.man[cell] : p.mannings;
+        if (c.index[cell] == -9999) {  // addGS(x, y)
+          grain_record_init(c, cell, e0, c.bed[cell]);
+          c.index[cell] = -2;  // record made, row number pending
+          atomicMin(&c.alloc_key[cell], pos * 5);
+          d->alloc_count = 1;
+        }
+        double temptot2 = 0, veltot = 0, vel = 0, qtot = 0, tau = 0, slopetot = 0;
+        double tempdir[4] = {0, 0, 0, 0};
+        const double edge0 = c.edge[EX(c, ix, jy)];
+        for (int k = 0; k < 4; k++) {
+          const int pp = 1 + 2 * k;
+          const int x2 = ix + kDXc[pp], y2 = jy + kDYc[pp];
+          const size_t nb = (size_t)x2 * W + y2;
+          if (c.h[nb] > thr) {
+            const double edge2 = c.edge[EX(c, x2, y2)];
+            if (edge0 > edge2) temptot2 += (edge0 - edge2);
+            const double vdir = c.vd[(size_t)k * N2 + cell];
+            if (vdir > 0) {
+              vel = vdir;
+              if (vel > p.max_vel) vel = p.max_vel;
+              tempdir[k] = vel * vel;
+              veltot += tempdir[k];
+              qtot += (vel * vel);
+              slopetot += ((e0 - c.elev[nb]) / DX) * vel;
+            }
+          }
+        }
+        if (qtot > 0) {
+          vel = (sqrt(qtot));
+          c.vel[cell] = vel;
+          if (vel > p.max_vel) vel = p.max_vel;
+          double ci = kG * (n_man * n_man) * pow(h, -0.33);
+          if (slopetot > 0) slopetot = 0;
+          tau = 1000 * ci * vel * vel * (1 + (1 * (slopetot / vel)));
+          c.tau[cell] = tau;
+        }
+        if (tau > 0) {
+          double temp_dist[HC_G] = {0};
+          double d_50 = 0, Fs = 0, graintot = 0;
+          const double ts = d->s.time_step;
+          if (p.wilcock) {
+            d_50 = d50_dev(c, cell);
+            if (d_50 < p.d[1]) d_50 = p.d[1];
+            Fs = sand_fraction_dev(c, cell);
+            for (int n = 1; n <= HC_G; n++) graintot += GRN(c, cell, n);
+          }
+          double temptot1 = 0;
+          for (int n = 1; n <= HC_G - 1; n++) {
+            const double Di = p.d[n];
+            double td = 0;
+            if (p.wilcock) {
+              double tau_ri = (0.021 + (0.015 * exp(-20 * Fs))) * (rho * kG * d_50) *
+                              pow((Di / d_50), (0.67 / (1 + exp(1.5 - (Di / d_50)))));
+              // pow(tau / rho, 0.5): the square root, correctly rounded
+              double U_star = sqrt(tau / rho);
+              double Fi = GRN(c, cell, n) / graintot;
+              double Wi_star;
+              if ((tau / tau_ri) < 1.35)
+                Wi_star = 0.002 * pow(tau / tau_ri, 7.5);
+              else
+                Wi_star = 14 * pow(1 - (0.894 / sqrt(tau / tau_ri)), 4.5);
+              td = mult * ts * ((Fi * (U_star * U_star * U_star)) / ((2.65 - 1) * kG)) * Wi_star / DX;
+            }
+            if (p.einstein) {
+              td = mult * ts * (40 * cube_rn((1 / (((2650 - 1000) * Di) / (tau / kG))))) /
+                   sqrt(1000 / ((2250 - 1000) * kG * (Di * Di * Di))) / DX;
+            }
+            if (td > GRN(c, cell, n)) td = GRN(c, cell, n);
+            if (p.isSuspended[n] && n == 1) {
+              if ((td + c.vs[cell]) / h > p.Csuspmax) td = (h * p.Csuspmax) - c.vs[cell];
+            }
+            if (td < 0) td = 0;
+            temp_dist[n] = td;
+            temptot1 += td;
+          }
+          const double bed = c.bed[cell];
+          if (e0 - temptot1 <= bed) {
+            double elevdiff = e0 - bed;
+            double temptot3 = temptot1;
+            temptot1 = 0;
+            for (int n = 1; n <= HC_G - 1; n++) {
+              if (e0 <= bed) {
+                temp_dist[n] = 0;
+              } else {
+                temp_dist[n] = elevdiff * (temp_dist[n] / temptot3);
+                if (temp_dist[n] < 0) temp_dist[n] = 0;
+              }
+              temptot1 += temp_dist[n];
+            }
+            if (tau > p.bedrock_erosion_threshold) {
+              double amount = pow(p.bedrock_erosion_rate * tau, 1.5) * ts * mult * 0.000000317;
+              c.bed[cell] = bed - amount;
+              for (int n2 = 1; n2 <= HC_G - 1; n2++) GRN(c, cell, n2) += amount * p.dprop[n2];
+            }
+          }
+          // vegetation terms (:4459-4488) vanish: vegetation is not supported
+          // (hc_create rejects vegetation_on) and veg stays zero.
+          tb = temptot1;
+          if (temptot1 > 0) {
+            for (int k = 0; k < 4; k++) {
+              const int pp = 1 + 2 * k;
+              const int x2 = ix + kDXc[pp], y2 = jy + kDYc[pp];
+              const size_t nb = (size_t)x2 * W + y2;
+              if (c.h[nb] > thr) {
+                if (c.index[nb] < 1) {  // no final row number yet: ask
+                  atomicMin(&c.alloc_key[nb], pos * 5 + 1 + k);
+                  d->alloc_count = 1;
+                }
+                double factor = 0;
+                if (c.vd[(size_t)k * N2 + cell] > 0) factor += 0.75 * tempdir[k] / veltot;
+                const double edge2 = c.edge[EX(c, x2, y2)];
+                if (edge0 > edge2) factor += 0.25 * ((edge0 - edge2) / temptot2);
+                for (int n = 1; n <= HC_G - 1; n++) {
+                  if (temp_dist[n] > 0) {
+                    if (n == 1 && p.isSuspended[n]) {
+                      c.ss[cell] = temp_dist[n];
+                    } else {
+                      SF(c, k, n, cell) = temp_dist[n] * factor;
+                    }
+                  }
+                }
+              }
+            }
+          }
+        }
+      }
+    }
+  }
+  // tempbmax: max over the pass (warp shuffle, block, grid via last block)
+  for (int o = 16; o > 0; o >>= 1) tb = smax(tb, __shfl_xor_sync(0xffffffffu, tb, o));
+  const int t = threadIdx.y * blockDim.x + threadIdx.x;
+  if ((t & 31) == 0) wmax[t >> 5] = tb;
+  __syncthreads();
+  if (t == 0) {
+    double b = 0;
+    for (int w = 0; w < (int)(blockDim.x * blockDim.y) / 32; w++) b = smax(b, wmax[w]);
+    if (b > 0) atomic_max_pos(&d->tempbmax_bits, b);
+    __threadfence();
+    last = (atomicAdd(&d->pass_done, 1u) == gridDim.x * gridDim.y - 1);
+  }
+  __syncthreads();
+  if (last && t == 0) {
+    __threadfence();
+    const double tempbmax = __longlong_as_double((long long)atomicExch(&d->tempbmax_bits, 0ull));
+    d->pass_done = 0;
+    d->erode_passes++;
+    const double EF = p.ERODEFACTOR;
+    if (tempbmax > EF) {
+      d->s.time_step *= (EF / tempbmax) * 0.5;
+      d->erode_retry = 1;
+      if (max_passes > 0 && d->erode_passes >= max_passes) {
+        d->pause |= HC_PAUSE_ERODE;
+        d->rest_active = 0;
+      }
+    } else {
+      d->erode_retry = 0;
+    }
+    d->s.tempbmax = tempbmax;  // tempbmax of the last pass
+  }
+}
+
+// ---------------------------------------------------------------------------
+// row numbers for the records requested in the pass just run
+// ---------------------------------------------------------------------------
+// Mark: for every requested cell set bit (key % 5) of position key / 5 and
+// make the record if the cell did not make it itself.
+__global__ void k_alloc_mark(const hc_view c, hc_dev* d, uint32_t* bits) {
+  if (!d->alloc_count) return;
+  const size_t cell = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (cell >= c.N2) return;
+  const unsigned long long key = c.alloc_key[cell];
+  if (key == ~0ull) return;
+  c.alloc_key[cell] = ~0ull;
+  if (c.index[cell] == -9999) {
+    grain_record_init(c, cell, c.elev[cell], c.bed[cell]);
+    c.index[cell] = -2;
+  }
+  const unsigned long long P = key / 5;
+  const unsigned sub = (unsigned)(key % 5);
+  atomicOr(&bits[P >> 2], (1u << sub) << ((P & 3) * 8));
+}
+
+// Per-block counts of requested records (1024 threads x 4 positions).
+__global__ void k_alloc_count(const hc_view c, const hc_dev* d, const uint32_t* bits,
+                              int32_t* block_sums, size_t nwords) {
+  __shared__ int ws[32];
+  if (!d->alloc_count) return;
+  const size_t w = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int cnt = (w < nwords) ? __popc(bits[w]) : 0;
+  for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = cnt;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int s = 0;
+    for (int k = 0; k < (int)blockDim.x / 32; k++) s += ws[k];
+    block_sums[blockIdx.x] = s;
+  }
+}
+
+// Exclusive scan of the block counts (one block, loops over chunks).
+__global__ void k_alloc_scan_blocks(const hc_dev* d, int32_t* block_sums, int nblocks,
+                                    int32_t* total_out) {
+  __shared__ int buf[1024];
+  __shared__ int carry;
+  if (!d->alloc_count) return;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (int base = 0; base < nblocks; base += 1024) {
+    int k = base + threadIdx.x;
+    int v = (k < nblocks) ? block_sums[k] : 0;
+    buf[threadIdx.x] = v;
+    __syncthreads();
+    for (int off = 1; off < 1024; off <<= 1) {
+      int t = (threadIdx.x >= (unsigned)off) ? buf[threadIdx.x - off] : 0;
+      __syncthreads();
+      buf[threadIdx.x] += t;
+      __syncthreads();
+    }
+    if (k < nblocks) block_sums[k] = carry + buf[threadIdx.x] - v;
+    __syncthreads();
+    if (threadIdx.x == 1023) carry += buf[1023];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *total_out = carry;
+}
+
+// Assign row numbers in key order and clear the bits.
+__global__ void k_alloc_assign(const hc_view c, hc_dev* d, uint32_t* bits,
+                               const int32_t* block_sums, size_t nwords) {
+  __shared__ int ws[32];
+  __shared__ int wbase[32];
+  if (!d->alloc_count) return;
+  const size_t w = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  uint32_t word = (w < nwords) ? bits[w] : 0u;
+  int cnt = __popc(word);
+  // inclusive warp scan
+  int incl = cnt;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int o = 1; o < 32; o <<= 1) {
+    int t = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += t;
+  }
+  if (lane == 31) ws[warp] = incl;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int s = 0;
+    for (int k = 0; k < (int)blockDim.x / 32; k++) {
+      wbase[k] = s;
+      s += ws[k];
+    }
+  }
+  __syncthreads();
+  if (word) {
+    int r = block_sums[blockIdx.x] + wbase[warp] + incl - cnt;
+    const int base = d->grain_tot + 1;
+    for (int byte = 0; byte < 4; byte++) {
+      const unsigned b = (word >> (byte * 8)) & 0xffu;
+      if (!b) continue;
+      const unsigned long long P = (unsigned long long)w * 4 + byte;
+      const int y = (int)(P / (unsigned long long)(c.imax + 2));
+      const int x = (int)(P % (unsigned long long)(c.imax + 2));
+      for (int sub = 0; sub < 5; sub++) {
+        if (!(b & (1u << sub))) continue;
+        int tx = x, ty = y;
+        if (sub > 0) {
+          const int pp = 2 * sub - 1;
+          tx += kDXc[pp];
+          ty += kDYc[pp];
+        }
+        c.index[(size_t)tx * c.W + ty] = base + r;
+        r++;
+      }
+    }
+    bits[w] = 0u;
+  }
+}
+
+__global__ void k_alloc_finish(hc_dev* d, const int32_t* total) {
+  if (!d->alloc_count) return;
+  d->grain_tot += *total;
+  d->s.grain_array_tot = d->grain_tot;
+  d->alloc_count = 0;
+}
+
+// ---------------------------------------------------------------------------
+// apply pass :4570-4682, one walker per column y in [2, jmax-1]
+// ---------------------------------------------------------------------------
+// One lateral step of the apply passes (:4630-4677, :4690-4744).  Returns
+// false when the raw amount is not positive; otherwise the (possibly zeroed
+// or capped) amount, which the caller applies and hands to slide_GS even when
+// it is zero, as the reference does.
+__device__ __forceinline__ bool lateral_amount(const hc_view& c, double mult, double ts,
+                                               double tau0, double et3, size_t nb, size_t ecell,
+                                               double e_nb, double e0, bool boundary,
+                                               double& amt) {
+  const hc_params& p = c.p;
+  const double DX = p.DX;
+  amt = 0;
+  if (c.h[nb] < p.water_depth_erosion_threshold)
+    amt = mult * p.lateral_constant * tau0 * c.edge[ecell] * ts / DX;
+  else
+    amt = p.chann_lateral_erosion * et3 * (e_nb - e0) / DX * 0.1;
+  if (!(amt > 0)) return false;
+  // amt *= 1 - veg * (1 - veg_lat_restriction): veg is zero (no vegetation)
+  if ((e_nb - amt) < c.bed[nb] || boundary) amt = 0;
+  if (amt > p.ERODEFACTOR * 0.1) amt = p.ERODEFACTOR * 0.1;
+  return true;
+}
+
+__global__ void __launch_bounds__(128) k_apply_cols(const hc_view c, hc_dev* d) {
+  if (!(d->it_active && d->rest_active && d->do_erode) || d->erode_retry) return;
+  const int y = 2 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (y > c.jmax - 1) return;
+  const hc_params& p = c.p;
+  const size_t W = c.W;
+  const double thr = p.water_depth_erosion_threshold;
+  const double mult = d->mult;
+  const double ts = d->s.time_step;
+  for (int x = 1; x <= c.imax; x++) {
+    const size_t cell = (size_t)x * W + y;
+    if (!c.mask[cell]) continue;
+    double et3 = 0;
+    if (c.h[cell] > thr && x < c.imax && x > 1) {
+      const double h = c.h[cell];
+      double erodetot = 0;
+      for (int n = 1; n <= HC_G - 1; n++) {
+        if (n == 1 && p.isSuspended[n]) {
+          const double ssv = c.ss[cell];
+          double vs = c.vs[cell] + ssv;
+          GRN(c, cell, n) -= ssv;
+          erodetot -= ssv;
+          // inputpointsarray is all false in the reference (zero_values
+          // clears it after the reach block), so settling applies everywhere
+          double coeff = (p.fallVelocity[n] * ts) / h;
+          if (coeff > 1) coeff = 1;
+          double Vpdrop = coeff * vs;
+          if (Vpdrop > 0.001) Vpdrop = 0.001;
+          GRN(c, cell, n) += Vpdrop;
+          erodetot += Vpdrop;
+          vs -= Vpdrop;
+          c.vs[cell] = vs;
+        } else {
+          double val1 = (SF(c, 0, n, cell) + SF(c, 1, n, cell) + SF(c, 2, n, cell) +
+                         SF(c, 3, n, cell));
+          double val2 = (SF(c, 0, n, cell + 1) + SF(c, 2, n, cell - 1) + SF(c, 3, n, cell + W) +
+                         SF(c, 1, n, cell - W));
+          GRN(c, cell, n) += val2 - val1;
+          erodetot += val2 - val1;
+          et3 += val1;
+        }
+      }
+      double e0 = c.elev[cell] + erodetot;
+      c.elev[cell] = e0;
+      if (erodetot < 0) sort_active_dev(c, d, cell, false);
+      if (et3 > 0) {
+        double elev_update = 0;
+        const double tau0 = c.tau[cell];
+        {
+          const size_t nb = cell - W;
+          const double en = c.elev[nb];
+          double amt;
+          if (en > e0 && x > 2 &&
+              lateral_amount(c, mult, ts, tau0, et3, nb, EX(c, x - 1, y), en, e0, x - 1 == 1, amt)) {
+            elev_update += amt;
+            c.elev[nb] = en - amt;
+            slide_GS_dev(c, d, nb, amt, cell, false);
+          }
+        }
+        {
+          const size_t nb = cell + W;
+          const double en = c.elev[nb];
+          double amt;
+          if (en > e0 && x < c.imax - 1 &&
+              lateral_amount(c, mult, ts, tau0, et3, nb, EX(c, x + 1, y), en, e0, x + 1 == c.imax,
+                             amt)) {
+            elev_update += amt;
+            c.elev[nb] = en - amt;
+            slide_GS_dev(c, d, nb, amt, cell, false);
+          }
+        }
+        c.elev[cell] = c.elev[cell] + elev_update;
+      }
+    }
+    c.erodetot3[cell] = et3;
+  }
+}
+
+// +/-y lateral pass :4684-4747, one walker per row x in [2, imax-1]
+__global__ void __launch_bounds__(128) k_apply_rows(const hc_view c, hc_dev* d) {
+  if (!(d->it_active && d->rest_active && d->do_erode) || d->erode_retry) return;
+  const int x = 2 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (x > c.imax - 1) return;
+  const size_t W = c.W;
+  const double mult = d->mult;
+  const double ts = d->s.time_step;
+  for (int y = 2; y <= c.jmax - 1; y++) {
+    const size_t cell = (size_t)x * W + y;
+    if (!c.mask[cell]) continue;
+    const double et3 = c.erodetot3[cell];
+    if (!(et3 > 0)) continue;
+    double elev_update = 0;
+    const double tau0 = c.tau[cell];
+    {
+      const size_t nb = cell - 1;
+      const double en = c.elev[nb], e0 = c.elev[cell];
+      double amt;
+      if (en > e0 &&
+          lateral_amount(c, mult, ts, tau0, et3, nb, EX(c, x, y - 1), en, e0, y - 1 == 1, amt)) {
+        elev_update += amt;
+        c.elev[nb] = en - amt;
+        slide_GS_dev(c, d, nb, amt, cell, false);
+      }
+    }
+    {
+      const size_t nb = cell + 1;
+      const double en = c.elev[nb], e0 = c.elev[cell];
+      double amt;
+      if (en > e0 &&
+          lateral_amount(c, mult, ts, tau0, et3, nb, EX(c, x, y + 1), en, e0, y + 1 == c.jmax, amt)) {
+        elev_update += amt;
+        c.elev[nb] = en - amt;
+        slide_GS_dev(c, d, nb, amt, cell, false);
+      }
+    }
+    c.elev[cell] = c.elev[cell] + elev_update;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// sediment leaving the edges :4750-4841.  The reference accumulates gtot2 in
+// float, entry by entry in its loop order: the contributions are laid out in
+// that order and each fraction's float sum is run in order by its own thread.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(1024) k_edge_out(const hc_view c, hc_dev* d, double* contrib,
+                                                    int32_t* list) {
+  __shared__ int cnt_s[1024];
+  __shared__ float gsum[HC_G + 1];
+  if (!(d->it_active && d->rest_active && d->do_erode) || d->erode_retry) return;
+  const hc_params& p = c.p;
+  const int imax = c.imax, jmax = c.jmax;
+  const double thr = p.water_depth_erosion_threshold;
+  const int nA = (jmax - 2 > 0) ? 2 * (jmax - 2) : 0;   // y = 2..jmax-1: (imax,y), (1,y)
+  const int nB = (imax - 2 > 0) ? 2 * (imax - 2) : 0;   // x = 2..imax-1: (x,jmax), (x,1)
+  const int ntot = nA + nB;
+  // entries handled by this thread: a contiguous chunk, so the block scan
+  // below keeps the loop order
+  const int per = (ntot + blockDim.x - 1) / blockDim.x;
+  const int k0 = threadIdx.x * per, k1 = min(ntot, k0 + per);
+  int mine = 0;
+  for (int k = k0; k < k1; k++) {
+    int x, y, srcx, srcy, dir;
+    if (k < nA) {
+      y = 2 + k / 2;
+      if ((k & 1) == 0) { x = imax; srcx = imax - 1; srcy = y; dir = 1; }  // sr[imax-1][y]
+      else { x = 1; srcx = 2; srcy = y; dir = 3; }                          // sl[2][y]
+    } else {
+      const int kk = k - nA;
+      x = 2 + kk / 2;
+      if ((kk & 1) == 0) { y = jmax; srcx = x; srcy = jmax - 1; dir = 2; }  // sd[x][jmax-1]
+      else { y = 1; srcx = x; srcy = 2; dir = 0; }                          // su[x][2]
+    }
+    const size_t cell = (size_t)x * c.W + y;
+    if (c.h[cell] > thr || c.vs[cell] > 0) mine++;
+  }
+  cnt_s[threadIdx.x] = mine;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int s = 0;
+    for (int t = 0; t < (int)blockDim.x; t++) {
+      int v = cnt_s[t];
+      cnt_s[t] = s;
+      s += v;
+    }
+    d->misc_done = s;
+  }
+  __syncthreads();
+  int o = cnt_s[threadIdx.x];
+  for (int k = k0; k < k1; k++) {
+    int x, y, srcx, srcy, dir;
+    if (k < nA) {
+      y = 2 + k / 2;
+      if ((k & 1) == 0) { x = imax; srcx = imax - 1; srcy = y; dir = 1; }
+      else { x = 1; srcx = 2; srcy = y; dir = 3; }
+    } else {
+      const int kk = k - nA;
+      x = 2 + kk / 2;
+      if ((kk & 1) == 0) { y = jmax; srcx = x; srcy = jmax - 1; dir = 2; }
+      else { y = 1; srcx = x; srcy = 2; dir = 0; }
+    }
+    const size_t cell = (size_t)x * c.W + y;
+    if (!(c.h[cell] > thr || c.vs[cell] > 0)) continue;
+    const size_t src = (size_t)srcx * c.W + srcy;
+    bool first_susp = true;  // Vsusptot is zeroed after the first suspended fraction
+    for (int n = 1; n <= HC_G - 1; n++) {
+      double v;
+      if (p.isSuspended[n]) {
+        v = first_susp ? c.vs[cell] : 0.0;
+        first_susp = false;
+      } else {
+        v = SF(c, dir, n, src);
+      }
+      contrib[(size_t)o * HC_G + n] = v;
+    }
+    o++;
+  }
+  __syncthreads();
+  // the suspended load leaves with the water (Vsusptot = 0 at these cells);
+  // done after all reads above
+  for (int k = k0; k < k1; k++) {
+    int x, y;
+    if (k < nA) {
+      y = 2 + k / 2;
+      x = ((k & 1) == 0) ? imax : 1;
+    } else {
+      const int kk = k - nA;
+      x = 2 + kk / 2;
+      y = ((kk & 1) == 0) ? jmax : 1;
+    }
+    const size_t cell = (size_t)x * c.W + y;
+    if (c.h[cell] > thr || c.vs[cell] > 0) {
+      bool anysusp = false;
+      for (int n = 1; n <= HC_G - 1; n++) anysusp |= (p.isSuspended[n] != 0);
+      if (anysusp) c.vs[cell] = 0;
+    }
+  }
+  __syncthreads();
+  const int total = d->misc_done;
+  if (threadIdx.x >= 1 && threadIdx.x <= HC_G - 1) {
+    const int n = threadIdx.x;
+    float g = 0.0f;
+    for (int e = 0; e < total; e++) g = (float)((double)g + contrib[(size_t)e * HC_G + n]);
+    gsum[n] = g;
+  }
+  if (threadIdx.x == 0) gsum[0] = 0.0f, gsum[HC_G] = 0.0f;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    hc_scalars& s = d->s;
+    const double DX = p.DX;
+    s.sediQ = 0;
+    for (int n = 1; n <= HC_G; n++) {
+      s.sediQ += gsum[n] * DX * DX;
+      s.globalsediq += gsum[n] * DX * DX;
+      s.sum_grain[n] += gsum[n] * DX * DX;
+    }
+  }
+}
+
+// call_erosion :2277-2294 after erode() returned
+__global__ void k_erode_post(const hc_view c, hc_dev* d, int gated) {
+  if (gated && !(d->it_active && d->rest_active && d->do_erode)) return;
+  if (d->erode_retry) return;
+  hc_scalars& s = d->s;
+  if (gated) {
+    s.erode_mult = x86_trunc_to_int(c.p.ERODEFACTOR / s.tempbmax);
+    if (s.erode_mult < 1) s.erode_mult = 1;
+    if (s.erode_mult > 5) s.erode_mult = 5;
+    s.erode_call = s.counter + s.erode_mult;
+  }
+}
+
+// call_lateral :2298-2305 (main.cpp:178, when enabled) is tested every
+// iteration after call_erosion; lateral3 itself runs on the host-driven path
+// before water_flux_out, so the rest of the iteration waits for it.
+__global__ void k_lateral_check(const hc_view c, hc_dev* d) {
+  if (!(d->it_active && d->rest_active)) return;
+  if (c.p.hydro_only || !(d->flags & HC_RUN_LATERAL)) return;
+  if (d->s.counter >= d->s.lateralcounter) {
+    d->do_lateral = 1;
+    d->rest_active = 0;
+    d->pause |= HC_PAUSE_LATERAL;
+  }
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ launches
+struct ErodeScratch {
+  uint32_t* bits;      // N2/4+1 words
+  int32_t* block_sums;
+  int32_t* total;
+  double* contrib;     // edge contributions
+};
+
+static ErodeScratch scratch_of(hc_ctx* c) {
+  ErodeScratch s;
+  char* base = (char*)c->v.red;
+  s.total = (int32_t*)(base + 64);
+  s.block_sums = (int32_t*)(base + 128);
+  size_t nwords = c->v.N2 / 4 + 1;
+  size_t nblocks = (nwords + 1023) / 1024;
+  s.bits = (uint32_t*)(base + 128 + ((nblocks * 4 + 255) / 256) * 256);
+  s.contrib = (double*)((char*)s.bits + ((nwords * 4 + 255) / 256) * 256);
+  return s;
+}
+
+size_t erode_scratch_bytes(size_t N2, int imax, int jmax) {
+  size_t nwords = N2 / 4 + 1;
+  size_t nblocks = (nwords + 1023) / 1024;
+  size_t ncontrib = (size_t)(2 * (imax + jmax) + 8) * HC_G;
+  return 128 + ((nblocks * 4 + 255) / 256) * 256 + ((nwords * 4 + 255) / 256) * 256 +
+         ncontrib * 8 + 256;
+}
+
+void launch_erode_begin(hc_ctx* c, int gated, double mult) {
+  k_erode_begin<<<1, 1, 0, c->s>>>(c->v, c->dev, gated, mult);
+  count_launch(c, 1);
+}
+
+void launch_erode_pass(hc_ctx* c, int max_passes) {
+  ErodeScratch s = scratch_of(c);
+  dim3 b(32, 4);
+  dim3 g((c->v.jmax - 1 + b.x - 1) / b.x, (c->v.imax + b.y - 1) / b.y);
+  if (g.x < 1) g.x = 1;
+  k_entrain<<<g, b, 0, c->s>>>(c->v, c->dev, max_passes);
+  count_launch(c, 1);
+  size_t nwords = c->v.N2 / 4 + 1;
+  int nb = (int)((c->v.N2 + 255) / 256);
+  k_alloc_mark<<<nb, 256, 0, c->s>>>(c->v, c->dev, s.bits);
+  count_launch(c, 1);
+  int nblocks = (int)((nwords + 1023) / 1024);
+  k_alloc_count<<<nblocks, 1024, 0, c->s>>>(c->v, c->dev, s.bits, s.block_sums, nwords);
+  count_launch(c, 1);
+  k_alloc_scan_blocks<<<1, 1024, 0, c->s>>>(c->dev, s.block_sums, nblocks, s.total);
+  count_launch(c, 1);
+  k_alloc_assign<<<nblocks, 1024, 0, c->s>>>(c->v, c->dev, s.bits, s.block_sums, nwords);
+  count_launch(c, 1);
+  k_alloc_finish<<<1, 1, 0, c->s>>>(c->dev, s.total);
+  count_launch(c, 1);
+}
+
+void launch_erode_finish(hc_ctx* c, int gated) {
+  ErodeScratch s = scratch_of(c);
+  int nc = (c->v.jmax - 2 + 127) / 128;
+  if (nc < 1) nc = 1;
+  k_apply_cols<<<nc, 128, 0, c->s>>>(c->v, c->dev);
+  count_launch(c, 1);
+  int nr = (c->v.imax - 2 + 127) / 128;
+  if (nr < 1) nr = 1;
+  k_apply_rows<<<nr, 128, 0, c->s>>>(c->v, c->dev);
+  count_launch(c, 1);
+  k_edge_out<<<1, 1024, 0, c->s>>>(c->v, c->dev, s.contrib, nullptr);
+  count_launch(c, 1);
+  k_erode_post<<<1, 1, 0, c->s>>>(c->v, c->dev, gated);
+  count_launch(c, 1);
+}
+
+void launch_lateral_check(hc_ctx* c) {
+  k_lateral_check<<<1, 1, 0, c->s>>>(c->v, c->dev);
+  count_launch(c, 1);
+}

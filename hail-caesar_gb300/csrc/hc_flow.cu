@@ -1,0 +1,571 @@
+// Hydraulic part of one iteration: the driver's scalar logic (timestep,
+// counters, water inputs, TOPMODEL), flow_route, depth_update, scan_area and
+// water_flux_out.
+//
+// Reference: src/catchmentmodel/LSDCatchmentModel.cpp (line numbers below)
+// and src/main.cpp:139-204.  Every expression that produces model state keeps
+// the reference's operand order and roundings (the library is compiled with
+// --fmad=false, so nothing is contracted into an FMA unless written so): the
+// hydraulic state is bit-identical to the reference's serial build.
+
+#include "hc_internal.cuh"
+
+#include <math.h>
+#include <algorithm>
+
+namespace {
+
+constexpr double kG = 9.81;  // gravity, LSDCatchmentModel.hpp:438
+
+__device__ __forceinline__ double cfl_dt(const hc_params& p, double maxdepth) {
+  // courant_friedrichs_lewy_condition :1884-1887
+  return p.courant_number * (p.DX / sqrt(kG * (maxdepth)));
+}
+
+__device__ __forceinline__ double flow_dt_of(const hc_params& p, const hc_scalars& s) {
+  // get_flow_timestep :1913-1923
+  double f = s.time_step;
+  double c = cfl_dt(p, s.maxdepth);
+  if (f > c) f = c;
+  return f;
+}
+
+// ---------------------------------------------------------------------------
+// control: set_loop_cycle .. catchment_waterinputs (main.cpp:142-158), one
+// thread.  Also decides which members run in this iteration.
+// ---------------------------------------------------------------------------
+__device__ void topmodel_step(hc_dev* d, const hc_params& p, const double* topm, int rows) {
+  // topmodel_runoff(time_1) :3649-3715: the recurrence depends only on the
+  // rain table, so the host evaluates it once (host_topmodel_table) and the
+  // device steps through the rows.
+  int t = (int)d->s.time_1;
+  const int rf = p.rfnum;
+  if (t < 0 || t >= rows) {
+    d->err_code = 101;
+    d->pause |= HC_PAUSE_ERROR;
+    return;
+  }
+  const double* row = topm + (size_t)t * 2 * (rf + 1);
+  for (int n = 1; n <= rf; n++) {
+    d->s.old_j_mean[n] = row[n];
+    d->s.new_j_mean[n] = row[(rf + 1) + n];
+  }
+}
+
+__global__ void k_control(const hc_view c, hc_dev* d) {
+  const hc_params& p = c.p;
+  hc_scalars& s = d->s;
+  if (d->pause || d->budget <= 0) {
+    // skipped iteration: every gated kernel of it returns at once; the
+    // switches of the iteration that paused stay as they are, for the host
+    // to finish that iteration
+    if (d->budget <= 0) d->pause |= HC_PAUSE_BUDGET;
+    d->it_active = 0;
+    return;
+  }
+  d->do_scan = d->do_erode = d->do_slide = d->do_lateral = 0;
+  d->erode_retry = 0;
+  d->erode_passes = 0;
+  d->budget--;
+  d->it_active = 1;
+  d->rest_active = 1;
+
+  s.previous = s.cycle;                                   // set_loop_cycle :1873
+  s.input_output_difference = fabs(s.waterinput - s.waterOut);  // :1879
+  if (s.maxdepth <= 0.1) s.maxdepth = 0.1;                // set_maximum_timestep :1890
+  if (s.time_step < cfl_dt(p, s.maxdepth)) s.time_step = cfl_dt(p, s.maxdepth);
+  if (s.input_output_difference > p.in_out_difference_allowed &&
+      s.time_step > (cfl_dt(p, s.maxdepth)))
+    s.time_step = cfl_dt(p, s.maxdepth);
+  s.counter += 1;                                         // increment_counters :1925
+  s.cycle += s.time_step / 60;
+
+  const double DX = p.DX;
+  // reach_water_and_sediment_input :3301-3452
+  if (p.reach_mode) {
+    const double fdt = flow_dt_of(p, s);
+    const int rdt = p.reach_input_data_timestep;
+    const int div = p.div_inputs;
+    const int row = (int)(s.cycle / rdt);
+    if (!p.hydro_only) {
+      for (int n = 0; n <= p.number_of_points - 1; n++) {
+        const int x = p.inpoints[n][0], y = p.inpoints[n][1];
+        const size_t cell = (size_t)x * c.W + y;
+        double adding_factor = 1, added_tot = 0;
+        if (c.h[cell] > p.water_depth_erosion_threshold) {
+          const float* r = c.reach[n] + (size_t)row * c.reach_cols[n];
+          for (int tn = 5; tn <= HC_G + 3; tn++) {
+            float q = fabsf(r[tn]) / div;  // float / int in the reference
+            added_tot += q / (DX * DX) / (rdt * 60) * s.time_step;
+          }
+          if (added_tot / p.number_of_points > p.ERODEFACTOR * 0.75)
+            adding_factor = (p.ERODEFACTOR * 0.75) / (added_tot / p.number_of_points);
+          if (c.index[cell] == -9999) {  // addGS :3949, serial position: now
+            d->grain_tot++;
+            c.index[cell] = d->grain_tot;
+            grain_record_init(c, cell, c.elev[cell], c.bed[cell]);
+          }
+          for (int tn = 5; tn <= HC_G + 3; tn++) {
+            double amt = adding_factor * (double)fabsf(r[tn]) / div / (DX * DX) / (rdt * 60) *
+                         s.time_step;
+            if (p.isSuspended[tn - 4]) {
+              c.vs[cell] += amt;
+            } else {
+              c.grain[(size_t)(tn - 4) * c.N2 + cell] += amt;
+              c.elev[cell] += amt;
+            }
+          }
+        }
+      }
+    }
+    for (int n = 0; n <= p.number_of_points - 1; n++) {
+      const int x = p.inpoints[n][0], y = p.inpoints[n][1];
+      const size_t cell = (size_t)x * c.W + y;
+      if (row + 1 >= c.reach_rows[n]) {
+        d->err_code = 102;
+        d->pause |= HC_PAUSE_ERROR;
+        continue;
+      }
+      double i1 = c.reach[n][(size_t)row * c.reach_cols[n] + 1];
+      double i2 = c.reach[n][(size_t)(row + 1) * c.reach_cols[n] + 1];
+      double prop = (((row + 1) * rdt) - s.cycle) / rdt;
+      double input = i1 + ((i2 - i1) * (1 - prop));
+      s.waterinput += (input / div);
+      c.h[cell] += (input / div) / (DX * DX) * fdt;
+    }
+  }
+
+  // catchment_waterinputs :2027 -> catchment_water_input_and_hydrology :3455
+  s.waterinput = 0;
+  const double fdt2 = flow_dt_of(p, s);
+  for (int i = 1; i <= p.rfnum; i++) s.waterinput += s.j_mean[i] * s.nActualGridCells[i] * DX * DX;
+  for (int i = 0; i <= p.rfnum; i++) d->j_mean_in[i] = s.j_mean[i];
+  d->input_dt = fdt2;
+  if (s.cycle >= s.time_1) {
+    do {
+      s.time_1++;
+      topmodel_step(d, p, c.topm, c.topm_rows);
+      if (s.time_step > p.max_time_step) {
+        double jmm = 0;
+        for (int n = 1; n <= p.rfnum; n++)
+          if (s.new_j_mean[n] > jmm) jmm = s.new_j_mean[n];
+        if (jmm > (0.2 / ((unsigned)p.imax * (unsigned)p.jmax * DX * DX))) {
+          s.cycle = s.time_1 + (p.max_time_step / 60);
+          s.time_step = p.max_time_step;
+        }
+      }
+    } while (s.time_1 < s.cycle && !(d->pause & HC_PAUSE_ERROR));
+  }
+  for (int n = 1; n <= p.rfnum; n++)  // calchydrograph :3718
+    s.j_mean[n] = s.old_j_mean[n] + (((s.new_j_mean[n] - s.old_j_mean[n]) / 2) * (2 - (s.time_1 - s.cycle)));
+  double jmeanmax = 0;
+  for (int n = 1; n <= p.rfnum; n++)
+    if (s.j_mean[n] > jmeanmax) jmeanmax = s.j_mean[n];
+  bool recalc = false;
+  if (jmeanmax >= s.baseflow) {
+    s.baseflow = s.baseflow * 3;
+    recalc = true;
+  }
+  if (s.baseflow > (jmeanmax * 3) && s.baseflow > 0.000001) {
+    s.baseflow = jmeanmax * 1.25;
+    recalc = true;
+  }
+  // The drainage area (a sort of all elevations) and the input-point list are
+  // recomputed on the host before the next iteration; within this iteration
+  // the reference applies the new list only from the next one as well.
+  if (recalc) d->pause |= HC_PAUSE_DRAINAGE;
+
+  s.flow_timestep = flow_dt_of(p, s);
+  d->do_scan = ((long long)s.counter % p.scan_area_interval_iter) == 0;
+  d->do_erode = !p.hydro_only && s.counter >= s.erode_call;
+  d->erode_retry = d->do_erode;
+  d->do_slide = !p.hydro_only && ((long long)s.counter % p.in_channel_landslide_iter_interval) == 0;
+}
+
+// catchment input points (:3463-3477): one thread per point
+__global__ void k_inputs(const hc_view c, hc_dev* d) {
+  if (!d->it_active) return;
+  const hc_scalars& s = d->s;
+  const int total = (int)s.totalinputpoints;
+  for (int z = 1 + blockIdx.x * blockDim.x + threadIdx.x; z <= total;
+       z += gridDim.x * blockDim.x) {
+    const int i = c.cin_x[z], j = c.cin_y[z];
+    const size_t cell = (size_t)i * c.W + j;
+    const int rf = c.rfarea[cell];
+    double amt = (d->j_mean_in[rf] * s.nActualGridCells[rf]) / (s.catchment_input_counter[rf]) *
+                 d->input_dt;
+    if (amt > c.p.ERODEFACTOR) amt = c.p.ERODEFACTOR;
+    c.h[cell] += amt;
+  }
+}
+
+__global__ void k_flow_dt(const hc_view c, hc_dev* d) {
+  d->s.flow_timestep = flow_dt_of(c.p, d->s);
+  d->it_active = 1;
+  d->rest_active = 1;
+}
+
+// ---------------------------------------------------------------------------
+// flow_route :3063-3247.  One thread per cell; cells outside the wet mask keep
+// their discharges (the reference does not visit them).
+// ---------------------------------------------------------------------------
+struct FaceOut {
+  double q, qs, vel;
+  int dir;  // 1: positive, -1: negative, 0: none
+};
+
+// Three-way test of a > b where both are only known to a relative 2^-18:
+// +1 surely greater, -1 surely not, 0 too close to call (the caller then
+// evaluates the reference's FP64 expression).
+__device__ __forceinline__ int decide_gt(float a, float b) {
+  if (a > b * 1.0001f) return 1;
+  if (a < b * 0.9999f) return -1;
+  return 0;
+}
+
+// One face of the inertial scheme (:3096-3191 / :3193-3242).  e0,h0: this
+// cell; e1,h1: the upstream neighbour (x-1 for qx, y-1 for qy); a0, a1 the
+// water surfaces e+h.  `edge_slope` is 0 for interior faces, +1 / -1 where
+// the reference replaces the slope by +/-edgeslope.
+//
+// The FP64 pipe (1.2 TFLOP/s on GB300) bounds this kernel, so the limiter
+// tests, which only pick a branch, are first decided on float estimates; the
+// reference's FP64 expression is evaluated only when the estimate is within
+// 1e-4 of the threshold.  The branch taken - and so the result - is always
+// the reference's.
+template <bool kSusp, bool kVel>
+__device__ __forceinline__ void inertial_face(double& q, double& qs, double& vel_out, int& vdir,
+                                              double e0, double h0, double a0, double e1,
+                                              double h1, double a1, double v0, double v1,
+                                              double nn, double dt, int edge_slope,
+                                              const hc_params& p, double rDX) {
+  const double DX = p.DX;
+  vdir = 0;
+  double hflow = smax(a0, a1) - smax(e1, e0);
+  if (!(hflow > p.hflow_threshold)) {
+    q = 0;
+    qs = 0;
+    return;
+  }
+  double slope = div_const(a1 - a0, DX, rDX);
+  if (edge_slope == 1) slope = p.edgeslope;
+  if (edge_slope == -1) slope = 0 - p.edgeslope;
+  const double ghd = kG * hflow * dt;
+  double qn;
+  if (q == 0) {
+    // (0 - ghd*slope) / (1 + (ghd*nn*0)/h^3) = (0 - ghd*slope) / 1
+    qn = q - (ghd * slope);
+  } else {
+    qn = ((q - (ghd * slope)) / (1 + ghd * nn * fabs(q) / cube_rn(hflow)));
+  }
+  const double fl = p.froude_limit;
+  const float hf = approx_abs_f(hflow);
+  // Froude limit: |q/hflow| / sqrt(g*hflow) > froude_limit
+  if (qn != 0) {
+    const float fr = approx_abs_f(qn) / (hf * sqrtf(9.81f * hf));
+    int t = decide_gt(fr, (float)fl);
+    if (t == 0) t = (fabs(qn / hflow) / sqrt(kG * hflow) > fl) ? 1 : -1;
+    if (t > 0) {
+      const double lim = hflow * (sqrt(kG * hflow) * fl);
+      qn = (qn > 0) ? lim : 0 - lim;
+    }
+  }
+  // depth limit: |q*dt/DX| > (depth of the giving cell)/4
+  if (qn > 0) {
+    int t = decide_gt(approx_abs_f(qn) * approx_abs_f(dt) / (float)DX, approx_abs_f(h0) * 0.25f);
+    if (t == 0) t = ((qn * dt / DX) > (h0 / 4)) ? 1 : -1;
+    if (t > 0) qn = ((h0 * DX) / 5) / dt;
+  } else if (qn < 0) {
+    int t = decide_gt(approx_abs_f(qn) * approx_abs_f(dt) / (float)DX, approx_abs_f(h1) * 0.25f);
+    if (t == 0) t = (fabs(qn * dt / DX) > (h1 / 4)) ? 1 : -1;
+    if (t > 0) qn = 0 - ((h1 * DX) / 5) / dt;
+  }
+  if (kSusp) {
+    if (qn > 0) qs = qn * (v0 / h0);
+    if (qn < 0) qs = qn * (v1 / h1);
+    if (qs > 0 && qs * dt > (v0 * DX) / 4) qs = ((v0 * DX) / 5) / dt;
+    if (qs < 0 && fabs(qs * dt) > (v1 * DX) / 4) qs = 0 - ((v1 * DX) / 5) / dt;
+  }
+  if (kVel) {
+    if (qn > 0) {
+      vel_out = qn / hflow;
+      vdir = 1;
+    }
+    if (qn < 0) {
+      vel_out = (0 - qn) / hflow;
+      vdir = -1;
+    }
+  }
+  q = qn;
+}
+
+// kSed: erosion is on.  Then the suspended-load discharges qxs/qys and the
+// face velocities vel_dir (read only by erode) are computed as the
+// reference does.  In hydro-only runs Vsusptot stays zero, so the
+// reference's qxs/qys are signed zeros and vel_dir is never read: both are
+// left untouched.
+template <bool kSed>
+__global__ void __launch_bounds__(256) k_flow_route(const hc_view c, const hc_dev* __restrict__ d,
+                                                     int gated) {
+  if (gated && !d->it_active) return;
+  const int j = 1 + blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = 1 + blockIdx.y * blockDim.y + threadIdx.y;
+  if (i > c.imax || j > c.jmax) return;
+  const size_t W = c.W, N2 = c.N2;
+  const size_t cell = (size_t)i * W + j;
+  if (!c.mask[cell]) return;
+  const double e0 = c.elev[cell];
+  if (!(e0 > -9999)) return;
+  const hc_params& p = c.p;
+  const double dt = d->s.flow_timestep;
+  const double n = p.spatially_var_mannings ? c.man[cell] : p.mannings;
+  const double nn = n * n;
+  const double rDX = c.rDX;
+  const bool susp = kSed && p.isSuspended[1] != 0;
+  const double h0 = c.h[cell];
+  const double a0 = e0 + h0;
+  const double v0 = susp ? c.vs[cell] : 0.0;
+  // x face (rows i-1, i)
+  {
+    const size_t up = cell - W;
+    const double h1 = c.h[up], e1 = c.elev[up];
+    if ((h0 > 0 || h1 > 0) && e1 > -9999) {
+      double q = c.qx[cell], qs = kSed ? c.qxs[cell] : 0.0, vel = 0;
+      int vdir;
+      const int es = (i == c.imax) ? 1 : ((i <= 2) ? -1 : 0);
+      if (susp)
+        inertial_face<true, kSed>(q, qs, vel, vdir, e0, h0, a0, e1, h1, e1 + h1, v0, c.vs[up],
+                                  nn, dt, es, p, rDX);
+      else
+        inertial_face<false, kSed>(q, qs, vel, vdir, e0, h0, a0, e1, h1, e1 + h1, v0, 0.0, nn,
+                                   dt, es, p, rDX);
+      c.qx[cell] = q;
+      if (kSed) {
+        c.qxs[cell] = qs;
+        if (vdir == 1) c.vd[3 * N2 + cell] = vel;  // vel_dir[x][y][7]
+        if (vdir == -1) c.vd[1 * N2 + up] = vel;   // vel_dir[x-1][y][3]
+      }
+    }
+  }
+  // y face (columns j-1, j).  The reference takes max(e0, e1) with the
+  // operands the other way round (:3197-3198); for ordered values max is
+  // symmetric, so one face routine serves both.
+  {
+    const size_t lf = cell - 1;
+    const double h1 = c.h[lf], e1 = c.elev[lf];
+    if ((h0 > 0 || h1 > 0) && e1 > -9999) {
+      double q = c.qy[cell], qs = kSed ? c.qys[cell] : 0.0, vel = 0;
+      int vdir;
+      const int es = (j == c.jmax) ? 1 : ((j <= 2) ? -1 : 0);
+      if (susp)
+        inertial_face<true, kSed>(q, qs, vel, vdir, e0, h0, a0, e1, h1, e1 + h1, v0, c.vs[lf],
+                                  nn, dt, es, p, rDX);
+      else
+        inertial_face<false, kSed>(q, qs, vel, vdir, e0, h0, a0, e1, h1, e1 + h1, v0, 0.0, nn,
+                                   dt, es, p, rDX);
+      c.qy[cell] = q;
+      if (kSed) {
+        c.qys[cell] = qs;
+        if (vdir == 1) c.vd[0 * N2 + cell] = vel;  // vel_dir[x][y][1]
+        if (vdir == -1) c.vd[2 * N2 + lf] = vel;   // vel_dir[x][y-1][5]
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// depth_update :3259-3299 with the maxdepth reduction (warp shuffle, block,
+// then the last block publishes the grid result).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_depth_update(const hc_view c, hc_dev* d, int gated) {
+  __shared__ double warp_max[8];
+  __shared__ bool last;
+  if (gated && !d->it_active) return;
+  const int j = 1 + blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = 1 + blockIdx.y * blockDim.y + threadIdx.y;
+  double m = 0;
+  if (i <= c.imax && j <= c.jmax) {
+    const size_t W = c.W;
+    const size_t cell = (size_t)i * W + j;
+    if (c.mask[cell]) {
+      const double dt = d->s.flow_timestep, DX = c.p.DX, rDX = c.rDX;
+      double h = c.h[cell];
+      h += div_const(dt * (c.qx[cell + W] - c.qx[cell] + c.qy[cell + 1] - c.qy[cell]), DX, rDX);
+      // hydro-only runs keep Vsusptot at zero (no sediment source exists)
+      if (c.p.isSuspended[1] && !c.p.hydro_only)
+        c.vs[cell] += div_const(dt * (c.qxs[cell + W] - c.qxs[cell] + c.qys[cell + 1] - c.qys[cell]),
+                                DX, rDX);
+      if (h > 0) {
+        if (c.elev[cell] == -9999) h = 0;
+        if (h > m) m = h;
+      }
+      c.h[cell] = h;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) m = smax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  const int t = threadIdx.y * blockDim.x + threadIdx.x;
+  if ((t & 31) == 0) warp_max[t >> 5] = m;
+  __syncthreads();
+  if (t == 0) {
+    double b = 0;
+    for (int w = 0; w < (int)(blockDim.x * blockDim.y) / 32; w++) b = smax(b, warp_max[w]);
+    if (b > 0) atomic_max_pos(&d->maxdepth_bits, b);
+    __threadfence();
+    unsigned int nb = gridDim.x * gridDim.y;
+    last = (atomicAdd(&d->depth_done, 1u) == nb - 1);
+  }
+  __syncthreads();
+  if (last && t == 0) {
+    __threadfence();
+    unsigned long long bits = atomicExch(&d->maxdepth_bits, 0ull);
+    d->s.maxdepth = __longlong_as_double((long long)bits);
+    d->maxdepth_step = d->s.maxdepth;
+    d->depth_done = 0;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// scan_area :3821-3849 (every scan_area_interval_iter iterations)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_scan_area(const hc_view c, const hc_dev* __restrict__ d,
+                                                    int gated) {
+  if (gated && !(d->it_active && d->do_scan)) return;
+  const int j = 1 + blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = 1 + blockIdx.y * blockDim.y + threadIdx.y;
+  if (i > c.imax || j > c.jmax) return;
+  const size_t W = c.W;
+  const size_t cell = (size_t)i * W + j;
+  const double* h = c.h;
+  bool wet = h[cell] > 0 || h[cell - 1] > 0 || h[cell + 1] > 0 || h[cell - W] > 0 ||
+             h[cell - W - 1] > 0 || h[cell - W + 1] > 0 || h[cell + W - 1] > 0 ||
+             h[cell + W + 1] > 0 || h[cell + W] > 0;
+  c.mask[cell] = wet ? 1 : 0;
+}
+
+// ---------------------------------------------------------------------------
+// water_flux_out :3005-3047, one block.  Each edge cell is clamped at its
+// first visit in the reference's loop order; the outflow sum is a fixed-order
+// tree (deterministic, equal to the serial sum up to rounding).
+// Also writes the iteration record and the end-of-loop test of main.cpp:204.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(1024) k_flux_out(const hc_view c, hc_dev* d, int gated, int record,
+                                                    hc_step_record* rec, int64_t rec_cap) {
+  __shared__ double part[1024];
+  if (gated && !(d->it_active && d->rest_active)) return;
+  const hc_params& p = c.p;
+  const int imax = c.imax, jmax = c.jmax;
+  const double thr = p.water_depth_erosion_threshold, DX = p.DX;
+  const double fdt = d->s.time_step;
+  const int n1 = 2 * imax, n2 = n1 + 2 * jmax;
+  double acc = 0;
+  for (int k = threadIdx.x; k < n2; k += blockDim.x) {
+    int i, j;
+    if (k < n1) {
+      i = 1 + k / 2;
+      if ((k & 1) == 0) {
+        j = jmax;
+      } else {
+        j = 1;
+        if (jmax == 1) continue;  // same cell as the right-hand edge
+      }
+    } else {
+      const int kk = k - n1;
+      j = 1 + kk / 2;
+      if (j == 1 || j == jmax) continue;  // already visited by the row loop
+      if ((kk & 1) == 0) {
+        i = 1;
+      } else {
+        i = imax;
+        if (imax == 1) continue;
+      }
+    }
+    double& h = c.h[(size_t)i * c.W + j];
+    if (h > thr) {
+      acc += (h - thr) * DX * DX / fdt;
+      h = thr;
+    }
+  }
+  part[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) part[threadIdx.x] += part[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    hc_scalars& s = d->s;
+    s.temptot = part[0];
+    s.waterOut = s.temptot;
+    if (record && rec && d->rec_index < rec_cap) {
+      hc_step_record& r = rec[d->rec_index];
+      r.counter = s.counter;
+      r.cycle = s.cycle;
+      r.time_step = s.time_step;
+      r.maxdepth = d->maxdepth_step;
+      r.waterOut = s.waterOut;
+      r.waterinput = s.waterinput;
+      r.erode_mult = s.erode_mult;
+      r.sediQ = s.sediQ;
+      r.globalsediq = s.globalsediq;
+      r.baseflow = s.baseflow;
+    }
+    if (record) d->rec_index++;
+    if (gated) {
+      if (!p.hydro_only && !(d->flags & HC_RUN_NOHILL) &&
+          (s.cycle > s.creep_time || s.cycle > s.creep_time2))
+        d->pause |= HC_PAUSE_HOSTSTEP;
+      if (!(s.cycle / 60 < p.maxcycle)) d->pause |= HC_PAUSE_FINISHED;
+    }
+  }
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ launches
+static dim3 grid2d(const hc_ctx* c, dim3 b) {
+  return dim3((c->v.jmax + b.x - 1) / b.x, (c->v.imax + b.y - 1) / b.y);
+}
+
+void launch_control(hc_ctx* c) {
+  k_control<<<1, 1, 0, c->s>>>(c->v, c->dev);
+  count_launch(c, 1);
+}
+
+void launch_inputs(hc_ctx* c) {
+  // grid-stride over the current list (its length lives on the device)
+  int n = c->v.cin_cap;
+  int blocks = std::min((n + 255) / 256, 152 * 4);
+  if (blocks < 1) blocks = 1;
+  k_inputs<<<blocks, 256, 0, c->s>>>(c->v, c->dev);
+  count_launch(c, 1);
+}
+
+void launch_flow_dt(hc_ctx* c) {
+  k_flow_dt<<<1, 1, 0, c->s>>>(c->v, c->dev);
+  count_launch(c, 1);
+}
+
+void launch_flow_route(hc_ctx* c, int gated) {
+  dim3 b(32, 8);
+  if (c->v.p.hydro_only)
+    k_flow_route<false><<<grid2d(c, b), b, 0, c->s>>>(c->v, c->dev, gated);
+  else
+    k_flow_route<true><<<grid2d(c, b), b, 0, c->s>>>(c->v, c->dev, gated);
+  count_launch(c, 1);
+}
+
+void launch_depth_update(hc_ctx* c, int gated) {
+  dim3 b(32, 8);
+  k_depth_update<<<grid2d(c, b), b, 0, c->s>>>(c->v, c->dev, gated);
+  count_launch(c, 1);
+}
+
+void launch_scan_area(hc_ctx* c, int gated) {
+  dim3 b(32, 8);
+  k_scan_area<<<grid2d(c, b), b, 0, c->s>>>(c->v, c->dev, gated);
+  count_launch(c, 1);
+}
+
+void launch_flux_out(hc_ctx* c, int gated, int record) {
+  k_flux_out<<<1, 1024, 0, c->s>>>(c->v, c->dev, gated, record, c->v.rec, c->v.rec_cap);
+  count_launch(c, 1);
+}

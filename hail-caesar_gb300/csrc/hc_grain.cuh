@@ -1,0 +1,161 @@
+// Grain-store members of the reference on the device record layout:
+// sort_active :3874-3947, sand_fraction :3985-4009, d50 :4038-4075,
+// slide_GS :4077-4171, mean_ws_elev :4011-4036.
+//
+// A cell's record lives in its own slot (plane n at offset n*N2 + cell);
+// index[cell] == -9999 means "no record" exactly as in the reference.
+#pragma once
+#include "hc_internal.cuh"
+
+HC_DEV double& GRN(const hc_view& c, size_t cell, int n) {
+  return c.grain[(size_t)n * c.N2 + cell];
+}
+HC_DEV double& STR(const hc_view& c, size_t cell, int z, int n) {
+  return c.strata[((size_t)z * HC_ST_N + n) * c.N2 + cell];
+}
+
+// addGS for contexts that run in the reference's serial order (one thread):
+// the record gets the next row number.
+HC_DEV void addGS_serial(const hc_view& c, hc_dev* d, size_t cell) {
+  d->grain_tot++;
+  c.index[cell] = d->grain_tot;
+  grain_record_init(c, cell, c.elev[cell], c.bed[cell]);
+}
+
+HC_DEV void sort_active_dev(const hc_view& c, hc_dev* d, size_t cell, bool may_alloc) {
+  if (c.index[cell] == -9999) {
+    if (may_alloc) {
+      addGS_serial(c, d, cell);
+    } else {
+      d->err_code = 201;  // allocation outside serial context (cannot happen)
+      d->pause |= HC_PAUSE_ERROR;
+      return;
+    }
+  }
+  const double active = c.p.active;
+  double total = 0.0;
+  for (int n = 0; n <= HC_G; n++) total += GRN(c, cell, n);
+  if (total > (active * 1.5)) {
+    for (int z = 9; z >= 1; z--)
+      for (int n = 0; n <= HC_G - 2; n++) STR(c, cell, z, n) = STR(c, cell, z - 1, n);
+    double coeff = active / total;
+    for (int n = 1; n <= HC_G - 1; n++) {
+      double g = GRN(c, cell, n);
+      if (g > 0.0) {
+        double amount = coeff * (g);
+        STR(c, cell, 0, n - 1) = amount;
+        GRN(c, cell, n) = g - amount;
+      }
+    }
+  }
+  if (total < (active / 4)) {
+    for (int n = 1; n <= HC_G - 1; n++) GRN(c, cell, n) += STR(c, cell, 0, n - 1);
+    for (int z = 0; z <= 8; z++)
+      for (int n = 0; n <= HC_G - 2; n++) STR(c, cell, z, n) = STR(c, cell, z + 1, n);
+    for (int n = 1; n <= HC_G - 1; n++) STR(c, cell, 9, n - 1) = active * c.p.dprop[n];
+  }
+}
+
+HC_DEV double sand_fraction_dev(const hc_view& c, size_t cell) {
+  double at = 0, st = 0;
+  for (int n = 1; n <= HC_G; n++) at += GRN(c, cell, n);
+  for (int n = 1; n <= 2; n++) st += GRN(c, cell, n);
+  if (at < 0.0001) return 0.0;
+  return st / at;
+}
+
+HC_DEV double d50_dev(const hc_view& c, size_t cell) {
+  double at = 0, mx = 0, mn = 0;
+  double cum[HC_G + 1];
+  cum[0] = 0;
+  for (int n = 1; n <= HC_G; n++) {
+    at += GRN(c, cell, n);
+    cum[n] = at;
+  }
+  int i = 1;
+  while (i <= 9 && cum[i] < (at * 0.5)) i++;
+  if (i <= 9) {
+    mn = c.dlog[(i == 1) ? 1 : i - 1];
+    mx = c.dlog[i];
+  }
+  double cum_i = (i <= HC_G) ? cum[i] : 0.0;
+  double Dfifty = exp(mx - ((mx - mn) * ((cum_i - (at * 0.5)) / (cum_i - cum[i - 1]))));
+  if (at < 0.0000001) Dfifty = 0;
+  return Dfifty;
+}
+
+// slide_GS(x,y -> x2,y2, amount).  may_alloc: the caller runs in serial order
+// (case 3 allocates the receiver's record).
+HC_DEV void slide_GS_dev(const hc_view& c, hc_dev* d, size_t a, double amount, size_t b,
+                         bool may_alloc) {
+  const double* dprop = c.p.dprop;
+  double total = 0;
+  const bool ha = c.index[a] != -9999, hb = c.index[b] != -9999;
+  if (ha && hb) {
+    for (int n = 1; n <= HC_G - 1; n++)
+      if (GRN(c, a, n) > 0) total += GRN(c, a, n);
+    if (amount > total) {
+      for (int n = 1; n <= HC_G - 1; n++) GRN(c, b, n) += (amount - total) * dprop[n];
+      amount = total;
+    }
+    if (total > 0) {
+      for (int n = 1; n <= HC_G - 1; n++) {
+        double t = amount * (GRN(c, a, n) / total);
+        GRN(c, b, n) += t;
+        GRN(c, a, n) -= t;
+        if (GRN(c, a, n) < 0) GRN(c, a, n) = 0;
+      }
+    }
+    sort_active_dev(c, d, a, may_alloc);
+    sort_active_dev(c, d, b, may_alloc);
+    return;
+  }
+  if (!ha && hb) {
+    for (int n = 1; n <= HC_G - 1; n++) GRN(c, b, n) += (amount)*dprop[n];
+    sort_active_dev(c, d, b, may_alloc);
+    return;
+  }
+  if (ha && !hb) {
+    if (!may_alloc) {
+      d->err_code = 202;
+      d->pause |= HC_PAUSE_ERROR;
+      return;
+    }
+    addGS_serial(c, d, b);
+    if (amount > c.p.active) {
+      for (int n = 1; n <= HC_G - 1; n++) GRN(c, b, n) += amount * dprop[n];
+      amount = c.p.active;
+    }
+    for (int n = 1; n <= HC_G - 1; n++)
+      if (GRN(c, a, n) > 0) total += GRN(c, a, n);
+    for (int n = 1; n <= HC_G - 1; n++) {
+      if (total > 0) {
+        GRN(c, b, n) += amount * (GRN(c, a, n) / total);
+        if (GRN(c, a, n) > 0.0001) GRN(c, a, n) -= amount * (GRN(c, a, n) / total);
+        if (GRN(c, a, n) < 0) GRN(c, a, n) = 0;
+      }
+    }
+    sort_active_dev(c, d, a, may_alloc);
+    sort_active_dev(c, d, b, may_alloc);
+    return;
+  }
+}
+
+HC_DEV double mean_ws_elev_dev(const hc_view& c, int x, int y) {
+  const int dX[9] = {0, 0, 1, 1, 1, 0, -1, -1, -1};
+  const int dY[9] = {0, -1, -1, 0, 1, 1, 1, 0, -1};
+  double et = 0;
+  int cnt = 0;
+  for (int dir = 1; dir <= 8; dir++) {
+    size_t q = (size_t)(x + dX[dir]) * c.W + (y + dY[dir]);
+    if (c.h[q] > c.p.water_depth_erosion_threshold) {
+      et += c.h[q] + c.elev[q];
+      cnt++;
+    }
+  }
+  if (cnt > 0) {
+    et /= cnt;
+    return et;
+  }
+  return 0;
+}

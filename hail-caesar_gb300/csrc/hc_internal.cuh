@@ -1,0 +1,236 @@
+// Internal definitions of libhc_gpu (not part of the C ABI).
+//
+// Device layout of the model state (all in HBM, resident for the whole run):
+//   padded 2-D fields: (imax+2) x (jmax+2) doubles, row pitch W = jmax+2,
+//                      the reference's TNT layout, so whole-field transfers
+//                      are single copies;
+//   vel_dir:           4 planes (directions 1,3,5,7 of the reference's
+//                      9-entry cell record; the other 5 are never used);
+//   sr/sl/su/sd:       4 x 10 planes, plane (dir, fraction);
+//   grain, strata:     one record slot per cell (SoA planes, 11 and 10x9),
+//                      instead of the reference's lazily numbered rows; the
+//                      reference's row numbers (index[][]) are still kept,
+//                      allocated in the reference's serial order, and
+//                      hc_download(HC_F_GRAIN/STRATA) writes rows by them;
+//   mask:              one byte per cell, 1 where the cell is in down_scan.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stddef.h>
+
+#include "../../include/hc_gpu.h"
+
+#define HC_G 10               // G_MAX
+#define HC_NFRAC 9            // fractions 1..9
+#define HC_ST_N 9             // strata fractions used (0..G_MAX-2)
+
+// pause reasons (hc_dev::pause)
+#define HC_PAUSE_NONE 0
+#define HC_PAUSE_DRAINAGE 1   // baseflow changed: host recomputes input points
+#define HC_PAUSE_ERODE 2      // erosion retry loop exceeded the in-graph passes
+#define HC_PAUSE_FINISHED 4   // cycle/60 >= maxcycle
+#define HC_PAUSE_BUDGET 8     // iteration budget of the current hc_run reached
+#define HC_PAUSE_ERROR 16     // device-side error (see err_code)
+#define HC_PAUSE_HOSTSTEP 32  // host-side step due (creep / global landsliding)
+#define HC_PAUSE_LATERAL 64   // lateral3 due (runs before water_flux_out)
+
+#define HC_ERODE_PASSES 4     // entrainment passes captured per iteration
+
+// Device-side control block.  One per context, in device memory; the single
+// thread control kernel owns the scalar logic of the reference's driver.
+struct hc_dev {
+  hc_scalars s;           // scalar model state (mirrors LSDCatchmentModel)
+  // per-iteration switches written by the control kernel
+  int it_active;          // this iteration runs
+  int do_scan;            // scan_area this iteration
+  int do_erode;           // erosion this iteration
+  int erode_retry;        // another entrainment pass is needed
+  int erode_passes;       // passes done in this erosion call
+  int rest_active;        // kernels after the entrainment passes run
+  int do_slide;           // in_channel_landsliding this iteration
+  int do_lateral;         // lateral3 this iteration
+  int pause;              // HC_PAUSE_* bits; set -> following iterations skip
+  int err_code;
+  int64_t budget;         // iterations left in the current hc_run
+  int64_t rec_index;      // next record slot
+  double maxdepth_step;   // maxdepth right after depth_update (for records)
+  double reach_dt;        // flow dt used by the water inputs this iteration
+  double j_mean_in[HC_MAX_RF + 1];  // j_mean used by the input points
+  double input_dt;        // flow dt used by the catchment input points
+  double mult;            // mult_factor of the current erode() call
+  unsigned long long maxdepth_bits;  // atomic max of h (positive doubles)
+  unsigned long long tempbmax_bits;  // atomic max of temptot1
+  int grain_tot;          // grain_array_tot as an int
+  int alloc_count;        // allocations pending in the current pass
+  int flags;              // HC_RUN_* of the current run
+  unsigned int depth_done;   // blocks finished in depth_update (last-block reduction)
+  unsigned int pass_done;    // blocks finished in an entrainment pass
+  unsigned int misc_done;
+};
+
+// Everything a kernel needs, passed by value (device pointers + parameters).
+struct hc_view {
+  hc_params p;
+  double rDX;             // RN(1/DX), for div_const
+  int imax, jmax;
+  size_t W, N2, E2;       // pitch, padded cells, edge-array cells
+
+  // fields
+  double *elev, *h, *qx, *qy, *qxs, *qys, *vs, *vel, *tau, *bed, *man, *area, *ss;
+  double *vd;        // 4 * N2
+  double *sflux;     // 4 dirs * 10 fractions * N2 ; dir order su, sr, sd, sl
+  double *grain;     // 11 * N2
+  double *strata;    // 10 * 9 * N2
+  int32_t *index;
+  uint8_t *mask;
+  int32_t *rfarea;
+  double *edge, *edge2, *veg;  // E2, E2, 4*E2 (reference layout)
+  int32_t *cin_x, *cin_y;      // catchment input points (1-based lists)
+  int cin_cap;
+
+  // time series
+  float *rain; int rain_rows, rain_cols;
+  float *reach[HC_MAX_POINTS]; int reach_rows[HC_MAX_POINTS], reach_cols[HC_MAX_POINTS];
+  double *topm; int topm_rows;   // precomputed TOPMODEL recurrence
+  double dlog[HC_G];             // log(d1..d9) for d50
+
+  // scratch
+  double *erodetot, *erodetot3;  // N2 each
+  unsigned long long *alloc_key; // N2: serial-order key of the first grain-record request
+  int32_t *alloc_list;           // N2: cells allocated, in order
+  int32_t *slide_list; int slide_cap;
+  uint8_t *touched;              // N2 bytes
+  double *red;                   // reduction scratch
+  int32_t *scan_tmp;             // scan scratch
+  hc_step_record *rec; int64_t rec_cap;
+};
+
+struct hc_ctx {
+  hc_view v;
+  cudaStream_t s;
+  int device;
+  char err[512];
+  size_t bytes, max_bytes;
+  hc_dev *dev;       // device control block
+  hc_dev *hdev;      // pinned host mirror
+  double *h_elev;    // pinned host buffer (drainage area)
+  bool prepared;
+  // host copy of the catchment input list (kept between recomputations, as
+  // the reference keeps its vector)
+  int32_t *h_cin_x, *h_cin_y;
+  // CUDA graph of K iterations
+  cudaGraphExec_t graph; int graph_iters; int graph_flags;
+  int64_t graph_kernels;   // kernel nodes in the graph
+  bool capturing;
+  // counters for measurement: kernels launched, bytes moved host<->device
+  int64_t launches, h2d_bytes, d2h_bytes;
+};
+
+inline void count_launch(hc_ctx* c, int n) {
+  if (!c->capturing) c->launches += n;
+}
+
+// ---------------------------------------------------------------- helpers
+#define HC_DEV __device__ __forceinline__
+
+// std::max(a, b) as libstdc++ defines it: (a < b) ? b : a
+HC_DEV double smax(double a, double b) { return (a < b) ? b : a; }
+
+// h^3 rounded to nearest.  The reference evaluates std::pow(hflow, 10/3),
+// i.e. pow(hflow, 3.0) in C++11, which glibc returns correctly rounded in
+// all but vanishingly rare cases.  Here: exact h^2 = p + e (two-product),
+// h^3 = p*h + e*h with p*h split exactly again, summed once.
+HC_DEV double cube_rn(double h) {
+  double p = __dmul_rn(h, h);
+  double e = fma(h, h, -p);
+  double q = __dmul_rn(p, h);
+  double f = fma(p, h, -q);
+  double c = fma(e, h, f);
+  return __dadd_rn(q, c);
+}
+
+// RN(x / y) for a divisor fixed for the run, with r = RN(1/y) precomputed:
+// q = RN(x*r) is within one ulp of x/y, the remainder x - q*y is exact in
+// one FMA, and RN(q + rem*r) is the correctly rounded quotient (Markstein's
+// theorem, Handbook of Floating-Point Arithmetic, 2nd ed., sec. 4.7).  Valid
+// away from underflow/overflow, so x outside [2^-900, 2^900] in magnitude
+// takes the ordinary division.  Three FP64 operations instead of a division.
+HC_DEV double div_const(double x, double y, double r) {
+  const int ex = (__double2hiint(x) >> 20) & 0x7ff;
+  if (ex < 1023 - 900 || ex > 1023 + 900) return __ddiv_rn(x, y);
+  const double q = __dmul_rn(x, r);
+  const double e = fma(-q, y, x);
+  return fma(e, r, q);
+}
+
+// A float within a relative 2^-20 of |x| (or 0 / +inf when |x| is outside
+// the float normal range), built with integer operations only: the FP64
+// pipe is the scarce resource on this GPU, and these estimates only decide
+// which side of a threshold a value lies on (see near_or_above).
+HC_DEV float approx_abs_f(double x) {
+  const int hi = __double2hiint(x);
+  const int e = ((hi >> 20) & 0x7ff) - 1023 + 127;
+  if (e <= 0) return 0.0f;
+  if (e >= 255) return __int_as_float(0x7f800000);
+  return __int_as_float((e << 23) | ((hi & 0xfffff) << 3));
+}
+
+// static_cast<int>(double) as the reference's x86-64 build executes it
+// (cvttsd2si): NaN or out-of-range values give INT_MIN.
+HC_DEV int x86_trunc_to_int(double v) {
+  if (!(v > -2147483649.0 && v < 2147483648.0)) return (int)0x80000000u;
+  return (int)v;
+}
+
+HC_DEV void atomic_max_pos(unsigned long long* a, double v) {
+  // valid for v >= +0.0: the IEEE bit pattern orders like the value
+  atomicMax(a, (unsigned long long)__double_as_longlong(v));
+}
+
+// addGS :3949-3983 for a record held in the cell's own slot (the caller
+// assigns the reference's row number).  sort_active on a fresh record is a
+// no-op whenever dprop[1..9] sums to about 1; callers that need it run it.
+HC_DEV void grain_record_init(const hc_view& c, size_t cell, double elev, double bedrock) {
+  const hc_params& p = c.p;
+  const double active = p.active;
+  const size_t N2 = c.N2;
+  c.grain[cell] = 0;
+  for (int n = 1; n <= HC_G - 1; n++) c.grain[(size_t)n * N2 + cell] = active * p.dprop[n];
+  c.grain[(size_t)HC_G * N2 + cell] = 0;
+  for (int z = 0; z <= 9; z++) {
+    bool below = elev - (active * (z + 1)) < (bedrock - active);
+    for (int n2 = 0; n2 <= HC_G - 2; n2++)
+      c.strata[((size_t)z * HC_ST_N + n2) * N2 + cell] = below ? 0.0 : (active)*p.dprop[n2 + 1];
+  }
+}
+
+// launch helpers (defined in hc_api.cu)
+hc_status hc_fail(hc_ctx* c, hc_status st, const char* fmt, ...);
+hc_status hc_cuda(hc_ctx* c, cudaError_t e, const char* what);
+
+// phases of one iteration (hc_flow.cu, hc_erode.cu, hc_slide.cu, hc_lateral.cu)
+void launch_control(hc_ctx* c);          // scalar driver logic up to flow_route
+void launch_inputs(hc_ctx* c);           // catchment input points
+void launch_flow_dt(hc_ctx* c);          // flow_timestep for member-level calls
+void launch_flow_route(hc_ctx* c, int gated);
+void launch_depth_update(hc_ctx* c, int gated);
+void launch_scan_area(hc_ctx* c, int gated);
+void launch_flux_out(hc_ctx* c, int gated, int record);
+void launch_erode_begin(hc_ctx* c, int gated, double mult);
+void launch_erode_pass(hc_ctx* c, int max_passes);
+void launch_erode_finish(hc_ctx* c, int gated);
+void launch_lateral_check(hc_ctx* c);
+size_t erode_scratch_bytes(size_t N2, int imax, int jmax);
+void launch_slide3(hc_ctx* c, int gated);
+hc_status run_lateral(hc_ctx* c);
+hc_status run_global_landsliding(hc_ctx* c);
+hc_status run_creep(hc_ctx* c, double time);
+size_t slide_scratch_bytes(size_t N2);
+
+// host helpers (hc_host.cpp)
+void host_drainage_and_points(const hc_params* p, const double* elev, const int32_t* rfarea,
+                              double baseflow, double* area_out, int32_t* cin_x,
+                              int32_t* cin_y, int* total, double* counters);
+void host_topmodel_table(const hc_params* p, const float* rain, int rows, int cols,
+                         int nsteps, double* table /* [nsteps][2][rfnum+1] */);

@@ -1,0 +1,210 @@
+"""Host-side mirror of the reference's hot-path members over libhc_gpu.
+
+`Model` holds one device-resident model state and exposes the members that
+src/main.cpp calls each iteration (flow_route, depth_update, scan_area,
+erode, lateral_channel_erode, in_channel_landsliding, water_flux_out, ...)
+plus `run`, which executes whole iterations of the main loop on the device.
+It is a thin ctypes layer: every call goes through the C ABI of
+include/hc_gpu.h, the same entry points a C++ caller binds.  There is no CPU
+fallback: constructing a Model without the built library raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from hc_abi import (hc_params, hc_scalars, hc_step_record, FIELD_ID, STATUS, STEP_FIELDS,
+                    field_shape, field_dtype)
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libhc_gpu.so")
+
+_lib = None
+
+
+class HCError(RuntimeError):
+    pass
+
+
+def load_library(path=LIB_PATH):
+    """Loads libhc_gpu.so (built by build.py) and declares its ABI."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise HCError("libhc_gpu.so is not built (run hail-caesar_gb300/build.py): " + path)
+    lib = C.CDLL(path)
+    P, vp = C.POINTER, C.c_void_p
+    sig = {
+        "hc_params_default": (None, [P(hc_params), C.c_int32, C.c_int32, C.c_double]),
+        "hc_field_count": (C.c_int64, [P(hc_params), C.c_int]),
+        "hc_field_elsize": (C.c_int32, [C.c_int]),
+        "hc_create": (C.c_int, [P(hc_params), C.c_size_t, P(vp)]),
+        "hc_destroy": (C.c_int, [vp]),
+        "hc_last_error": (C.c_char_p, [vp]),
+        "hc_upload": (C.c_int, [vp, C.c_int, vp, C.c_size_t]),
+        "hc_download": (C.c_int, [vp, C.c_int, vp, C.c_size_t]),
+        "hc_set_rain": (C.c_int, [vp, vp, C.c_int32, C.c_int32]),
+        "hc_set_reach": (C.c_int, [vp, C.c_int32, vp, C.c_int32, C.c_int32]),
+        "hc_get_scalars": (C.c_int, [vp, P(hc_scalars)]),
+        "hc_set_scalars": (C.c_int, [vp, P(hc_scalars)]),
+        "hc_prepare": (C.c_int, [vp]),
+        "hc_set_maximum_timestep": (C.c_int, [vp]),
+        "hc_flow_route": (C.c_int, [vp]),
+        "hc_depth_update": (C.c_int, [vp]),
+        "hc_scan_area": (C.c_int, [vp]),
+        "hc_water_flux_out": (C.c_int, [vp]),
+        "hc_erode": (C.c_int, [vp, C.c_double, P(C.c_double)]),
+        "hc_lateral_channel_erode": (C.c_int, [vp]),
+        "hc_in_channel_landsliding": (C.c_int, [vp]),
+        "hc_run": (C.c_int, [vp, C.c_int64, C.c_int32, vp, P(C.c_int64)]),
+        "hc_stream": (vp, [vp]),
+        "hc_bench_kernel": (C.c_int, [vp, C.c_char_p, C.c_int32, P(C.c_double), P(C.c_int64)]),
+        "hc_get_counters": (C.c_int, [vp, P(C.c_int64), P(C.c_int64), P(C.c_int64)]),
+        "hc_profile_iteration": (C.c_int, [vp, C.c_int32, P(C.c_double)]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib
+
+
+class Model:
+    """One model state on the GPU, set up from a synth.Case (or any object
+    with .params, .elev, .rain, .reach, .mannings, .water_init)."""
+
+    def __init__(self, case, max_bytes=0, prepare=True):
+        self.lib = load_library()
+        self.case = case
+        self.p = case.params
+        self.h = C.c_void_p()
+        self._check(self.lib.hc_create(C.byref(self.p), max_bytes, C.byref(self.h)), "create")
+        p = self.p
+        elev = np.full((p.imax + 2, p.jmax + 2), -9999.0)
+        elev[1:-1, 1:-1] = case.elev
+        self.upload("elev", elev)
+        if case.mannings is not None:
+            m = np.zeros((p.imax + 2, p.jmax + 2))
+            m[1:-1, 1:-1] = case.mannings
+            self.upload("spat_var_mannings", m)
+        if case.water_init is not None:
+            w = np.zeros((p.imax + 2, p.jmax + 2))
+            w[1:-1, 1:-1] = case.water_init
+            self.upload("water_depth", w)
+        r = np.ascontiguousarray(case.rain, dtype=np.float32)
+        self._check(self.lib.hc_set_rain(self.h, r.ctypes.data, r.shape[0], r.shape[1]), "rain")
+        for k, t in enumerate(case.reach):
+            t = np.ascontiguousarray(t, dtype=np.float32)
+            self._check(self.lib.hc_set_reach(self.h, k, t.ctypes.data, t.shape[0], t.shape[1]),
+                        "reach")
+        if prepare:
+            self.prepare()
+
+    def close(self):
+        if self.h:
+            self.lib.hc_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st, what):
+        if st != 0:
+            msg = self.lib.hc_last_error(self.h) if self.h else b""
+            raise HCError("%s failed: %s %s" % (what, STATUS.get(st, st),
+                                                (msg or b"").decode(errors="replace")))
+
+    # ---- fields
+    def upload(self, name, a):
+        a = np.ascontiguousarray(a, dtype=field_dtype(name)).reshape(field_shape(self.p, name))
+        self._check(self.lib.hc_upload(self.h, FIELD_ID[name], a.ctypes.data, a.nbytes),
+                    "upload " + name)
+
+    def field(self, name):
+        a = np.empty(field_shape(self.p, name), dtype=field_dtype(name))
+        self._check(self.lib.hc_download(self.h, FIELD_ID[name], a.ctypes.data, a.nbytes),
+                    "download " + name)
+        return a
+
+    def scalars(self):
+        s = hc_scalars()
+        self._check(self.lib.hc_get_scalars(self.h, C.byref(s)), "get_scalars")
+        return s
+
+    def set_scalars(self, s):
+        self._check(self.lib.hc_set_scalars(self.h, C.byref(s)), "set_scalars")
+
+    # ---- members
+    def prepare(self):
+        self._check(self.lib.hc_prepare(self.h), "prepare")
+
+    def set_maximum_timestep(self):
+        self._check(self.lib.hc_set_maximum_timestep(self.h), "set_maximum_timestep")
+
+    def flow_route(self):
+        self._check(self.lib.hc_flow_route(self.h), "flow_route")
+
+    def depth_update(self):
+        self._check(self.lib.hc_depth_update(self.h), "depth_update")
+
+    def scan_area(self):
+        self._check(self.lib.hc_scan_area(self.h), "scan_area")
+
+    def water_flux_out(self):
+        self._check(self.lib.hc_water_flux_out(self.h), "water_flux_out")
+
+    def erode(self, mult):
+        t = C.c_double()
+        self._check(self.lib.hc_erode(self.h, float(mult), C.byref(t)), "erode")
+        return t.value
+
+    def lateral_channel_erode(self):
+        self._check(self.lib.hc_lateral_channel_erode(self.h), "lateral_channel_erode")
+
+    def in_channel_landsliding(self):
+        self._check(self.lib.hc_in_channel_landsliding(self.h), "in_channel_landsliding")
+
+    # ---- whole iterations
+    def run(self, n, flags=None, records=True):
+        """Runs up to n iterations of the main loop; returns the per-iteration
+        records as an (iterations, 10) float64 array (fields STEP_FIELDS)."""
+        flags = self.case.flags if flags is None else flags
+        rec = np.zeros((max(n, 1), len(STEP_FIELDS)), dtype=np.float64) if records else None
+        done = C.c_int64()
+        self._check(self.lib.hc_run(self.h, n, flags, rec.ctypes.data if records else None,
+                                    C.byref(done)), "run")
+        return rec[:done.value] if records else done.value
+
+    def stream(self):
+        return self.lib.hc_stream(self.h)
+
+    def bench_kernel(self, kernel, reps):
+        """(mean ms per launch, wet cells) of one kernel, timed with CUDA
+        events on the context's stream."""
+        ms = C.c_double()
+        wet = C.c_int64()
+        self._check(self.lib.hc_bench_kernel(self.h, kernel.encode(), reps, C.byref(ms),
+                                             C.byref(wet)), "bench_kernel")
+        return ms.value, wet.value
+
+    def counters(self):
+        """(kernels launched, bytes host->device, bytes device->host) so far."""
+        a, b, c = C.c_int64(), C.c_int64(), C.c_int64()
+        self._check(self.lib.hc_get_counters(self.h, C.byref(a), C.byref(b), C.byref(c)),
+                    "counters")
+        return a.value, b.value, c.value
+
+    PHASES = ["control_inputs", "flow_route", "depth_update", "scan_area", "entrain_passes",
+              "apply_lateral_edge", "lateral3", "water_flux_out", "slide_3"]
+
+    def profile_iteration(self, flags=None):
+        """{phase: ms} for one iteration run phase by phase with CUDA events."""
+        flags = self.case.flags if flags is None else flags
+        ms = (C.c_double * 9)()
+        self._check(self.lib.hc_profile_iteration(self.h, flags, ms), "profile_iteration")
+        return dict(zip(self.PHASES, list(ms)))

@@ -222,6 +222,28 @@ hc_status hc_run(hc_ctx* ctx, int64_t n, int32_t flags, hc_step_record* rec,
 /* Stream the context issues its work on (a cudaStream_t). */
 void* hc_stream(hc_ctx* ctx);
 
+/* Measurement hook (no counterpart in the reference): launches one kernel of
+ * the path `reps` times on the current state between two CUDA events on the
+ * context's stream and returns the mean time per launch in ms.  `kernel` is
+ * "flow_route", "depth_update", "scan_area" or "entrain".  The launches
+ * change the state like real calls would.  *wet receives the number of cells
+ * in the wet mask. */
+hc_status hc_bench_kernel(hc_ctx* ctx, const char* kernel, int32_t reps, double* avg_ms,
+                          int64_t* wet);
+
+/* Measurement hook (no counterpart in the reference): kernels this context
+ * has launched (graph kernel nodes included) and bytes it has copied
+ * host->device and device->host, since hc_create. */
+hc_status hc_get_counters(hc_ctx* ctx, int64_t* launches, int64_t* h2d_bytes,
+                          int64_t* d2h_bytes);
+
+/* Measurement hook (no counterpart in the reference): runs one iteration of
+ * hc_run's sequence phase by phase, without the graph, timing each phase with
+ * CUDA events: ms[0..8] = control+inputs, flow_route, depth_update,
+ * scan_area, entrainment passes, apply and lateral passes with the edge
+ * output, lateral3, water_flux_out, slide_3. */
+hc_status hc_profile_iteration(hc_ctx* ctx, int32_t flags, double* ms);
+
 #ifdef __cplusplus
 }
 #endif

@@ -131,13 +131,15 @@ extern "C" hco_model* hco_create(const hc_params* prm) {
   m->ss.assign(N2, 0.0);
   m->tempcreep.assign(N2, 0.0);
   m->vel_dir.assign(N2 * 9, 0.0);
-  m->sr.assign(N2 * 10, 0.0);
-  m->sl.assign(N2 * 10, 0.0);
-  m->su.assign(N2 * 10, 0.0);
-  m->sd.assign(N2 * 10, 0.0);
-  size_t nrec = N2 / (size_t)std::max(1, prm->LIMIT);
-  m->grain.assign(nrec * 11, 0.0);
-  m->strata.assign(nrec * 10 * 11, 0.0);
+  if (!prm->hydro_only) {  // only erosion runs allocate these (:1752-1762)
+    m->sr.assign(N2 * 10, 0.0);
+    m->sl.assign(N2 * 10, 0.0);
+    m->su.assign(N2 * 10, 0.0);
+    m->sd.assign(N2 * 10, 0.0);
+    size_t nrec = N2 / (size_t)std::max(1, prm->LIMIT);
+    m->grain.assign(nrec * 11, 0.0);
+    m->strata.assign(nrec * 10 * 11, 0.0);
+  }
   m->index.assign(N2, -9999);
   m->down_scan.assign((size_t)(m->jmax + 2) * (m->imax + 2), 0);
   m->rfarea.assign(N2, 1);
@@ -1537,11 +1539,46 @@ extern "C" double hco_get_scalar(hco_model* m, const char* name) {
 extern "C" int hco_set_scalar(hco_model* m, const char* name, double v) {
   std::string s(name);
   if (s == "cycle") m->cycle = v;
+  else if (s == "previous") m->previous = v;
   else if (s == "time_step") m->time_step = v;
   else if (s == "maxdepth") m->maxdepth = v;
   else if (s == "waterinput") m->waterinput = v;
   else if (s == "waterOut") m->waterOut = v;
   else if (s == "counter") m->counter = (int)v;
+  else if (s == "erode_call") m->erode_call = v;
+  else if (s == "erode_mult") m->erode_mult = v;
+  else if (s == "lateralcounter") m->lateralcounter = v;
+  else if (s == "time_1") m->time_1 = v;
+  else if (s == "baseflow") m->baseflow = v;
+  else if (s == "grain_array_tot") m->grain_array_tot = (int)v;
+  else if (s == "sediQ") m->sediQ = v;
+  else if (s == "globalsediq") m->globalsediq = v;
+  else if (s == "creep_time") m->creep_time = v;
+  else if (s == "creep_time2") m->creep_time2 = v;
+  else if (s.rfind("j_mean", 0) == 0) m->j_mean[std::atoi(s.c_str() + 6)] = v;
+  else if (s.rfind("sum_grain", 0) == 0) m->sum_grain[std::atoi(s.c_str() + 9)] = v;
   else return -1;
   return 0;
+}
+
+// Continues from a state loaded field by field (e.g. a GPU snapshot): the
+// catchment cell counts from the elevations, the TOPMODEL recurrence replayed
+// to time_1 (it depends only on the rain table), the input points from the
+// drainage area at the current baseflow.  Scalars must be set first.
+extern "C" void hco_resume(hco_model* m) {
+  for (size_t k = 0; k < m->nActualGridCells.size(); k++) m->nActualGridCells[k] = 0;
+  for (unsigned i = 1; i < m->imax; i++)
+    for (unsigned j = 1; j < m->jmax; j++)
+      if (m->E(i, j) > -9999) m->nActualGridCells[m->rfarea[m->ix(i, j)]]++;
+  const int rf = m->p.rfnum;
+  std::vector<double> keep(m->j_mean);
+  for (int n = 0; n <= rf; n++) {
+    m->jv[n] = m->jo[n] = 0.000000001;
+    m->old_j_mean[n] = m->new_j_mean[n] = 0;
+  }
+  topmodel_runoff(m, 1.0);
+  for (int t = 1; t <= (int)m->time_1; t++) topmodel_runoff(m, (double)t);
+  m->j_mean = keep;
+  zero_and_calc_drainage_area(m);
+  get_catchment_input_points(m);
 }

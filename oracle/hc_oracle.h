@@ -63,6 +63,9 @@ void hco_prepare(hco_model* m);
  * Returns the number of iterations run. */
 long hco_iterate(hco_model* m, long n, int flags, hco_step_record* rec);
 
+/* Continue from a state loaded field by field (after the scalars are set). */
+void hco_resume(hco_model* m);
+
 /* Single members, for unit tests. */
 void hco_flow_route(hco_model* m);
 void hco_depth_update(hco_model* m);

@@ -72,6 +72,7 @@ def _lib(omp=False):
         lib.hco_set_rain.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int]
         lib.hco_set_reach.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_int]
         lib.hco_prepare.argtypes = [C.c_void_p]
+        lib.hco_resume.argtypes = [C.c_void_p]
         lib.hco_iterate.restype = C.c_long
         lib.hco_iterate.argtypes = [C.c_void_p, C.c_long, C.c_int, C.c_void_p]
         lib.hco_erode.restype = C.c_double
@@ -149,6 +150,29 @@ class Oracle:
         rec = np.zeros((cap, len(STEP_FIELDS)), dtype=np.float64)
         done = self.lib.hco_iterate(self.h, n, flags, rec.ctypes.data)
         return rec[:done]
+
+    def load_from(self, model):
+        """Copies the whole state of a GPU model (hc.Model) into this oracle
+        and continues from it (fields in the reference layout, scalars, then
+        hco_resume)."""
+        names = ["elev", "water_depth", "qx", "qy", "qxs", "qys", "Vsusptot", "Vel", "Tau",
+                 "bedrock", "spat_var_mannings", "area", "index", "down_scan", "edge", "veg",
+                 "rfarea", "vel_dir"]
+        if not self.p.hydro_only:
+            names += ["ss", "sr", "sl", "su", "sd", "grain", "strata"]
+        for k in names:
+            self.field(k)[...] = model.field(k)
+        s = model.scalars()
+        for k in ("cycle", "previous", "time_step", "maxdepth", "waterinput", "waterOut",
+                  "counter", "erode_call", "erode_mult", "lateralcounter", "time_1", "baseflow",
+                  "grain_array_tot", "sediQ", "globalsediq", "creep_time", "creep_time2"):
+            self.set_scalar(k, getattr(s, k))
+        for n in range(1, self.p.rfnum + 1):
+            self.set_scalar("j_mean%d" % n, s.j_mean[n])
+        for n in range(1, 11):
+            self.set_scalar("sum_grain%d" % n, s.sum_grain[n])
+        self.lib.hco_resume(self.h)
+        self.prepared = True
 
     def state(self, names=None):
         names = names or ["elev", "water_depth", "qx", "qy", "qxs", "qys", "Vsusptot",

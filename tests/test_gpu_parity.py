@@ -1,0 +1,144 @@
+"""GPU parity: libhc_gpu (through its C ABI) against the oracle, the CPU
+restatement of the reference that tests/test_oracle_pin.py pins to the
+reference's own sources.
+
+The device evaluates every operation of the reference in the same order with
+the same IEEE roundings (no FMA contraction), with two exceptions that
+differ in the last bit only: the friction term's pow(hflow, 3), which the
+device computes correctly rounded while glibc's pow misrounds about 0.08 % of
+arguments, and the erosion transcendentals (CUDA exp/log/pow, within 2 ulp
+of glibc's).  States therefore agree to rounding level, and the tests hold
+them to the specification's tolerances: water depth and elevation within
+1e-9 m, wet masks and grain-record indices identical, discharge and sediment
+yield within 1e-6 relative.
+"""
+import numpy as np
+import pytest
+
+import synth
+from helpers import HYDRO_FIELDS, SED_FIELDS, assert_bitwise, assert_close, max_abs_diff
+
+pytestmark = pytest.mark.gpu
+
+# record columns: counter cycle time_step maxdepth waterOut waterinput
+#                 erode_mult sediQ globalsediq baseflow
+EXACT_COLS = [0, 1, 2, 3, 5, 6, 9]
+
+
+def run_pair(case, n, oracle_mod, flags=None):
+    import hc
+    m = hc.Model(case)
+    g = m.run(n, flags)
+    o = oracle_mod.Oracle(case)
+    r = o.iterate(n, flags)
+    return m, g, o, r
+
+
+H_ATOL = 1e-9  # m, water depth and elevation
+
+
+def check_records(g, r):
+    assert g.shape == r.shape, (g.shape, r.shape)
+    for c in (0, 6):
+        assert_bitwise(g[:, c], r[:, c], "record column %d" % c)
+    # cycle, time_step, maxdepth, waterinput, baseflow
+    assert_close(g[:, [1, 2, 3, 5, 9]], r[:, [1, 2, 3, 5, 9]], 0, "records", rtol=1e-9)
+    # water leaving the domain (outlet discharge)
+    assert_close(g[:, 4], r[:, 4], 1e-12, "waterOut", rtol=1e-6)
+
+
+# Hydro-only runs: the reference's qxs/qys/Vsusptot are (signed) zeros and its
+# vel_dir is never read; the device leaves them untouched.
+HYDRO_ONLY_FIELDS = ["elev", "water_depth", "qx", "qy", "down_scan"]
+
+
+def check_hydro(m, o):
+    assert_bitwise(m.field("down_scan"), o.field("down_scan"), "down_scan")
+    for k in ("elev", "water_depth"):
+        assert_close(m.field(k), o.field(k), H_ATOL, k)
+    for k in ("qx", "qy"):
+        assert_close(m.field(k), o.field(k), 1e-9, k, rtol=1e-6)
+
+
+def test_hydro_reach(gpu_lib, oracle_mod):
+    case = synth.reach_case(imax=60, jmax=24, DX=10.0, hours=24, hydro_only=True)
+    m, g, o, r = run_pair(case, 2500, oracle_mod)
+    check_records(g, r)
+    check_hydro(m, o)
+
+
+def test_hydro_reach_first_steps_bitwise(gpu_lib, oracle_mod):
+    """Until a friction pow() lands on one of glibc's misrounded arguments
+    the two are bit-identical; the first few hundred steps are."""
+    case = synth.reach_case(imax=60, jmax=24, DX=10.0, hours=24, hydro_only=True)
+    m, g, o, r = run_pair(case, 300, oracle_mod)
+    assert_bitwise(g[:, [0, 1, 2, 3, 5, 9]], r[:, [0, 1, 2, 3, 5, 9]], "records")
+    for k in HYDRO_ONLY_FIELDS:
+        assert_bitwise(m.field(k), o.field(k), k)
+    assert not np.any(m.field("Vsusptot")), "Vsusptot must stay zero without erosion"
+
+
+def test_hydro_catchment(gpu_lib, oracle_mod):
+    case = synth.catchment_case(n=40, DX=20.0, hours=72, relief=60.0, hydro_only=True,
+                                lateral=False)
+    m, g, o, r = run_pair(case, 6000, oracle_mod)
+    check_records(g, r)
+    check_hydro(m, o)
+    assert_close(m.field("area"), o.field("area"), 0, "area", rtol=1e-12)
+
+
+def test_hydro_nonsquare_odd(gpu_lib, oracle_mod):
+    case = synth.catchment_case(n=33, jmax=17, DX=10.0, hours=72, relief=30.0, hydro_only=True,
+                                lateral=False)
+    m, g, o, r = run_pair(case, 4000, oracle_mod)
+    check_records(g, r)
+    check_hydro(m, o)
+
+
+def _check_sediment(m, o, atol=H_ATOL):
+    assert_bitwise(m.field("index"), o.field("index"), "index")
+    assert_bitwise(m.field("down_scan"), o.field("down_scan"), "down_scan")
+    for k in ("elev", "water_depth"):
+        assert_close(m.field(k), o.field(k), atol, k)
+    for k in ("grain", "strata", "Vsusptot", "qx", "qy"):
+        assert_close(m.field(k), o.field(k), atol, k)
+
+
+def test_erosion_reach(gpu_lib, oracle_mod):
+    case = synth.reach_case(imax=60, jmax=24, DX=10.0, hours=24)
+    m, g, o, r = run_pair(case, 1000, oracle_mod)
+    check_records(g, r)
+    _check_sediment(m, o)
+    assert_close(g[:, 8], r[:, 8], 1e-12, "globalsediq", rtol=1e-6)
+
+
+def test_erosion_catchment_lateral(gpu_lib, oracle_mod):
+    case = synth.catchment_case(n=33, DX=20.0, hours=72, relief=60.0, lateral=True)
+    m, g, o, r = run_pair(case, 1000, oracle_mod)
+    check_records(g, r)
+    _check_sediment(m, o)
+    assert_close(m.field("edge"), o.field("edge"), 1e-9, "edge")
+
+
+def test_run_deterministic(gpu_lib):
+    import hc
+    case = synth.reach_case(imax=60, jmax=24, DX=10.0, hours=24)
+    a = hc.Model(case)
+    ra = a.run(800)
+    b = hc.Model(case)
+    rb = b.run(800)
+    assert_bitwise(ra, rb, "records")
+    for k in ("elev", "water_depth", "grain", "index"):
+        assert_bitwise(a.field(k), b.field(k), k)
+
+
+def test_run_chunks_equal_one_run(gpu_lib):
+    """hc_run in pieces continues exactly where it stopped."""
+    import hc
+    case = synth.reach_case(imax=60, jmax=24, DX=10.0, hours=24)
+    a = hc.Model(case)
+    ra = a.run(600)
+    b = hc.Model(case)
+    rb = np.concatenate([b.run(100), b.run(250), b.run(250)])
+    assert_bitwise(ra, rb, "records")
+    assert_bitwise(a.field("elev"), b.field("elev"), "elev")

@@ -1,0 +1,56 @@
+"""The device's exact-arithmetic building blocks, checked on the CPU.
+
+cube_rn (the friction term's h^3) is correctly rounded; glibc's
+pow(h, 3.0), which the reference calls, is not always (about 0.08 % of
+arguments), which is why hydraulic parity is to rounding level rather than
+bitwise.  div_const (division by the cell size) equals IEEE division."""
+import ctypes as C
+import os
+import subprocess
+import tempfile
+from fractions import Fraction
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+@pytest.fixture(scope="module")
+def numlib():
+    d = tempfile.mkdtemp()
+    so = os.path.join(d, "numerics_check.so")
+    subprocess.run(["gcc", "-O2", "-ffp-contract=off", "-shared", "-fPIC", "-o", so,
+                    os.path.join(HERE, "numerics_check.c"), "-lm"], check=True)
+    lib = C.CDLL(so)
+    lib.cube_rn.restype = C.c_double
+    lib.cube_rn.argtypes = [C.c_double]
+    lib.div_const.restype = C.c_double
+    lib.div_const.argtypes = [C.c_double, C.c_double, C.c_double]
+    lib.div_mismatches.restype = C.c_long
+    lib.div_mismatches.argtypes = [C.c_double, C.c_long, C.c_uint64]
+    return lib
+
+
+def test_cube_is_correctly_rounded(numlib):
+    rng = np.random.default_rng(5)
+    hs = 10.0 ** rng.uniform(-5, 1.5, 20000)
+    for h in hs:
+        want = float(Fraction(float(h)) ** 3)
+        assert numlib.cube_rn(float(h)) == want, h
+
+
+def test_glibc_pow_cube_is_not_always_correctly_rounded(numlib):
+    # documents the source of the last-bit differences against the reference
+    rng = np.random.default_rng(6)
+    hs = 10.0 ** rng.uniform(-5, 1.5, 200000)
+    libm = C.CDLL("libm.so.6")
+    libm.pow.restype = C.c_double
+    libm.pow.argtypes = [C.c_double, C.c_double]
+    diff = sum(1 for h in hs if libm.pow(float(h), 3.0) != numlib.cube_rn(float(h)))
+    assert diff < 0.01 * len(hs)
+
+
+@pytest.mark.parametrize("y", [5.0, 10.0, 20.0, 50.0, 12.5, 9.81, 3.0, 100.0])
+def test_div_const_equals_division(numlib, y):
+    assert numlib.div_mismatches(y, 400000, 1234) == 0
