@@ -9,8 +9,8 @@ Workloads (seeded synthetic inputs with the benchmark configurations' shapes):
   catchment2000  (default) catchment mode, 2000 x 2000 cells at 20 m, fractal
                  DEM with 300 m relief pit-filled to one outlet edge,
                  gamma rain + 60 mm/h storm, per-cell Manning's n, Einstein
-                 transport, lateral3 and slide_3 on; timed after a spin-up
-                 to storm onset (12 simulated hours)
+                 transport, lateral3 and slide_3 on; the storm starts at
+                 1 h and the timed steps begin 30 min into it
   flow8192       flow-only 8192 x 8192 at 5 m, 30 mm/h rain, erosion off
   reach          reach mode 300 x 100 at 10 m, Wilcock-Crowe
 
@@ -47,8 +47,9 @@ UNIT = "cell-steps/s"
 def make_workload(name):
     """(case, spin-up simulated minutes, description)."""
     if name == "catchment2000":
-        case = synth.catchment_case(n=2000, DX=20.0, hours=72, lateral=True)
-        return case, 12 * 60.0, "catchment 2000x2000 @20 m, erosion + lateral3 + slide_3, after 12 h"
+        case = synth.catchment_case(n=2000, DX=20.0, hours=72, lateral=True, storm_start_h=1.0)
+        return case, 90.0, ("catchment 2000x2000 @20 m, erosion + lateral3 + slide_3, timed 30 min "
+                            "into the 60 mm/h storm (storm from 1 h, spin-up to 1.5 h)")
     if name == "flow8192":
         case = synth.flow_case(n=8192, DX=5.0, hours=2)
         return case, 30.0, "flow-only 8192x8192 @5 m, 30 mm/h, after 30 min"
@@ -139,6 +140,20 @@ def flow_bytes_per_cell(p):
     return b
 
 
+def aggregate_replicas(ms, done, dist, device="cpu"):
+    """Replicas: the job's time is the slowest rank's, its work the sum of all
+    ranks' steps (each rank runs its own full model).  Returns (max ms,
+    total steps)."""
+    if dist is None:
+        return ms, done
+    import torch
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    n = torch.tensor([float(done)], dtype=torch.float64, device=device)
+    dist.all_reduce(n, op=dist.ReduceOp.SUM)
+    return float(t.item()), float(n.item())
+
+
 # ---------------------------------------------------------------- GPU arm
 def run_gpu(args, rank, world, dist):
     import torch
@@ -166,15 +181,7 @@ def run_gpu(args, rank, world, dist):
     ms = e0.elapsed_time(e1)
     launches = model.counters()[0] - l0
     clk = clocks.stop() if clocks else None
-    if dist:
-        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-        n = torch.tensor([done], dtype=torch.float64, device="cuda")
-        dist.all_reduce(n, op=dist.ReduceOp.SUM)
-        total_steps = float(n.item())
-    else:
-        total_steps = done
+    ms, total_steps = aggregate_replicas(ms, done, dist, "cuda")
     cells = case.cells
     value = cells * total_steps / (ms / 1e3)
     out = {"ms": ms, "done": done, "value": value, "clocks": clk, "cells": cells, "desc": desc,
@@ -200,8 +207,10 @@ def run_gpu(args, rank, world, dist):
                   "d2h_bytes_per_step": (d1 - d0) // e2e_steps,
                   "steps": e2e_steps, "api": "hc_run(ctx, 1, flags, host_records) per step"}
     # per-phase breakdown of a few iterations (phase by phase, no graph)
-    prof = [model.profile_iteration(flags) for _ in range(5)]
-    out["phases_ms"] = {k: float(np.median([p_[k] for p_ in prof])) for k in prof[0]}
+    nprof = int(os.environ.get("HC_PROFILE_ITERS", "60"))
+    prof = [model.profile_iteration(flags) for _ in range(nprof)]
+    out["phases_ms"] = {k: float(np.mean([p_[k] for p_ in prof])) for k in prof[0]}
+    out["phases_ms"]["iterations_profiled"] = nprof
     # dominant kernel, timed alone with events on the library's stream
     reps = 20
     ms_flow, wet = model.bench_kernel("flow_route", reps)

@@ -6,11 +6,9 @@
 //                    its last block evaluates the retry test (:4550-4565)
 //   k_alloc_*        grain records requested during the pass get the
 //                    reference's row numbers in the reference's serial order
-//   k_apply_cols     the gather-apply pass with the in-line +/-x lateral
-//                    erosion (:4570-4682): one walker per column, because a
-//                    cell's lateral step changes its x-neighbours before the
-//                    next cell of the same column is processed
-//   k_apply_rows     the +/-y lateral pass (:4684-4747): one walker per row
+//   k_apply_*        the gather-apply pass with the in-line +/-x lateral
+//                    erosion (:4570-4682) and the +/-y lateral pass
+//                    (:4684-4747), walked in order along independent chains
 //   k_edge_out       sediment leaving the four edges (:4750-4841)
 //   k_erode_post     erode_mult / erode_call of call_erosion
 //
@@ -398,122 +396,171 @@ __device__ __forceinline__ bool lateral_amount(const hc_view& c, double mult, do
   return true;
 }
 
-__global__ void __launch_bounds__(128) k_apply_cols(const hc_view c, hc_dev* d) {
-  if (!(d->it_active && d->rest_active && d->do_erode) || d->erode_retry) return;
-  const int y = 2 + blockIdx.x * blockDim.x + threadIdx.x;
-  if (y > c.jmax - 1) return;
-  const hc_params& p = c.p;
-  const size_t W = c.W;
-  const double thr = p.water_depth_erosion_threshold;
-  const double mult = d->mult;
-  const double ts = d->s.time_step;
-  for (int x = 1; x <= c.imax; x++) {
-    const size_t cell = (size_t)x * W + y;
-    if (!c.mask[cell]) continue;
-    double et3 = 0;
-    if (c.h[cell] > thr && x < c.imax && x > 1) {
-      const double h = c.h[cell];
-      double erodetot = 0;
-      for (int n = 1; n <= HC_G - 1; n++) {
-        if (n == 1 && p.isSuspended[n]) {
-          const double ssv = c.ss[cell];
-          double vs = c.vs[cell] + ssv;
-          GRN(c, cell, n) -= ssv;
-          erodetot -= ssv;
-          // inputpointsarray is all false in the reference (zero_values
-          // clears it after the reach block), so settling applies everywhere
-          double coeff = (p.fallVelocity[n] * ts) / h;
-          if (coeff > 1) coeff = 1;
-          double Vpdrop = coeff * vs;
-          if (Vpdrop > 0.001) Vpdrop = 0.001;
-          GRN(c, cell, n) += Vpdrop;
-          erodetot += Vpdrop;
-          vs -= Vpdrop;
-          c.vs[cell] = vs;
-        } else {
-          double val1 = (SF(c, 0, n, cell) + SF(c, 1, n, cell) + SF(c, 2, n, cell) +
-                         SF(c, 3, n, cell));
-          double val2 = (SF(c, 0, n, cell + 1) + SF(c, 2, n, cell - 1) + SF(c, 3, n, cell + W) +
-                         SF(c, 1, n, cell - W));
-          GRN(c, cell, n) += val2 - val1;
-          erodetot += val2 - val1;
-          et3 += val1;
-        }
-      }
-      double e0 = c.elev[cell] + erodetot;
-      c.elev[cell] = e0;
-      if (erodetot < 0) sort_active_dev(c, d, cell, false);
-      if (et3 > 0) {
-        double elev_update = 0;
-        const double tau0 = c.tau[cell];
-        {
-          const size_t nb = cell - W;
-          const double en = c.elev[nb];
-          double amt;
-          if (en > e0 && x > 2 &&
-              lateral_amount(c, mult, ts, tau0, et3, nb, EX(c, x - 1, y), en, e0, x - 1 == 1, amt)) {
-            elev_update += amt;
-            c.elev[nb] = en - amt;
-            slide_GS_dev(c, d, nb, amt, cell, false);
-          }
-        }
-        {
-          const size_t nb = cell + W;
-          const double en = c.elev[nb];
-          double amt;
-          if (en > e0 && x < c.imax - 1 &&
-              lateral_amount(c, mult, ts, tau0, et3, nb, EX(c, x + 1, y), en, e0, x + 1 == c.imax,
-                             amt)) {
-            elev_update += amt;
-            c.elev[nb] = en - amt;
-            slide_GS_dev(c, d, nb, amt, cell, false);
-          }
-        }
-        c.elev[cell] = c.elev[cell] + elev_update;
-      }
-    }
-    c.erodetot3[cell] = et3;
-  }
+// The apply passes are sequential in the reference: along a column the
+// +/-x lateral step of row x changes rows x-1 and x+1 before row x+1 is
+// processed (and along a row for the +/-y pass).  Only cells with bedload
+// leaving them (erodetot3 > 0, "lateral cells") take that step, so a column
+// splits into independent chains: rows x and x+1 are linked when either is a
+// lateral cell.  Each chain is walked in order by one thread, chains in
+// parallel; cells of different chains never read or write each other, so the
+// result is the serial loop's.
+
+// erodetot3 of every cell of the pass (0 where the cell is not processed)
+__device__ __forceinline__ bool apply_active(const hc_view& c, size_t cell, int x) {
+  return c.mask[cell] && c.h[cell] > c.p.water_depth_erosion_threshold && x < c.imax && x > 1;
 }
 
-// +/-y lateral pass :4684-4747, one walker per row x in [2, imax-1]
-__global__ void __launch_bounds__(128) k_apply_rows(const hc_view c, hc_dev* d) {
+__global__ void __launch_bounds__(256) k_apply_et3(const hc_view c, const hc_dev* d) {
   if (!(d->it_active && d->rest_active && d->do_erode) || d->erode_retry) return;
-  const int x = 2 + blockIdx.x * blockDim.x + threadIdx.x;
-  if (x > c.imax - 1) return;
+  const int y = 2 + blockIdx.x * blockDim.x + threadIdx.x;
+  const int x = 1 + blockIdx.y * blockDim.y + threadIdx.y;
+  if (y > c.jmax - 1 || x > c.imax) return;
+  const size_t cell = (size_t)x * c.W + y;
+  double et3 = 0;
+  if (apply_active(c, cell, x)) {
+    for (int n = 1; n <= HC_G - 1; n++) {
+      if (n == 1 && c.p.isSuspended[n]) continue;
+      et3 += (SF(c, 0, n, cell) + SF(c, 1, n, cell) + SF(c, 2, n, cell) + SF(c, 3, n, cell));
+    }
+  }
+  c.erodetot3[cell] = et3;
+}
+
+// one cell of the gather-apply pass with its +/-x lateral step (:4579-4680)
+__device__ void apply_cell(const hc_view& c, hc_dev* d, size_t cell, int x, int y, double mult,
+                           double ts) {
+  const hc_params& p = c.p;
   const size_t W = c.W;
-  const double mult = d->mult;
-  const double ts = d->s.time_step;
-  for (int y = 2; y <= c.jmax - 1; y++) {
-    const size_t cell = (size_t)x * W + y;
-    if (!c.mask[cell]) continue;
-    const double et3 = c.erodetot3[cell];
-    if (!(et3 > 0)) continue;
+  const double h = c.h[cell];
+  double erodetot = 0, et3 = 0;
+  for (int n = 1; n <= HC_G - 1; n++) {
+    if (n == 1 && p.isSuspended[n]) {
+      const double ssv = c.ss[cell];
+      double vs = c.vs[cell] + ssv;
+      GRN(c, cell, n) -= ssv;
+      erodetot -= ssv;
+      // inputpointsarray is all false in the reference (zero_values clears it
+      // after the reach block), so settling applies everywhere
+      double coeff = (p.fallVelocity[n] * ts) / h;
+      if (coeff > 1) coeff = 1;
+      double Vpdrop = coeff * vs;
+      if (Vpdrop > 0.001) Vpdrop = 0.001;
+      GRN(c, cell, n) += Vpdrop;
+      erodetot += Vpdrop;
+      vs -= Vpdrop;
+      c.vs[cell] = vs;
+    } else {
+      double val1 = (SF(c, 0, n, cell) + SF(c, 1, n, cell) + SF(c, 2, n, cell) +
+                     SF(c, 3, n, cell));
+      double val2 = (SF(c, 0, n, cell + 1) + SF(c, 2, n, cell - 1) + SF(c, 3, n, cell + W) +
+                     SF(c, 1, n, cell - W));
+      GRN(c, cell, n) += val2 - val1;
+      erodetot += val2 - val1;
+      et3 += val1;
+    }
+  }
+  double e0 = c.elev[cell] + erodetot;
+  c.elev[cell] = e0;
+  if (erodetot < 0) sort_active_dev(c, d, cell, false);
+  if (et3 > 0) {
     double elev_update = 0;
     const double tau0 = c.tau[cell];
     {
-      const size_t nb = cell - 1;
-      const double en = c.elev[nb], e0 = c.elev[cell];
+      const size_t nb = cell - W;
+      const double en = c.elev[nb];
       double amt;
-      if (en > e0 &&
-          lateral_amount(c, mult, ts, tau0, et3, nb, EX(c, x, y - 1), en, e0, y - 1 == 1, amt)) {
+      if (en > e0 && x > 2 &&
+          lateral_amount(c, mult, ts, tau0, et3, nb, EX(c, x - 1, y), en, e0, x - 1 == 1, amt)) {
         elev_update += amt;
         c.elev[nb] = en - amt;
         slide_GS_dev(c, d, nb, amt, cell, false);
       }
     }
     {
-      const size_t nb = cell + 1;
-      const double en = c.elev[nb], e0 = c.elev[cell];
+      const size_t nb = cell + W;
+      const double en = c.elev[nb];
       double amt;
-      if (en > e0 &&
-          lateral_amount(c, mult, ts, tau0, et3, nb, EX(c, x, y + 1), en, e0, y + 1 == c.jmax, amt)) {
+      if (en > e0 && x < c.imax - 1 &&
+          lateral_amount(c, mult, ts, tau0, et3, nb, EX(c, x + 1, y), en, e0, x + 1 == c.imax,
+                         amt)) {
         elev_update += amt;
         c.elev[nb] = en - amt;
         slide_GS_dev(c, d, nb, amt, cell, false);
       }
     }
     c.elev[cell] = c.elev[cell] + elev_update;
+  }
+}
+
+// chains along the columns: thread (x, y) walks the chain that starts at row x
+__global__ void __launch_bounds__(256) k_apply_xchains(const hc_view c, hc_dev* d) {
+  if (!(d->it_active && d->rest_active && d->do_erode) || d->erode_retry) return;
+  const int y = 2 + blockIdx.x * blockDim.x + threadIdx.x;
+  const int x = 1 + blockIdx.y * blockDim.y + threadIdx.y;
+  if (y > c.jmax - 1 || x > c.imax) return;
+  const size_t W = c.W;
+  auto lat = [&](int r) { return r >= 1 && r <= c.imax && c.erodetot3[(size_t)r * W + y] > 0; };
+  const bool link_prev = lat(x - 1) || lat(x);
+  if (link_prev && x > 1) return;  // inside a chain that starts above
+  const bool link_next = lat(x) || lat(x + 1);
+  size_t cell = (size_t)x * W + y;
+  if (!link_next && !apply_active(c, cell, x)) return;
+  const double mult = d->mult, ts = d->s.time_step;
+  for (int r = x; r <= c.imax; r++) {
+    cell = (size_t)r * W + y;
+    if (apply_active(c, cell, r)) apply_cell(c, d, cell, r, y, mult, ts);
+    if (!(lat(r) || lat(r + 1))) break;
+  }
+}
+
+// one cell of the +/-y lateral pass (:4690-4744)
+__device__ void yside_cell(const hc_view& c, hc_dev* d, size_t cell, int x, int y, double mult,
+                           double ts, double et3) {
+  double elev_update = 0;
+  const double tau0 = c.tau[cell];
+  {
+    const size_t nb = cell - 1;
+    const double en = c.elev[nb], e0 = c.elev[cell];
+    double amt;
+    if (en > e0 &&
+        lateral_amount(c, mult, ts, tau0, et3, nb, EX(c, x, y - 1), en, e0, y - 1 == 1, amt)) {
+      elev_update += amt;
+      c.elev[nb] = en - amt;
+      slide_GS_dev(c, d, nb, amt, cell, false);
+    }
+  }
+  {
+    const size_t nb = cell + 1;
+    const double en = c.elev[nb], e0 = c.elev[cell];
+    double amt;
+    if (en > e0 &&
+        lateral_amount(c, mult, ts, tau0, et3, nb, EX(c, x, y + 1), en, e0, y + 1 == c.jmax, amt)) {
+      elev_update += amt;
+      c.elev[nb] = en - amt;
+      slide_GS_dev(c, d, nb, amt, cell, false);
+    }
+  }
+  c.elev[cell] = c.elev[cell] + elev_update;
+}
+
+// chains along the rows for the +/-y pass: lateral cells are the wet-listed
+// cells with erodetot3 > 0 in columns 2..jmax-1
+__global__ void __launch_bounds__(256) k_apply_ychains(const hc_view c, hc_dev* d) {
+  if (!(d->it_active && d->rest_active && d->do_erode) || d->erode_retry) return;
+  const int y = 2 + blockIdx.x * blockDim.x + threadIdx.x;
+  const int x = 2 + blockIdx.y * blockDim.y + threadIdx.y;
+  if (y > c.jmax - 1 || x > c.imax - 1) return;
+  const size_t W = c.W;
+  const size_t row = (size_t)x * W;
+  auto lat = [&](int q) {
+    return q >= 2 && q <= c.jmax - 1 && c.mask[row + q] && c.erodetot3[row + q] > 0;
+  };
+  if ((lat(y - 1) || lat(y)) && y > 2) return;
+  if (!(lat(y) || lat(y + 1))) return;
+  const double mult = d->mult, ts = d->s.time_step;
+  for (int q = y; q <= c.jmax - 1; q++) {
+    if (lat(q)) yside_cell(c, d, row + q, x, q, mult, ts, c.erodetot3[row + q]);
+    if (!(lat(q) || lat(q + 1))) break;
   }
 }
 
@@ -721,13 +768,13 @@ void launch_erode_pass(hc_ctx* c, int max_passes) {
 
 void launch_erode_finish(hc_ctx* c, int gated) {
   ErodeScratch s = scratch_of(c);
-  int nc = (c->v.jmax - 2 + 127) / 128;
-  if (nc < 1) nc = 1;
-  k_apply_cols<<<nc, 128, 0, c->s>>>(c->v, c->dev);
+  dim3 b(32, 8);
+  dim3 g((c->v.jmax - 2 + 31) / 32, (c->v.imax + 7) / 8);
+  k_apply_et3<<<g, b, 0, c->s>>>(c->v, c->dev);
   count_launch(c, 1);
-  int nr = (c->v.imax - 2 + 127) / 128;
-  if (nr < 1) nr = 1;
-  k_apply_rows<<<nr, 128, 0, c->s>>>(c->v, c->dev);
+  k_apply_xchains<<<g, b, 0, c->s>>>(c->v, c->dev);
+  count_launch(c, 1);
+  k_apply_ychains<<<g, b, 0, c->s>>>(c->v, c->dev);
   count_launch(c, 1);
   k_edge_out<<<1, 1024, 0, c->s>>>(c->v, c->dev, s.contrib, nullptr);
   count_launch(c, 1);

@@ -214,10 +214,10 @@ def gamma_rain(hours, step_min, mean_mmh, shape_k, storm_mmh, storm_start_h,
 
 
 def catchment_case(n=2000, DX=20.0, seed=2, hours=72, lateral=True, hydro_only=False,
-                   jmax=None, relief=300.0, fill=True):
+                   jmax=None, relief=300.0, fill=True, storm_start_h=12.0):
     """Catchment mode: fractal DEM (beta 2, `relief` m) pit-filled toward the
     bottom edge; rain in 10-min steps ~ gamma(k=0.5, mean 2 mm/h) plus a
-    60 mm/h storm of 3 h; TOPMODEL m = 0.01; Manning's n from a smooth field
+    60 mm/h storm of 3 h starting at `storm_start_h`; TOPMODEL m = 0.01; Manning's n from a smooth field
     in [0.03, 0.06]; Einstein transport; slide_3 (always on with erosion) and
     lateral3 (called after erosion)."""
     imax = n
@@ -240,7 +240,7 @@ def catchment_case(n=2000, DX=20.0, seed=2, hours=72, lateral=True, hydro_only=F
     p.MIN_Q = 0.01
     sizes = geometric_sizes(0.001, 0.256)
     set_grains(p, sizes, lognormal_dprop(sizes, 0.016))
-    rain = gamma_rain(hours, 10, 2.0, 0.5, 60.0, 12.0, 3.0, seed + 2000)
+    rain = gamma_rain(hours, 10, 2.0, 0.5, 60.0, storm_start_h, 3.0, seed + 2000)
     flags = 1 if lateral else 0
     return Case("catchment_%dx%d" % (imax, jmax), p, z, rain, mannings=man, flags=flags)
 
