@@ -44,15 +44,16 @@ METRIC = "cell-steps/s on 1 GB300 (plain vs batched ensemble); adjoint/forward c
 UNIT = "cell-steps/s"
 
 
-def make_workload(name):
+def make_workload(name, size=0):
     """(case, spin-up simulated minutes, description)."""
     if name == "catchment2000":
-        case = synth.catchment_case(n=2000, DX=20.0, hours=72, lateral=True, storm_start_h=1.0)
+        case = synth.catchment_case(n=size or 2000, DX=20.0, hours=72, lateral=True,
+                                    storm_start_h=1.0)
         return case, 90.0, ("catchment 2000x2000 @20 m, erosion + lateral3 + slide_3, timed 30 min "
                             "into the 60 mm/h storm (storm from 1 h, spin-up to 1.5 h)")
     if name == "flow8192":
-        case = synth.flow_case(n=8192, DX=5.0, hours=2)
-        return case, 30.0, "flow-only 8192x8192 @5 m, 30 mm/h, after 30 min"
+        case = synth.flow_case(n=size or 8192, DX=5.0, hours=2)
+        return case, 75.0, "flow-only 8192x8192 @5 m, 30 mm/h, after 75 min"
     if name == "reach":
         case = synth.reach_case(imax=300, jmax=100, DX=10.0, hours=24)
         return case, 6 * 60.0, "reach 300x100 @10 m, Wilcock, after 6 h (hydrograph peak)"
@@ -120,11 +121,18 @@ def measured_peak_hbm():
 
 def spin_up(model, minutes, flags):
     """Runs the model until the simulated clock passes `minutes`."""
+    t0 = time.perf_counter()
     while True:
-        model.run(2000, flags, records=False)
+        n = model.run(500, flags, records=False)
         s = model.scalars()
-        if s.cycle >= minutes or s.cycle / 60 >= model.p.maxcycle:
+        log("spin-up: cycle %.1f min, iteration %d, %.1f s" % (s.cycle, s.counter,
+                                                               time.perf_counter() - t0))
+        if s.cycle >= minutes or s.cycle / 60 >= model.p.maxcycle or n == 0:
             return s
+
+
+def log(msg):
+    print(msg, file=sys.stderr, flush=True)
 
 
 # per-cell algorithmic bytes of flow_route: elevation, depth, qx, qy read and
@@ -159,12 +167,17 @@ def run_gpu(args, rank, world, dist):
     import torch
     import hc
     torch.cuda.set_device(rank % max(1, torch.cuda.device_count()))
-    case, spin_min, desc = make_workload(args.workload)
+    t0 = time.perf_counter()
+    case, spin_min, desc = make_workload(args.workload, args.size)
+    if args.spinup >= 0:
+        spin_min = args.spinup
+    log("workload generated in %.1f s" % (time.perf_counter() - t0))
     flags = case.flags
     model = hc.Model(case)
     spin_up(model, spin_min, flags)
     stream = torch.cuda.ExternalStream(model.stream())
     model.run(args.warmup, flags, records=False)
+    log("warm-up done")
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
@@ -174,10 +187,12 @@ def run_gpu(args, rank, world, dist):
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     l0 = model.counters()[0]
+    torch.cuda.nvtx.range_push("timed")
     e0.record(stream)
     done = model.run(args.steps, flags, records=False)
     e1.record(stream)
     torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
     ms = e0.elapsed_time(e1)
     launches = model.counters()[0] - l0
     clk = clocks.stop() if clocks else None
@@ -186,7 +201,7 @@ def run_gpu(args, rank, world, dist):
     value = cells * total_steps / (ms / 1e3)
     out = {"ms": ms, "done": done, "value": value, "clocks": clk, "cells": cells, "desc": desc,
            "launches": launches}
-    if rank != 0:
+    if rank != 0 or args.timed_only:
         return out, model, case
     # end-to-end through the public API: one hc_run call per step with the
     # step's record read back to host memory (the drop-in call pattern)
@@ -247,7 +262,7 @@ def run_reference(args):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     oracle.build()
-    case, spin_min, desc = make_workload(args.workload)
+    case, spin_min, desc = make_workload(args.workload, args.size)
     flags = case.flags
     o = oracle.Oracle(case, omp=True)
     while True:
@@ -279,6 +294,13 @@ def main():
     ap.add_argument("--workload", default="catchment2000",
                     choices=["catchment2000", "flow8192", "reach"])
     ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--size", type=int, default=0,
+                    help="override the grid side (smaller runs for profiling)")
+    ap.add_argument("--spinup", type=float, default=-1,
+                    help="override the spin-up, simulated minutes")
+    ap.add_argument("--timed-only", action="store_true",
+                    help="only the timed steps (no e2e, profile, kernel timing or CPU leg); "
+                         "for runs under a profiler")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     rank = int(os.environ.get("RANK", "0"))
@@ -293,7 +315,10 @@ def main():
         tdist.init_process_group("nccl")
         dist = tdist
     out, model, case = run_gpu(args, rank, world, dist)
-    if rank == 0:
+    if rank == 0 and args.timed_only:
+        print(json.dumps({"timed_only": True, "ms_per_step": out["ms"] / max(1, out["done"]),
+                          "value": out["value"], "launches": out["launches"]}))
+    elif rank == 0:
         line = {
             "metric": METRIC, "value": out["value"], "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": out["ms"] / out["done"],

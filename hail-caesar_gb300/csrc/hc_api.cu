@@ -225,6 +225,12 @@ extern "C" hc_status hc_create(const hc_params* p, size_t max_bytes, hc_ctx** ou
   hc_view& v = c->v;
   v.p = *p;
   v.rDX = 1.0 / p->DX;
+  for (int n = 1; n <= 9; n++) {
+    const double Di = p->d[n], g = 9.81;
+    v.einA[n] = (2650 - 1000) * Di;
+    v.einS[n] = std::sqrt(1000 / ((2250 - 1000) * g * (Di * Di * Di)));
+    v.einRS[n] = 1.0 / v.einS[n];
+  }
   v.imax = p->imax;
   v.jmax = p->jmax;
   v.W = (size_t)p->jmax + 2;
@@ -233,11 +239,13 @@ extern "C" hc_status hc_create(const hc_params* p, size_t max_bytes, hc_ctx** ou
   const size_t N2 = v.N2, E2 = v.E2;
   const bool sed = !p->hydro_only;
   cudaGetDevice(&c->device);
-  if (cudaStreamCreateWithFlags(&c->s, cudaStreamNonBlocking) != cudaSuccess) {
+  if (cudaStreamCreateWithFlags(&c->s, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&c->s2, cudaStreamNonBlocking) != cudaSuccess) {
     cudaGetLastError();
     delete c;
     return HC_ERR_CUDA;
   }
+  c->cs = c->s;
   hc_status st = HC_OK;
 #define A(ptr, n)                                    \
   if (st == HC_OK) st = dalloc(c, &(ptr), (n));
@@ -246,9 +254,10 @@ extern "C" hc_status hc_create(const hc_params* p, size_t max_bytes, hc_ctx** ou
   A(v.vd, 4 * N2) A(v.index, N2) A(v.mask, N2) A(v.rfarea, N2)
   A(v.edge, E2) A(v.edge2, E2) A(v.veg, 4 * E2)
   A(v.cin_x, (size_t)p->imax * p->jmax + 2) A(v.cin_y, (size_t)p->imax * p->jmax + 2)
+  A(v.wet, N2) A(v.wet_sums, (N2 + 1023) / 1024 + 1)
   if (sed) {
     A(v.sflux, 40 * N2) A(v.grain, 11 * N2) A(v.strata, 90 * N2) A(v.alloc_key, N2)
-    A(v.erodetot, N2) A(v.erodetot3, N2)
+    A(v.erodetot, N2) A(v.erodetot3, N2) A(v.pre, 11 * N2)
   } else {
     A(v.erodetot, N2)
   }
@@ -329,8 +338,9 @@ static hc_status free_all(hc_ctx* c) {
   hc_view& v = c->v;
   void* ptrs[] = {v.elev, v.h, v.qx, v.qy, v.qxs, v.qys, v.vs, v.vel, v.tau, v.bed, v.man,
                   v.area, v.ss, v.vd, v.sflux, v.grain, v.strata, v.index, v.mask, v.rfarea,
-                  v.edge, v.edge2, v.veg, v.cin_x, v.cin_y, v.erodetot, v.erodetot3,
-                  v.alloc_key, v.red, v.touched, v.topm, v.rain, v.rec, c->dev,
+                  v.edge, v.edge2, v.veg, v.cin_x, v.cin_y, v.erodetot, v.erodetot3, v.pre,
+                  v.alloc_key, v.red, v.touched, v.topm, v.rain, v.rec, c->dev, v.wet,
+                  v.wet_sums,
                   v.reach[0], v.reach[1], v.reach[2], extra(c).lateral};
   for (void* q : ptrs)
     if (q) cudaFree(q);
@@ -338,9 +348,11 @@ static hc_status free_all(hc_ctx* c) {
   if (c->h_elev) cudaFreeHost(c->h_elev);
   free(c->h_cin_x);
   free(c->h_cin_y);
+  if (c->drainage_cache) host_drainage_cache_free(c->drainage_cache);
   free(extra(c).h_rain);
   if (c->graph) cudaGraphExecDestroy(c->graph);
   if (c->s) cudaStreamDestroy(c->s);
+  if (c->s2) cudaStreamDestroy(c->s2);
   drop_extra(c);
   delete c;
   return HC_OK;
@@ -407,6 +419,10 @@ extern "C" hc_status hc_upload(hc_ctx* c, hc_field f, const void* host, size_t n
   if (double* d = plain_field(c, f)) {
     HC_CU(cudaMemcpyAsync(d, host, nbytes, cudaMemcpyHostToDevice, s), "upload");
     HC_CU(cudaStreamSynchronize(s), "upload");
+    if (f == HC_F_ELEV && c->drainage_cache) {  // the cached elevation order is stale
+      host_drainage_cache_free(c->drainage_cache);
+      c->drainage_cache = nullptr;
+    }
     return HC_OK;
   }
   switch (f) {
@@ -480,6 +496,7 @@ extern "C" hc_status hc_upload(hc_ctx* c, hc_field f, const void* host, size_t n
         }
       }
       HC_CU(cudaMemcpy(v.mask, m.data(), N2, cudaMemcpyHostToDevice), "upload");
+      launch_wet_list(c, 0);
       break;
     }
     default:
@@ -653,8 +670,11 @@ static hc_status recompute_points(hc_ctx* c) {
   HC_TRY(pull(c));
   hc_scalars& s = c->hdev->s;
   int total = 0;
+  if (!c->drainage_cache) c->drainage_cache = host_drainage_cache_new();
+  // hydro-only runs never change elevations
   host_drainage_and_points(&v.p, elev.data(), rf.data(), s.baseflow, area.data(), c->h_cin_x,
-                           c->h_cin_y, &total, s.catchment_input_counter);
+                           c->h_cin_y, &total, s.catchment_input_counter, c->drainage_cache,
+                           v.p.hydro_only != 0);
   s.totalinputpoints = total;
   const size_t ncin = (size_t)v.imax * v.jmax + 2;
   HC_CU(cudaMemcpy(v.area, area.data(), N2 * 8, cudaMemcpyHostToDevice), "points");
@@ -801,6 +821,83 @@ static void launch_iteration(hc_ctx* c, int flags) {
   if (!c->v.p.hydro_only) launch_slide3(c, 1);
 }
 
+// Adds an IF node at the current capture position of c->s whose body is
+// captured from the launches `fn` issues (on the side stream).
+template <class F>
+static hc_status capture_if(hc_ctx* c, cudaGraphConditionalHandle h, F fn) {
+  cudaStreamCaptureStatus st;
+  cudaGraph_t cg;
+  const cudaGraphNode_t* deps = nullptr;
+  size_t nd = 0;
+  HC_CU(cudaStreamGetCaptureInfo(c->s, &st, nullptr, &cg, &deps, nullptr, &nd), "capture info");
+  cudaGraphNodeParams prm = {};
+  prm.type = cudaGraphNodeTypeConditional;
+  prm.conditional.handle = h;
+  prm.conditional.type = cudaGraphCondTypeIf;
+  prm.conditional.size = 1;
+  cudaGraphNode_t node;
+  HC_CU(cudaGraphAddNode(&node, cg, deps, nullptr, nd, &prm), "conditional node");
+  cudaGraph_t body = prm.conditional.phGraph_out[0];
+  HC_CU(cudaStreamBeginCaptureToGraph(c->s2, body, nullptr, nullptr, 0,
+                                      cudaStreamCaptureModeRelaxed), "body capture");
+  c->cs = c->s2;
+  fn();
+  c->cs = c->s;
+  cudaGraph_t out;
+  HC_CU(cudaStreamEndCapture(c->s2, &out), "body capture");
+  HC_CU(cudaStreamUpdateCaptureDependencies(c->s, &node, nullptr, 1,
+                                            cudaStreamSetCaptureDependencies), "dependencies");
+  return HC_OK;
+}
+
+// One iteration as captured into the graph: the same launches as
+// launch_iteration, with the steps that are not due every iteration behind
+// IF nodes (scan_area, the erosion block and its extra passes, slide_3).
+static hc_status capture_iteration(hc_ctx* c, int flags) {
+  cudaStreamCaptureStatus st;
+  cudaGraph_t cg;
+  HC_CU(cudaStreamGetCaptureInfo(c->s, &st, nullptr, &cg, nullptr, nullptr, nullptr), "capture info");
+  hc_iter_handles& H = c->hcur;
+  std::memset(&H, 0, sizeof H);
+  const bool sed = !c->v.p.hydro_only;
+  auto mk = [&](cudaGraphConditionalHandle* h) {
+    return cudaGraphConditionalHandleCreate(h, cg, 0, cudaGraphCondAssignDefault);
+  };
+  HC_CU(mk(&H.scan), "handle");
+  if (sed) {
+    HC_CU(mk(&H.erode), "handle");
+    HC_CU(mk(&H.retry2), "handle");
+    HC_CU(mk(&H.retry3), "handle");
+    HC_CU(mk(&H.retry4), "handle");
+    HC_CU(mk(&H.erode_fin), "handle");
+    HC_CU(mk(&H.slide), "handle");
+  }
+  H.has = 1;
+  launch_control(c);
+  H.has = 0;  // no other launch sets the iteration's conditions
+  launch_inputs(c);
+  launch_flow_route(c, 1);
+  launch_depth_update(c, 1);
+  HC_TRY(capture_if(c, H.scan, [&] { launch_scan_area(c, 1); }));
+  if (sed) {
+    const hc_iter_handles h = H;
+    HC_TRY(capture_if(c, h.erode, [&] {
+      launch_erode_begin(c, 1, -1);
+      launch_erode_pass(c, HC_ERODE_PASSES, h.retry2, 1);
+    }));
+    HC_TRY(capture_if(c, h.retry2, [&] { launch_erode_pass(c, HC_ERODE_PASSES, h.retry3, 1); }));
+    HC_TRY(capture_if(c, h.retry3, [&] { launch_erode_pass(c, HC_ERODE_PASSES, h.retry4, 1); }));
+    HC_TRY(capture_if(c, h.retry4, [&] { launch_erode_pass(c, HC_ERODE_PASSES); }));
+    HC_TRY(capture_if(c, h.erode_fin, [&] { launch_erode_finish(c, 1); }));
+    if (flags & HC_RUN_LATERAL) launch_lateral_check(c);
+    launch_flux_out(c, 1, 1);
+    HC_TRY(capture_if(c, h.slide, [&] { launch_slide3(c, 1); }));
+  } else {
+    launch_flux_out(c, 1, 1);
+  }
+  return HC_OK;
+}
+
 static int graph_chunk() {
   const char* e = getenv("HC_GRAPH_ITERS");
   int k = e ? atoi(e) : 32;
@@ -812,11 +909,21 @@ static hc_status build_graph(hc_ctx* c, int flags) {
   c->graph = nullptr;
   const int K = graph_chunk();
   cudaGraph_t g;
-  HC_CU(cudaStreamBeginCapture(c->s, cudaStreamCaptureModeThreadLocal), "capture");
+  HC_CU(cudaStreamBeginCapture(c->s, cudaStreamCaptureModeRelaxed), "capture");
   c->capturing = true;
-  for (int k = 0; k < K; k++) launch_iteration(c, flags);
+  hc_status cst = HC_OK;
+  for (int k = 0; k < K && cst == HC_OK; k++) cst = capture_iteration(c, flags);
   c->capturing = false;
-  HC_CU(cudaStreamEndCapture(c->s, &g), "capture");
+  c->cs = c->s;
+  std::memset(&c->hcur, 0, sizeof c->hcur);
+  cudaError_t ee = cudaStreamEndCapture(c->s, &g);
+  if (cst != HC_OK) {
+    if (ee == cudaSuccess) cudaGraphDestroy(g);
+    return cst;
+  }
+  HC_CU(ee, "capture");
+  // kernel nodes outside conditional bodies run on every launch; those
+  // inside run only when their condition is set (counted by the device)
   size_t nn = 0;
   cudaGraphGetNodes(g, nullptr, &nn);
   std::vector<cudaGraphNode_t> nodes(nn);
@@ -925,9 +1032,11 @@ extern "C" hc_status hc_run(hc_ctx* c, int64_t n, int32_t flags, hc_step_record*
   if (!c->graph_iters || c->graph_flags != flags) HC_TRY(build_graph(c, flags));
   int64_t ran = 0;
   while (true) {
+    const unsigned long long bk0 = hd->body_kernels;
     HC_CU(cudaGraphLaunch(c->graph, c->s), "graph launch");
     c->launches += c->graph_kernels;
     HC_TRY(pull(c));
+    c->launches += (int64_t)(hd->body_kernels - bk0);
     if (hd->pause & HC_PAUSE_ERROR)
       return hc_fail(c, HC_ERR_STATE, "device error %d", hd->err_code);
     if (hd->pause & (HC_PAUSE_ERODE | HC_PAUSE_LATERAL)) HC_TRY(finish_iteration(c, flags));

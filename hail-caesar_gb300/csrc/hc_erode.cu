@@ -58,7 +58,8 @@ __global__ void k_erode_begin(const hc_view c, hc_dev* d, int gated, double mult
 // ---------------------------------------------------------------------------
 // entrainment pass
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(128) k_entrain(const hc_view c, hc_dev* d, int max_passes) {
+__global__ void __launch_bounds__(128) k_entrain(const hc_view c, hc_dev* d, int max_passes,
+                                                  cudaGraphConditionalHandle next, int has_next) {
   __shared__ double wmax[4];
   __shared__ bool last;
   if (!(d->it_active && d->erode_retry)) return;
@@ -134,6 +135,10 @@ __global__ void __launch_bounds__(128) k_entrain(const hc_view c, hc_dev* d, int
             for (int n = 1; n <= HC_G; n++) graintot += GRN(c, cell, n);
           }
           double temptot1 = 0;
+          const double mts = mult * ts;
+          // Einstein: 1 / ((1650 Di) / (tau/g)); the nine quotients by tau/g
+          // share one reciprocal (div_const, exact)
+          const double Bq = tau / kG, rB = 1.0 / Bq;
           for (int n = 1; n <= HC_G - 1; n++) {
             const double Di = p.d[n];
             double td = 0;
@@ -148,11 +153,13 @@ __global__ void __launch_bounds__(128) k_entrain(const hc_view c, hc_dev* d, int
                 Wi_star = 0.002 * pow(tau / tau_ri, 7.5);
               else
                 Wi_star = 14 * pow(1 - (0.894 / sqrt(tau / tau_ri)), 4.5);
-              td = mult * ts * ((Fi * (U_star * U_star * U_star)) / ((2.65 - 1) * kG)) * Wi_star / DX;
+              td = div_const(mts * ((Fi * (U_star * U_star * U_star)) / ((2.65 - 1) * kG)) * Wi_star,
+                             DX, c.rDX);
             }
             if (p.einstein) {
-              td = mult * ts * (40 * cube_rn((1 / (((2650 - 1000) * Di) / (tau / kG))))) /
-                   sqrt(1000 / ((2250 - 1000) * kG * (Di * Di * Di))) / DX;
+              const double x = div_const(c.einA[n], Bq, rB);
+              td = div_const(div_const(mts * (40 * cube_rn(1 / x)), c.einS[n], c.einRS[n]), DX,
+                             c.rDX);
             }
             if (td > GRN(c, cell, n)) td = GRN(c, cell, n);
             if (p.isSuspended[n] && n == 1) {
@@ -243,6 +250,10 @@ __global__ void __launch_bounds__(128) k_entrain(const hc_view c, hc_dev* d, int
       }
     } else {
       d->erode_retry = 0;
+    }
+    if (has_next) {
+      cudaGraphSetConditional(next, d->erode_retry ? 1u : 0u);
+      if (d->erode_retry) d->body_kernels += 6;  // the next pass's kernels
     }
     d->s.tempbmax = tempbmax;  // tempbmax of the last pass
   }
@@ -410,55 +421,74 @@ __device__ __forceinline__ bool apply_active(const hc_view& c, size_t cell, int 
   return c.mask[cell] && c.h[cell] > c.p.water_depth_erosion_threshold && x < c.imax && x > 1;
 }
 
-__global__ void __launch_bounds__(256) k_apply_et3(const hc_view c, const hc_dev* d) {
+// Per-cell terms of the apply pass that depend on the cell's own state and
+// the (constant) outgoing fluxes only, computed for all cells in parallel:
+// plane n (1..9) = incoming - outgoing bedload of fraction n, plane 0 =
+// settled suspended load Vpdrop, plane 10 = erodetot.  The new Vsusptot is
+// written directly (nothing else in the pass touches it).  The chain walker
+// then applies them in the reference's order.
+__device__ __forceinline__ double& PRE(const hc_view& c, int k, size_t cell) {
+  return c.pre[(size_t)k * c.N2 + cell];
+}
+
+__global__ void __launch_bounds__(256) k_apply_pre(const hc_view c, const hc_dev* d) {
   if (!(d->it_active && d->rest_active && d->do_erode) || d->erode_retry) return;
   const int y = 2 + blockIdx.x * blockDim.x + threadIdx.x;
   const int x = 1 + blockIdx.y * blockDim.y + threadIdx.y;
   if (y > c.jmax - 1 || x > c.imax) return;
   const size_t cell = (size_t)x * c.W + y;
+  const size_t W = c.W;
   double et3 = 0;
   if (apply_active(c, cell, x)) {
+    const hc_params& p = c.p;
+    const double ts = d->s.time_step;
+    double erodetot = 0;
     for (int n = 1; n <= HC_G - 1; n++) {
-      if (n == 1 && c.p.isSuspended[n]) continue;
-      et3 += (SF(c, 0, n, cell) + SF(c, 1, n, cell) + SF(c, 2, n, cell) + SF(c, 3, n, cell));
+      if (n == 1 && p.isSuspended[n]) {
+        const double ssv = c.ss[cell];
+        double vs = c.vs[cell] + ssv;
+        erodetot -= ssv;
+        // inputpointsarray is all false in the reference (zero_values clears
+        // it after the reach block), so settling applies everywhere
+        double coeff = (p.fallVelocity[n] * ts) / c.h[cell];
+        if (coeff > 1) coeff = 1;
+        double Vpdrop = coeff * vs;
+        if (Vpdrop > 0.001) Vpdrop = 0.001;
+        erodetot += Vpdrop;
+        vs -= Vpdrop;
+        c.vs[cell] = vs;
+        PRE(c, 0, cell) = Vpdrop;
+      } else {
+        double val1 = (SF(c, 0, n, cell) + SF(c, 1, n, cell) + SF(c, 2, n, cell) +
+                       SF(c, 3, n, cell));
+        double val2 = (SF(c, 0, n, cell + 1) + SF(c, 2, n, cell - 1) + SF(c, 3, n, cell + W) +
+                       SF(c, 1, n, cell - W));
+        const double dn = val2 - val1;
+        PRE(c, n, cell) = dn;
+        erodetot += dn;
+        et3 += val1;
+      }
     }
+    PRE(c, 10, cell) = erodetot;
   }
   c.erodetot3[cell] = et3;
 }
 
 // one cell of the gather-apply pass with its +/-x lateral step (:4579-4680)
-__device__ void apply_cell(const hc_view& c, hc_dev* d, size_t cell, int x, int y, double mult,
-                           double ts) {
+__device__ __forceinline__ void apply_cell(const hc_view& c, hc_dev* d, size_t cell, int x, int y,
+                                           double mult, double ts) {
   const hc_params& p = c.p;
   const size_t W = c.W;
-  const double h = c.h[cell];
-  double erodetot = 0, et3 = 0;
   for (int n = 1; n <= HC_G - 1; n++) {
     if (n == 1 && p.isSuspended[n]) {
-      const double ssv = c.ss[cell];
-      double vs = c.vs[cell] + ssv;
-      GRN(c, cell, n) -= ssv;
-      erodetot -= ssv;
-      // inputpointsarray is all false in the reference (zero_values clears it
-      // after the reach block), so settling applies everywhere
-      double coeff = (p.fallVelocity[n] * ts) / h;
-      if (coeff > 1) coeff = 1;
-      double Vpdrop = coeff * vs;
-      if (Vpdrop > 0.001) Vpdrop = 0.001;
-      GRN(c, cell, n) += Vpdrop;
-      erodetot += Vpdrop;
-      vs -= Vpdrop;
-      c.vs[cell] = vs;
+      double g = GRN(c, cell, n) - c.ss[cell];
+      GRN(c, cell, n) = g + PRE(c, 0, cell);
     } else {
-      double val1 = (SF(c, 0, n, cell) + SF(c, 1, n, cell) + SF(c, 2, n, cell) +
-                     SF(c, 3, n, cell));
-      double val2 = (SF(c, 0, n, cell + 1) + SF(c, 2, n, cell - 1) + SF(c, 3, n, cell + W) +
-                     SF(c, 1, n, cell - W));
-      GRN(c, cell, n) += val2 - val1;
-      erodetot += val2 - val1;
-      et3 += val1;
+      GRN(c, cell, n) += PRE(c, n, cell);
     }
   }
+  const double erodetot = PRE(c, 10, cell);
+  const double et3 = c.erodetot3[cell];
   double e0 = c.elev[cell] + erodetot;
   c.elev[cell] = e0;
   if (erodetot < 0) sort_active_dev(c, d, cell, false);
@@ -740,29 +770,29 @@ size_t erode_scratch_bytes(size_t N2, int imax, int jmax) {
 }
 
 void launch_erode_begin(hc_ctx* c, int gated, double mult) {
-  k_erode_begin<<<1, 1, 0, c->s>>>(c->v, c->dev, gated, mult);
+  k_erode_begin<<<1, 1, 0, c->cs>>>(c->v, c->dev, gated, mult);
   count_launch(c, 1);
 }
 
-void launch_erode_pass(hc_ctx* c, int max_passes) {
+void launch_erode_pass(hc_ctx* c, int max_passes, cudaGraphConditionalHandle next, int has_next) {
   ErodeScratch s = scratch_of(c);
   dim3 b(32, 4);
   dim3 g((c->v.jmax - 1 + b.x - 1) / b.x, (c->v.imax + b.y - 1) / b.y);
   if (g.x < 1) g.x = 1;
-  k_entrain<<<g, b, 0, c->s>>>(c->v, c->dev, max_passes);
+  k_entrain<<<g, b, 0, c->cs>>>(c->v, c->dev, max_passes, next, has_next);
   count_launch(c, 1);
   size_t nwords = c->v.N2 / 4 + 1;
   int nb = (int)((c->v.N2 + 255) / 256);
-  k_alloc_mark<<<nb, 256, 0, c->s>>>(c->v, c->dev, s.bits);
+  k_alloc_mark<<<nb, 256, 0, c->cs>>>(c->v, c->dev, s.bits);
   count_launch(c, 1);
   int nblocks = (int)((nwords + 1023) / 1024);
-  k_alloc_count<<<nblocks, 1024, 0, c->s>>>(c->v, c->dev, s.bits, s.block_sums, nwords);
+  k_alloc_count<<<nblocks, 1024, 0, c->cs>>>(c->v, c->dev, s.bits, s.block_sums, nwords);
   count_launch(c, 1);
-  k_alloc_scan_blocks<<<1, 1024, 0, c->s>>>(c->dev, s.block_sums, nblocks, s.total);
+  k_alloc_scan_blocks<<<1, 1024, 0, c->cs>>>(c->dev, s.block_sums, nblocks, s.total);
   count_launch(c, 1);
-  k_alloc_assign<<<nblocks, 1024, 0, c->s>>>(c->v, c->dev, s.bits, s.block_sums, nwords);
+  k_alloc_assign<<<nblocks, 1024, 0, c->cs>>>(c->v, c->dev, s.bits, s.block_sums, nwords);
   count_launch(c, 1);
-  k_alloc_finish<<<1, 1, 0, c->s>>>(c->dev, s.total);
+  k_alloc_finish<<<1, 1, 0, c->cs>>>(c->dev, s.total);
   count_launch(c, 1);
 }
 
@@ -770,19 +800,19 @@ void launch_erode_finish(hc_ctx* c, int gated) {
   ErodeScratch s = scratch_of(c);
   dim3 b(32, 8);
   dim3 g((c->v.jmax - 2 + 31) / 32, (c->v.imax + 7) / 8);
-  k_apply_et3<<<g, b, 0, c->s>>>(c->v, c->dev);
+  k_apply_pre<<<g, b, 0, c->cs>>>(c->v, c->dev);
   count_launch(c, 1);
-  k_apply_xchains<<<g, b, 0, c->s>>>(c->v, c->dev);
+  k_apply_xchains<<<g, b, 0, c->cs>>>(c->v, c->dev);
   count_launch(c, 1);
-  k_apply_ychains<<<g, b, 0, c->s>>>(c->v, c->dev);
+  k_apply_ychains<<<g, b, 0, c->cs>>>(c->v, c->dev);
   count_launch(c, 1);
-  k_edge_out<<<1, 1024, 0, c->s>>>(c->v, c->dev, s.contrib, nullptr);
+  k_edge_out<<<1, 1024, 0, c->cs>>>(c->v, c->dev, s.contrib, nullptr);
   count_launch(c, 1);
-  k_erode_post<<<1, 1, 0, c->s>>>(c->v, c->dev, gated);
+  k_erode_post<<<1, 1, 0, c->cs>>>(c->v, c->dev, gated);
   count_launch(c, 1);
 }
 
 void launch_lateral_check(hc_ctx* c) {
-  k_lateral_check<<<1, 1, 0, c->s>>>(c->v, c->dev);
+  k_lateral_check<<<1, 1, 0, c->cs>>>(c->v, c->dev);
   count_launch(c, 1);
 }

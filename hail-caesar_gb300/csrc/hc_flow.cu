@@ -52,7 +52,7 @@ __device__ void topmodel_step(hc_dev* d, const hc_params& p, const double* topm,
   }
 }
 
-__global__ void k_control(const hc_view c, hc_dev* d) {
+__global__ void k_control(const hc_view c, hc_dev* d, hc_iter_handles hh) {
   const hc_params& p = c.p;
   hc_scalars& s = d->s;
   if (d->pause || d->budget <= 0) {
@@ -180,6 +180,17 @@ __global__ void k_control(const hc_view c, hc_dev* d) {
   d->do_erode = !p.hydro_only && s.counter >= s.erode_call;
   d->erode_retry = d->do_erode;
   d->do_slide = !p.hydro_only && ((long long)s.counter % p.in_channel_landslide_iter_interval) == 0;
+  if (hh.has) {
+    // kernels inside the bodies enabled here: scan 4, erosion 7 + 5, slide_3 5
+    d->body_kernels += (d->do_scan ? 4 : 0) + (d->do_erode && !p.hydro_only ? 12 : 0) +
+                       (d->do_slide ? 5 : 0);
+    cudaGraphSetConditional(hh.scan, d->do_scan ? 1u : 0u);
+    if (!p.hydro_only) {
+      cudaGraphSetConditional(hh.erode, d->do_erode ? 1u : 0u);
+      cudaGraphSetConditional(hh.erode_fin, d->do_erode ? 1u : 0u);
+      cudaGraphSetConditional(hh.slide, d->do_slide ? 1u : 0u);
+    }
+  }
 }
 
 // catchment input points (:3463-3477): one thread per point
@@ -305,15 +316,10 @@ __device__ __forceinline__ void inertial_face(double& q, double& qs, double& vel
 // reference's qxs/qys are signed zeros and vel_dir is never read: both are
 // left untouched.
 template <bool kSed>
-__global__ void __launch_bounds__(256) k_flow_route(const hc_view c, const hc_dev* __restrict__ d,
-                                                     int gated) {
-  if (gated && !d->it_active) return;
-  const int j = 1 + blockIdx.x * blockDim.x + threadIdx.x;
-  const int i = 1 + blockIdx.y * blockDim.y + threadIdx.y;
-  if (i > c.imax || j > c.jmax) return;
+__device__ __forceinline__ void flow_cell(const hc_view& c, const hc_dev* __restrict__ d,
+                                          size_t cell) {
   const size_t W = c.W, N2 = c.N2;
-  const size_t cell = (size_t)i * W + j;
-  if (!c.mask[cell]) return;
+  const int i = (int)(cell / W), j = (int)(cell % W);
   const double e0 = c.elev[cell];
   if (!(e0 > -9999)) return;
   const hc_params& p = c.p;
@@ -373,6 +379,17 @@ __global__ void __launch_bounds__(256) k_flow_route(const hc_view c, const hc_de
   }
 }
 
+// One thread per wet cell, grid-stride over the wet list: cells outside the
+// mask are never touched, as in the reference's down_scan loops.
+template <bool kSed>
+__global__ void __launch_bounds__(256) k_flow_route(const hc_view c, const hc_dev* __restrict__ d,
+                                                     int gated) {
+  if (gated && !d->it_active) return;
+  const int n = d->wet_count;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
+    flow_cell<kSed>(c, d, (size_t)c.wet[k]);
+}
+
 // ---------------------------------------------------------------------------
 // depth_update :3259-3299 with the maxdepth reduction (warp shuffle, block,
 // then the last block publishes the grid result).
@@ -381,38 +398,35 @@ __global__ void __launch_bounds__(256) k_depth_update(const hc_view c, hc_dev* d
   __shared__ double warp_max[8];
   __shared__ bool last;
   if (gated && !d->it_active) return;
-  const int j = 1 + blockIdx.x * blockDim.x + threadIdx.x;
-  const int i = 1 + blockIdx.y * blockDim.y + threadIdx.y;
+  const size_t W = c.W;
+  const double dt = d->s.flow_timestep, DX = c.p.DX, rDX = c.rDX;
+  const bool susp = c.p.isSuspended[1] && !c.p.hydro_only;
+  const int nw = d->wet_count;
   double m = 0;
-  if (i <= c.imax && j <= c.jmax) {
-    const size_t W = c.W;
-    const size_t cell = (size_t)i * W + j;
-    if (c.mask[cell]) {
-      const double dt = d->s.flow_timestep, DX = c.p.DX, rDX = c.rDX;
-      double h = c.h[cell];
-      h += div_const(dt * (c.qx[cell + W] - c.qx[cell] + c.qy[cell + 1] - c.qy[cell]), DX, rDX);
-      // hydro-only runs keep Vsusptot at zero (no sediment source exists)
-      if (c.p.isSuspended[1] && !c.p.hydro_only)
-        c.vs[cell] += div_const(dt * (c.qxs[cell + W] - c.qxs[cell] + c.qys[cell + 1] - c.qys[cell]),
-                                DX, rDX);
-      if (h > 0) {
-        if (c.elev[cell] == -9999) h = 0;
-        if (h > m) m = h;
-      }
-      c.h[cell] = h;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nw; k += gridDim.x * blockDim.x) {
+    const size_t cell = (size_t)c.wet[k];
+    double h = c.h[cell];
+    h += div_const(dt * (c.qx[cell + W] - c.qx[cell] + c.qy[cell + 1] - c.qy[cell]), DX, rDX);
+    // hydro-only runs keep Vsusptot at zero (no sediment source exists)
+    if (susp)
+      c.vs[cell] += div_const(dt * (c.qxs[cell + W] - c.qxs[cell] + c.qys[cell + 1] - c.qys[cell]),
+                              DX, rDX);
+    if (h > 0) {
+      if (c.elev[cell] == -9999) h = 0;
+      if (h > m) m = h;
     }
+    c.h[cell] = h;
   }
   for (int o = 16; o > 0; o >>= 1) m = smax(m, __shfl_xor_sync(0xffffffffu, m, o));
-  const int t = threadIdx.y * blockDim.x + threadIdx.x;
+  const int t = threadIdx.x;
   if ((t & 31) == 0) warp_max[t >> 5] = m;
   __syncthreads();
   if (t == 0) {
     double b = 0;
-    for (int w = 0; w < (int)(blockDim.x * blockDim.y) / 32; w++) b = smax(b, warp_max[w]);
+    for (int w = 0; w < (int)blockDim.x / 32; w++) b = smax(b, warp_max[w]);
     if (b > 0) atomic_max_pos(&d->maxdepth_bits, b);
     __threadfence();
-    unsigned int nb = gridDim.x * gridDim.y;
-    last = (atomicAdd(&d->depth_done, 1u) == nb - 1);
+    last = (atomicAdd(&d->depth_done, 1u) == gridDim.x - 1);
   }
   __syncthreads();
   if (last && t == 0) {
@@ -440,6 +454,73 @@ __global__ void __launch_bounds__(256) k_scan_area(const hc_view c, const hc_dev
              h[cell - W - 1] > 0 || h[cell - W + 1] > 0 || h[cell + W - 1] > 0 ||
              h[cell + W + 1] > 0 || h[cell + W] > 0;
   c.mask[cell] = wet ? 1 : 0;
+}
+
+// The wet list: mask bytes counted per block of 1024 cells, the counts
+// scanned, the cell numbers written in ascending order.
+__global__ void __launch_bounds__(1024) k_wet_count(const hc_view c, const hc_dev* d, int gated) {
+  __shared__ int ws[32];
+  if (gated && !(d->it_active && d->do_scan)) return;
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int v = (i < c.N2) ? c.mask[i] : 0;
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int s = 0;
+    for (int k = 0; k < 32; k++) s += ws[k];
+    c.wet_sums[blockIdx.x] = s;
+  }
+}
+
+__global__ void __launch_bounds__(1024) k_wet_scan(const hc_view c, hc_dev* d, int nblocks,
+                                                   int gated) {
+  __shared__ int buf[1024];
+  __shared__ int carry;
+  if (gated && !(d->it_active && d->do_scan)) return;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (int base = 0; base < nblocks; base += 1024) {
+    const int k = base + threadIdx.x;
+    const int v = (k < nblocks) ? c.wet_sums[k] : 0;
+    buf[threadIdx.x] = v;
+    __syncthreads();
+    for (int off = 1; off < 1024; off <<= 1) {
+      const int t = (threadIdx.x >= (unsigned)off) ? buf[threadIdx.x - off] : 0;
+      __syncthreads();
+      buf[threadIdx.x] += t;
+      __syncthreads();
+    }
+    if (k < nblocks) c.wet_sums[k] = carry + buf[threadIdx.x] - v;
+    __syncthreads();
+    if (threadIdx.x == 1023) carry += buf[1023];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) d->wet_count = carry;
+}
+
+__global__ void __launch_bounds__(1024) k_wet_write(const hc_view c, const hc_dev* d, int gated) {
+  __shared__ int ws[32], wb[32];
+  if (gated && !(d->it_active && d->do_scan)) return;
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int v = (i < c.N2) ? c.mask[i] : 0;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int incl = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int t = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += t;
+  }
+  if (lane == 31) ws[warp] = incl;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int s = 0;
+    for (int k = 0; k < 32; k++) {
+      wb[k] = s;
+      s += ws[k];
+    }
+  }
+  __syncthreads();
+  if (v) c.wet[c.wet_sums[blockIdx.x] + wb[warp] + incl - 1] = (int32_t)i;
 }
 
 // ---------------------------------------------------------------------------
@@ -526,7 +607,7 @@ static dim3 grid2d(const hc_ctx* c, dim3 b) {
 }
 
 void launch_control(hc_ctx* c) {
-  k_control<<<1, 1, 0, c->s>>>(c->v, c->dev);
+  k_control<<<1, 1, 0, c->cs>>>(c->v, c->dev, c->hcur);
   count_launch(c, 1);
 }
 
@@ -535,37 +616,51 @@ void launch_inputs(hc_ctx* c) {
   int n = c->v.cin_cap;
   int blocks = std::min((n + 255) / 256, 152 * 4);
   if (blocks < 1) blocks = 1;
-  k_inputs<<<blocks, 256, 0, c->s>>>(c->v, c->dev);
+  k_inputs<<<blocks, 256, 0, c->cs>>>(c->v, c->dev);
   count_launch(c, 1);
 }
 
 void launch_flow_dt(hc_ctx* c) {
-  k_flow_dt<<<1, 1, 0, c->s>>>(c->v, c->dev);
+  k_flow_dt<<<1, 1, 0, c->cs>>>(c->v, c->dev);
   count_launch(c, 1);
 }
 
+// grid-stride kernels over the wet list: enough blocks to fill the GPU, no
+// more (the list length lives on the device)
+static int list_blocks(const hc_ctx* c) {
+  const size_t need = (c->v.N2 + 255) / 256;
+  return (int)std::min<size_t>(need, 152 * 8);
+}
+
 void launch_flow_route(hc_ctx* c, int gated) {
-  dim3 b(32, 8);
   if (c->v.p.hydro_only)
-    k_flow_route<false><<<grid2d(c, b), b, 0, c->s>>>(c->v, c->dev, gated);
+    k_flow_route<false><<<list_blocks(c), 256, 0, c->cs>>>(c->v, c->dev, gated);
   else
-    k_flow_route<true><<<grid2d(c, b), b, 0, c->s>>>(c->v, c->dev, gated);
+    k_flow_route<true><<<list_blocks(c), 256, 0, c->cs>>>(c->v, c->dev, gated);
   count_launch(c, 1);
 }
 
 void launch_depth_update(hc_ctx* c, int gated) {
-  dim3 b(32, 8);
-  k_depth_update<<<grid2d(c, b), b, 0, c->s>>>(c->v, c->dev, gated);
+  k_depth_update<<<list_blocks(c), 256, 0, c->cs>>>(c->v, c->dev, gated);
   count_launch(c, 1);
 }
 
 void launch_scan_area(hc_ctx* c, int gated) {
   dim3 b(32, 8);
-  k_scan_area<<<grid2d(c, b), b, 0, c->s>>>(c->v, c->dev, gated);
+  k_scan_area<<<grid2d(c, b), b, 0, c->cs>>>(c->v, c->dev, gated);
   count_launch(c, 1);
+  launch_wet_list(c, gated);
+}
+
+void launch_wet_list(hc_ctx* c, int gated) {
+  const int nb = (int)((c->v.N2 + 1023) / 1024);
+  k_wet_count<<<nb, 1024, 0, c->cs>>>(c->v, c->dev, gated);
+  k_wet_scan<<<1, 1024, 0, c->cs>>>(c->v, c->dev, nb, gated);
+  k_wet_write<<<nb, 1024, 0, c->cs>>>(c->v, c->dev, gated);
+  count_launch(c, 3);
 }
 
 void launch_flux_out(hc_ctx* c, int gated, int record) {
-  k_flux_out<<<1, 1024, 0, c->s>>>(c->v, c->dev, gated, record, c->v.rec, c->v.rec_cap);
+  k_flux_out<<<1, 1024, 0, c->cs>>>(c->v, c->dev, gated, record, c->v.rec, c->v.rec_cap);
   count_launch(c, 1);
 }

@@ -33,18 +33,34 @@ HC_DEV void sort_active_dev(const hc_view& c, hc_dev* d, size_t cell, bool may_a
     }
   }
   const double active = c.p.active;
+  // total of the record decides between "deposit a stratum", "eat into the
+  // stratum below" and nothing.  A float sum with a bound on its error
+  // decides the two tests; the FP64 sum of the reference (needed anyway when
+  // a stratum moves) is formed only when the float sum is too close to call.
+  double g[HC_G + 1];
+  float sf = 0.0f, af = 0.0f;
+  for (int n = 0; n <= HC_G; n++) {
+    g[n] = GRN(c, cell, n);
+    const float f = approx_f(g[n]);
+    sf += f;
+    af += fabsf(f);
+  }
+  const float tol = 1e-5f * af + 1e-30f;
+  const float hi = (float)(active * 1.5), lo = (float)(active / 4);
+  int dep = (sf > hi + tol) ? 1 : ((sf < hi - tol) ? -1 : 0);
+  int ero = (sf < lo - tol) ? 1 : ((sf > lo + tol) ? -1 : 0);
+  if (dep == -1 && ero == -1) return;
   double total = 0.0;
-  for (int n = 0; n <= HC_G; n++) total += GRN(c, cell, n);
+  for (int n = 0; n <= HC_G; n++) total += g[n];
   if (total > (active * 1.5)) {
     for (int z = 9; z >= 1; z--)
       for (int n = 0; n <= HC_G - 2; n++) STR(c, cell, z, n) = STR(c, cell, z - 1, n);
     double coeff = active / total;
     for (int n = 1; n <= HC_G - 1; n++) {
-      double g = GRN(c, cell, n);
-      if (g > 0.0) {
-        double amount = coeff * (g);
+      if (g[n] > 0.0) {
+        double amount = coeff * (g[n]);
         STR(c, cell, 0, n - 1) = amount;
-        GRN(c, cell, n) = g - amount;
+        GRN(c, cell, n) = g[n] - amount;
       }
     }
   }
@@ -99,11 +115,16 @@ HC_DEV void slide_GS_dev(const hc_view& c, hc_dev* d, size_t a, double amount, s
       amount = total;
     }
     if (total > 0) {
+      // grain/total for the nine fractions: one reciprocal, then the exact
+      // quotient of each (div_const)
+      const double rt = 1.0 / total;
       for (int n = 1; n <= HC_G - 1; n++) {
-        double t = amount * (GRN(c, a, n) / total);
+        const double ga = GRN(c, a, n);
+        double t = amount * div_const(ga, total, rt);
         GRN(c, b, n) += t;
-        GRN(c, a, n) -= t;
-        if (GRN(c, a, n) < 0) GRN(c, a, n) = 0;
+        double na = ga - t;
+        if (na < 0) na = 0;
+        GRN(c, a, n) = na;
       }
     }
     sort_active_dev(c, d, a, may_alloc);
@@ -128,11 +149,16 @@ HC_DEV void slide_GS_dev(const hc_view& c, hc_dev* d, size_t a, double amount, s
     }
     for (int n = 1; n <= HC_G - 1; n++)
       if (GRN(c, a, n) > 0) total += GRN(c, a, n);
-    for (int n = 1; n <= HC_G - 1; n++) {
-      if (total > 0) {
-        GRN(c, b, n) += amount * (GRN(c, a, n) / total);
-        if (GRN(c, a, n) > 0.0001) GRN(c, a, n) -= amount * (GRN(c, a, n) / total);
-        if (GRN(c, a, n) < 0) GRN(c, a, n) = 0;
+    if (total > 0) {
+      const double rt = 1.0 / total;
+      for (int n = 1; n <= HC_G - 1; n++) {
+        const double ga = GRN(c, a, n);
+        const double t = amount * div_const(ga, total, rt);
+        GRN(c, b, n) += t;
+        double na = ga;
+        if (na > 0.0001) na -= t;
+        if (na < 0) na = 0;
+        GRN(c, a, n) = na;
       }
     }
     sort_active_dev(c, d, a, may_alloc);

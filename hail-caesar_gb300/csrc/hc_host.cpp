@@ -11,6 +11,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <cstring>
 #include <utility>
 #include <vector>
@@ -22,12 +23,47 @@ const int kDX[9] = {0, 0, 1, 1, 1, 0, -1, -1, -1};
 const int kDY[9] = {0, -1, -1, 0, 1, 1, 1, 0, -1};
 }
 
+// The reference sorts the row keys and the column keys of all cells in two
+// separate std::sort calls on (key, elevation) pairs.  std::sort's moves
+// depend only on the comparisons, which see only the elevations, so both
+// calls apply the same permutation: one sort carrying the cell number gives
+// both orders, ties included.  The permutation is kept and reused while the
+// elevations are unchanged (always in hydro-only runs).
+struct DrainageCache {
+  std::vector<uint32_t> order;   // cell numbers in the reference's processing order
+  std::vector<double> elev;      // elevations the order was made from
+};
+
+void* host_drainage_cache_new() { return new DrainageCache(); }
+void host_drainage_cache_free(void* p) { delete (DrainageCache*)p; }
+
 void host_drainage_and_points(const hc_params* p, const double* elev, const int32_t* rfarea,
                               double baseflow, double* area, int32_t* cin_x, int32_t* cin_y,
-                              int* total, double* counters) {
+                              int* total, double* counters, void* cache_p, bool elev_fixed) {
   const unsigned imax = p->imax, jmax = p->jmax;
   const size_t W = jmax + 2, N2 = (size_t)(imax + 2) * W;
   auto ix = [&](unsigned i, unsigned j) { return (size_t)i * W + j; };
+  DrainageCache* cache = (DrainageCache*)cache_p;
+  bool reuse = cache && !cache->order.empty();
+  if (reuse && !elev_fixed)
+    reuse = std::memcmp(cache->elev.data(), elev, N2 * sizeof(double)) == 0;
+  if (!reuse) {
+    std::vector<std::pair<double, double>> pr(N2);
+    for (size_t k = 0; k < N2; k++) pr[k] = std::make_pair(0.0, 0.0);
+    size_t inc = 1;
+    for (unsigned i = 1; i <= imax; i++)
+      for (unsigned j = 1; j <= jmax; j++) {
+        pr[inc] = std::make_pair((double)ix(i, j), elev[ix(i, j)]);
+        inc++;
+      }
+    std::sort(pr.begin(), pr.end(),
+              [](const std::pair<double, double>& a, const std::pair<double, double>& b) {
+                return a.second < b.second;
+              });
+    cache->order.resize(N2);
+    for (size_t k = 0; k < N2; k++) cache->order[k] = (uint32_t)pr[k].first;
+    cache->elev.assign(elev, elev + N2);
+  }
   std::vector<double> ad(N2, 0.0);
   for (unsigned i = 1; i <= imax; i++)
     for (unsigned j = 1; j <= jmax; j++) {
@@ -35,25 +71,9 @@ void host_drainage_and_points(const hc_params* p, const double* elev, const int3
       area[ix(i, j)] = 0;
       if (elev[ix(i, j)] == -9999) ad[ix(i, j)] = 0.0;
     }
-  // cells sorted by elevation; the reference sorts the row keys and the column
-  // keys in two separate sorts of (key, elevation) pairs, so ties take
-  // whatever order std::sort gives each sort
-  std::vector<std::pair<double, double>> xp(N2), yp(N2);
-  for (size_t k = 0; k < N2; k++) xp[k] = yp[k] = std::make_pair(0.0, 0.0);
-  size_t inc = 1;
-  for (unsigned i = 1; i <= imax; i++)
-    for (unsigned j = 1; j <= jmax; j++) {
-      xp[inc] = std::make_pair((double)i, elev[ix(i, j)]);
-      yp[inc] = std::make_pair((double)j, elev[ix(i, j)]);
-      inc++;
-    }
-  auto by_second = [](const std::pair<double, double>& a, const std::pair<double, double>& b) {
-    return a.second < b.second;
-  };
-  std::sort(xp.begin(), xp.end(), by_second);
-  std::sort(yp.begin(), yp.end(), by_second);
+  const std::vector<uint32_t>& ord = cache->order;
   for (unsigned n = jmax * imax; n >= 1; n--) {
-    const int i = (int)xp[n].first, j = (int)yp[n].first;
+    const int i = (int)(ord[n] / W), j = (int)(ord[n] % W);
     double& a = ad[ix(i, j)];
     if (!(a > 0)) continue;
     if (a > area[ix(i, j)]) area[ix(i, j)] = a;
@@ -143,4 +163,44 @@ void host_topmodel_table(const hc_params* p, const float* rain, int rows, int co
       row[(rf + 1) + n] = newm[n];
     }
   }
+}
+
+// global_landsliding :5529-5654.  A serial relaxation over the whole grid
+// (x outer, y inner; every test sees the moves before it; up to 200 sweeps
+// until nothing moves).  It changes elevations only and runs once a
+// simulated day, so it runs here on the host, in the reference's order,
+// on a downloaded copy of elev.  Returns the number of sweeps.
+int host_global_landsliding(const hc_params* p, const double* bedrock, double* elev) {
+  const unsigned imax = p->imax, jmax = p->jmax;
+  const size_t W = jmax + 2;
+  const double factor = std::tan((p->failureangle * (3.141592654 / 180))) * p->DX;
+  const double active = p->active, EF = p->ERODEFACTOR;
+  static const int ox[8] = {1, 0, -1, -1, -1, 0, 1, 1};
+  static const int oy[8] = {1, 1, 1, 0, -1, -1, -1, 0};
+  unsigned inc = 0;
+  double total = 0;
+  do {
+    total = 0;
+    inc++;
+    for (unsigned x = 2; x < imax; x++)
+      for (unsigned y = 2; y < jmax; y++) {
+        const size_t c = (size_t)x * W + y;
+        double wet_factor = factor;
+        if (elev[c] <= (bedrock[c] + active)) wet_factor = 10 * p->DX;
+        for (int k = 0; k < 8; k++) {
+          const size_t nb = (size_t)(x + ox[k]) * W + (y + oy[k]);
+          const bool diag = (ox[k] != 0 && oy[k] != 0);
+          const double drop = diag ? ((elev[c] - elev[nb]) / 1.41) : (elev[c] - elev[nb]);
+          if (drop > wet_factor && elev[nb] > -9999) {
+            double diff = (diag ? ((elev[c] - elev[nb]) / 1.41) : (elev[c] - elev[nb])) - wet_factor;
+            if ((elev[c] - diff) < (bedrock[c] + active)) diff = (elev[c] - (bedrock[c] + active));
+            if (diff > EF) diff = EF;
+            elev[c] -= diff;
+            elev[nb] += diff;
+            total += diff;
+          }
+        }
+      }
+  } while (total > 0 && inc < 200);
+  return (int)inc;
 }

@@ -67,6 +67,8 @@ struct hc_dev {
   unsigned int depth_done;   // blocks finished in depth_update (last-block reduction)
   unsigned int pass_done;    // blocks finished in an entrainment pass
   unsigned int misc_done;
+  unsigned long long body_kernels;  // kernels run inside conditional graph nodes
+  int wet_count;          // length of hc_view::wet
 };
 
 // Everything a kernel needs, passed by value (device pointers + parameters).
@@ -87,6 +89,9 @@ struct hc_view {
   int32_t *rfarea;
   double *edge, *edge2, *veg;  // E2, E2, 4*E2 (reference layout)
   int32_t *cin_x, *cin_y;      // catchment input points (1-based lists)
+  int32_t *wet;                // cells of the wet mask, ascending (the down_scan
+                               // lists as one array); length in hc_dev::wet_count
+  int32_t *wet_sums;           // per-block counts for building it
   int cin_cap;
 
   // time series
@@ -94,9 +99,14 @@ struct hc_view {
   float *reach[HC_MAX_POINTS]; int reach_rows[HC_MAX_POINTS], reach_cols[HC_MAX_POINTS];
   double *topm; int topm_rows;   // precomputed TOPMODEL recurrence
   double dlog[HC_G];             // log(d1..d9) for d50
+  // Einstein per-fraction constants, evaluated on the host with the
+  // reference's expressions (:4393-4394): (2650-1000)*Di, the square root
+  // sqrt(1000/((2250-1000)*g*Di^3)) and its reciprocal
+  double einA[HC_G], einS[HC_G], einRS[HC_G];
 
   // scratch
   double *erodetot, *erodetot3;  // N2 each
+  double *pre;                   // 11 * N2: per-cell apply-pass terms (see hc_erode.cu)
   unsigned long long *alloc_key; // N2: serial-order key of the first grain-record request
   int32_t *alloc_list;           // N2: cells allocated, in order
   int32_t *slide_list; int slide_cap;
@@ -106,9 +116,21 @@ struct hc_view {
   hc_step_record *rec; int64_t rec_cap;
 };
 
+// Conditional-node handles of one captured iteration (CUDA graph IF nodes):
+// the control kernel and the entrainment passes set them, so steps that are
+// not due this iteration are not launched at all.
+struct hc_iter_handles {
+  cudaGraphConditionalHandle scan, erode, retry2, retry3, retry4, erode_fin, slide;
+  int has;  // 0 outside graph capture: nothing to set
+};
+
 struct hc_ctx {
   hc_view v;
-  cudaStream_t s;
+  cudaStream_t s;         // the context's stream
+  cudaStream_t cs;        // stream launches go to (a side stream while a
+                          // conditional node's body is captured)
+  cudaStream_t s2;
+  hc_iter_handles hcur;   // handles of the iteration being captured
   int device;
   char err[512];
   size_t bytes, max_bytes;
@@ -119,6 +141,7 @@ struct hc_ctx {
   // host copy of the catchment input list (kept between recomputations, as
   // the reference keeps its vector)
   int32_t *h_cin_x, *h_cin_y;
+  void* drainage_cache;   // sorted cell order, reused while elevations are unchanged
   // CUDA graph of K iterations
   cudaGraphExec_t graph; int graph_iters; int graph_flags;
   int64_t graph_kernels;   // kernel nodes in the graph
@@ -176,6 +199,13 @@ HC_DEV float approx_abs_f(double x) {
   return __int_as_float((e << 23) | ((hi & 0xfffff) << 3));
 }
 
+// Signed variant of approx_abs_f.
+HC_DEV float approx_f(double x) {
+  const int hi = __double2hiint(x);
+  const float a = approx_abs_f(x);
+  return (hi < 0) ? -a : a;
+}
+
 // static_cast<int>(double) as the reference's x86-64 build executes it
 // (cvttsd2si): NaN or out-of-range values give INT_MIN.
 HC_DEV int x86_trunc_to_int(double v) {
@@ -211,14 +241,19 @@ hc_status hc_cuda(hc_ctx* c, cudaError_t e, const char* what);
 
 // phases of one iteration (hc_flow.cu, hc_erode.cu, hc_slide.cu, hc_lateral.cu)
 void launch_control(hc_ctx* c);          // scalar driver logic up to flow_route
+                                         // (sets c->hcur's conditions when capturing)
 void launch_inputs(hc_ctx* c);           // catchment input points
 void launch_flow_dt(hc_ctx* c);          // flow_timestep for member-level calls
 void launch_flow_route(hc_ctx* c, int gated);
 void launch_depth_update(hc_ctx* c, int gated);
 void launch_scan_area(hc_ctx* c, int gated);
+void launch_wet_list(hc_ctx* c, int gated);  // rebuild the wet-cell list from the mask
 void launch_flux_out(hc_ctx* c, int gated, int record);
 void launch_erode_begin(hc_ctx* c, int gated, double mult);
-void launch_erode_pass(hc_ctx* c, int max_passes);
+// next: the conditional handle of the following pass (set when retrying);
+// has_next 0 outside graph capture
+void launch_erode_pass(hc_ctx* c, int max_passes, cudaGraphConditionalHandle next = 0,
+                       int has_next = 0);
 void launch_erode_finish(hc_ctx* c, int gated);
 void launch_lateral_check(hc_ctx* c);
 size_t erode_scratch_bytes(size_t N2, int imax, int jmax);
@@ -231,6 +266,10 @@ size_t slide_scratch_bytes(size_t N2);
 // host helpers (hc_host.cpp)
 void host_drainage_and_points(const hc_params* p, const double* elev, const int32_t* rfarea,
                               double baseflow, double* area_out, int32_t* cin_x,
-                              int32_t* cin_y, int* total, double* counters);
+                              int32_t* cin_y, int* total, double* counters, void* cache,
+                              bool elev_fixed);
+void* host_drainage_cache_new();
+void host_drainage_cache_free(void* p);
+int host_global_landsliding(const hc_params* p, const double* bedrock, double* elev);
 void host_topmodel_table(const hc_params* p, const float* rain, int rows, int cols,
                          int nsteps, double* table /* [nsteps][2][rfnum+1] */);

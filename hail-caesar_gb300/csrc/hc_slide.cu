@@ -1,6 +1,7 @@
 // Slope failure and creep:
 //   in_channel_landsliding :5429-5527 ("slide_3", every 10 iterations)
-//   global_landsliding     :5529-5654 (host-driven, daily)
+//   global_landsliding     :5529-5654 (daily; its serial sweep runs on a host
+//                          core, hc_host.cpp)
 //   creep                  :5293-5427 (host-driven, every 10 days)
 //
 // slide_3 and global landsliding are sequential relaxations: every test sees
@@ -19,6 +20,7 @@
 #include <math.h>
 #include <climits>
 #include <cmath>
+#include <vector>
 
 namespace {
 
@@ -427,18 +429,18 @@ static void slide_sweep(hc_ctx* c, int global, double factor, int gated) {
   dim3 b(32, 8);
   dim3 g((c->v.jmax + b.x - 1) / b.x, (c->v.imax + b.y - 1) / b.y);
   // positions span the whole padded grid; unflagged positions must read 0
-  cudaMemsetAsync(s.flag, 0, c->v.N2, c->s);
-  k_slide_probe<<<g, b, 0, c->s>>>(c->v, c->dev, s.flag, global, factor, gated);
+  cudaMemsetAsync(s.flag, 0, c->v.N2, c->cs);
+  k_slide_probe<<<g, b, 0, c->cs>>>(c->v, c->dev, s.flag, global, factor, gated);
   count_launch(c, 1);
   const size_t n = c->v.N2;
   const int nblocks = (int)((n + 1023) / 1024);
-  k_flag_count<<<nblocks, 1024, 0, c->s>>>(s.flag, n, s.block_sums, c->dev, gated);
+  k_flag_count<<<nblocks, 1024, 0, c->cs>>>(s.flag, n, s.block_sums, c->dev, gated);
   count_launch(c, 1);
-  k_flag_scan<<<1, 1024, 0, c->s>>>(s.block_sums, nblocks, s.count, c->dev, gated);
+  k_flag_scan<<<1, 1024, 0, c->cs>>>(s.block_sums, nblocks, s.count, c->dev, gated);
   count_launch(c, 1);
-  k_flag_compact<<<nblocks, 1024, 0, c->s>>>(s.flag, n, s.block_sums, s.list, c->dev, gated);
+  k_flag_compact<<<nblocks, 1024, 0, c->cs>>>(s.flag, n, s.block_sums, s.list, c->dev, gated);
   count_launch(c, 1);
-  k_slide_replay<<<1, 1, 0, c->s>>>(c->v, c->dev, s.list, s.count, s.heap, s.heap_cap, global,
+  k_slide_replay<<<1, 1, 0, c->cs>>>(c->v, c->dev, s.list, s.count, s.heap, s.heap_cap, global,
                                     factor, s.total, gated);
   count_launch(c, 1);
 }
@@ -452,19 +454,19 @@ static double slide_factor(const hc_ctx* c) {
 void launch_slide3(hc_ctx* c, int gated) { slide_sweep(c, 0, slide_factor(c), gated); }
 
 hc_status run_global_landsliding(hc_ctx* c) {
-  SlideScratch s = slide_scratch(c);
-  const double factor = slide_factor(c);
-  unsigned inc = 0;
-  double total = 0;
-  do {
-    total = 0;
-    inc++;
-    slide_sweep(c, 1, factor, 0);
-    cudaError_t e = cudaMemcpyAsync(&total, s.total, sizeof(double), cudaMemcpyDeviceToHost, c->s);
-    if (e != cudaSuccess) return hc_cuda(c, e, "global_landsliding");
-    e = cudaStreamSynchronize(c->s);
-    if (e != cudaSuccess) return hc_cuda(c, e, "global_landsliding");
-  } while (total > 0 && inc < 200);
+  // a serial sweep over every cell, up to 200 times: one host core runs it
+  // far faster than one GPU thread, and it touches elevations only
+  const size_t N2 = c->v.N2;
+  std::vector<double> elev(N2), bed(N2);
+  cudaError_t e = cudaStreamSynchronize(c->s);
+  if (e == cudaSuccess) e = cudaMemcpy(elev.data(), c->v.elev, N2 * 8, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(bed.data(), c->v.bed, N2 * 8, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return hc_cuda(c, e, "global_landsliding");
+  c->d2h_bytes += 2 * N2 * 8;
+  host_global_landsliding(&c->v.p, bed.data(), elev.data());
+  e = cudaMemcpy(c->v.elev, elev.data(), N2 * 8, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return hc_cuda(c, e, "global_landsliding");
+  c->h2d_bytes += N2 * 8;
   return HC_OK;
 }
 
