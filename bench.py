@@ -178,6 +178,18 @@ def run_gpu(args, rank, world, dist):
     stream = torch.cuda.ExternalStream(model.stream())
     model.run(args.warmup, flags, records=False)
     log("warm-up done")
+    if args.profile_only:
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_push("profiled")
+        prof = [model.profile_iteration(flags) for _ in range(args.profile_only)]
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
+        torch.cuda.nvtx.range_push("kernel")
+        ms_flow, wet = model.bench_kernel("flow_route", 3)
+        torch.cuda.nvtx.range_pop()
+        phases = {k: float(np.mean([p_[k] for p_ in prof])) for k in prof[0]}
+        return {"profile_only": True, "phases_ms": phases, "flow_route_ms": ms_flow,
+                "wet_cells": wet}, model, case
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
@@ -301,6 +313,10 @@ def main():
     ap.add_argument("--timed-only", action="store_true",
                     help="only the timed steps (no e2e, profile, kernel timing or CPU leg); "
                          "for runs under a profiler")
+    ap.add_argument("--profile-only", type=int, default=0, metavar="N",
+                    help="after the warm-up, run N iterations launch by launch (no graph) "
+                         "inside the NVTX range 'profiled', then the dominant kernel alone "
+                         "inside 'kernel'; for profilers that do not see into graphs")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     rank = int(os.environ.get("RANK", "0"))
@@ -315,7 +331,9 @@ def main():
         tdist.init_process_group("nccl")
         dist = tdist
     out, model, case = run_gpu(args, rank, world, dist)
-    if rank == 0 and args.timed_only:
+    if rank == 0 and args.profile_only:
+        print(json.dumps(out))
+    elif rank == 0 and args.timed_only:
         print(json.dumps({"timed_only": True, "ms_per_step": out["ms"] / max(1, out["done"]),
                           "value": out["value"], "launches": out["launches"]}))
     elif rank == 0:

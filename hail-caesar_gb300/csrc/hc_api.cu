@@ -12,6 +12,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
 
 size_t lateral_scratch_bytes(int imax, int jmax);
@@ -351,6 +352,7 @@ static hc_status free_all(hc_ctx* c) {
   if (c->drainage_cache) host_drainage_cache_free(c->drainage_cache);
   free(extra(c).h_rain);
   if (c->graph) cudaGraphExecDestroy(c->graph);
+  if (c->chunk_done) cudaEventDestroy(c->chunk_done);
   if (c->s) cudaStreamDestroy(c->s);
   if (c->s2) cudaStreamDestroy(c->s2);
   drop_extra(c);
@@ -1005,15 +1007,16 @@ static hc_status host_steps(hc_ctx* c, int flags) {
   return HC_OK;
 }
 
-extern "C" hc_status hc_run(hc_ctx* c, int64_t n, int32_t flags, hc_step_record* rec,
-                            int64_t* done) {
+// hc_run in pieces, so that hc_run_ensemble can keep several contexts' graphs
+// in flight at once.
+static hc_status run_begin(hc_ctx* c, int64_t n, int32_t flags, bool want_rec, bool* finished) {
   if (!c || n < 0) return HC_ERR_ARG;
-  if (done) *done = 0;
+  *finished = false;
   if (!c->prepared) return hc_fail(c, HC_ERR_STATE, "hc_prepare must come before hc_run");
   if ((flags & HC_RUN_LATERAL) && c->v.imax != c->v.jmax && !c->v.p.hydro_only)
     return hc_fail(c, HC_ERR_UNSUPPORTED, "lateral3 needs a square grid");
   hc_view& v = c->v;
-  if (rec && v.rec_cap < n) {
+  if (want_rec && v.rec_cap < n) {
     if (v.rec) cudaFree(v.rec);
     v.rec = nullptr;
     v.rec_cap = 0;
@@ -1023,43 +1026,120 @@ extern "C" hc_status hc_run(hc_ctx* c, int64_t n, int32_t flags, hc_step_record*
   }
   HC_TRY(pull(c));
   hc_dev* hd = c->hdev;
-  if (hd->pause & HC_PAUSE_FINISHED) return HC_OK;
+  c->run_n = n;
+  if (hd->pause & HC_PAUSE_FINISHED) {
+    *finished = true;
+    hd->budget = n;  // nothing runs
+    return HC_OK;
+  }
   hd->pause = 0;
   hd->budget = n;
   hd->rec_index = 0;
   hd->flags = flags;
   HC_TRY(push(c));
   if (!c->graph_iters || c->graph_flags != flags) HC_TRY(build_graph(c, flags));
-  int64_t ran = 0;
-  while (true) {
-    const unsigned long long bk0 = hd->body_kernels;
-    HC_CU(cudaGraphLaunch(c->graph, c->s), "graph launch");
-    c->launches += c->graph_kernels;
+  if (!c->chunk_done) HC_CU(cudaEventCreateWithFlags(&c->chunk_done, cudaEventDisableTiming),
+                            "event");
+  return HC_OK;
+}
+
+// one graph chunk, then the control block copied back; chunk_done marks both
+static hc_status run_launch(hc_ctx* c) {
+  c->body_k0 = c->hdev->body_kernels;
+  HC_CU(cudaGraphLaunch(c->graph, c->s), "graph launch");
+  c->launches += c->graph_kernels;
+  c->d2h_bytes += sizeof(hc_dev);
+  HC_CU(cudaMemcpyAsync(c->hdev, c->dev, sizeof(hc_dev), cudaMemcpyDeviceToHost, c->s), "pull");
+  HC_CU(cudaEventRecord(c->chunk_done, c->s), "event");
+  return HC_OK;
+}
+
+// after a chunk: host-side work the device asked for; *finished when done
+static hc_status run_after_chunk(hc_ctx* c, int32_t flags, bool* finished) {
+  hc_dev* hd = c->hdev;
+  *finished = false;
+  c->launches += (int64_t)(hd->body_kernels - c->body_k0);
+  if (hd->pause & HC_PAUSE_ERROR) return hc_fail(c, HC_ERR_STATE, "device error %d", hd->err_code);
+  if (hd->pause & (HC_PAUSE_ERODE | HC_PAUSE_LATERAL)) HC_TRY(finish_iteration(c, flags));
+  HC_TRY(host_steps(c, flags));
+  if ((hd->pause & HC_PAUSE_FINISHED) || hd->budget <= 0) {
+    *finished = true;
+    return HC_OK;
+  }
+  if (hd->pause & ~(HC_PAUSE_BUDGET)) {
     HC_TRY(pull(c));
-    c->launches += (int64_t)(hd->body_kernels - bk0);
     if (hd->pause & HC_PAUSE_ERROR)
       return hc_fail(c, HC_ERR_STATE, "device error %d", hd->err_code);
-    if (hd->pause & (HC_PAUSE_ERODE | HC_PAUSE_LATERAL)) HC_TRY(finish_iteration(c, flags));
-    HC_TRY(host_steps(c, flags));
-    ran = n - hd->budget;
-    if ((hd->pause & HC_PAUSE_FINISHED) || hd->budget <= 0) break;
-    if (hd->pause & ~(HC_PAUSE_BUDGET)) {
-      HC_TRY(pull(c));
-      if (hd->pause & HC_PAUSE_ERROR)
-        return hc_fail(c, HC_ERR_STATE, "device error %d", hd->err_code);
-    }
-    hd->pause &= HC_PAUSE_FINISHED;
-    HC_TRY(push(c));
   }
+  hd->pause &= HC_PAUSE_FINISHED;
+  return push(c);
+}
+
+static hc_status run_end(hc_ctx* c, hc_step_record* rec, int64_t* done) {
+  hc_dev* hd = c->hdev;
+  const int64_t n = c->run_n;
+  const int64_t ran = n - hd->budget;
   if (rec && ran > 0) {
     const int64_t nrec = std::min<int64_t>(hd->rec_index, n);
     c->d2h_bytes += nrec * (int64_t)sizeof(hc_step_record);
-    HC_CU(cudaMemcpy(rec, v.rec, (size_t)nrec * sizeof(hc_step_record), cudaMemcpyDeviceToHost),
-          "records");
+    HC_CU(cudaMemcpy(rec, c->v.rec, (size_t)nrec * sizeof(hc_step_record),
+                     cudaMemcpyDeviceToHost), "records");
   }
   if (done) *done = ran;
   hd->pause &= HC_PAUSE_FINISHED;
-  HC_TRY(push(c));
+  return push(c);
+}
+
+extern "C" hc_status hc_run(hc_ctx* c, int64_t n, int32_t flags, hc_step_record* rec,
+                            int64_t* done) {
+  if (done) *done = 0;
+  bool finished = false;
+  HC_TRY(run_begin(c, n, flags, rec != nullptr, &finished));
+  while (!finished) {
+    HC_TRY(run_launch(c));
+    HC_CU(cudaEventSynchronize(c->chunk_done), "graph");
+    HC_TRY(run_after_chunk(c, flags, &finished));
+  }
+  return run_end(c, rec, done);
+}
+
+extern "C" hc_status hc_run_ensemble(hc_ctx** ctxs, int32_t m, int64_t n, int32_t flags,
+                                     int64_t* done) {
+  if (!ctxs || m <= 0 || n < 0) return HC_ERR_ARG;
+  std::vector<char> live(m, 0);
+  for (int k = 0; k < m; k++) {
+    if (!ctxs[k]) return HC_ERR_ARG;
+    if (done) done[k] = 0;
+    bool fin = false;
+    HC_TRY(run_begin(ctxs[k], n, flags, false, &fin));
+    if (!fin) {
+      HC_TRY(run_launch(ctxs[k]));
+      live[k] = 1;
+    }
+  }
+  int left = 0;
+  for (int k = 0; k < m; k++) left += live[k];
+  while (left > 0) {
+    bool progressed = false;
+    for (int k = 0; k < m; k++) {
+      if (!live[k]) continue;
+      hc_ctx* c = ctxs[k];
+      const cudaError_t q = cudaEventQuery(c->chunk_done);
+      if (q == cudaErrorNotReady) continue;
+      if (q != cudaSuccess) return hc_cuda(c, q, "ensemble");
+      progressed = true;
+      bool fin = false;
+      HC_TRY(run_after_chunk(c, flags, &fin));
+      if (fin) {
+        HC_TRY(run_end(c, nullptr, done ? &done[k] : nullptr));
+        live[k] = 0;
+        left--;
+      } else {
+        HC_TRY(run_launch(c));
+      }
+    }
+    if (!progressed) std::this_thread::yield();
+  }
   return HC_OK;
 }
 

@@ -248,7 +248,7 @@ template <bool kSusp, bool kVel>
 __device__ __forceinline__ void inertial_face(double& q, double& qs, double& vel_out, int& vdir,
                                               double e0, double h0, double a0, double e1,
                                               double h1, double a1, double v0, double v1,
-                                              double nn, double dt, int edge_slope,
+                                              double c0, double nn, double dt, int edge_slope,
                                               const hc_params& p, double rDX) {
   const double DX = p.DX;
   vdir = 0;
@@ -271,50 +271,69 @@ __device__ __forceinline__ void inertial_face(double& q, double& qs, double& vel
   }
   const double fl = p.froude_limit;
   const float hf = approx_abs_f(hflow);
+  // q/hflow: exact when the face velocity is kept (erosion runs), where it
+  // also serves the Froude test
+  double qoh = 0;
+  bool qoh_valid = false;
   // Froude limit: |q/hflow| / sqrt(g*hflow) > froude_limit
   if (qn != 0) {
-    const float fr = approx_abs_f(qn) / (hf * sqrtf(9.81f * hf));
+    float fr;
+    if (kVel) {
+      qoh = qn / hflow;
+      qoh_valid = true;
+      fr = approx_abs_f(qoh) / sqrtf(9.81f * hf);
+    } else {
+      fr = approx_abs_f(qn) / (hf * sqrtf(9.81f * hf));
+    }
     int t = decide_gt(fr, (float)fl);
-    if (t == 0) t = (fabs(qn / hflow) / sqrt(kG * hflow) > fl) ? 1 : -1;
+    if (t == 0) {
+      if (!qoh_valid) qoh = qn / hflow;
+      t = (fabs(qoh) / sqrt(kG * hflow) > fl) ? 1 : -1;
+    }
     if (t > 0) {
       const double lim = hflow * (sqrt(kG * hflow) * fl);
       qn = (qn > 0) ? lim : 0 - lim;
+      qoh_valid = false;
     }
   }
   // depth limit: |q*dt/DX| > (depth of the giving cell)/4
   if (qn > 0) {
     int t = decide_gt(approx_abs_f(qn) * approx_abs_f(dt) / (float)DX, approx_abs_f(h0) * 0.25f);
     if (t == 0) t = ((qn * dt / DX) > (h0 / 4)) ? 1 : -1;
-    if (t > 0) qn = ((h0 * DX) / 5) / dt;
+    if (t > 0) {
+      qn = ((h0 * DX) / 5) / dt;
+      qoh_valid = false;
+    }
   } else if (qn < 0) {
     int t = decide_gt(approx_abs_f(qn) * approx_abs_f(dt) / (float)DX, approx_abs_f(h1) * 0.25f);
     if (t == 0) t = (fabs(qn * dt / DX) > (h1 / 4)) ? 1 : -1;
-    if (t > 0) qn = 0 - ((h1 * DX) / 5) / dt;
+    if (t > 0) {
+      qn = 0 - ((h1 * DX) / 5) / dt;
+      qoh_valid = false;
+    }
   }
   if (kSusp) {
-    if (qn > 0) qs = qn * (v0 / h0);
-    if (qn < 0) qs = qn * (v1 / h1);
+    // qs = q * (V/h) of the giving cell; V = 0 gives 0 * q (a signed zero)
+    if (qn > 0) qs = qn * c0;
+    if (qn < 0) qs = qn * ((v1 == 0) ? v1 : v1 / h1);  // h1 > 0 here, as h0 above
     if (qs > 0 && qs * dt > (v0 * DX) / 4) qs = ((v0 * DX) / 5) / dt;
     if (qs < 0 && fabs(qs * dt) > (v1 * DX) / 4) qs = 0 - ((v1 * DX) / 5) / dt;
   }
   if (kVel) {
+    // (0 - q)/hflow = -(q/hflow) exactly: division rounds symmetrically
+    if (qn != 0 && !qoh_valid) qoh = qn / hflow;
     if (qn > 0) {
-      vel_out = qn / hflow;
+      vel_out = qoh;
       vdir = 1;
     }
     if (qn < 0) {
-      vel_out = (0 - qn) / hflow;
+      vel_out = 0 - qoh;
       vdir = -1;
     }
   }
   q = qn;
 }
 
-// kSed: erosion is on.  Then the suspended-load discharges qxs/qys and the
-// face velocities vel_dir (read only by erode) are computed as the
-// reference does.  In hydro-only runs Vsusptot stays zero, so the
-// reference's qxs/qys are signed zeros and vel_dir is never read: both are
-// left untouched.
 template <bool kSed>
 __device__ __forceinline__ void flow_cell(const hc_view& c, const hc_dev* __restrict__ d,
                                           size_t cell) {
@@ -331,6 +350,10 @@ __device__ __forceinline__ void flow_cell(const hc_view& c, const hc_dev* __rest
   const double h0 = c.h[cell];
   const double a0 = e0 + h0;
   const double v0 = susp ? c.vs[cell] : 0.0;
+  // V/h of this cell, shared by both faces.  Only used where q > 0 after
+  // the depth limit, which implies h > 0, so a zero V gives V itself (with
+  // its sign) without the division.
+  const double c0 = (susp && v0 != 0) ? v0 / h0 : v0;
   // x face (rows i-1, i)
   {
     const size_t up = cell - W;
@@ -341,10 +364,10 @@ __device__ __forceinline__ void flow_cell(const hc_view& c, const hc_dev* __rest
       const int es = (i == c.imax) ? 1 : ((i <= 2) ? -1 : 0);
       if (susp)
         inertial_face<true, kSed>(q, qs, vel, vdir, e0, h0, a0, e1, h1, e1 + h1, v0, c.vs[up],
-                                  nn, dt, es, p, rDX);
+                                  c0, nn, dt, es, p, rDX);
       else
-        inertial_face<false, kSed>(q, qs, vel, vdir, e0, h0, a0, e1, h1, e1 + h1, v0, 0.0, nn,
-                                   dt, es, p, rDX);
+        inertial_face<false, kSed>(q, qs, vel, vdir, e0, h0, a0, e1, h1, e1 + h1, v0, 0.0, c0,
+                                   nn, dt, es, p, rDX);
       c.qx[cell] = q;
       if (kSed) {
         c.qxs[cell] = qs;
@@ -365,10 +388,10 @@ __device__ __forceinline__ void flow_cell(const hc_view& c, const hc_dev* __rest
       const int es = (j == c.jmax) ? 1 : ((j <= 2) ? -1 : 0);
       if (susp)
         inertial_face<true, kSed>(q, qs, vel, vdir, e0, h0, a0, e1, h1, e1 + h1, v0, c.vs[lf],
-                                  nn, dt, es, p, rDX);
+                                  c0, nn, dt, es, p, rDX);
       else
-        inertial_face<false, kSed>(q, qs, vel, vdir, e0, h0, a0, e1, h1, e1 + h1, v0, 0.0, nn,
-                                   dt, es, p, rDX);
+        inertial_face<false, kSed>(q, qs, vel, vdir, e0, h0, a0, e1, h1, e1 + h1, v0, 0.0, c0,
+                                   nn, dt, es, p, rDX);
       c.qy[cell] = q;
       if (kSed) {
         c.qys[cell] = qs;

@@ -145,6 +145,9 @@ struct hc_ctx {
   // CUDA graph of K iterations
   cudaGraphExec_t graph; int graph_iters; int graph_flags;
   int64_t graph_kernels;   // kernel nodes in the graph
+  cudaEvent_t chunk_done;  // a launched chunk and its control-block copy are done
+  int64_t run_n;           // iterations asked of the current run
+  unsigned long long body_k0;
   bool capturing;
   // counters for measurement: kernels launched, bytes moved host<->device
   int64_t launches, h2d_bytes, d2h_bytes;

@@ -59,6 +59,7 @@ def load_library(path=LIB_PATH):
         "hc_in_channel_landsliding": (C.c_int, [vp]),
         "hc_run": (C.c_int, [vp, C.c_int64, C.c_int32, vp, P(C.c_int64)]),
         "hc_stream": (vp, [vp]),
+        "hc_run_ensemble": (C.c_int, [P(vp), C.c_int32, C.c_int64, C.c_int32, P(C.c_int64)]),
         "hc_bench_kernel": (C.c_int, [vp, C.c_char_p, C.c_int32, P(C.c_double), P(C.c_int64)]),
         "hc_get_counters": (C.c_int, [vp, P(C.c_int64), P(C.c_int64), P(C.c_int64)]),
         "hc_profile_iteration": (C.c_int, [vp, C.c_int32, P(C.c_double)]),
@@ -208,3 +209,18 @@ class Model:
         ms = (C.c_double * 9)()
         self._check(self.lib.hc_profile_iteration(self.h, flags, ms), "profile_iteration")
         return dict(zip(self.PHASES, list(ms)))
+
+
+def run_ensemble(models, n, flags=0):
+    """Runs up to n iterations of every model at once (hc_run_ensemble);
+    returns the iteration counts."""
+    lib = load_library()
+    m = len(models)
+    arr = (C.c_void_p * m)(*[mod.h.value for mod in models])
+    done = (C.c_int64 * m)()
+    st = lib.hc_run_ensemble(arr, m, n, flags, done)
+    if st != 0:
+        msgs = [(mod.lib.hc_last_error(mod.h) or b"").decode() for mod in models]
+        raise HCError("run_ensemble failed: %s %s" % (STATUS.get(st, st),
+                                                    "; ".join(x for x in msgs if x)))
+    return list(done)

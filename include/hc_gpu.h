@@ -219,6 +219,13 @@ hc_status hc_in_channel_landsliding(hc_ctx* ctx);
 hc_status hc_run(hc_ctx* ctx, int64_t n, int32_t flags, hc_step_record* rec,
                  int64_t* done);
 
+/* Ensemble (no counterpart in the reference, which runs one catchment per
+ * process): runs up to n iterations of each of m independent contexts at
+ * once, each on its own stream with its own CUDA graph, adaptive dt and
+ * host-side steps; done[k] receives member k's iteration count.  Members may
+ * differ in size and parameters. */
+hc_status hc_run_ensemble(hc_ctx** ctxs, int32_t m, int64_t n, int32_t flags, int64_t* done);
+
 /* Stream the context issues its work on (a cudaStream_t). */
 void* hc_stream(hc_ctx* ctx);
 

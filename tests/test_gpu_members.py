@@ -1,4 +1,4 @@
-"""The member-level entry points (the drop-in path of INTEGRATION.md): a state
+"""The member-level entry points (the member-by-member drop-in path): a state
 computed by the oracle is uploaded field by field in the reference's layout,
 one member is called on the GPU and the same member on the oracle, and the
 results are compared.  This exercises hc_upload/hc_download layout
