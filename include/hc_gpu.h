@@ -197,6 +197,31 @@ hc_status hc_set_maximum_timestep(hc_ctx* ctx);
 hc_status hc_flow_route(hc_ctx* ctx);
 /* depth_update :3259-3299; maxdepth lands in the scalars */
 hc_status hc_depth_update(hc_ctx* ctx);
+
+/* depth_update :3259-3299 on caller-owned device buffers, allocating nothing.
+ * No counterpart in the reference (its member works on the object's own
+ * arrays).  For callers that cannot allocate: a program that mirrors the TNT
+ * arrays in device memory of its own under a fixed budget (cudaMalloc would
+ * fail there), or that shares the GPU with other streams (cudaFree waits for
+ * the whole device).  Buffers are device pointers in the reference's layout:
+ * fields (imax+2)*(jmax+2) doubles, down_scan (jmax+2)*(imax+2) int32 lists
+ * of distinct rows as scan_area writes them.  Vsusptot may be null (no
+ * suspended fraction); if given, qxs and qys are needed.  *maxdepth (device)
+ * receives the reference's maxdepth.  flow_timestep is get_flow_timestep's
+ * value.  The call is asynchronous on `stream` (a cudaStream_t, 0 for the
+ * legacy stream) on the current device.  Working memory is one fixed array
+ * of the library (128 KiB per device), so jmax is limited to
+ * HC_DEPTH_NOALLOC_MAX_COLS; larger grids get HC_ERR_ARG.  The first call on
+ * each device looks up that array's address, so make it before any stream
+ * capture.  All calls on a device share the array: calls that overlap in
+ * time (other streams, other threads) race; order them on one stream.  err
+ * (optional, err_len bytes) receives a one-line reason for a failure. */
+#define HC_DEPTH_NOALLOC_MAX_COLS 16383
+hc_status hc_depth_update_noalloc(int32_t imax, int32_t jmax, double DX, double flow_timestep,
+                                  const int32_t* down_scan, const double* elev,
+                                  const double* qx, const double* qy, const double* qxs,
+                                  const double* qys, double* water_depth, double* Vsusptot,
+                                  double* maxdepth, void* stream, char* err, size_t err_len);
 /* scan_area :3821-3849 */
 hc_status hc_scan_area(hc_ctx* ctx);
 /* water_flux_out :3005-3047 */
