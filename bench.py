@@ -179,6 +179,8 @@ def run_gpu(args, rank, world, dist):
     model.run(args.warmup, flags, records=False)
     log("warm-up done")
     if args.profile_only:
+        if args.profile_skip:
+            model.run(args.profile_skip, flags, records=False)
         torch.cuda.synchronize()
         torch.cuda.nvtx.range_push("profiled")
         prof = [model.profile_iteration(flags) for _ in range(args.profile_only)]
@@ -199,6 +201,8 @@ def run_gpu(args, rank, world, dist):
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     l0 = model.counters()[0]
+    st0 = model.run_stats()
+    cyc0 = model.scalars().cycle
     torch.cuda.nvtx.range_push("timed")
     e0.record(stream)
     done = model.run(args.steps, flags, records=False)
@@ -207,14 +211,23 @@ def run_gpu(args, rank, world, dist):
     torch.cuda.nvtx.range_pop()
     ms = e0.elapsed_time(e1)
     launches = model.counters()[0] - l0
+    sim_min = model.scalars().cycle - cyc0
+    st1 = model.run_stats()
+    host_work = {k: {"count": st1[k][0] - st0[k][0], "host_ms": round(st1[k][1] - st0[k][1], 3)}
+                 for k in st1}
     clk = clocks.stop() if clocks else None
     ms, total_steps = aggregate_replicas(ms, done, dist, "cuda")
     cells = case.cells
     value = cells * total_steps / (ms / 1e3)
     out = {"ms": ms, "done": done, "value": value, "clocks": clk, "cells": cells, "desc": desc,
-           "launches": launches}
+           "launches": launches, "host_work": host_work, "sim_minutes": sim_min}
     if rank != 0 or args.timed_only:
         return out, model, case
+    # per-phase breakdown of a few iterations (phase by phase, no graph)
+    nprof = int(os.environ.get("HC_PROFILE_ITERS", "60"))
+    prof = [model.profile_iteration(flags) for _ in range(nprof)]
+    out["phases_ms"] = {k: float(np.mean([p_[k] for p_ in prof])) for k in prof[0]}
+    out["phases_ms"]["iterations_profiled"] = nprof
     # end-to-end through the public API: one hc_run call per step with the
     # step's record read back to host memory (the drop-in call pattern)
     e2e_steps = max(3, min(args.steps, 50))
@@ -233,11 +246,6 @@ def run_gpu(args, rank, world, dist):
                   "h2d_bytes_per_step": (h1 - h0) // e2e_steps,
                   "d2h_bytes_per_step": (d1 - d0) // e2e_steps,
                   "steps": e2e_steps, "api": "hc_run(ctx, 1, flags, host_records) per step"}
-    # per-phase breakdown of a few iterations (phase by phase, no graph)
-    nprof = int(os.environ.get("HC_PROFILE_ITERS", "60"))
-    prof = [model.profile_iteration(flags) for _ in range(nprof)]
-    out["phases_ms"] = {k: float(np.mean([p_[k] for p_ in prof])) for k in prof[0]}
-    out["phases_ms"]["iterations_profiled"] = nprof
     # dominant kernel, timed alone with events on the library's stream
     reps = 20
     ms_flow, wet = model.bench_kernel("flow_route", reps)
@@ -313,6 +321,9 @@ def main():
     ap.add_argument("--timed-only", action="store_true",
                     help="only the timed steps (no e2e, profile, kernel timing or CPU leg); "
                          "for runs under a profiler")
+    ap.add_argument("--profile-skip", type=int, default=0, metavar="S",
+                    help="with --profile-only: run S iterations first (e.g. --steps, to "
+                         "profile the state at the end of the timed region)")
     ap.add_argument("--profile-only", type=int, default=0, metavar="N",
                     help="after the warm-up, run N iterations launch by launch (no graph) "
                          "inside the NVTX range 'profiled', then the dominant kernel alone "
@@ -347,6 +358,7 @@ def main():
                        "l2": "inputs larger than L2 (model state several GB)"},
             "clocks": out["clocks"], "e2e": out["e2e"], "roofline": out["roofline"],
             "gpu_launches": out["launches"], "phases_ms": out["phases_ms"],
+            "host_work": out["host_work"], "simulated_minutes_timed": out["sim_minutes"],
         }
         if world == 1:
             line["cpu_baseline"] = cpu_sample(model, case, case.flags, args.cpu_budget)

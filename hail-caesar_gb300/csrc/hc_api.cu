@@ -6,6 +6,7 @@
 #include "hc_internal.cuh"
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -226,6 +227,14 @@ extern "C" hc_status hc_create(const hc_params* p, size_t max_bytes, hc_ctx** ou
   hc_view& v = c->v;
   v.p = *p;
   v.rDX = 1.0 / p->DX;
+  v.DXf = (float)p->DX;
+  v.flf = (float)p->froude_limit;
+  {
+    long long b;
+    std::memcpy(&b, &p->hflow_threshold, 8);
+    const long long sgn = b >> 63;
+    v.thr_key = ((b & 0x7fffffffffffffffLL) ^ sgn) - sgn;  // dkey on the host
+  }
   for (int n = 1; n <= 9; n++) {
     const double Di = p->d[n], g = 9.81;
     v.einA[n] = (2650 - 1000) * Di;
@@ -256,9 +265,12 @@ extern "C" hc_status hc_create(const hc_params* p, size_t max_bytes, hc_ctx** ou
   A(v.edge, E2) A(v.edge2, E2) A(v.veg, 4 * E2)
   A(v.cin_x, (size_t)p->imax * p->jmax + 2) A(v.cin_y, (size_t)p->imax * p->jmax + 2)
   A(v.wet, N2) A(v.wet_sums, (N2 + 1023) / 1024 + 1)
+  A(v.drain_pos, N2) A(v.drain_f0, N2) A(v.drain_f1, N2) A(v.drain_pend, N2) A(v.drain_dt, N2)
+  A(v.drain_aux, 1)
   if (sed) {
     A(v.sflux, 40 * N2) A(v.grain, 11 * N2) A(v.strata, 90 * N2) A(v.alloc_key, N2)
-    A(v.erodetot, N2) A(v.erodetot3, N2) A(v.pre, 11 * N2)
+    A(v.erodetot, N2) A(v.erodetot3, N2) A(v.pre, 11 * N2) A(v.chains, 2 * N2)
+    A(v.drain_snap, N2)
   } else {
     A(v.erodetot, N2)
   }
@@ -281,8 +293,6 @@ extern "C" hc_status hc_create(const hc_params* p, size_t max_bytes, hc_ctx** ou
     free_all(c);
     return HC_ERR_NOMEM;
   }
-  c->h_cin_x = (int32_t*)calloc((size_t)p->imax * p->jmax + 2, 4);
-  c->h_cin_y = (int32_t*)calloc((size_t)p->imax * p->jmax + 2, 4);
   // zero_values :2891-2982
   cudaStream_t s = c->s;
   for (double* a : {v.h, v.qx, v.qy, v.qxs, v.qys, v.vs, v.vel, v.tau, v.man, v.area, v.ss})
@@ -340,15 +350,14 @@ static hc_status free_all(hc_ctx* c) {
   void* ptrs[] = {v.elev, v.h, v.qx, v.qy, v.qxs, v.qys, v.vs, v.vel, v.tau, v.bed, v.man,
                   v.area, v.ss, v.vd, v.sflux, v.grain, v.strata, v.index, v.mask, v.rfarea,
                   v.edge, v.edge2, v.veg, v.cin_x, v.cin_y, v.erodetot, v.erodetot3, v.pre,
-                  v.alloc_key, v.red, v.touched, v.topm, v.rain, v.rec, c->dev, v.wet,
+                  v.chains, v.drain_pos, v.drain_f0, v.drain_f1, v.drain_pend, v.drain_dt,
+                  v.drain_snap, v.drain_aux, v.alloc_key, v.red, v.touched, v.topm, v.rain, v.rec, c->dev, v.wet,
                   v.wet_sums,
                   v.reach[0], v.reach[1], v.reach[2], extra(c).lateral};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   if (c->hdev) cudaFreeHost(c->hdev);
   if (c->h_elev) cudaFreeHost(c->h_elev);
-  free(c->h_cin_x);
-  free(c->h_cin_y);
   if (c->drainage_cache) host_drainage_cache_free(c->drainage_cache);
   free(extra(c).h_rain);
   if (c->graph) cudaGraphExecDestroy(c->graph);
@@ -421,6 +430,7 @@ extern "C" hc_status hc_upload(hc_ctx* c, hc_field f, const void* host, size_t n
   if (double* d = plain_field(c, f)) {
     HC_CU(cudaMemcpyAsync(d, host, nbytes, cudaMemcpyHostToDevice, s), "upload");
     HC_CU(cudaStreamSynchronize(s), "upload");
+    if (f == HC_F_ELEV || f == HC_F_AREA) c->area_valid = false;
     if (f == HC_F_ELEV && c->drainage_cache) {  // the cached elevation order is stale
       host_drainage_cache_free(c->drainage_cache);
       c->drainage_cache = nullptr;
@@ -631,6 +641,13 @@ extern "C" hc_status hc_set_reach(hc_ctx* c, int32_t point, const float* data, i
 }
 
 // ------------------------------------------------------------------ scalars
+// a device-side error (HC_PAUSE_ERROR) as a status
+static hc_status device_error(hc_ctx* c) {
+  const int e = c->hdev->err_code;
+  if (e == 301) return hc_fail(c, HC_ERR_NONFINITE, "non-finite water depth (device error 301)");
+  return hc_fail(c, HC_ERR_STATE, "device error %d", e);
+}
+
 static hc_status pull(hc_ctx* c) {
   c->d2h_bytes += sizeof(hc_dev);
   HC_CU(cudaMemcpyAsync(c->hdev, c->dev, sizeof(hc_dev), cudaMemcpyDeviceToHost, c->s), "pull");
@@ -661,28 +678,51 @@ extern "C" hc_status hc_set_scalars(hc_ctx* c, const hc_scalars* s) {
 }
 
 // ------------------------------------------------------------------ prepare
-static hc_status recompute_points(hc_ctx* c) {
-  hc_view& v = c->v;
-  const size_t N2 = v.N2;
-  std::vector<double> elev(N2), area(N2);
-  std::vector<int32_t> rf(N2);
-  HC_CU(cudaStreamSynchronize(c->s), "points");
-  HC_CU(cudaMemcpy(elev.data(), v.elev, N2 * 8, cudaMemcpyDeviceToHost), "points");
-  HC_CU(cudaMemcpy(rf.data(), v.rfarea, N2 * 4, cudaMemcpyDeviceToHost), "points");
-  HC_TRY(pull(c));
-  hc_scalars& s = c->hdev->s;
-  int total = 0;
+// accumulates the host wall time of a piece of hc_run's host work
+namespace {
+struct StatTimer {
+  hc_ctx* c;
+  int k;
+  std::chrono::steady_clock::time_point t0;
+  StatTimer(hc_ctx* c_, int k_) : c(c_), k(k_), t0(std::chrono::steady_clock::now()) {}
+  ~StatTimer() {
+    c->stat_n[k]++;
+    c->stat_ms[k] +=
+        std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  }
+};
+}  // namespace
+
+// the drainage sweep order from the host sort, when the device needs it
+static const uint32_t* drainage_sort(hc_ctx* c, const double* del) {
+  const size_t N2 = c->v.N2;
+  std::vector<double> elev(N2);
+  if (cudaMemcpy(elev.data(), del, N2 * 8, cudaMemcpyDeviceToHost) != cudaSuccess) return nullptr;
+  c->d2h_bytes += N2 * 8;
   if (!c->drainage_cache) c->drainage_cache = host_drainage_cache_new();
-  // hydro-only runs never change elevations
-  host_drainage_and_points(&v.p, elev.data(), rf.data(), s.baseflow, area.data(), c->h_cin_x,
-                           c->h_cin_y, &total, s.catchment_input_counter, c->drainage_cache,
-                           v.p.hydro_only != 0);
-  s.totalinputpoints = total;
-  const size_t ncin = (size_t)v.imax * v.jmax + 2;
-  HC_CU(cudaMemcpy(v.area, area.data(), N2 * 8, cudaMemcpyHostToDevice), "points");
-  HC_CU(cudaMemcpy(v.cin_x, c->h_cin_x, ncin * 4, cudaMemcpyHostToDevice), "points");
-  HC_CU(cudaMemcpy(v.cin_y, c->h_cin_y, ncin * 4, cudaMemcpyHostToDevice), "points");
-  return push(c);
+  StatTimer st(c, HC_STAT_DRAINAGE_SORT);
+  bool reused = false;
+  return host_drainage_order(&c->v.p, elev.data(), c->drainage_cache, &reused);
+}
+
+// zero_and_calc_drainage_area + get_catchment_input_points (hc_drain.cu).
+// `snapshot`: use the elevations copied at the start of the iteration that
+// moved the baseflow threshold (erosion has changed elev since).  Hydro-only
+// runs never change elevations, so their area is computed once.
+static hc_status recompute_points(hc_ctx* c, bool snapshot) {
+  hc_view& v = c->v;
+  const double* del = (snapshot && v.drain_snap) ? v.drain_snap : v.elev;
+  HC_TRY(push(c));  // baseflow
+  bool sorted = false;
+  const bool keep_area = c->area_valid && v.p.hydro_only;
+  if (run_drainage_device(c, del, keep_area, drainage_sort, &sorted) != HC_OK)
+    return hc_cuda(c, cudaGetLastError(), "drainage");
+  HC_CU(cudaStreamSynchronize(c->s), "drainage");
+  c->area_valid = true;
+  HC_TRY(pull(c));
+  if (c->hdev->pause & HC_PAUSE_ERROR) return device_error(c);
+  if (!keep_area) c->stat_n[HC_STAT_DRAINAGE_LEVELS] += c->hdev->drain_levels;
+  return HC_OK;
 }
 
 extern "C" hc_status hc_prepare(hc_ctx* c) {
@@ -725,7 +765,7 @@ extern "C" hc_status hc_prepare(hc_ctx* c) {
   }
   for (int n = 1; n <= 9; n++) v.dlog[n] = std::log(p.d[n]);
   HC_TRY(push(c));
-  HC_TRY(recompute_points(c));
+  HC_TRY(recompute_points(c, false));
   c->prepared = true;
   c->graph_iters = 0;  // parameters of the view changed: rebuild the graph
   return HC_OK;
@@ -751,7 +791,8 @@ extern "C" hc_status hc_depth_update(hc_ctx* c) {
   if (!c) return HC_ERR_ARG;
   launch_flow_dt(c);
   launch_depth_update(c, 0);
-  HC_CU(cudaStreamSynchronize(c->s), "depth_update");
+  HC_TRY(pull(c));
+  if (c->hdev->pause & HC_PAUSE_ERROR) return device_error(c);
   return HC_OK;
 }
 
@@ -780,7 +821,7 @@ extern "C" hc_status hc_erode(hc_ctx* c, double mult, double* tempbmax) {
     launch_erode_pass(c, 0);
     HC_TRY(pull(c));
     if (c->hdev->pause & HC_PAUSE_ERROR)
-      return hc_fail(c, HC_ERR_STATE, "device error %d", c->hdev->err_code);
+      return device_error(c);
     if (!c->hdev->erode_retry) break;
     if (guard > 100000) return hc_fail(c, HC_ERR_TIMEOUT, "erosion retry loop did not end");
   }
@@ -802,13 +843,14 @@ extern "C" hc_status hc_in_channel_landsliding(hc_ctx* c) {
   launch_slide3(c, 0);
   HC_TRY(pull(c));
   if (c->hdev->pause & HC_PAUSE_ERROR)
-    return hc_fail(c, HC_ERR_STATE, "device error %d", c->hdev->err_code);
+    return device_error(c);
   return HC_OK;
 }
 
 // ------------------------------------------------------------------ hc_run
 static void launch_iteration(hc_ctx* c, int flags) {
   launch_control(c);
+  if (!c->v.p.hydro_only) launch_drain_snapshot(c);
   launch_inputs(c);
   launch_flow_route(c, 1);
   launch_depth_update(c, 1);
@@ -877,6 +919,7 @@ static hc_status capture_iteration(hc_ctx* c, int flags) {
   H.has = 1;
   launch_control(c);
   H.has = 0;  // no other launch sets the iteration's conditions
+  if (sed) launch_drain_snapshot(c);
   launch_inputs(c);
   launch_flow_route(c, 1);
   launch_depth_update(c, 1);
@@ -944,6 +987,7 @@ static hc_status build_graph(hc_ctx* c, int flags) {
   return HC_OK;
 }
 
+
 // Finishes an iteration that stopped before water_flux_out (erosion retry
 // beyond the captured passes, or lateral3 due).
 static hc_status finish_iteration(hc_ctx* c, int flags) {
@@ -952,6 +996,7 @@ static hc_status finish_iteration(hc_ctx* c, int flags) {
   hd->it_active = 1;
   HC_TRY(push(c));
   if (hd->pause & HC_PAUSE_ERODE) {
+    StatTimer st(c, HC_STAT_ERODE_RETRY);
     for (int guard = 0; hd->erode_retry; guard++) {
       launch_erode_pass(c, 0);
       HC_TRY(pull(c));
@@ -965,6 +1010,7 @@ static hc_status finish_iteration(hc_ctx* c, int flags) {
     HC_TRY(pull(c));
   }
   if (hd->pause & HC_PAUSE_LATERAL) {
+    StatTimer st(c, HC_STAT_LATERAL);
     HC_TRY(run_lateral(c));
     HC_TRY(pull(c));
     hd->s.lateralcounter = hd->s.counter + (50 * hd->s.erode_mult);  // call_lateral :2302
@@ -985,12 +1031,14 @@ static hc_status host_steps(hc_ctx* c, int flags) {
     hd->pause &= ~HC_PAUSE_HOSTSTEP;
     if (!p.hydro_only && !(flags & HC_RUN_NOHILL)) {
       if (hd->s.cycle > hd->s.creep_time) {  // slope_creep :1976
+        StatTimer st(c, HC_STAT_CREEP);
         hd->s.creep_time += p.creep_time_interval;
         HC_TRY(push(c));
         HC_TRY(run_creep(c, p.creep_coeff));
         HC_TRY(pull(c));
       }
       if (hd->s.cycle > hd->s.creep_time2) {  // call_global_landsliding :1986
+        StatTimer st(c, HC_STAT_GLOBAL_SLIDE);
         hd->s.creep_time2 += p.global_landsliding_interval;
         HC_TRY(push(c));
         HC_TRY(run_global_landsliding(c));
@@ -1000,9 +1048,10 @@ static hc_status host_steps(hc_ctx* c, int flags) {
     HC_TRY(push(c));
   }
   if (hd->pause & HC_PAUSE_DRAINAGE) {
+    StatTimer st(c, HC_STAT_DRAINAGE);
     hd->pause &= ~HC_PAUSE_DRAINAGE;
     HC_TRY(push(c));
-    HC_TRY(recompute_points(c));
+    HC_TRY(recompute_points(c, true));
   }
   return HC_OK;
 }
@@ -1046,6 +1095,8 @@ static hc_status run_begin(hc_ctx* c, int64_t n, int32_t flags, bool want_rec, b
 // one graph chunk, then the control block copied back; chunk_done marks both
 static hc_status run_launch(hc_ctx* c) {
   c->body_k0 = c->hdev->body_kernels;
+  c->budget0 = c->hdev->budget;
+  c->stat_n[HC_STAT_CHUNKS]++;
   HC_CU(cudaGraphLaunch(c->graph, c->s), "graph launch");
   c->launches += c->graph_kernels;
   c->d2h_bytes += sizeof(hc_dev);
@@ -1059,7 +1110,9 @@ static hc_status run_after_chunk(hc_ctx* c, int32_t flags, bool* finished) {
   hc_dev* hd = c->hdev;
   *finished = false;
   c->launches += (int64_t)(hd->body_kernels - c->body_k0);
-  if (hd->pause & HC_PAUSE_ERROR) return hc_fail(c, HC_ERR_STATE, "device error %d", hd->err_code);
+  c->stat_n[HC_STAT_IDLE_ITERS] += std::max<int64_t>(
+      0, std::min<int64_t>(c->graph_iters, c->budget0) - (c->budget0 - hd->budget));
+  if (hd->pause & HC_PAUSE_ERROR) return device_error(c);
   if (hd->pause & (HC_PAUSE_ERODE | HC_PAUSE_LATERAL)) HC_TRY(finish_iteration(c, flags));
   HC_TRY(host_steps(c, flags));
   if ((hd->pause & HC_PAUSE_FINISHED) || hd->budget <= 0) {
@@ -1069,7 +1122,7 @@ static hc_status run_after_chunk(hc_ctx* c, int32_t flags, bool* finished) {
   if (hd->pause & ~(HC_PAUSE_BUDGET)) {
     HC_TRY(pull(c));
     if (hd->pause & HC_PAUSE_ERROR)
-      return hc_fail(c, HC_ERR_STATE, "device error %d", hd->err_code);
+      return device_error(c);
   }
   hd->pause &= HC_PAUSE_FINISHED;
   return push(c);
@@ -1139,6 +1192,15 @@ extern "C" hc_status hc_run_ensemble(hc_ctx** ctxs, int32_t m, int64_t n, int32_
       }
     }
     if (!progressed) std::this_thread::yield();
+  }
+  return HC_OK;
+}
+
+extern "C" hc_status hc_get_run_stats(hc_ctx* c, int64_t* counts, double* host_ms, int32_t n) {
+  if (!c || n < 0) return HC_ERR_ARG;
+  for (int k = 0; k < n && k < HC_STAT_COUNT; k++) {
+    if (counts) counts[k] = c->stat_n[k];
+    if (host_ms) host_ms[k] = c->stat_ms[k];
   }
   return HC_OK;
 }
@@ -1219,6 +1281,7 @@ extern "C" hc_status hc_profile_iteration(hc_ctx* c, int32_t flags, double* ms) 
   for (int k = 0; k < 10; k++) HC_CU(cudaEventCreate(&ev[k]), "profile");
   cudaEventRecord(ev[0], c->s);
   launch_control(c);
+  if (!c->v.p.hydro_only) launch_drain_snapshot(c);
   launch_inputs(c);
   cudaEventRecord(ev[1], c->s);
   launch_flow_route(c, 1);

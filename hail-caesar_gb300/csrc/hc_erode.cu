@@ -383,30 +383,9 @@ __global__ void k_alloc_finish(hc_dev* d, const int32_t* total) {
 }
 
 // ---------------------------------------------------------------------------
-// apply pass :4570-4682, one walker per column y in [2, jmax-1]
+// apply pass :4570-4682 (gather + lateral step along the columns) and the
+// +/-y lateral pass :4684-4748
 // ---------------------------------------------------------------------------
-// One lateral step of the apply passes (:4630-4677, :4690-4744).  Returns
-// false when the raw amount is not positive; otherwise the (possibly zeroed
-// or capped) amount, which the caller applies and hands to slide_GS even when
-// it is zero, as the reference does.
-__device__ __forceinline__ bool lateral_amount(const hc_view& c, double mult, double ts,
-                                               double tau0, double et3, size_t nb, size_t ecell,
-                                               double e_nb, double e0, bool boundary,
-                                               double& amt) {
-  const hc_params& p = c.p;
-  const double DX = p.DX;
-  amt = 0;
-  if (c.h[nb] < p.water_depth_erosion_threshold)
-    amt = mult * p.lateral_constant * tau0 * c.edge[ecell] * ts / DX;
-  else
-    amt = p.chann_lateral_erosion * et3 * (e_nb - e0) / DX * 0.1;
-  if (!(amt > 0)) return false;
-  // amt *= 1 - veg * (1 - veg_lat_restriction): veg is zero (no vegetation)
-  if ((e_nb - amt) < c.bed[nb] || boundary) amt = 0;
-  if (amt > p.ERODEFACTOR * 0.1) amt = p.ERODEFACTOR * 0.1;
-  return true;
-}
-
 // The apply passes are sequential in the reference: along a column the
 // +/-x lateral step of row x changes rows x-1 and x+1 before row x+1 is
 // processed (and along a row for the +/-y pass).  Only cells with bedload
@@ -414,7 +393,14 @@ __device__ __forceinline__ bool lateral_amount(const hc_view& c, double mult, do
 // splits into independent chains: rows x and x+1 are linked when either is a
 // lateral cell.  Each chain is walked in order by one thread, chains in
 // parallel; cells of different chains never read or write each other, so the
-// result is the serial loop's.
+// result is the serial loop's.  Cells linked to neither neighbour (most of
+// them) only gather, all in parallel.
+//
+// A walker keeps the rows it works on - the previous, current and next row
+// of its chain - in registers (ApplyRow) and touches memory once per row:
+// all loads of the next row are issued together at the top of a step, and a
+// row is written back when it leaves the window.  The grain store helpers
+// below are sort_active :3874-3947 and slide_GS :4077-4171 on such rows.
 
 // erodetot3 of every cell of the pass (0 where the cell is not processed)
 __device__ __forceinline__ bool apply_active(const hc_view& c, size_t cell, int x) {
@@ -425,16 +411,19 @@ __device__ __forceinline__ bool apply_active(const hc_view& c, size_t cell, int 
 // the (constant) outgoing fluxes only, computed for all cells in parallel:
 // plane n (1..9) = incoming - outgoing bedload of fraction n, plane 0 =
 // settled suspended load Vpdrop, plane 10 = erodetot.  The new Vsusptot is
-// written directly (nothing else in the pass touches it).  The chain walker
-// then applies them in the reference's order.
+// written directly (nothing else in the pass touches it).
 __device__ __forceinline__ double& PRE(const hc_view& c, int k, size_t cell) {
   return c.pre[(size_t)k * c.N2 + cell];
 }
 
-__global__ void __launch_bounds__(256) k_apply_pre(const hc_view c, const hc_dev* d) {
+__global__ void __launch_bounds__(256) k_apply_pre(const hc_view c, hc_dev* d) {
   if (!(d->it_active && d->rest_active && d->do_erode) || d->erode_retry) return;
   const int y = 2 + blockIdx.x * blockDim.x + threadIdx.x;
   const int x = 1 + blockIdx.y * blockDim.y + threadIdx.y;
+  if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0 && threadIdx.y == 0) {
+    d->xchains = 0;  // the chain lists are rebuilt by k_apply_gather
+    d->ychains = 0;
+  }
   if (y > c.jmax - 1 || x > c.imax) return;
   const size_t cell = (size_t)x * c.W + y;
   const size_t W = c.W;
@@ -474,123 +463,344 @@ __global__ void __launch_bounds__(256) k_apply_pre(const hc_view c, const hc_dev
   c.erodetot3[cell] = et3;
 }
 
-// one cell of the gather-apply pass with its +/-x lateral step (:4579-4680)
-__device__ __forceinline__ void apply_cell(const hc_view& c, hc_dev* d, size_t cell, int x, int y,
-                                           double mult, double ts) {
-  const hc_params& p = c.p;
-  const size_t W = c.W;
-  for (int n = 1; n <= HC_G - 1; n++) {
-    if (n == 1 && p.isSuspended[n]) {
-      double g = GRN(c, cell, n) - c.ss[cell];
-      GRN(c, cell, n) = g + PRE(c, 0, cell);
-    } else {
-      GRN(c, cell, n) += PRE(c, n, cell);
-    }
+// A cell as the apply walkers hold it.
+struct ApplyRow {
+  double g[HC_G + 1];  // grain record, planes 0..HC_G
+  double elev, h, bed, edge;
+  int idx;             // index[] (-9999: no record)
+  bool dirty;          // g[1..9] or elev changed
+};
+
+__device__ __forceinline__ void row_load(const hc_view& c, size_t cell, size_t ecell,
+                                         ApplyRow& r) {
+#pragma unroll
+  for (int n = 0; n <= HC_G; n++) r.g[n] = GRN(c, cell, n);
+  r.elev = c.elev[cell];
+  r.h = c.h[cell];
+  r.bed = c.bed[cell];
+  r.edge = c.edge[ecell];
+  r.idx = c.index[cell];
+  r.dirty = false;
+}
+
+__device__ __forceinline__ void row_store(const hc_view& c, size_t cell, const ApplyRow& r) {
+  if (!r.dirty) return;
+#pragma unroll
+  for (int n = 1; n <= HC_G - 1; n++) GRN(c, cell, n) = r.g[n];
+  c.elev[cell] = r.elev;
+}
+
+// sort_active on a held row; the strata stay in memory (they move only when
+// the record crosses a threshold).  Same decisions as sort_active_dev.
+__device__ void sort_active_row(const hc_view& c, hc_dev* d, size_t cell, ApplyRow& r) {
+  if (r.idx == -9999) {
+    d->err_code = 201;  // records were allocated before the pass (cannot happen)
+    d->pause |= HC_PAUSE_ERROR;
+    return;
   }
-  const double erodetot = PRE(c, 10, cell);
-  const double et3 = c.erodetot3[cell];
-  double e0 = c.elev[cell] + erodetot;
-  c.elev[cell] = e0;
-  if (erodetot < 0) sort_active_dev(c, d, cell, false);
-  if (et3 > 0) {
-    double elev_update = 0;
-    const double tau0 = c.tau[cell];
-    {
-      const size_t nb = cell - W;
-      const double en = c.elev[nb];
-      double amt;
-      if (en > e0 && x > 2 &&
-          lateral_amount(c, mult, ts, tau0, et3, nb, EX(c, x - 1, y), en, e0, x - 1 == 1, amt)) {
-        elev_update += amt;
-        c.elev[nb] = en - amt;
-        slide_GS_dev(c, d, nb, amt, cell, false);
+  const double active = c.p.active;
+  float sf = 0.0f, af = 0.0f;
+#pragma unroll
+  for (int n = 0; n <= HC_G; n++) {
+    const float f = approx_f(r.g[n]);
+    sf += f;
+    af += fabsf(f);
+  }
+  const float tol = 1e-5f * af + 1e-30f;
+  const float hi = (float)(active * 1.5), lo = (float)(active / 4);
+  const int dep = (sf > hi + tol) ? 1 : ((sf < hi - tol) ? -1 : 0);
+  const int ero = (sf < lo - tol) ? 1 : ((sf > lo + tol) ? -1 : 0);
+  if (dep == -1 && ero == -1) return;
+  double total = 0.0;
+#pragma unroll
+  for (int n = 0; n <= HC_G; n++) total += r.g[n];
+  if (total > (active * 1.5)) {
+    for (int z = 9; z >= 1; z--)
+      for (int n = 0; n <= HC_G - 2; n++) STR(c, cell, z, n) = STR(c, cell, z - 1, n);
+    const double coeff = active / total;
+#pragma unroll
+    for (int n = 1; n <= HC_G - 1; n++) {
+      if (r.g[n] > 0.0) {
+        const double amount = coeff * (r.g[n]);
+        STR(c, cell, 0, n - 1) = amount;
+        r.g[n] = r.g[n] - amount;
       }
     }
-    {
-      const size_t nb = cell + W;
-      const double en = c.elev[nb];
-      double amt;
-      if (en > e0 && x < c.imax - 1 &&
-          lateral_amount(c, mult, ts, tau0, et3, nb, EX(c, x + 1, y), en, e0, x + 1 == c.imax,
-                         amt)) {
-        elev_update += amt;
-        c.elev[nb] = en - amt;
-        slide_GS_dev(c, d, nb, amt, cell, false);
-      }
-    }
-    c.elev[cell] = c.elev[cell] + elev_update;
+    r.dirty = true;
+  }
+  if (total < (active / 4)) {
+#pragma unroll
+    for (int n = 1; n <= HC_G - 1; n++) r.g[n] += STR(c, cell, 0, n - 1);
+    for (int z = 0; z <= 8; z++)
+      for (int n = 0; n <= HC_G - 2; n++) STR(c, cell, z, n) = STR(c, cell, z + 1, n);
+    for (int n = 1; n <= HC_G - 1; n++) STR(c, cell, 9, n - 1) = active * c.p.dprop[n];
+    r.dirty = true;
   }
 }
 
-// chains along the columns: thread (x, y) walks the chain that starts at row x
-__global__ void __launch_bounds__(256) k_apply_xchains(const hc_view c, hc_dev* d) {
+// slide_GS(a -> b, amount) on held rows (records exist: allocated before the
+// pass).  Same arithmetic as slide_GS_dev.
+__device__ void slide_GS_rows(const hc_view& c, hc_dev* d, size_t a, ApplyRow& A, double amount,
+                              size_t b, ApplyRow& B) {
+  const double* dprop = c.p.dprop;
+  const bool ha = A.idx != -9999, hb = B.idx != -9999;
+  if (ha && hb) {
+    double total = 0;
+#pragma unroll
+    for (int n = 1; n <= HC_G - 1; n++)
+      if (A.g[n] > 0) total += A.g[n];
+    if (amount > total) {
+#pragma unroll
+      for (int n = 1; n <= HC_G - 1; n++) B.g[n] += (amount - total) * dprop[n];
+      amount = total;
+    }
+    if (total > 0) {
+      const double rt = 1.0 / total;
+#pragma unroll
+      for (int n = 1; n <= HC_G - 1; n++) {
+        const double ga = A.g[n];
+        const double t = amount * div_const(ga, total, rt);
+        B.g[n] += t;
+        double na = ga - t;
+        if (na < 0) na = 0;
+        A.g[n] = na;
+      }
+    }
+    A.dirty = B.dirty = true;
+    sort_active_row(c, d, a, A);
+    sort_active_row(c, d, b, B);
+    return;
+  }
+  if (!ha && hb) {
+#pragma unroll
+    for (int n = 1; n <= HC_G - 1; n++) B.g[n] += (amount)*dprop[n];
+    B.dirty = true;
+    sort_active_row(c, d, b, B);
+    return;
+  }
+  if (ha && !hb) {
+    d->err_code = 202;  // receiver without a record outside a serial context
+    d->pause |= HC_PAUSE_ERROR;
+  }
+}
+
+// One lateral step of the apply passes (:4630-4677, :4690-4744) from a cell
+// at elevation e0 (tau0, erodetot3 et3) toward its neighbour N.  Returns
+// false when the raw amount is not positive; otherwise the (possibly zeroed
+// or capped) amount, which the caller applies and hands to slide_GS even
+// when it is zero, as the reference does.
+__device__ __forceinline__ bool lateral_amount(const hc_params& p, double mult, double ts,
+                                               double tau0, double et3, const ApplyRow& N,
+                                               double e0, bool boundary, double& amt) {
+  const double DX = p.DX;
+  const double e_nb = N.elev;
+  amt = 0;
+  if (N.h < p.water_depth_erosion_threshold)
+    amt = mult * p.lateral_constant * tau0 * N.edge * ts / DX;
+  else
+    amt = p.chann_lateral_erosion * et3 * (e_nb - e0) / DX * 0.1;
+  if (!(amt > 0)) return false;
+  // amt *= 1 - veg * (1 - veg_lat_restriction): veg is zero (no vegetation)
+  if ((e_nb - amt) < N.bed || boundary) amt = 0;
+  if (amt > p.ERODEFACTOR * 0.1) amt = p.ERODEFACTOR * 0.1;
+  return true;
+}
+
+// the lateral step of cell C (elevation e0) toward neighbour N
+__device__ __forceinline__ void lateral_step(const hc_view& c, hc_dev* d, double mult, double ts,
+                                             double tau0, double et3, size_t ccell, ApplyRow& C,
+                                             double e0, size_t ncell, ApplyRow& N, bool boundary,
+                                             double& elev_update) {
+  const double en = N.elev;
+  double amt;
+  if (en > e0 && lateral_amount(c.p, mult, ts, tau0, et3, N, e0, boundary, amt)) {
+    elev_update += amt;
+    N.elev = en - amt;
+    N.dirty = true;
+    slide_GS_rows(c, d, ncell, N, amt, ccell, C);
+  }
+}
+
+// the gather of an active cell (:4579-4628): grain += incoming - outgoing,
+// elev += erodetot, sort_active when the cell lost material.  Returns the
+// new elevation.
+__device__ __forceinline__ double gather_row(const hc_view& c, hc_dev* d, size_t cell,
+                                             ApplyRow& r, const double* pre, double ss) {
+  const bool susp1 = c.p.isSuspended[1] != 0;
+#pragma unroll
+  for (int n = 1; n <= HC_G - 1; n++) {
+    if (n == 1 && susp1) {
+      const double g = r.g[1] - ss;
+      r.g[1] = g + pre[0];
+    } else {
+      r.g[n] += pre[n];
+    }
+  }
+  const double erodetot = pre[10];
+  const double e0 = r.elev + erodetot;
+  r.elev = e0;
+  r.dirty = true;
+  if (erodetot < 0) sort_active_row(c, d, cell, r);
+  return e0;
+}
+
+__device__ __forceinline__ void load_pre(const hc_view& c, size_t cell, double* pre,
+                                         double& ss) {
+#pragma unroll
+  for (int k = 0; k <= HC_G; k++) pre[k] = PRE(c, k, cell);
+  ss = c.ss[cell];
+}
+
+// Isolated cells gather here, in parallel; chain starts of both passes go to
+// the lists.  x pass: lat(r) = erodetot3 > 0 (r in 1..imax); a chain starts
+// at x when rows x-1, x are not linked (or x == 1) and x is linked to x+1.
+// y pass: lat(q) = wet-listed with erodetot3 > 0 (q in 2..jmax-1, rows
+// 2..imax-1).
+__global__ void __launch_bounds__(256) k_apply_gather(const hc_view c, hc_dev* d) {
   if (!(d->it_active && d->rest_active && d->do_erode) || d->erode_retry) return;
   const int y = 2 + blockIdx.x * blockDim.x + threadIdx.x;
   const int x = 1 + blockIdx.y * blockDim.y + threadIdx.y;
   if (y > c.jmax - 1 || x > c.imax) return;
   const size_t W = c.W;
-  auto lat = [&](int r) { return r >= 1 && r <= c.imax && c.erodetot3[(size_t)r * W + y] > 0; };
-  const bool link_prev = lat(x - 1) || lat(x);
-  if (link_prev && x > 1) return;  // inside a chain that starts above
-  const bool link_next = lat(x) || lat(x + 1);
-  size_t cell = (size_t)x * W + y;
-  if (!link_next && !apply_active(c, cell, x)) return;
-  const double mult = d->mult, ts = d->s.time_step;
-  for (int r = x; r <= c.imax; r++) {
-    cell = (size_t)r * W + y;
-    if (apply_active(c, cell, r)) apply_cell(c, d, cell, r, y, mult, ts);
-    if (!(lat(r) || lat(r + 1))) break;
+  const size_t cell = (size_t)x * W + y;
+  const double* et3 = c.erodetot3;
+  const bool lat0 = et3[cell] > 0;
+  const bool latm = x - 1 >= 1 && et3[cell - W] > 0;
+  const bool latp = x + 1 <= c.imax && et3[cell + W] > 0;
+  const bool link_prev = latm || lat0, link_next = lat0 || latp;
+  if (!(link_prev && x > 1)) {
+    if (link_next) {
+      const unsigned k = atomicAdd(&d->xchains, 1u);
+      c.chains[k] = (uint32_t)cell;
+    } else if (apply_active(c, cell, x)) {
+      ApplyRow r;
+      row_load(c, cell, EX(c, x, y), r);
+      double pre[HC_G + 1], ss;
+      load_pre(c, cell, pre, ss);
+      gather_row(c, d, cell, r, pre, ss);
+      row_store(c, cell, r);
+    }
+  }
+  if (x >= 2 && x <= c.imax - 1) {
+    auto lat = [&](int q) {
+      return q >= 2 && q <= c.jmax - 1 && c.mask[cell - y + q] && et3[cell - y + q] > 0;
+    };
+    const bool l0 = lat(y);
+    if (!((lat(y - 1) || l0) && y > 2) && (l0 || lat(y + 1))) {
+      const unsigned k = atomicAdd(&d->ychains, 1u);
+      c.chains[c.N2 + k] = (uint32_t)cell;
+    }
   }
 }
 
-// one cell of the +/-y lateral pass (:4690-4744)
-__device__ void yside_cell(const hc_view& c, hc_dev* d, size_t cell, int x, int y, double mult,
-                           double ts, double et3) {
-  double elev_update = 0;
-  const double tau0 = c.tau[cell];
-  {
-    const size_t nb = cell - 1;
-    const double en = c.elev[nb], e0 = c.elev[cell];
-    double amt;
-    if (en > e0 &&
-        lateral_amount(c, mult, ts, tau0, et3, nb, EX(c, x, y - 1), en, e0, y - 1 == 1, amt)) {
-      elev_update += amt;
-      c.elev[nb] = en - amt;
-      slide_GS_dev(c, d, nb, amt, cell, false);
-    }
-  }
-  {
-    const size_t nb = cell + 1;
-    const double en = c.elev[nb], e0 = c.elev[cell];
-    double amt;
-    if (en > e0 &&
-        lateral_amount(c, mult, ts, tau0, et3, nb, EX(c, x, y + 1), en, e0, y + 1 == c.jmax, amt)) {
-      elev_update += amt;
-      c.elev[nb] = en - amt;
-      slide_GS_dev(c, d, nb, amt, cell, false);
-    }
-  }
-  c.elev[cell] = c.elev[cell] + elev_update;
-}
-
-// chains along the rows for the +/-y pass: lateral cells are the wet-listed
-// cells with erodetot3 > 0 in columns 2..jmax-1
-__global__ void __launch_bounds__(256) k_apply_ychains(const hc_view c, hc_dev* d) {
+// chains along the columns, one per thread: rows r-1, r, r+1 held in U, C, D
+__global__ void __launch_bounds__(128) k_apply_xchains(const hc_view c, hc_dev* d) {
   if (!(d->it_active && d->rest_active && d->do_erode) || d->erode_retry) return;
-  const int y = 2 + blockIdx.x * blockDim.x + threadIdx.x;
-  const int x = 2 + blockIdx.y * blockDim.y + threadIdx.y;
-  if (y > c.jmax - 1 || x > c.imax - 1) return;
-  const size_t W = c.W;
-  const size_t row = (size_t)x * W;
-  auto lat = [&](int q) {
-    return q >= 2 && q <= c.jmax - 1 && c.mask[row + q] && c.erodetot3[row + q] > 0;
-  };
-  if ((lat(y - 1) || lat(y)) && y > 2) return;
-  if (!(lat(y) || lat(y + 1))) return;
+  const unsigned nch = d->xchains;
   const double mult = d->mult, ts = d->s.time_step;
-  for (int q = y; q <= c.jmax - 1; q++) {
-    if (lat(q)) yside_cell(c, d, row + q, x, q, mult, ts, c.erodetot3[row + q]);
-    if (!(lat(q) || lat(q + 1))) break;
+  const size_t W = c.W;
+  for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < nch; k += gridDim.x * blockDim.x) {
+    size_t cell = c.chains[k];
+    const int y = (int)(cell % W);
+    int r = (int)(cell / W);
+    ApplyRow U, C, D;
+    bool hasU = false;
+    size_t ucell = 0;
+    row_load(c, cell, EX(c, r, y), C);
+    double Cet3 = c.erodetot3[cell];
+    bool Cact = apply_active(c, cell, r);
+    for (;;) {
+      // everything this step reads, issued together
+      const bool hasD = r + 1 <= c.imax;
+      const size_t dcell = cell + W;
+      double Det3 = 0;
+      bool Dact = false;
+      if (hasD) {
+        row_load(c, dcell, EX(c, r + 1, y), D);
+        Det3 = c.erodetot3[dcell];
+        Dact = apply_active(c, dcell, r + 1);
+      }
+      if (Cact) {
+        double pre[HC_G + 1], ss;
+        load_pre(c, cell, pre, ss);
+        const double tau0 = c.tau[cell];
+        const double e0 = gather_row(c, d, cell, C, pre, ss);
+        if (Cet3 > 0) {
+          double elev_update = 0;
+          if (r > 2 && hasU)
+            lateral_step(c, d, mult, ts, tau0, Cet3, cell, C, e0, ucell, U, r - 1 == 1,
+                         elev_update);
+          if (r < c.imax - 1 && hasD)
+            lateral_step(c, d, mult, ts, tau0, Cet3, cell, C, e0, dcell, D, r + 1 == c.imax,
+                         elev_update);
+          C.elev = C.elev + elev_update;
+        }
+      }
+      if (hasU) row_store(c, ucell, U);  // row r-1 is final
+      if (!(Cet3 > 0 || Det3 > 0) || !hasD) {
+        row_store(c, cell, C);
+        if (hasD) row_store(c, dcell, D);
+        break;
+      }
+      U = C;
+      hasU = true;
+      ucell = cell;
+      C = D;
+      Cet3 = Det3;
+      Cact = Dact;
+      cell = dcell;
+      r++;
+    }
+  }
+}
+
+// chains along the rows for the +/-y pass: columns q-1, q, q+1 held in
+// U, C, D
+__global__ void __launch_bounds__(128) k_apply_ychains(const hc_view c, hc_dev* d) {
+  if (!(d->it_active && d->rest_active && d->do_erode) || d->erode_retry) return;
+  const unsigned nch = d->ychains;
+  const double mult = d->mult, ts = d->s.time_step;
+  const size_t W = c.W;
+  for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < nch; k += gridDim.x * blockDim.x) {
+    size_t cell = c.chains[c.N2 + k];
+    const int x = (int)(cell / W);
+    int q = (int)(cell % W);
+    const size_t row = (size_t)x * W;
+    auto lat = [&](int qq) {
+      return qq >= 2 && qq <= c.jmax - 1 && c.mask[row + qq] && c.erodetot3[row + qq] > 0;
+    };
+    ApplyRow U, C, D;
+    row_load(c, cell - 1, EX(c, x, q - 1), U);
+    row_load(c, cell, EX(c, x, q), C);
+    bool Clat = lat(q);
+    for (;;) {
+      const size_t dcell = cell + 1;
+      row_load(c, dcell, EX(c, x, q + 1), D);  // q + 1 <= jmax
+      const bool Dlat = lat(q + 1);
+      if (Clat) {
+        const double tau0 = c.tau[cell];
+        const double et3 = c.erodetot3[cell];
+        const double e0 = C.elev;
+        double elev_update = 0;
+        lateral_step(c, d, mult, ts, tau0, et3, cell, C, e0, cell - 1, U, q - 1 == 1,
+                     elev_update);
+        lateral_step(c, d, mult, ts, tau0, et3, cell, C, e0, dcell, D, q + 1 == c.jmax,
+                     elev_update);
+        C.elev = C.elev + elev_update;
+        C.dirty = true;
+      }
+      row_store(c, cell - 1, U);  // column q-1 is final
+      if (!(Clat || Dlat) || q + 1 > c.jmax - 1) {
+        row_store(c, cell, C);
+        row_store(c, dcell, D);
+        break;
+      }
+      U = C;
+      C = D;
+      Clat = Dlat;
+      cell = dcell;
+      q++;
+    }
   }
 }
 
@@ -796,16 +1006,18 @@ void launch_erode_pass(hc_ctx* c, int max_passes, cudaGraphConditionalHandle nex
   count_launch(c, 1);
 }
 
+// walkers: grid-stride over the chain lists, several blocks per SM
+constexpr int kWalkBlocks = 152 * 8;
+
 void launch_erode_finish(hc_ctx* c, int gated) {
   ErodeScratch s = scratch_of(c);
   dim3 b(32, 8);
   dim3 g((c->v.jmax - 2 + 31) / 32, (c->v.imax + 7) / 8);
   k_apply_pre<<<g, b, 0, c->cs>>>(c->v, c->dev);
-  count_launch(c, 1);
-  k_apply_xchains<<<g, b, 0, c->cs>>>(c->v, c->dev);
-  count_launch(c, 1);
-  k_apply_ychains<<<g, b, 0, c->cs>>>(c->v, c->dev);
-  count_launch(c, 1);
+  k_apply_gather<<<g, b, 0, c->cs>>>(c->v, c->dev);
+  k_apply_xchains<<<kWalkBlocks, 128, 0, c->cs>>>(c->v, c->dev);
+  k_apply_ychains<<<kWalkBlocks, 128, 0, c->cs>>>(c->v, c->dev);
+  count_launch(c, 4);
   k_edge_out<<<1, 1024, 0, c->cs>>>(c->v, c->dev, s.contrib, nullptr);
   count_launch(c, 1);
   k_erode_post<<<1, 1, 0, c->cs>>>(c->v, c->dev, gated);

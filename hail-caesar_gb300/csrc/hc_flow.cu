@@ -170,9 +170,11 @@ __global__ void k_control(const hc_view c, hc_dev* d, hc_iter_handles hh) {
     s.baseflow = jmeanmax * 1.25;
     recalc = true;
   }
-  // The drainage area (a sort of all elevations) and the input-point list are
-  // recomputed on the host before the next iteration; within this iteration
-  // the reference applies the new list only from the next one as well.
+  // The drainage area and the input-point list are recomputed before the
+  // next iteration (the host sorts the elevations, hc_drain.cu does the
+  // rest), from the elevations as they are now (k_drain_snapshot); the
+  // reference, too, applies the new list from the next iteration on.
+  d->do_drain = recalc;
   if (recalc) d->pause |= HC_PAUSE_DRAINAGE;
 
   s.flow_timestep = flow_dt_of(p, s);
@@ -225,12 +227,17 @@ struct FaceOut {
   int dir;  // 1: positive, -1: negative, 0: none
 };
 
-// Three-way test of a > b where both are only known to a relative 2^-18:
+// Three-way test of A > B from float estimates a, b, each within a relative
+// 2^-18 of A, B (or flushed to 0 below 2^-126, inf above the float range):
 // +1 surely greater, -1 surely not, 0 too close to call (the caller then
-// evaluates the reference's FP64 expression).
+// evaluates the reference's FP64 expression).  Tiny pairs, where a flushed
+// estimate carries no relative bound, are never decided here.
 __device__ __forceinline__ int decide_gt(float a, float b) {
-  if (a > b * 1.0001f) return 1;
-  if (a < b * 0.9999f) return -1;
+  const float m = 1e-4f * (fabsf(a) + fabsf(b));
+  if (!(m >= 1e-34f) || !(m < 1e30f)) return 0;
+  const float dd = a - b;
+  if (dd > m) return 1;
+  if (dd < -m) return -1;
   return 0;
 }
 
@@ -239,7 +246,9 @@ __device__ __forceinline__ int decide_gt(float a, float b) {
 // water surfaces e+h.  `edge_slope` is 0 for interior faces, +1 / -1 where
 // the reference replaces the slope by +/-edgeslope.
 //
-// The FP64 pipe (1.2 TFLOP/s on GB300) bounds this kernel, so the limiter
+// The FP64 pipe (1.2 TFLOP/s on GB300) bounds this kernel, and compares
+// occupy it as much as arithmetic does.  So every test runs on the integer
+// pipe (dgt0, dlt, ...: IEEE results for non-NaN operands), and the limiter
 // tests, which only pick a branch, are first decided on float estimates; the
 // reference's FP64 expression is evaluated only when the estimate is within
 // 1e-4 of the threshold.  The branch taken - and so the result - is always
@@ -249,34 +258,35 @@ __device__ __forceinline__ void inertial_face(double& q, double& qs, double& vel
                                               double e0, double h0, double a0, double e1,
                                               double h1, double a1, double v0, double v1,
                                               double c0, double nn, double dt, int edge_slope,
-                                              const hc_params& p, double rDX) {
+                                              const hc_view& c) {
+  const hc_params& p = c.p;
   const double DX = p.DX;
   vdir = 0;
-  double hflow = smax(a0, a1) - smax(e1, e0);
-  if (!(hflow > p.hflow_threshold)) {
+  double hflow = imax_d(a0, a1) - imax_d(e1, e0);
+  if (!(dkey(hflow) > c.thr_key)) {  // hflow > hflow_threshold
     q = 0;
     qs = 0;
     return;
   }
-  double slope = div_const(a1 - a0, DX, rDX);
+  double slope = div_const(a1 - a0, DX, c.rDX);
   if (edge_slope == 1) slope = p.edgeslope;
-  if (edge_slope == -1) slope = 0 - p.edgeslope;
+  if (edge_slope == -1) slope = zero_minus(p.edgeslope);
   const double ghd = kG * hflow * dt;
   double qn;
-  if (q == 0) {
+  if (deq0(q)) {
     // (0 - ghd*slope) / (1 + (ghd*nn*0)/h^3) = (0 - ghd*slope) / 1
     qn = q - (ghd * slope);
   } else {
     qn = ((q - (ghd * slope)) / (1 + ghd * nn * fabs(q) / cube_rn(hflow)));
   }
-  const double fl = p.froude_limit;
   const float hf = approx_abs_f(hflow);
+  const float dtf = approx_abs_f(dt);
   // q/hflow: exact when the face velocity is kept (erosion runs), where it
   // also serves the Froude test
   double qoh = 0;
   bool qoh_valid = false;
   // Froude limit: |q/hflow| / sqrt(g*hflow) > froude_limit
-  if (qn != 0) {
+  if (!deq0(qn)) {
     float fr;
     if (kVel) {
       qoh = qn / hflow;
@@ -285,49 +295,61 @@ __device__ __forceinline__ void inertial_face(double& q, double& qs, double& vel
     } else {
       fr = approx_abs_f(qn) / (hf * sqrtf(9.81f * hf));
     }
-    int t = decide_gt(fr, (float)fl);
+    int t = decide_gt(fr, c.flf);
     if (t == 0) {
       if (!qoh_valid) qoh = qn / hflow;
-      t = (fabs(qoh) / sqrt(kG * hflow) > fl) ? 1 : -1;
+      t = (fabs(qoh) / sqrt(kG * hflow) > p.froude_limit) ? 1 : -1;
     }
     if (t > 0) {
-      const double lim = hflow * (sqrt(kG * hflow) * fl);
-      qn = (qn > 0) ? lim : 0 - lim;
+      const double lim = hflow * (sqrt(kG * hflow) * p.froude_limit);
+      qn = dgt0(qn) ? lim : zero_minus(lim);
       qoh_valid = false;
     }
   }
-  // depth limit: |q*dt/DX| > (depth of the giving cell)/4
-  if (qn > 0) {
-    int t = decide_gt(approx_abs_f(qn) * approx_abs_f(dt) / (float)DX, approx_abs_f(h0) * 0.25f);
+  // depth limit: |q*dt/DX| > (depth of the giving cell)/4; the two tests
+  // run one after the other, as in the reference
+  if (dgt0(qn)) {
+    int t = decide_gt(approx_abs_f(qn) * dtf / c.DXf, approx_f(h0) * 0.25f);
     if (t == 0) t = ((qn * dt / DX) > (h0 / 4)) ? 1 : -1;
     if (t > 0) {
       qn = ((h0 * DX) / 5) / dt;
       qoh_valid = false;
     }
-  } else if (qn < 0) {
-    int t = decide_gt(approx_abs_f(qn) * approx_abs_f(dt) / (float)DX, approx_abs_f(h1) * 0.25f);
+  }
+  if (dlt0(qn)) {
+    int t = decide_gt(approx_abs_f(qn) * dtf / c.DXf, approx_f(h1) * 0.25f);
     if (t == 0) t = (fabs(qn * dt / DX) > (h1 / 4)) ? 1 : -1;
     if (t > 0) {
-      qn = 0 - ((h1 * DX) / 5) / dt;
+      qn = zero_minus(((h1 * DX) / 5) / dt);
       qoh_valid = false;
     }
   }
+  const bool qpos = dgt0(qn), qneg = dlt0(qn);
   if (kSusp) {
     // qs = q * (V/h) of the giving cell; V = 0 gives 0 * q (a signed zero)
-    if (qn > 0) qs = qn * c0;
-    if (qn < 0) qs = qn * ((v1 == 0) ? v1 : v1 / h1);  // h1 > 0 here, as h0 above
-    if (qs > 0 && qs * dt > (v0 * DX) / 4) qs = ((v0 * DX) / 5) / dt;
-    if (qs < 0 && fabs(qs * dt) > (v1 * DX) / 4) qs = 0 - ((v1 * DX) / 5) / dt;
+    if (qpos) qs = qn * c0;
+    if (qneg) qs = qn * (deq0(v1) ? v1 : v1 / h1);  // h1 > 0 here, as h0 above
+    // qs*dt > V*DX/4 (giving cell) caps the sediment flux
+    if (dgt0(qs)) {
+      int t = decide_gt(approx_abs_f(qs) * dtf, approx_f(v0) * c.DXf * 0.25f);
+      if (t == 0) t = (qs * dt > (v0 * DX) / 4) ? 1 : -1;
+      if (t > 0) qs = ((v0 * DX) / 5) / dt;
+    }
+    if (dlt0(qs)) {
+      int t = decide_gt(approx_abs_f(qs) * dtf, approx_f(v1) * c.DXf * 0.25f);
+      if (t == 0) t = (fabs(qs * dt) > (v1 * DX) / 4) ? 1 : -1;
+      if (t > 0) qs = zero_minus(((v1 * DX) / 5) / dt);
+    }
   }
   if (kVel) {
     // (0 - q)/hflow = -(q/hflow) exactly: division rounds symmetrically
-    if (qn != 0 && !qoh_valid) qoh = qn / hflow;
-    if (qn > 0) {
+    if ((qpos || qneg) && !qoh_valid) qoh = qn / hflow;
+    if (qpos) {
       vel_out = qoh;
       vdir = 1;
     }
-    if (qn < 0) {
-      vel_out = 0 - qoh;
+    if (qneg) {
+      vel_out = zero_minus(qoh);
       vdir = -1;
     }
   }
@@ -340,12 +362,13 @@ __device__ __forceinline__ void flow_cell(const hc_view& c, const hc_dev* __rest
   const size_t W = c.W, N2 = c.N2;
   const int i = (int)(cell / W), j = (int)(cell % W);
   const double e0 = c.elev[cell];
-  if (!(e0 > -9999)) return;
+  // e > -9999 (no-data and below are skipped)
+  auto above_nodata = [](double e) { return dkey(e) > kNoDataKey; };
+  if (!above_nodata(e0)) return;
   const hc_params& p = c.p;
   const double dt = d->s.flow_timestep;
   const double n = p.spatially_var_mannings ? c.man[cell] : p.mannings;
   const double nn = n * n;
-  const double rDX = c.rDX;
   const bool susp = kSed && p.isSuspended[1] != 0;
   const double h0 = c.h[cell];
   const double a0 = e0 + h0;
@@ -353,21 +376,22 @@ __device__ __forceinline__ void flow_cell(const hc_view& c, const hc_dev* __rest
   // V/h of this cell, shared by both faces.  Only used where q > 0 after
   // the depth limit, which implies h > 0, so a zero V gives V itself (with
   // its sign) without the division.
-  const double c0 = (susp && v0 != 0) ? v0 / h0 : v0;
+  const double c0 = (susp && !deq0(v0)) ? v0 / h0 : v0;
+  const bool wet0 = dgt0(h0);
   // x face (rows i-1, i)
   {
     const size_t up = cell - W;
     const double h1 = c.h[up], e1 = c.elev[up];
-    if ((h0 > 0 || h1 > 0) && e1 > -9999) {
+    if ((wet0 || dgt0(h1)) && above_nodata(e1)) {
       double q = c.qx[cell], qs = kSed ? c.qxs[cell] : 0.0, vel = 0;
       int vdir;
       const int es = (i == c.imax) ? 1 : ((i <= 2) ? -1 : 0);
       if (susp)
         inertial_face<true, kSed>(q, qs, vel, vdir, e0, h0, a0, e1, h1, e1 + h1, v0, c.vs[up],
-                                  c0, nn, dt, es, p, rDX);
+                                  c0, nn, dt, es, c);
       else
         inertial_face<false, kSed>(q, qs, vel, vdir, e0, h0, a0, e1, h1, e1 + h1, v0, 0.0, c0,
-                                   nn, dt, es, p, rDX);
+                                   nn, dt, es, c);
       c.qx[cell] = q;
       if (kSed) {
         c.qxs[cell] = qs;
@@ -382,16 +406,16 @@ __device__ __forceinline__ void flow_cell(const hc_view& c, const hc_dev* __rest
   {
     const size_t lf = cell - 1;
     const double h1 = c.h[lf], e1 = c.elev[lf];
-    if ((h0 > 0 || h1 > 0) && e1 > -9999) {
+    if ((wet0 || dgt0(h1)) && above_nodata(e1)) {
       double q = c.qy[cell], qs = kSed ? c.qys[cell] : 0.0, vel = 0;
       int vdir;
       const int es = (j == c.jmax) ? 1 : ((j <= 2) ? -1 : 0);
       if (susp)
         inertial_face<true, kSed>(q, qs, vel, vdir, e0, h0, a0, e1, h1, e1 + h1, v0, c.vs[lf],
-                                  c0, nn, dt, es, p, rDX);
+                                  c0, nn, dt, es, c);
       else
         inertial_face<false, kSed>(q, qs, vel, vdir, e0, h0, a0, e1, h1, e1 + h1, v0, 0.0, c0,
-                                   nn, dt, es, p, rDX);
+                                   nn, dt, es, c);
       c.qy[cell] = q;
       if (kSed) {
         c.qys[cell] = qs;
@@ -418,14 +442,17 @@ __global__ void __launch_bounds__(256) k_flow_route(const hc_view c, const hc_de
 // then the last block publishes the grid result).
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_depth_update(const hc_view c, hc_dev* d, int gated) {
-  __shared__ double warp_max[8];
+  __shared__ long long warp_max[8];
   __shared__ bool last;
   if (gated && !d->it_active) return;
   const size_t W = c.W;
   const double dt = d->s.flow_timestep, DX = c.p.DX, rDX = c.rDX;
   const bool susp = c.p.isSuspended[1] && !c.p.hydro_only;
   const int nw = d->wet_count;
-  double m = 0;
+  // the running maximum is kept as the bits of a non-negative double, which
+  // order like the values; tests run on the integer pipe (dgt0 etc.)
+  long long m = 0;
+  bool nonfinite = false;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nw; k += gridDim.x * blockDim.x) {
     const size_t cell = (size_t)c.wet[k];
     double h = c.h[cell];
@@ -434,20 +461,25 @@ __global__ void __launch_bounds__(256) k_depth_update(const hc_view c, hc_dev* d
     if (susp)
       c.vs[cell] += div_const(dt * (c.qxs[cell + W] - c.qxs[cell] + c.qys[cell + 1] - c.qys[cell]),
                               DX, rDX);
-    if (h > 0) {
-      if (c.elev[cell] == -9999) h = 0;
-      if (h > m) m = h;
+    nonfinite |= disnan(h);
+    if (dgt0(h)) {
+      if (dbits(c.elev[cell]) == kNoDataBits) h = 0;
+      else m = max(m, dbits(h));
     }
     c.h[cell] = h;
   }
-  for (int o = 16; o > 0; o >>= 1) m = smax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if (nonfinite) {
+    d->err_code = 301;  // a NaN water depth: the run cannot continue
+    atomicOr((unsigned int*)&d->pause, HC_PAUSE_ERROR);
+  }
+  for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
   const int t = threadIdx.x;
   if ((t & 31) == 0) warp_max[t >> 5] = m;
   __syncthreads();
   if (t == 0) {
-    double b = 0;
-    for (int w = 0; w < (int)blockDim.x / 32; w++) b = smax(b, warp_max[w]);
-    if (b > 0) atomic_max_pos(&d->maxdepth_bits, b);
+    long long b = 0;
+    for (int w = 0; w < (int)blockDim.x / 32; w++) b = max(b, warp_max[w]);
+    if (b > 0) atomicMax(&d->maxdepth_bits, (unsigned long long)b);
     __threadfence();
     last = (atomicAdd(&d->depth_done, 1u) == gridDim.x - 1);
   }

@@ -1,8 +1,9 @@
 // Host-side pieces of the path that the reference itself runs rarely and
 // that depend only on inputs or on a full sort:
-//   * drainage area + catchment input points (drainage_area_D8 :2091-2271,
-//     zero_and_calc_drainage_area :2072-2089, get_catchment_input_points
-//     :3741-3767), recomputed when the baseflow threshold moves;
+//   * the processing order of the drainage area (drainage_area_D8
+//     :2091-2271), a sort of all elevations, recomputed when the baseflow
+//     threshold moves (the accumulation itself runs on the device,
+//     hc_drain.cu);
 //   * the TOPMODEL recurrence (topmodel_runoff :3649-3715), which depends
 //     only on the rain table and is tabulated once per run.
 // Both use the host C library exactly as the reference does (std::sort with
@@ -13,118 +14,165 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <mutex>
+#include <thread>
 #include <utility>
 #include <vector>
 
 #include "../../include/hc_gpu.h"
 
-namespace {
-const int kDX[9] = {0, 0, 1, 1, 1, 0, -1, -1, -1};
-const int kDY[9] = {0, -1, -1, 0, 1, 1, 1, 0, -1};
+// The reference sorts the row keys and the column keys of all cells in two
+// separate std::sort calls on (key, elevation) pairs, comparing elevations
+// only (drainage_area_D8 :2091-2180).  std::sort's moves depend only on the
+// comparisons, which see only the elevations, so both calls apply the same
+// permutation: one sort carrying the cell number gives both orders, ties
+// included.
+//
+// That permutation, including the order it gives to equal elevations, is
+// what GCC's std::sort produces: introsort (Musser, "Introspective Sorting
+// and Selection Algorithms", 1997) with median-of-three pivots, a two-sided
+// partition, heapsort below a depth of 2*floor(log2 n), and a final
+// insertion sort over runs of at most 16.  sort_exact below performs exactly
+// those steps; only the independent sub-ranges left of and right of each cut
+// are sorted by separate threads, which cannot change the result.  A CPU test
+// checks the permutation against std::sort on inputs with many ties.
+namespace exact_sort {
+
+using Pair = std::pair<double, double>;  // (cell number, elevation)
+constexpr std::ptrdiff_t kRun = 16;
+
+inline bool before(const Pair& a, const Pair& b) { return a.second < b.second; }
+
+// median of *a, *b, *c moved to *result
+inline void median_to_first(Pair* result, Pair* a, Pair* b, Pair* c) {
+  if (before(*a, *b)) {
+    if (before(*b, *c)) std::swap(*result, *b);
+    else if (before(*a, *c)) std::swap(*result, *c);
+    else std::swap(*result, *a);
+  } else if (before(*a, *c)) {
+    std::swap(*result, *a);
+  } else if (before(*b, *c)) {
+    std::swap(*result, *c);
+  } else {
+    std::swap(*result, *b);
+  }
 }
 
-// The reference sorts the row keys and the column keys of all cells in two
-// separate std::sort calls on (key, elevation) pairs.  std::sort's moves
-// depend only on the comparisons, which see only the elevations, so both
-// calls apply the same permutation: one sort carrying the cell number gives
-// both orders, ties included.  The permutation is kept and reused while the
-// elevations are unchanged (always in hydro-only runs).
+// partition of [first, last) around *pivot (which lies before first)
+inline Pair* split_at(Pair* first, Pair* last, const Pair* pivot) {
+  for (;;) {
+    while (before(*first, *pivot)) ++first;
+    --last;
+    while (before(*pivot, *last)) --last;
+    if (!(first < last)) return first;
+    std::swap(*first, *last);
+    ++first;
+  }
+}
+
+inline void insertion_run(Pair* first, Pair* last) {
+  for (Pair* i = first + 1; i < last; ++i) {
+    Pair v = *i;
+    Pair* j = i;
+    while (j > first && before(v, *(j - 1))) {
+      *j = *(j - 1);
+      --j;
+    }
+    *j = v;
+  }
+}
+
+inline void heap_run(Pair* first, Pair* last) {
+  auto cmp = [](const Pair& a, const Pair& b) { return a.second < b.second; };
+  std::make_heap(first, last, cmp);
+  std::sort_heap(first, last, cmp);
+}
+
+// The introsort loop on [first, last).  Right-hand ranges of at least
+// `spawn_min` elements go to a new thread while `spawn` threads remain.
+void loop(Pair* first, Pair* last, long depth, int spawn, std::ptrdiff_t spawn_min,
+          std::vector<std::thread>* threads, std::mutex* mu) {
+  while (last - first > kRun) {
+    if (depth == 0) {
+      heap_run(first, last);
+      return;
+    }
+    --depth;
+    Pair* mid = first + (last - first) / 2;
+    median_to_first(first, first + 1, mid, last - 1);
+    Pair* cut = split_at(first + 1, last, first);
+    if (spawn > 0 && last - cut >= spawn_min) {
+      const int child = spawn / 2;
+      spawn -= child + 1;
+      std::lock_guard<std::mutex> lock(*mu);
+      threads->emplace_back(loop, cut, last, depth, child, spawn_min, threads, mu);
+    } else {
+      loop(cut, last, depth, 0, spawn_min, threads, mu);
+    }
+    last = cut;
+  }
+  // the final insertion sort, restricted to this run: no element moves past
+  // a cut (everything left of a cut is <= the pivot <= everything right)
+  insertion_run(first, last);
+}
+
+}  // namespace exact_sort
+
+void host_sort_exact(std::pair<double, double>* a, size_t n, int threads) {
+  if (n < 2) return;
+  long lg = 0;
+  for (size_t m = n; m > 1; m >>= 1) lg++;
+  std::vector<std::thread> th;
+  th.reserve(2 * threads + 2);
+  std::mutex mu;
+  exact_sort::loop(a, a + n, 2 * lg, threads - 1, 1 << 16, &th, &mu);
+  // joined in creation order; a thread may add more while we wait
+  for (size_t k = 0;; k++) {
+    std::thread t;
+    {
+      std::lock_guard<std::mutex> lock(mu);
+      if (k >= th.size()) break;
+      t = std::move(th[k]);
+    }
+    t.join();
+  }
+}
+
+// The processing order of drainage_area_D8 for these elevations: order[n]
+// is the cell at sorted position n (0 for the reference's padding pairs).
+// Kept and reused while the elevations are unchanged (always in hydro-only
+// runs).
 struct DrainageCache {
-  std::vector<uint32_t> order;   // cell numbers in the reference's processing order
+  std::vector<uint32_t> order;
   std::vector<double> elev;      // elevations the order was made from
 };
 
 void* host_drainage_cache_new() { return new DrainageCache(); }
 void host_drainage_cache_free(void* p) { delete (DrainageCache*)p; }
 
-void host_drainage_and_points(const hc_params* p, const double* elev, const int32_t* rfarea,
-                              double baseflow, double* area, int32_t* cin_x, int32_t* cin_y,
-                              int* total, double* counters, void* cache_p, bool elev_fixed) {
+const uint32_t* host_drainage_order(const hc_params* p, const double* elev, void* cache_p,
+                                    bool* reused) {
   const unsigned imax = p->imax, jmax = p->jmax;
   const size_t W = jmax + 2, N2 = (size_t)(imax + 2) * W;
-  auto ix = [&](unsigned i, unsigned j) { return (size_t)i * W + j; };
   DrainageCache* cache = (DrainageCache*)cache_p;
-  bool reuse = cache && !cache->order.empty();
-  if (reuse && !elev_fixed)
-    reuse = std::memcmp(cache->elev.data(), elev, N2 * sizeof(double)) == 0;
-  if (!reuse) {
-    std::vector<std::pair<double, double>> pr(N2);
-    for (size_t k = 0; k < N2; k++) pr[k] = std::make_pair(0.0, 0.0);
-    size_t inc = 1;
-    for (unsigned i = 1; i <= imax; i++)
-      for (unsigned j = 1; j <= jmax; j++) {
-        pr[inc] = std::make_pair((double)ix(i, j), elev[ix(i, j)]);
-        inc++;
-      }
-    std::sort(pr.begin(), pr.end(),
-              [](const std::pair<double, double>& a, const std::pair<double, double>& b) {
-                return a.second < b.second;
-              });
-    cache->order.resize(N2);
-    for (size_t k = 0; k < N2; k++) cache->order[k] = (uint32_t)pr[k].first;
-    cache->elev.assign(elev, elev + N2);
-  }
-  std::vector<double> ad(N2, 0.0);
+  *reused = !cache->order.empty() &&
+            std::memcmp(cache->elev.data(), elev, N2 * sizeof(double)) == 0;
+  if (*reused) return cache->order.data();
+  // the reference's pair vector: (imax+2)(jmax+2) pairs, (0, 0) except
+  // positions 1 .. imax*jmax, which hold the cells row by row
+  std::vector<std::pair<double, double>> pr(N2, std::make_pair(0.0, 0.0));
+  size_t inc = 1;
   for (unsigned i = 1; i <= imax; i++)
     for (unsigned j = 1; j <= jmax; j++) {
-      ad[ix(i, j)] = 1;
-      area[ix(i, j)] = 0;
-      if (elev[ix(i, j)] == -9999) ad[ix(i, j)] = 0.0;
+      const size_t cell = (size_t)i * W + j;
+      pr[inc++] = std::make_pair((double)cell, elev[cell]);
     }
-  const std::vector<uint32_t>& ord = cache->order;
-  for (unsigned n = jmax * imax; n >= 1; n--) {
-    const int i = (int)(ord[n] / W), j = (int)(ord[n] % W);
-    double& a = ad[ix(i, j)];
-    if (!(a > 0)) continue;
-    if (a > area[ix(i, j)]) area[ix(i, j)] = a;
-    const double e = elev[ix(i, j)];
-    double difftot = 0;
-    int nb[9][2];
-    for (int dir = 1; dir <= 8; dir++) {
-      int j2 = j + kDY[dir], i2 = i + kDX[dir];
-      if (j2 < 1) j2 = 1;
-      if (i2 < 1) i2 = 1;
-      if (j2 > (int)jmax) j2 = jmax;
-      if (i2 > (int)imax) i2 = imax;
-      nb[dir][0] = i2;
-      nb[dir][1] = j2;
-      const double e2 = elev[ix(i2, j2)];
-      if (dir % 2 != 0) {
-        if (e2 < e) difftot += e - e2;
-      } else {
-        if (e2 < e) difftot += (e - e2) / 1.414;
-      }
-    }
-    if (difftot > 0) {
-      for (int dir = 1; dir <= 8; dir++) {
-        const int i2 = nb[dir][0], j2 = nb[dir][1];
-        const double e2 = elev[ix(i2, j2)];
-        if (dir % 2 != 0) {
-          if (e2 < e) ad[ix(i2, j2)] += a * ((e - e2) / difftot);
-        } else {
-          if (e2 < e) ad[ix(i2, j2)] += a * (((e - e2) / 1.414) / difftot);
-        }
-      }
-    }
-    a = 0;
-  }
-  // input points: cin_x/cin_y keep their old contents beyond the new count,
-  // as the reference's vectors do
-  const double DX = p->DX;
-  int t = 0;
-  for (int n = 1; n <= p->rfnum; n++) counters[n] = 0;
-  for (unsigned i = 1; i <= imax; i++)
-    for (unsigned j = 1; j <= jmax; j++) {
-      const double q = area[ix(i, j)] * baseflow * 3 * DX * DX;
-      if (q > p->MIN_Q && q < p->MIN_Q_MAXVAL) {
-        t++;
-        cin_x[t] = i;
-        cin_y[t] = j;
-        counters[rfarea[ix(i, j)]] += 1;
-      }
-    }
-  if (t == 0) t = 1;
-  *total = t;
+  unsigned hw = std::thread::hardware_concurrency();
+  host_sort_exact(pr.data(), N2, (int)std::max(1u, std::min(hw, 16u)));
+  cache->order.resize(N2);
+  for (size_t k = 0; k < N2; k++) cache->order[k] = (uint32_t)pr[k].first;
+  cache->elev.assign(elev, elev + N2);
+  return cache->order.data();
 }
 
 void host_topmodel_table(const hc_params* p, const float* rain, int rows, int cols, int nsteps,

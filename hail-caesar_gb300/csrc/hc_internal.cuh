@@ -69,12 +69,29 @@ struct hc_dev {
   unsigned int misc_done;
   unsigned long long body_kernels;  // kernels run inside conditional graph nodes
   int wet_count;          // length of hc_view::wet
+  int do_drain;           // this iteration moved the baseflow threshold
+  unsigned int drain_front, drain_done, drain_points, drain_levels;
+  unsigned int drain_rf[HC_MAX_RF + 1];
+  unsigned int xchains;   // chain starts of the +/-x apply pass (hc_view::chains)
+  unsigned int ychains;   // chain starts of the +/-y apply pass
+};
+
+// Working state of a drainage recomputation (hc_drain.cu): the radix
+// selection of the sweep's last reached position and the checks that decide
+// whether the sort's tie order can matter.
+struct hc_drain_aux {
+  unsigned long long prefix, mask, k, gt, real_eq;  // selection of the P-th largest
+  unsigned long long min_u;                         // smallest elevation key
+  unsigned int min_count, min_matters, contrib_tie, pad;
+  unsigned int hist[256];
 };
 
 // Everything a kernel needs, passed by value (device pointers + parameters).
 struct hc_view {
   hc_params p;
   double rDX;             // RN(1/DX), for div_const
+  float DXf, flf;         // DX and froude_limit as floats (estimates only)
+  long long thr_key;      // dkey(hflow_threshold)
   int imax, jmax;
   size_t W, N2, E2;       // pitch, padded cells, edge-array cells
 
@@ -107,6 +124,13 @@ struct hc_view {
   // scratch
   double *erodetot, *erodetot3;  // N2 each
   double *pre;                   // 11 * N2: per-cell apply-pass terms (see hc_erode.cu)
+  uint32_t *chains;              // 2 * N2: apply-pass chain starts (x pass, then y pass)
+  // drainage area (hc_drain.cu): sweep position, sum of drops, higher
+  // neighbours pending, two frontiers, and the elevation snapshot
+  uint32_t *drain_pos, *drain_f0, *drain_f1;
+  int32_t *drain_pend;
+  double *drain_dt, *drain_snap;
+  struct hc_drain_aux *drain_aux;
   unsigned long long *alloc_key; // N2: serial-order key of the first grain-record request
   int32_t *alloc_list;           // N2: cells allocated, in order
   int32_t *slide_list; int slide_cap;
@@ -141,16 +165,22 @@ struct hc_ctx {
   // host copy of the catchment input list (kept between recomputations, as
   // the reference keeps its vector)
   int32_t *h_cin_x, *h_cin_y;
-  void* drainage_cache;   // sorted cell order, reused while elevations are unchanged
+  void* drainage_cache;    // sweep order of the drainage area, reused while elev is unchanged
+  bool area_valid;         // device area matches the cached sweep order
   // CUDA graph of K iterations
   cudaGraphExec_t graph; int graph_iters; int graph_flags;
   int64_t graph_kernels;   // kernel nodes in the graph
   cudaEvent_t chunk_done;  // a launched chunk and its control-block copy are done
   int64_t run_n;           // iterations asked of the current run
   unsigned long long body_k0;
+  int64_t budget0;         // budget when the current chunk was launched
   bool capturing;
   // counters for measurement: kernels launched, bytes moved host<->device
   int64_t launches, h2d_bytes, d2h_bytes;
+  // hc_run statistics (HC_STAT_*): how often each kind of host work ran and
+  // the host wall time it took
+  int64_t stat_n[HC_STAT_COUNT];
+  double stat_ms[HC_STAT_COUNT];
 };
 
 inline void count_launch(hc_ctx* c, int n) {
@@ -162,6 +192,35 @@ inline void count_launch(hc_ctx* c, int n) {
 
 // std::max(a, b) as libstdc++ defines it: (a < b) ? b : a
 HC_DEV double smax(double a, double b) { return (a < b) ? b : a; }
+
+// Comparisons of doubles on the integer pipe.  On this GPU a compare,
+// like any FP64-pipe instruction, costs the issue slots of dozens of
+// integer instructions, and the stencils are FP64-pipe bound.  Results are
+// the IEEE ones for every operand that is not a NaN, with +0 == -0.
+HC_DEV long long dbits(double x) { return __double_as_longlong(x); }
+// monotone key: x < y  <=>  dkey(x) < dkey(y); dkey(+0) == dkey(-0) == 0
+HC_DEV long long dkey(double x) {
+  const long long b = dbits(x);
+  const long long s = b >> 63;
+  return ((b & 0x7fffffffffffffffLL) ^ s) - s;
+}
+HC_DEV bool dgt0(double x) { return dbits(x) > 0; }                     // x > 0
+HC_DEV bool dlt0(double x) { return dbits(x) < 0 && (dbits(x) << 1) != 0; }  // x < 0
+HC_DEV bool deq0(double x) { return (dbits(x) << 1) == 0; }             // x == 0
+HC_DEV bool dlt(double a, double b) { return dkey(a) < dkey(b); }       // a < b
+HC_DEV bool dgt(double a, double b) { return dkey(a) > dkey(b); }       // a > b
+constexpr long long kNoDataKey = -0x40C3878000000000LL;  // dkey(-9999.0)
+constexpr long long kNoDataBits = (long long)0xC0C3878000000000ULL;  // dbits(-9999.0)
+// smax on the integer pipe
+HC_DEV double imax_d(double a, double b) { return dlt(a, b) ? b : a; }
+// 0 - x (the reference's spelling of a negation: +0 for x = +0)
+HC_DEV double zero_minus(double x) {
+  return deq0(x) ? 0.0 : __longlong_as_double(dbits(x) ^ (long long)0x8000000000000000ULL);
+}
+// x is a NaN
+HC_DEV bool disnan(double x) {
+  return (dbits(x) & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL;
+}
 
 // h^3 rounded to nearest.  The reference evaluates std::pow(hflow, 10/3),
 // i.e. pow(hflow, 3.0) in C++11, which glibc returns correctly rounded in
@@ -267,10 +326,14 @@ hc_status run_creep(hc_ctx* c, double time);
 size_t slide_scratch_bytes(size_t N2);
 
 // host helpers (hc_host.cpp)
-void host_drainage_and_points(const hc_params* p, const double* elev, const int32_t* rfarea,
-                              double baseflow, double* area_out, int32_t* cin_x,
-                              int32_t* cin_y, int* total, double* counters, void* cache,
-                              bool elev_fixed);
+// the drainage sweep order (std::sort's permutation, exact); cached while
+// the elevations are unchanged (*reused)
+const uint32_t* host_drainage_order(const hc_params* p, const double* elev, void* cache,
+                                    bool* reused);
+hc_status run_drainage_device(hc_ctx* c, const double* el, bool area_valid,
+                              const uint32_t* (*sort_order)(hc_ctx*, const double*),
+                              bool* sorted);
+void launch_drain_snapshot(hc_ctx* c);
 void* host_drainage_cache_new();
 void host_drainage_cache_free(void* p);
 int host_global_landsliding(const hc_params* p, const double* bedrock, double* elev);

@@ -62,6 +62,7 @@ def load_library(path=LIB_PATH):
         "hc_run_ensemble": (C.c_int, [P(vp), C.c_int32, C.c_int64, C.c_int32, P(C.c_int64)]),
         "hc_bench_kernel": (C.c_int, [vp, C.c_char_p, C.c_int32, P(C.c_double), P(C.c_int64)]),
         "hc_get_counters": (C.c_int, [vp, P(C.c_int64), P(C.c_int64), P(C.c_int64)]),
+        "hc_get_run_stats": (C.c_int, [vp, P(C.c_int64), P(C.c_double), C.c_int32]),
         "hc_profile_iteration": (C.c_int, [vp, C.c_int32, P(C.c_double)]),
     }
     for name, (res, args) in sig.items():
@@ -199,6 +200,17 @@ class Model:
         self._check(self.lib.hc_get_counters(self.h, C.byref(a), C.byref(b), C.byref(c)),
                     "counters")
         return a.value, b.value, c.value
+
+    RUN_STATS = ["chunks", "erode_retry", "lateral", "creep", "global_slide", "drainage",
+                 "drainage_sort", "drainage_sweep", "drainage_levels", "idle_iters"]
+
+    def run_stats(self):
+        """{kind: (count, host ms)} of hc_run's host-side work so far."""
+        n = len(self.RUN_STATS)
+        cnt = (C.c_int64 * n)()
+        ms = (C.c_double * n)()
+        self._check(self.lib.hc_get_run_stats(self.h, cnt, ms, n), "run_stats")
+        return {k: (cnt[i], ms[i]) for i, k in enumerate(self.RUN_STATS)}
 
     PHASES = ["control_inputs", "flow_route", "depth_update", "scan_area", "entrain_passes",
               "apply_lateral_edge", "lateral3", "water_flux_out", "slide_3"]

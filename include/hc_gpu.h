@@ -251,6 +251,25 @@ hc_status hc_run(hc_ctx* ctx, int64_t n, int32_t flags, hc_step_record* rec,
  * differ in size and parameters. */
 hc_status hc_run_ensemble(hc_ctx** ctxs, int32_t m, int64_t n, int32_t flags, int64_t* done);
 
+/* What hc_run spent on the host (no counterpart in the reference): for
+ * each kind below, how many times it ran and its host wall time in ms,
+ * accumulated since hc_create.  Pauses leave the rest of a graph chunk as
+ * no-op iterations; HC_STAT_IDLE_ITERS counts those. */
+enum {
+  HC_STAT_CHUNKS = 0,      /* graph launches */
+  HC_STAT_ERODE_RETRY,     /* erosion retries past the captured passes */
+  HC_STAT_LATERAL,         /* lateral3 runs (host-driven convergence loop) */
+  HC_STAT_CREEP,           /* slope creep */
+  HC_STAT_GLOBAL_SLIDE,    /* global landsliding */
+  HC_STAT_DRAINAGE,        /* drainage area + input points (baseflow change) */
+  HC_STAT_DRAINAGE_SORT,   /* of those, host sorts (equal elevations that matter) */
+  HC_STAT_DRAINAGE_SWEEP,  /* device accumulation (ms: device time) */
+  HC_STAT_DRAINAGE_LEVELS, /* frontiers the accumulations went through (count) */
+  HC_STAT_IDLE_ITERS,      /* captured iterations skipped after a pause */
+  HC_STAT_COUNT
+};
+hc_status hc_get_run_stats(hc_ctx* ctx, int64_t* counts, double* host_ms, int32_t n);
+
 /* Stream the context issues its work on (a cudaStream_t). */
 void* hc_stream(hc_ctx* ctx);
 

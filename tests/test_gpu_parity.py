@@ -118,6 +118,25 @@ def test_erosion_catchment_lateral(gpu_lib, oracle_mod):
     check_records(g, r)
     _check_sediment(m, o)
     assert_close(m.field("edge"), o.field("edge"), 1e-9, "edge")
+    # the drainage area of the last baseflow change, from the elevations at
+    # the start of that iteration
+    assert_close(m.field("area"), o.field("area"), 0, "area", rtol=1e-12)
+
+
+def test_drainage_area_ties_and_nodata(gpu_lib, oracle_mod):
+    """Plateaus (many equal elevations, so the sort's tie order decides the
+    order of the pushes) and no-data cells (the sweep's unreached positions):
+    the device sweep reproduces the reference's areas bit for bit."""
+    case = synth.catchment_case(n=48, DX=20.0, hours=72, relief=60.0, hydro_only=True,
+                                lateral=False, storm_start_h=0.5)
+    z = np.round(case.elev * 2) / 2
+    z[:, :5] = -9999.0
+    z[30:34, 10:14] = -9999.0
+    case.elev = np.ascontiguousarray(z)
+    m, g, o, r = run_pair(case, 1500, oracle_mod)
+    assert_bitwise(m.field("area"), o.field("area"), "area")
+    check_records(g, r)
+    check_hydro(m, o)
 
 
 def test_run_deterministic(gpu_lib):

@@ -54,3 +54,15 @@ def test_glibc_pow_cube_is_not_always_correctly_rounded(numlib):
 @pytest.mark.parametrize("y", [5.0, 10.0, 20.0, 50.0, 12.5, 9.81, 3.0, 100.0])
 def test_div_const_equals_division(numlib, y):
     assert numlib.div_mismatches(y, 400000, 1234) == 0
+
+
+def test_exact_sort_matches_std_sort(tmp_path):
+    """The drainage order (hc_host.cpp) is std::sort's permutation, ties
+    included, also when its sub-ranges are sorted by several threads."""
+    root = os.path.dirname(HERE)
+    exe = str(tmp_path / "sort_check")
+    subprocess.run(["g++", "-O2", "-std=c++17", "-pthread", "-o", exe,
+                    os.path.join(HERE, "sort_check.cpp"),
+                    os.path.join(root, "hail-caesar_gb300", "csrc", "hc_host.cpp")], check=True)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
