@@ -139,6 +139,9 @@ def log(msg):
 # qx, qy written (48 B); + Manning's n (8 B) when spatially variable;
 # + suspended load (Vsusptot read, qxs, qys written: 24 B) and the two
 # vel_dir entries erosion consumes (16 B) when erosion is on.
+TRAFFIC_SED_FLOW = 121.5  # B per wet cell, profiles/k_flow_route_catchment1400.md
+
+
 def flow_bytes_per_cell(p):
     b = 48
     if p.spatially_var_mannings:
@@ -252,11 +255,66 @@ def run_gpu(args, rank, world, dist):
     peak, kind = measured_peak_hbm()
     per_cell = flow_bytes_per_cell(case.params)
     ach = wet * per_cell / (ms_flow / 1e3) / 1e9
+    # DRAM bytes per wet cell of one k_flow_route launch, from the ncu
+    # capture summarised in profiles/ (a smaller case of the same generator),
+    # scaled to this launch by its wet cells
+    traffic_per_cell = None if case.params.hydro_only else TRAFFIC_SED_FLOW
     out["roofline"] = {"bound": "hbm", "kernel": "k_flow_route", "achieved": ach, "peak": peak,
-                       "unit": "GB/s", "frac": ach / peak, "traffic": None,
+                       "unit": "GB/s", "frac": ach / peak,
+                       "traffic": None if traffic_per_cell is None else traffic_per_cell * wet,
                        "peak_kind": kind, "bytes_per_wet_cell": per_cell, "wet_cells": wet,
-                       "launch_ms": ms_flow}
+                       "launch_ms": ms_flow,
+                       "limiter": "FP64 pipe (ncu: 85 % busy, HBM 4 %)"}
     return out, model, case
+
+
+def run_ensemble_bench(args, rank):
+    """C5: independent catchments (synth.ensemble_member) advanced together by
+    hc_run_ensemble, against the same members run one after the other with
+    hc_run.  Both timed with the host clock between device-wide
+    synchronisations (each member has its own stream)."""
+    import torch
+    import hc
+    torch.cuda.set_device(0)
+    t0 = time.perf_counter()
+    n = args.members
+    cases = [synth.ensemble_member(k, fill=False) for k in range(n)]
+    log("%d members generated in %.1f s" % (n, time.perf_counter() - t0))
+    models = [hc.Model(c) for c in cases]
+    cells = sum(c.cells for c in cases)
+    log("%d members on the device, %.1f M cells" % (n, cells / 1e6))
+    warm = max(3, args.warmup)
+    hc.run_ensemble(models, max(warm, args.spinup_iters), 0)
+    torch.cuda.synchronize()
+    k = args.steps
+    # plain: one member after the other
+    t0 = time.perf_counter()
+    done_plain = [m.run(k, 0, records=False) for m in models]
+    torch.cuda.synchronize()
+    t_plain = time.perf_counter() - t0
+    # batched: all members in flight
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
+    t0 = time.perf_counter()
+    done = hc.run_ensemble(models, k, 0)
+    torch.cuda.synchronize()
+    t_ens = time.perf_counter() - t0
+    clk = clocks.stop()
+    steps_plain = sum(c.cells * d for c, d in zip(cases, done_plain))
+    steps_ens = sum(c.cells * d for c, d in zip(cases, done))
+    value = steps_ens / t_ens
+    return {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": k,
+            "warmup": warm, "ms_per_step": t_ens * 1e3 / k, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded generators, hail-caesar_gb300/synth.py)",
+            "config": {"workload": "ensemble%d" % n, "members": n, "cells": cells,
+                       "description": "%d independent catchments, sides 256-1536 @10 m, erosion "
+                                      "+ slide_3, own dt each; %d iterations per member"
+                                      % (n, k),
+                       "parallelism": "one stream + graph per member",
+                       "timing": "host clock between device synchronisations"},
+            "clocks": clk, "plain_value": steps_plain / t_plain,
+            "batched_over_plain": (steps_ens / t_ens) / (steps_plain / t_plain)}
 
 
 def cpu_sample(model, case, flags, budget_s=15.0):
@@ -278,10 +336,42 @@ def cpu_sample(model, case, flags, budget_s=15.0):
 
 
 # ---------------------------------------------------------------- reference arm
+def run_reference_ensemble(args, oracle):
+    """The OpenMP port on a bounded sample of the ensemble: the first members,
+    one after the other (the reference runs one catchment per process)."""
+    n_sample = min(args.members, 4)
+    steps = 0
+    cells_steps = 0
+    t_all = 0.0
+    for k in range(n_sample):
+        case = synth.ensemble_member(k, fill=False)
+        o = oracle.Oracle(case, omp=True)
+        o.iterate(max(3, args.warmup), 0)
+        m = max(1, min(args.steps, 40))
+        t0 = time.perf_counter()
+        o.iterate(m, 0)
+        t_all += time.perf_counter() - t0
+        cells_steps += case.cells * m
+        steps += m
+    v = cells_steps / t_all
+    cores = os.cpu_count()
+    return {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_all * 1e3 / steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": "ensemble%d" % args.members,
+                                            "members": args.members},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": "members 0-%d, %d iterations in all, OpenMP port"
+                                       % (n_sample - 1, steps)},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
 def run_reference(args):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     oracle.build()
+    if args.workload == "ensemble":
+        return run_reference_ensemble(args, oracle)
     case, spin_min, desc = make_workload(args.workload, args.size)
     flags = case.flags
     o = oracle.Oracle(case, omp=True)
@@ -312,7 +402,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="catchment2000",
-                    choices=["catchment2000", "flow8192", "reach"])
+                    choices=["catchment2000", "flow8192", "reach", "ensemble"])
+    ap.add_argument("--members", type=int, default=96, help="ensemble members")
+    ap.add_argument("--spinup-iters", type=int, default=300,
+                    help="ensemble: iterations each member runs before timing")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--size", type=int, default=0,
                     help="override the grid side (smaller runs for profiling)")
@@ -335,6 +428,10 @@ def main():
     if args.impl == "reference":
         if rank == 0:
             print(json.dumps(run_reference(args)))
+        return
+    if args.workload == "ensemble":
+        if rank == 0:
+            print(json.dumps(run_ensemble_bench(args, rank)))
         return
     dist = None
     if world > 1:

@@ -361,6 +361,7 @@ static hc_status free_all(hc_ctx* c) {
   if (c->drainage_cache) host_drainage_cache_free(c->drainage_cache);
   free(extra(c).h_rain);
   if (c->graph) cudaGraphExecDestroy(c->graph);
+  if (c->graph1) cudaGraphExecDestroy(c->graph1);
   if (c->chunk_done) cudaEventDestroy(c->chunk_done);
   if (c->s) cudaStreamDestroy(c->s);
   if (c->s2) cudaStreamDestroy(c->s2);
@@ -949,10 +950,13 @@ static int graph_chunk() {
   return std::max(1, std::min(k, 4096));
 }
 
-static hc_status build_graph(hc_ctx* c, int flags) {
-  if (c->graph) cudaGraphExecDestroy(c->graph);
-  c->graph = nullptr;
-  const int K = graph_chunk();
+// Captures K iterations into *exec; *kernels = kernel nodes outside
+// conditional bodies (they run on every launch; those inside run only when
+// their condition is set, and the device counts them).
+static hc_status build_one(hc_ctx* c, int flags, int K, cudaGraphExec_t* exec,
+                           int64_t* kernels) {
+  if (*exec) cudaGraphExecDestroy(*exec);
+  *exec = nullptr;
   cudaGraph_t g;
   HC_CU(cudaStreamBeginCapture(c->s, cudaStreamCaptureModeRelaxed), "capture");
   c->capturing = true;
@@ -967,26 +971,33 @@ static hc_status build_graph(hc_ctx* c, int flags) {
     return cst;
   }
   HC_CU(ee, "capture");
-  // kernel nodes outside conditional bodies run on every launch; those
-  // inside run only when their condition is set (counted by the device)
   size_t nn = 0;
   cudaGraphGetNodes(g, nullptr, &nn);
   std::vector<cudaGraphNode_t> nodes(nn);
   cudaGraphGetNodes(g, nodes.data(), &nn);
-  c->graph_kernels = 0;
+  *kernels = 0;
   for (auto nd : nodes) {
     cudaGraphNodeType t;
     cudaGraphNodeGetType(nd, &t);
-    if (t == cudaGraphNodeTypeKernel) c->graph_kernels++;
+    if (t == cudaGraphNodeTypeKernel) (*kernels)++;
   }
-  cudaError_t e = cudaGraphInstantiate(&c->graph, g, 0);
+  cudaError_t e = cudaGraphInstantiate(exec, g, 0);
   cudaGraphDestroy(g);
   HC_CU(e, "graph instantiate");
+  return HC_OK;
+}
+
+// The chunk graph (K iterations) and a one-iteration graph for the tail of
+// a run shorter than K (a paused chunk skips the rest of its iterations, so
+// short runs would pay for K).
+static hc_status build_graph(hc_ctx* c, int flags) {
+  const int K = graph_chunk();
+  HC_TRY(build_one(c, flags, K, &c->graph, &c->graph_kernels));
+  HC_TRY(build_one(c, flags, 1, &c->graph1, &c->graph1_kernels));
   c->graph_iters = K;
   c->graph_flags = flags;
   return HC_OK;
 }
-
 
 // Finishes an iteration that stopped before water_flux_out (erosion retry
 // beyond the captured passes, or lateral3 due).
@@ -1097,8 +1108,10 @@ static hc_status run_launch(hc_ctx* c) {
   c->body_k0 = c->hdev->body_kernels;
   c->budget0 = c->hdev->budget;
   c->stat_n[HC_STAT_CHUNKS]++;
-  HC_CU(cudaGraphLaunch(c->graph, c->s), "graph launch");
-  c->launches += c->graph_kernels;
+  const bool small = c->budget0 < c->graph_iters;
+  c->chunk_iters = small ? 1 : c->graph_iters;
+  HC_CU(cudaGraphLaunch(small ? c->graph1 : c->graph, c->s), "graph launch");
+  c->launches += small ? c->graph1_kernels : c->graph_kernels;
   c->d2h_bytes += sizeof(hc_dev);
   HC_CU(cudaMemcpyAsync(c->hdev, c->dev, sizeof(hc_dev), cudaMemcpyDeviceToHost, c->s), "pull");
   HC_CU(cudaEventRecord(c->chunk_done, c->s), "event");
@@ -1111,7 +1124,7 @@ static hc_status run_after_chunk(hc_ctx* c, int32_t flags, bool* finished) {
   *finished = false;
   c->launches += (int64_t)(hd->body_kernels - c->body_k0);
   c->stat_n[HC_STAT_IDLE_ITERS] += std::max<int64_t>(
-      0, std::min<int64_t>(c->graph_iters, c->budget0) - (c->budget0 - hd->budget));
+      0, std::min<int64_t>(c->chunk_iters, c->budget0) - (c->budget0 - hd->budget));
   if (hd->pause & HC_PAUSE_ERROR) return device_error(c);
   if (hd->pause & (HC_PAUSE_ERODE | HC_PAUSE_LATERAL)) HC_TRY(finish_iteration(c, flags));
   HC_TRY(host_steps(c, flags));

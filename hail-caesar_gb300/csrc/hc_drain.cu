@@ -227,7 +227,7 @@ __device__ __forceinline__ bool grid_barrier(DrainSync* g, unsigned nblocks) {
           ok = false;
           break;
         }
-        __nanosleep(64);
+        __nanosleep(20);
       }
     }
     __threadfence();
@@ -304,7 +304,7 @@ __device__ void drain_cell_g(const hc_view& c, const double* __restrict__ el, ui
 // All frontiers in one cooperative launch, one grid barrier between
 // frontiers.  Each cell enters exactly one frontier, so at most imax*jmax
 // cells are processed.
-__global__ void __launch_bounds__(256) k_drain_sweep(const hc_view c, hc_dev* d,
+__global__ void __launch_bounds__(512) k_drain_sweep(const hc_view c, hc_dev* d,
                                                       const double* __restrict__ el,
                                                       DrainSync* g) {
   const unsigned nblocks = gridDim.x;
@@ -493,8 +493,10 @@ hc_status run_drainage_device(hc_ctx* c, const double* el, bool area_valid,
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_drain_sweep, 256, 0);
-    const int nblocks = std::max(1, sms * std::min(per_sm, 4));
+    // one block per SM: fewer arrivals at each barrier; a frontier averages a
+    // few thousand cells
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_drain_sweep, 512, 0);
+    const int nblocks = std::max(1, sms * std::min(per_sm, 1));
     // the barrier lives in the selection's histogram, which is finished
     static_assert(sizeof(DrainSync) <= sizeof(hc_drain_aux::hist), "barrier fits");
     DrainSync* gs = (DrainSync*)((char*)v.drain_aux + offsetof(hc_drain_aux, hist));
@@ -510,7 +512,7 @@ hc_status run_drainage_device(hc_ctx* c, const double* el, bool area_valid,
     const double* elp = el;
     hc_dev* devp = c->dev;
     void* args[] = {(void*)&v, (void*)&devp, (void*)&elp, (void*)&gs};
-    const cudaError_t le = cudaLaunchCooperativeKernel((const void*)k_drain_sweep, nblocks, 256,
+    const cudaError_t le = cudaLaunchCooperativeKernel((const void*)k_drain_sweep, nblocks, 512,
                                                        args, 0, s);
     cudaEventRecord(e1, s);
     c->launches += 1;

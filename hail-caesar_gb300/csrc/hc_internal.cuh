@@ -170,6 +170,9 @@ struct hc_ctx {
   // CUDA graph of K iterations
   cudaGraphExec_t graph; int graph_iters; int graph_flags;
   int64_t graph_kernels;   // kernel nodes in the graph
+  cudaGraphExec_t graph1;  // the same for one iteration
+  int64_t graph1_kernels;
+  int chunk_iters;         // iterations in the chunk last launched
   cudaEvent_t chunk_done;  // a launched chunk and its control-block copy are done
   int64_t run_n;           // iterations asked of the current run
   unsigned long long body_k0;

@@ -265,6 +265,36 @@ def flow_case(n=8192, DX=5.0, seed=3, hours=2, rain_mmh=30.0, jmax=None, relief=
     return Case("flow_%dx%d" % (imax, jmax), p, z, rain)
 
 
+def ensemble_member(k, seed=5, DX=10.0, hours=12, side_min=256, side_max=1536, fill=True):
+    """Member k of the ensemble: sides U[side_min, side_max] per axis,
+    relief U[100, 400] m, uniform rain U[5, 50] mm/h for the first 4 h, one
+    Manning's n U[0.02, 0.08]; flow and erosion (Einstein, 9 fractions,
+    slide_3), no lateral3 (members need not be square)."""
+    rng = np.random.default_rng(seed * 100003 + k)
+    imax = int(rng.integers(side_min, side_max + 1))
+    jmax = int(rng.integers(side_min, side_max + 1))
+    relief = float(rng.uniform(100.0, 400.0))
+    rain_mmh = float(rng.uniform(5.0, 50.0))
+    n_man = float(np.round(rng.uniform(0.02, 0.08), 6))
+    z = fractal_dem(imax, jmax, relief, seed * 7919 + k, fill=fill)
+    p = default_params(imax, jmax, DX)
+    p.maxcycle = hours
+    p.max_time_step = 300
+    p.rain_data_time_step = 10
+    p.M = 0.01
+    p.mannings = n_man
+    p.wilcock, p.einstein = 0, 1
+    p.active = 0.2
+    p.edgeslope = 0.005
+    p.MIN_Q = 0.01
+    sizes = geometric_sizes(0.001, 0.256)
+    set_grains(p, sizes, lognormal_dprop(sizes, 0.016))
+    rows = int(hours * 60 / 10) + 200
+    rain = np.zeros((rows, 1), dtype=np.float32)
+    rain[: 4 * 6] = rain_mmh
+    return Case("member%d_%dx%d" % (k, imax, jmax), p, z, rain, flags=0)
+
+
 # ---------------------------------------------------------------- padding
 def padded(case, a, fill):
     p = case.params
