@@ -317,6 +317,49 @@ def run_ensemble_bench(args, rank):
             "batched_over_plain": (steps_ens / t_ens) / (steps_plain / t_plain)}
 
 
+def run_adjoint_bench(args):
+    """C4: gradient of the outlet-Q loss with respect to every cell's n and
+    the rain table over `--steps` iterations (default 4000), checkpoints
+    every 200, against the same iterations run forward only."""
+    import torch
+    import hc
+    torch.cuda.set_device(0)
+    n_it = args.adj_iterations
+    case = synth.adjoint_case(n=args.size or 1024)
+    tcase = synth.adjoint_case(n=args.size or 1024, n_seed=99)
+    spin = args.spinup if args.spinup >= 0 else 90.0
+
+    def spun(c):
+        m = hc.Model(c)
+        spin_up(m, spin, 0)
+        return m
+    _, target = spun(tcase).adj_forward(n_it)
+    mf = spun(case)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    mf.run(n_it, 0, records=False)
+    torch.cuda.synchronize()
+    t_fwd = time.perf_counter() - t0
+    ma = spun(case)
+    loss, gn, gr, ms = ma.adj_gradient(n_it, 200, target)
+    ratio = ms[2] / (t_fwd * 1e3)
+    cells = case.cells
+    return {"metric": METRIC, "value": ratio, "unit": "adjoint/forward wall-time ratio",
+            "n_gpus": 1, "steps": n_it, "warmup": 0, "ms_per_step": ms[2] / n_it,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded generators, hail-caesar_gb300/synth.py)",
+            "config": {"workload": "adjoint%d" % (args.size or 1024), "cells": cells,
+                       "description": "hydro-only %dx%d @10 m, 20 mm/h for 3 h; loss = MSE of "
+                                      "outlet Q per simulated minute vs a run with another n "
+                                      "field; gradient w.r.t. per-cell n and the rain table; "
+                                      "checkpoints every 200 iterations" % (case.params.imax,
+                                                                           case.params.jmax)},
+            "forward_ms": t_fwd * 1e3, "forward_cell_steps_per_s": cells * n_it / t_fwd,
+            "gradient_ms": {"forward_checkpointed": ms[0], "reverse": ms[1], "total": ms[2]},
+            "loss": loss, "grad_n_norm": float(np.sqrt((gn ** 2).sum())),
+            "grad_rain_norm": float(np.sqrt((gr ** 2).sum()))}
+
+
 def cpu_sample(model, case, flags, budget_s=15.0):
     """The oracle port (OpenMP build) timed on the host from the GPU state."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -372,6 +415,9 @@ def run_reference(args):
     oracle.build()
     if args.workload == "ensemble":
         return run_reference_ensemble(args, oracle)
+    if args.workload == "adjoint":
+        return {"impl": "reference", "unavailable": "the reference has no adjoint of its "
+                "iteration; nothing to time on the CPU for this workload"}
     case, spin_min, desc = make_workload(args.workload, args.size)
     flags = case.flags
     o = oracle.Oracle(case, omp=True)
@@ -402,8 +448,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="catchment2000",
-                    choices=["catchment2000", "flow8192", "reach", "ensemble"])
+                    choices=["catchment2000", "flow8192", "reach", "ensemble", "adjoint"])
     ap.add_argument("--members", type=int, default=96, help="ensemble members")
+    ap.add_argument("--adj-iterations", type=int, default=4000,
+                    help="adjoint: iterations of the differentiated run")
     ap.add_argument("--spinup-iters", type=int, default=300,
                     help="ensemble: iterations each member runs before timing")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
@@ -432,6 +480,10 @@ def main():
     if args.workload == "ensemble":
         if rank == 0:
             print(json.dumps(run_ensemble_bench(args, rank)))
+        return
+    if args.workload == "adjoint":
+        if rank == 0:
+            print(json.dumps(run_adjoint_bench(args)))
         return
     dist = None
     if world > 1:

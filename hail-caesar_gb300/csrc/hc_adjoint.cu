@@ -1,0 +1,548 @@
+// Adjoint of the hydraulic iteration (no counterpart in the reference).
+//
+// For hydro-only catchment runs: the loss is the mean squared difference
+// between the outlet discharge (water_flux_out's sum, :3005-3047) at the
+// first iteration of every simulated minute and a target series.  Its
+// gradient with respect to every cell's Manning's n and to every entry of
+// the rain table is obtained by reverse-mode differentiation of the
+// iteration as the device runs it:
+//   catchment input points  h += min(j*N/count*dt, ERODEFACTOR)   (:3463-3477)
+//   flow_route              the inertial face update and its limiters
+//                           (:3063-3247), differentiated branch by branch
+//   depth_update            h += dt*(div q)/DX                     (:3259-3299)
+//   water_flux_out          edge clamp to the threshold, Q = sum
+// with the time steps, the wet mask and the input points held at their
+// recorded values (they are piecewise constant in the parameters).  The
+// rain enters through TOPMODEL's j (host_topmodel_tangent).
+//
+// Memory: the state (h, qx, qy and the small run state) is checkpointed
+// every K iterations during the forward run; the reverse pass replays one
+// segment at a time from its checkpoint, keeping every iteration's state
+// of the segment, and runs the adjoint iterations backwards through it.
+
+#include "hc_internal.cuh"
+
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#define HC_TRY(expr)                         \
+  do {                                       \
+    hc_status st_ = (expr);                  \
+    if (st_ != HC_OK) return st_;            \
+  } while (0)
+#define HC_CU(expr, what) HC_TRY(hc_cuda(c, (expr), what))
+
+namespace {
+
+constexpr double kG = 9.81;
+
+// value and partial derivatives of a face discharge with respect to the
+// previous discharge q, the two depths and n^2
+struct DQ {
+  double v, dq, dh0, dh1, dnn;
+};
+
+// One face (:3096-3191), as the device evaluates it, with derivatives.
+// Branch decisions are the reference's expressions evaluated in FP64, the
+// same decisions the forward kernel takes.
+__device__ DQ face_dq(double q, double e0, double h0, double e1, double h1, double nn, double dt,
+                      int es, const hc_params& p) {
+  const double DX = p.DX;
+  DQ r = {0, 0, 0, 0, 0};
+  const double a0 = e0 + h0, a1 = e1 + h1;
+  const bool a1max = a0 < a1;
+  const double hflow = smax(a0, a1) - smax(e1, e0);
+  if (!(hflow > p.hflow_threshold)) return r;  // q = 0
+  const double dhf0 = a1max ? 0.0 : 1.0, dhf1 = a1max ? 1.0 : 0.0;
+  double slope = (a1 - a0) / DX, ds0 = -1 / DX, ds1 = 1 / DX;
+  if (es == 1) slope = p.edgeslope, ds0 = ds1 = 0;
+  if (es == -1) slope = 0 - p.edgeslope, ds0 = ds1 = 0;
+  const double ghd = kG * hflow * dt;
+  // qn and its derivatives with respect to q, hflow, slope, nn
+  double qn, d_q, d_hf, d_s, d_nn;
+  if (q == 0) {
+    qn = q - (ghd * slope);
+    d_q = 1;
+    d_hf = -kG * dt * slope;
+    d_s = -ghd;
+    d_nn = 0;
+  } else {
+    const double c3 = cube_rn(hflow);
+    const double F = ghd * nn * fabs(q) / c3;
+    const double D = 1 + F, N = q - (ghd * slope);
+    qn = N / D;
+    const double dF_q = ghd * nn * (q > 0 ? 1.0 : -1.0) / c3;
+    const double dF_hf = -2 * F / hflow;
+    const double dF_nn = ghd * fabs(q) / c3;
+    d_q = 1 / D - qn * dF_q / D;
+    d_hf = (-kG * dt * slope) / D - qn * dF_hf / D;
+    d_s = -ghd / D;
+    d_nn = -qn * dF_nn / D;
+  }
+  double dh0 = d_hf * dhf0 + d_s * ds0, dh1 = d_hf * dhf1 + d_s * ds1;
+  // Froude limit (:3124-3134)
+  const double fl = p.froude_limit;
+  if (qn > 0 && (qn / hflow) / sqrt(kG * hflow) > fl) {
+    qn = hflow * (sqrt(kG * hflow) * fl);
+    const double g = 1.5 * sqrt(kG * hflow) * fl;
+    d_q = 0, d_nn = 0, dh0 = g * dhf0, dh1 = g * dhf1;
+  }
+  if (qn < 0 && fabs(qn / hflow) / sqrt(kG * hflow) > fl) {
+    qn = 0 - (hflow * (sqrt(kG * hflow) * fl));
+    const double g = -1.5 * sqrt(kG * hflow) * fl;
+    d_q = 0, d_nn = 0, dh0 = g * dhf0, dh1 = g * dhf1;
+  }
+  // depth limits (:3138-3148)
+  if (qn > 0 && (qn * dt / DX) > (h0 / 4)) {
+    qn = ((h0 * DX) / 5) / dt;
+    d_q = 0, d_nn = 0, dh0 = DX / 5 / dt, dh1 = 0;
+  }
+  if (qn < 0 && fabs(qn * dt / DX) > (h1 / 4)) {
+    qn = 0 - ((h1 * DX) / 5) / dt;
+    d_q = 0, d_nn = 0, dh0 = 0, dh1 = -DX / 5 / dt;
+  }
+  r.v = qn;
+  r.dq = d_q;
+  r.dh0 = dh0;
+  r.dh1 = dh1;
+  r.dnn = d_nn;
+  return r;
+}
+
+struct AdjStep {
+  double fdt, ts, input_dt, gQ;  // flow dt, time_step at water_flux_out, dL/dQ
+  double amt[HC_MAX_RF + 1];     // input amount per zone
+  double damt[HC_MAX_RF + 1];    // d amount / d j per zone (0 where clamped)
+};
+
+struct AdjBufs {
+  // one iteration of the segment: state before it
+  const double *h0, *qx0, *qy0;
+  const uint8_t* mask;
+  // discharges after it
+  const double *qx1, *qy1;
+  const uint8_t* point;  // input-point cells of this iteration
+  double *lam, *mux, *muy;  // adjoints of h, qx, qy (in: after, out: before)
+  double *lamd, *p0x, *p0y, *p1x, *p1y;
+  double *gn;   // accumulated dL/dn per cell
+  double *gj;   // dL/dj per zone for this iteration
+};
+
+__device__ __forceinline__ bool edge_cell(const hc_view& c, int i, int j) {
+  return i == 1 || i == c.imax || j == 1 || j == c.jmax;
+}
+
+// water_flux_out and depth_update, reversed: lamd = adjoint of the depth
+// after inputs, through the depth update (0 for no-data cells it zeroes)
+__global__ void k_adj_depth(const hc_view c, AdjBufs b, AdjStep st) {
+  const int j = 1 + blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = 1 + blockIdx.y * blockDim.y + threadIdx.y;
+  if (i > c.imax || j > c.jmax) return;
+  const size_t W = c.W, cell = (size_t)i * W + j;
+  const int rf = c.rfarea[cell];
+  double ha = b.h0[cell];
+  if (b.point[cell] && rf >= 0 && rf <= HC_MAX_RF) ha += st.amt[rf];
+  double hd = ha;
+  bool zeroed = false;
+  if (b.mask[cell]) {
+    hd += st.fdt * (b.qx1[cell + W] - b.qx1[cell] + b.qy1[cell + 1] - b.qy1[cell]) / c.p.DX;
+    if (hd > 0 && c.elev[cell] == -9999) zeroed = true;
+  }
+  double lam = b.lam[cell];
+  // water_flux_out clamps an edge cell above the threshold: its depth after
+  // the iteration is a constant, and the excess went into Q
+  if (edge_cell(c, i, j) && !zeroed && hd > c.p.water_depth_erosion_threshold)
+    lam = st.gQ * c.p.DX * c.p.DX / st.ts;
+  b.lamd[cell] = zeroed ? 0.0 : lam;
+}
+
+// flow_route reversed, per cell for its two faces: discharge adjoints
+// before the iteration, the depth terms each face passes to its two cells,
+// and the n gradient
+__global__ void k_adj_flow(const hc_view c, AdjBufs b, AdjStep st) {
+  const int j = 1 + blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = 1 + blockIdx.y * blockDim.y + threadIdx.y;
+  if (i > c.imax || j > c.jmax) return;
+  const size_t W = c.W, cell = (size_t)i * W + j;
+  const double k = st.fdt / c.p.DX;
+  auto ml = [&](size_t q) { return b.mask[q] ? b.lamd[q] : 0.0; };
+  // depth_update reads qx[cell] (-) and, for the cell above, qx[cell] (+)
+  const double mux = b.mux[cell] + k * (ml(cell - W) - ml(cell));
+  const double muy = b.muy[cell] + k * (ml(cell - 1) - ml(cell));
+  double ox = mux, oy = muy, p0x = 0, p1x = 0, p0y = 0, p1y = 0, gn = 0;
+  const double e0 = c.elev[cell];
+  if (b.mask[cell] && e0 > -9999) {
+    const hc_params& p = c.p;
+    const double n = p.spatially_var_mannings ? c.man[cell] : p.mannings;
+    const double nn = n * n;
+    auto hin = [&](size_t q) {
+      const int rf = c.rfarea[q];
+      double h = b.h0[q];
+      if (b.point[q] && rf >= 0 && rf <= HC_MAX_RF) h += st.amt[rf];
+      return h;
+    };
+    const double h0 = hin(cell);
+    {
+      const size_t up = cell - W;
+      const double h1 = hin(up), e1 = c.elev[up];
+      if ((h0 > 0 || h1 > 0) && e1 > -9999) {
+        const int es = (i == c.imax) ? 1 : ((i <= 2) ? -1 : 0);
+        const DQ r = face_dq(b.qx0[cell], e0, h0, e1, h1, nn, st.fdt, es, p);
+        ox = r.dq * mux;
+        p0x = r.dh0 * mux;
+        p1x = r.dh1 * mux;
+        gn += r.dnn * mux;
+      }
+    }
+    {
+      const size_t lf = cell - 1;
+      const double h1 = hin(lf), e1 = c.elev[lf];
+      if ((h0 > 0 || h1 > 0) && e1 > -9999) {
+        const int es = (j == c.jmax) ? 1 : ((j <= 2) ? -1 : 0);
+        const DQ r = face_dq(b.qy0[cell], e0, h0, e1, h1, nn, st.fdt, es, p);
+        oy = r.dq * muy;
+        p0y = r.dh0 * muy;
+        p1y = r.dh1 * muy;
+        gn += r.dnn * muy;
+      }
+    }
+    b.gn[cell] += gn * 2 * n;
+  }
+  b.mux[cell] = ox;
+  b.muy[cell] = oy;
+  b.p0x[cell] = p0x;
+  b.p1x[cell] = p1x;
+  b.p0y[cell] = p0y;
+  b.p1y[cell] = p1y;
+}
+
+// the depth adjoint before the iteration (inputs add a constant), and the
+// input points' dL/dj
+__global__ void __launch_bounds__(256) k_adj_gather(const hc_view c, AdjBufs b, AdjStep st) {
+  __shared__ double sj[8][HC_MAX_RF + 1];
+  const int j = 1 + blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = 1 + blockIdx.y * blockDim.y + threadIdx.y;
+  const int t = threadIdx.y * blockDim.x + threadIdx.x;
+  const int warp = t >> 5, lane = t & 31;
+  double mine = 0;
+  int myrf = -1;
+  if (i <= c.imax && j <= c.jmax) {
+    const size_t W = c.W, cell = (size_t)i * W + j;
+    const double la = b.lamd[cell] + b.p0x[cell] + b.p0y[cell] + b.p1x[cell + W] + b.p1y[cell + 1];
+    b.lam[cell] = la;
+    const int rf = c.rfarea[cell];
+    if (b.point[cell] && rf >= 0 && rf <= HC_MAX_RF) {
+      mine = la * st.damt[rf];
+      myrf = rf;
+    }
+  }
+  // per zone: warp sums, then block sums, then one atomic per zone and block
+  for (int z = 0; z <= c.p.rfnum && z <= HC_MAX_RF; z++) {
+    double v = (myrf == z) ? mine : 0.0;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) sj[warp][z] = v;
+  }
+  __syncthreads();
+  if (t <= c.p.rfnum && t <= HC_MAX_RF) {
+    double s = 0;
+    for (int w = 0; w < (int)(blockDim.x * blockDim.y) / 32; w++) s += sj[w][t];
+    if (s != 0) atomicAdd(&b.gj[t], s);
+  }
+}
+
+__global__ void k_point_flags(const hc_view c, uint8_t* flags, int total) {
+  for (int z = 1 + blockIdx.x * blockDim.x + threadIdx.x; z <= total;
+       z += gridDim.x * blockDim.x)
+    flags[(size_t)c.cin_x[z] * c.W + c.cin_y[z]] = 1;
+}
+
+// ------------------------------------------------------------------ host
+struct Dev {
+  void* p = nullptr;
+  ~Dev() { if (p) cudaFree(p); }
+  template <class T> T* as() { return (T*)p; }
+};
+
+cudaError_t dmalloc(Dev& d, size_t bytes) { return cudaMalloc(&d.p, bytes ? bytes : 8); }
+
+double ms_since(std::chrono::steady_clock::time_point t0) {
+  return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
+// the run state a hydro-only iteration reads and writes
+struct Checkpoint {
+  Dev h, qx, qy, mask, wet, cinx, ciny, dev;
+};
+
+hc_status save_state(hc_ctx* c, Checkpoint& k, bool alloc) {
+  hc_view& v = c->v;
+  const size_t N2 = v.N2, nc = (size_t)v.cin_cap + 2;
+  if (alloc) {
+    if (dmalloc(k.h, N2 * 8) || dmalloc(k.qx, N2 * 8) || dmalloc(k.qy, N2 * 8) ||
+        dmalloc(k.mask, N2) || dmalloc(k.wet, N2 * 4) || dmalloc(k.cinx, nc * 4) ||
+        dmalloc(k.ciny, nc * 4) || dmalloc(k.dev, sizeof(hc_dev)))
+      return hc_fail(c, HC_ERR_NOMEM, "adjoint checkpoint: out of device memory");
+  }
+  cudaStream_t s = c->s;
+  cudaMemcpyAsync(k.h.p, v.h, N2 * 8, cudaMemcpyDeviceToDevice, s);
+  cudaMemcpyAsync(k.qx.p, v.qx, N2 * 8, cudaMemcpyDeviceToDevice, s);
+  cudaMemcpyAsync(k.qy.p, v.qy, N2 * 8, cudaMemcpyDeviceToDevice, s);
+  cudaMemcpyAsync(k.mask.p, v.mask, N2, cudaMemcpyDeviceToDevice, s);
+  cudaMemcpyAsync(k.wet.p, v.wet, N2 * 4, cudaMemcpyDeviceToDevice, s);
+  cudaMemcpyAsync(k.cinx.p, v.cin_x, nc * 4, cudaMemcpyDeviceToDevice, s);
+  cudaMemcpyAsync(k.ciny.p, v.cin_y, nc * 4, cudaMemcpyDeviceToDevice, s);
+  cudaMemcpyAsync(k.dev.p, c->dev, sizeof(hc_dev), cudaMemcpyDeviceToDevice, s);
+  return hc_cuda(c, cudaGetLastError(), "adjoint checkpoint");
+}
+
+hc_status load_state(hc_ctx* c, Checkpoint& k) {
+  hc_view& v = c->v;
+  const size_t N2 = v.N2, nc = (size_t)v.cin_cap + 2;
+  cudaStream_t s = c->s;
+  cudaMemcpyAsync(v.h, k.h.p, N2 * 8, cudaMemcpyDeviceToDevice, s);
+  cudaMemcpyAsync(v.qx, k.qx.p, N2 * 8, cudaMemcpyDeviceToDevice, s);
+  cudaMemcpyAsync(v.qy, k.qy.p, N2 * 8, cudaMemcpyDeviceToDevice, s);
+  cudaMemcpyAsync(v.mask, k.mask.p, N2, cudaMemcpyDeviceToDevice, s);
+  cudaMemcpyAsync(v.wet, k.wet.p, N2 * 4, cudaMemcpyDeviceToDevice, s);
+  cudaMemcpyAsync(v.cin_x, k.cinx.p, nc * 4, cudaMemcpyDeviceToDevice, s);
+  cudaMemcpyAsync(v.cin_y, k.ciny.p, nc * 4, cudaMemcpyDeviceToDevice, s);
+  cudaMemcpyAsync(c->dev, k.dev.p, sizeof(hc_dev), cudaMemcpyDeviceToDevice, s);
+  if (cudaGetLastError() != cudaSuccess) return hc_fail(c, HC_ERR_CUDA, "adjoint restore");
+  return ctx_pull(c);
+}
+
+// switches the time-step recording on (mode 1) or imposes recorded steps
+// (mode 2) for the next iterations, from record index i0
+hc_status adj_mode(hc_ctx* c, double* buf, int64_t n, int mode, int64_t i0) {
+  if (c->v.adj_dt != buf) {
+    c->v.adj_dt = buf;
+    c->graph_iters = 0;  // the graphs hold the view by value
+  }
+  HC_TRY(ctx_pull(c));
+  c->hdev->adj_mode = buf ? mode : 0;
+  c->hdev->adj_i = i0;
+  c->hdev->adj_n = buf ? n : 0;
+  return ctx_push(c);
+}
+
+// sample rule: the first iteration whose cycle (minutes) passes a whole minute
+void samples_of(const std::vector<hc_step_record>& rec, double cycle0, std::vector<int64_t>* at) {
+  double prev = cycle0;
+  for (size_t t = 0; t < rec.size(); t++) {
+    if (std::floor(rec[t].cycle) > std::floor(prev)) at->push_back((int64_t)t);
+    prev = rec[t].cycle;
+  }
+}
+
+}  // namespace
+
+extern "C" hc_status hc_adj_forward(hc_ctx* c, int64_t n, const double* fixed, double* rec_out,
+                                    double* q_samples, int64_t q_cap, int64_t* n_samples) {
+  if (!c || n <= 0) return HC_ERR_ARG;
+  if (!c->v.p.hydro_only) return hc_fail(c, HC_ERR_UNSUPPORTED, "adjoint runs are hydro-only");
+  if (!c->prepared) return hc_fail(c, HC_ERR_STATE, "hc_prepare must come before the run");
+  Dev dt;
+  const size_t nrec = (size_t)n * HC_ADJ_REC;
+  HC_CU(dmalloc(dt, nrec * 8), "adjoint record");
+  if (fixed) HC_CU(cudaMemcpy(dt.p, fixed, nrec * 8, cudaMemcpyHostToDevice), "adjoint record");
+  HC_TRY(ctx_pull(c));
+  const double cycle0 = c->hdev->s.cycle;
+  HC_TRY(adj_mode(c, dt.as<double>(), n, fixed ? 2 : 1, 0));
+  std::vector<hc_step_record> rec((size_t)n);
+  int64_t done = 0;
+  const hc_status st = hc_run(c, n, 0, rec.data(), &done);
+  const hc_status st2 = adj_mode(c, nullptr, 0, 0, 0);
+  if (st != HC_OK) return st;
+  if (st2 != HC_OK) return st2;
+  rec.resize((size_t)done);
+  if (rec_out) HC_CU(cudaMemcpy(rec_out, dt.p, nrec * 8, cudaMemcpyDeviceToHost), "adjoint record");
+  std::vector<int64_t> at;
+  samples_of(rec, cycle0, &at);
+  int64_t k = 0;
+  for (int64_t t : at) {
+    if (q_samples && k < q_cap) q_samples[k] = rec[(size_t)t].waterOut;
+    k++;
+  }
+  if (n_samples) *n_samples = k;
+  return HC_OK;
+}
+
+extern "C" hc_status hc_adj_gradient(hc_ctx* c, int64_t n, int32_t every, const double* q_target,
+                                     int64_t n_target, double* loss, double* grad_n,
+                                     double* grad_rain, double* ms) {
+  if (!c || n <= 0 || every <= 0 || !q_target || n_target < 0) return HC_ERR_ARG;
+  hc_view& v = c->v;
+  if (!v.p.hydro_only) return hc_fail(c, HC_ERR_UNSUPPORTED, "adjoint runs are hydro-only");
+  if (!c->prepared) return hc_fail(c, HC_ERR_STATE, "hc_prepare must come before the run");
+  const auto t_all = std::chrono::steady_clock::now();
+  const size_t N2 = v.N2;
+  const int64_t nseg = (n + every - 1) / every;
+  cudaStream_t s = c->s;
+  // ---------------- forward, checkpointed, recording time steps and Q
+  Dev dt;
+  HC_CU(dmalloc(dt, (size_t)n * HC_ADJ_REC * 8), "adjoint record");
+  std::vector<Checkpoint> cps((size_t)nseg + 1);
+  HC_TRY(ctx_pull(c));
+  const double cycle0 = c->hdev->s.cycle, time1_0 = c->hdev->s.time_1;
+  HC_TRY(adj_mode(c, dt.as<double>(), n, 1, 0));
+  std::vector<hc_step_record> rec((size_t)n);
+  const auto t_fwd = std::chrono::steady_clock::now();
+  int64_t done_all = 0;
+  for (int64_t g = 0; g < nseg; g++) {
+    HC_TRY(save_state(c, cps[(size_t)g], true));
+    const int64_t len = std::min<int64_t>(every, n - g * every);
+    int64_t done = 0;
+    HC_TRY(hc_run(c, len, 0, rec.data() + g * every, &done));
+    done_all += done;
+    if (done != len) {
+      adj_mode(c, nullptr, 0, 0, 0);
+      return hc_fail(c, HC_ERR_STATE, "the run ended (maxcycle) after %lld of %lld iterations",
+                     (long long)done_all, (long long)n);
+    }
+  }
+  HC_TRY(save_state(c, cps[(size_t)nseg], true));
+  HC_CU(cudaStreamSynchronize(s), "adjoint forward");
+  const double ms_fwd = ms_since(t_fwd);
+  std::vector<double> arec((size_t)n * HC_ADJ_REC);
+  HC_CU(cudaMemcpy(arec.data(), dt.p, arec.size() * 8, cudaMemcpyDeviceToHost), "adjoint record");
+  // loss and dL/dQ per iteration
+  std::vector<int64_t> at;
+  samples_of(rec, cycle0, &at);
+  const int64_t S = std::min<int64_t>((int64_t)at.size(), n_target);
+  std::vector<double> gQ((size_t)n, 0.0);
+  double L = 0;
+  for (int64_t k = 0; k < S; k++) {
+    const double d = rec[(size_t)at[(size_t)k]].waterOut - q_target[k];
+    L += d * d / (double)S;
+    gQ[(size_t)at[(size_t)k]] = 2 * d / (double)S;
+  }
+  if (loss) *loss = L;
+  // ---------------- reverse, one segment at a time
+  const auto t_rev = std::chrono::steady_clock::now();
+  const int64_t K = every;
+  Dev sh, sqx, sqy, smask, lam, mux, muy, lamd, p0x, p0y, p1x, p1y, gn, gj, pts;
+  if (dmalloc(sh, (size_t)K * N2 * 8) || dmalloc(sqx, (size_t)(K + 1) * N2 * 8) ||
+      dmalloc(sqy, (size_t)(K + 1) * N2 * 8) || dmalloc(smask, (size_t)K * N2) ||
+      dmalloc(lam, N2 * 8) || dmalloc(mux, N2 * 8) || dmalloc(muy, N2 * 8) ||
+      dmalloc(lamd, N2 * 8) || dmalloc(p0x, N2 * 8) || dmalloc(p0y, N2 * 8) ||
+      dmalloc(p1x, N2 * 8) || dmalloc(p1y, N2 * 8) || dmalloc(gn, N2 * 8) ||
+      dmalloc(gj, (size_t)n * (HC_MAX_RF + 1) * 8) || dmalloc(pts, (size_t)(K + 1) * N2)) {
+    adj_mode(c, nullptr, 0, 0, 0);
+    return hc_fail(c, HC_ERR_NOMEM, "adjoint: out of device memory (segment of %d)", every);
+  }
+  for (Dev* d : {&lam, &mux, &muy, &lamd, &p0x, &p0y, &p1x, &p1y, &gn})
+    cudaMemsetAsync(d->p, 0, N2 * 8, s);
+  cudaMemsetAsync(gj.p, 0, (size_t)n * (HC_MAX_RF + 1) * 8, s);
+  dim3 b(32, 8), gr((v.jmax + 31) / 32, (v.imax + 7) / 8);
+  for (int64_t g = nseg - 1; g >= 0; g--) {
+    const int64_t t0 = g * K, len = std::min<int64_t>(K, n - t0);
+    HC_TRY(load_state(c, cps[(size_t)g]));
+    HC_TRY(adj_mode(c, dt.as<double>(), n, 2, t0));
+    // replay: keep every iteration's state, its input points and the
+    // counters its inputs divide by
+    std::vector<double> nact((size_t)len * (HC_MAX_RF + 1)), cnt(nact.size());
+    for (int64_t k = 0; k < len; k++) {
+      for (int z = 0; z <= HC_MAX_RF; z++) {
+        nact[(size_t)k * (HC_MAX_RF + 1) + z] = c->hdev->s.nActualGridCells[z];
+        cnt[(size_t)k * (HC_MAX_RF + 1) + z] = c->hdev->s.catchment_input_counter[z];
+      }
+      cudaMemcpyAsync(sh.as<double>() + k * N2, v.h, N2 * 8, cudaMemcpyDeviceToDevice, s);
+      cudaMemcpyAsync(sqx.as<double>() + k * N2, v.qx, N2 * 8, cudaMemcpyDeviceToDevice, s);
+      cudaMemcpyAsync(sqy.as<double>() + k * N2, v.qy, N2 * 8, cudaMemcpyDeviceToDevice, s);
+      cudaMemcpyAsync(smask.as<uint8_t>() + k * N2, v.mask, N2, cudaMemcpyDeviceToDevice, s);
+      uint8_t* pf = pts.as<uint8_t>() + k * N2;
+      cudaMemsetAsync(pf, 0, N2, s);
+      const int total = (int)c->hdev->s.totalinputpoints;
+      k_point_flags<<<152 * 4, 256, 0, s>>>(v, pf, total);
+      int64_t done = 0;
+      HC_TRY(hc_run(c, 1, 0, nullptr, &done));
+    }
+    cudaMemcpyAsync(sqx.as<double>() + len * N2, v.qx, N2 * 8, cudaMemcpyDeviceToDevice, s);
+    cudaMemcpyAsync(sqy.as<double>() + len * N2, v.qy, N2 * 8, cudaMemcpyDeviceToDevice, s);
+    // adjoint iterations, last first
+    for (int64_t k = len - 1; k >= 0; k--) {
+      const int64_t t = t0 + k;
+      const double* r = arec.data() + (size_t)t * HC_ADJ_REC;
+      AdjStep st;
+      std::memset(&st, 0, sizeof st);
+      st.input_dt = r[1];
+      st.fdt = r[2];
+      st.ts = rec[(size_t)t].time_step;
+      st.gQ = gQ[(size_t)t];
+      AdjBufs bb;
+      bb.h0 = sh.as<double>() + k * N2;
+      bb.qx0 = sqx.as<double>() + k * N2;
+      bb.qy0 = sqy.as<double>() + k * N2;
+      bb.mask = smask.as<uint8_t>() + k * N2;
+      bb.qx1 = sqx.as<double>() + (k + 1) * N2;
+      bb.qy1 = sqy.as<double>() + (k + 1) * N2;
+      bb.point = pts.as<uint8_t>() + k * N2;
+      bb.lam = lam.as<double>();
+      bb.mux = mux.as<double>();
+      bb.muy = muy.as<double>();
+      bb.lamd = lamd.as<double>();
+      bb.p0x = p0x.as<double>();
+      bb.p0y = p0y.as<double>();
+      bb.p1x = p1x.as<double>();
+      bb.p1y = p1y.as<double>();
+      bb.gn = gn.as<double>();
+      bb.gj = gj.as<double>() + (size_t)t * (HC_MAX_RF + 1);
+      for (int z = 0; z <= v.p.rfnum && z <= HC_MAX_RF; z++) {
+        const double na = nact[(size_t)k * (HC_MAX_RF + 1) + z];
+        const double ct = cnt[(size_t)k * (HC_MAX_RF + 1) + z];
+        double a = (r[3 + z] * na) / (ct) * st.input_dt;
+        double da = na / ct * st.input_dt;
+        if (a > v.p.ERODEFACTOR) a = v.p.ERODEFACTOR, da = 0;
+        st.amt[z] = a;
+        st.damt[z] = da;
+      }
+      k_adj_depth<<<gr, b, 0, s>>>(v, bb, st);
+      k_adj_flow<<<gr, b, 0, s>>>(v, bb, st);
+      k_adj_gather<<<gr, b, 0, s>>>(v, bb, st);
+    }
+    HC_CU(cudaGetLastError(), "adjoint kernels");
+  }
+  HC_CU(cudaStreamSynchronize(s), "adjoint");
+  const double ms_rev = ms_since(t_rev);
+  // ---------------- results
+  if (grad_n) HC_CU(cudaMemcpy(grad_n, gn.p, N2 * 8, cudaMemcpyDeviceToHost), "adjoint gradient");
+  if (grad_rain) {
+    int rows = 0, cols = 0;
+    const float* rain = ctx_rain(c, &rows, &cols);
+    std::fill(grad_rain, grad_rain + (size_t)rows * cols, 0.0);
+    std::vector<double> gjh((size_t)n * (HC_MAX_RF + 1));
+    HC_CU(cudaMemcpy(gjh.data(), gj.p, gjh.size() * 8, cudaMemcpyDeviceToHost), "adjoint gradient");
+    // j used by iteration t was made by the iteration before it (time_1,
+    // cycle of that calchydrograph); the first by the state before the run
+    int max_row = (int)time1_0;
+    for (int64_t t = 0; t < n; t++)
+      max_row = std::max(max_row, (int)arec[(size_t)t * HC_ADJ_REC + HC_ADJ_T1]);
+    const int nsteps = max_row + 1, rf = v.p.rfnum;
+    std::vector<double> dold((size_t)nsteps * (rf + 1) * rows), dnew(dold.size());
+    host_topmodel_tangent(&v.p, rain, rows, cols, nsteps, dold.data(), dnew.data());
+    for (int64_t t = 0; t < n; t++) {
+      const double t1 = (t == 0) ? time1_0 : arec[(size_t)(t - 1) * HC_ADJ_REC + HC_ADJ_T1];
+      const double cyc = (t == 0) ? cycle0 : arec[(size_t)(t - 1) * HC_ADJ_REC + HC_ADJ_T1 + 1];
+      const double w = (2 - (t1 - cyc)) / 2;
+      const int row = (int)t1;
+      for (int z = 1; z <= rf && z - 1 < cols; z++) {
+        const double g = gjh[(size_t)t * (HC_MAX_RF + 1) + z];
+        if (g == 0) continue;
+        const double* ro = dold.data() + ((size_t)row * (rf + 1) + z) * rows;
+        const double* rn = dnew.data() + ((size_t)row * (rf + 1) + z) * rows;
+        for (int k = 0; k < rows; k++) grad_rain[(size_t)k * cols + (z - 1)] += g * (ro[k] * (1 - w) + rn[k] * w);
+      }
+    }
+  }
+  // leave the model where the forward run ended
+  HC_TRY(load_state(c, cps[(size_t)nseg]));
+  HC_TRY(adj_mode(c, nullptr, 0, 0, 0));
+  if (ms) {
+    ms[0] = ms_fwd;
+    ms[1] = ms_rev;
+    ms[2] = ms_since(t_all);
+  }
+  return HC_OK;
+}

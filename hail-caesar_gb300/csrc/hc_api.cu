@@ -662,6 +662,16 @@ static hc_status push(hc_ctx* c) {
   return HC_OK;
 }
 
+// for the other translation units of the library
+hc_status ctx_pull(hc_ctx* c) { return pull(c); }
+hc_status ctx_push(hc_ctx* c) { return push(c); }
+const float* ctx_rain(hc_ctx* c, int* rows, int* cols) {
+  Extra& x = extra(c);
+  *rows = x.h_rain_rows;
+  *cols = x.h_rain_cols;
+  return x.h_rain;
+}
+
 extern "C" hc_status hc_get_scalars(hc_ctx* c, hc_scalars* s) {
   if (!c || !s) return HC_ERR_ARG;
   HC_TRY(pull(c));

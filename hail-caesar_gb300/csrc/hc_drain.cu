@@ -236,8 +236,9 @@ __device__ __forceinline__ bool grid_barrier(DrainSync* g, unsigned nblocks) {
   return ok;
 }
 
-// one ready cell, multi-block variant of drain_cell: values written by other
-// blocks in earlier frontiers are read past L1
+// One ready cell: pull the pushes of its higher neighbours in sweep order,
+// then release its lower neighbours into the next frontier.  Values written
+// by other blocks in earlier frontiers are read past L1.
 __device__ void drain_cell_g(const hc_view& c, const double* __restrict__ el, uint32_t cell,
                              uint32_t* fout, unsigned* n_out) {
   const int W = (int)c.W;
@@ -289,16 +290,19 @@ __device__ void drain_cell_g(const hc_view& c, const double* __restrict__ el, ui
     if (a > 0) __stcg(&c.area[cell], a);
   }
   __threadfence();  // the area is visible before any lower neighbour is released
-  for (int dx = -1, kk = 0; dx <= 1; dx++)
-    for (int dy = -1; dy <= 1; dy++, kk++) {
-      if (dx == 0 && dy == 0) continue;
-      if (!(en[kk] < e)) continue;
-      const uint32_t q = (uint32_t)((i + dx) * W + (j + dy));
-      if (atomicSub(&c.drain_pend[q], 1) == 1) {
-        const unsigned k = atomicAdd(n_out, 1u);
-        __stcg(&fout[k], q);
-      }
-    }
+  // the eight decrements do not depend on one another: issue them together
+  int old[9];
+#pragma unroll
+  for (int kk = 0; kk < 9; kk++) {
+    const int dx = kk / 3 - 1, dy = kk % 3 - 1;
+    old[kk] = (kk != 4 && en[kk] < e) ? atomicSub(&c.drain_pend[(i + dx) * W + (j + dy)], 1) : 0;
+  }
+#pragma unroll
+  for (int kk = 0; kk < 9; kk++) {
+    if (old[kk] != 1) continue;
+    const unsigned m = atomicAdd(n_out, 1u);
+    __stcg(&fout[m], (uint32_t)((i + kk / 3 - 1) * W + (j + kk % 3 - 1)));
+  }
 }
 
 // All frontiers in one cooperative launch, one grid barrier between

@@ -77,6 +77,13 @@ __global__ void k_control(const hc_view c, hc_dev* d, hc_iter_handles hh) {
   if (s.input_output_difference > p.in_out_difference_allowed &&
       s.time_step > (cfl_dt(p, s.maxdepth)))
     s.time_step = cfl_dt(p, s.maxdepth);
+  // adjoint runs record the time steps, or impose recorded ones
+  const bool adj = c.adj_dt && d->adj_mode && d->adj_i < d->adj_n;
+  double* arec = adj ? c.adj_dt + (size_t)d->adj_i * HC_ADJ_REC : nullptr;
+  if (adj) {
+    if (d->adj_mode == 2) s.time_step = arec[0];
+    else arec[0] = s.time_step;
+  }
   s.counter += 1;                                         // increment_counters :1925
   s.cycle += s.time_step / 60;
 
@@ -137,9 +144,15 @@ __global__ void k_control(const hc_view c, hc_dev* d, hc_iter_handles hh) {
 
   // catchment_waterinputs :2027 -> catchment_water_input_and_hydrology :3455
   s.waterinput = 0;
-  const double fdt2 = flow_dt_of(p, s);
+  double fdt2 = flow_dt_of(p, s);
+  if (adj) {
+    if (d->adj_mode == 2) fdt2 = arec[1];
+    else arec[1] = fdt2;
+  }
   for (int i = 1; i <= p.rfnum; i++) s.waterinput += s.j_mean[i] * s.nActualGridCells[i] * DX * DX;
   for (int i = 0; i <= p.rfnum; i++) d->j_mean_in[i] = s.j_mean[i];
+  if (arec)
+    for (int i = 0; i <= HC_MAX_RF; i++) arec[3 + i] = (i <= p.rfnum) ? s.j_mean[i] : 0.0;
   d->input_dt = fdt2;
   if (s.cycle >= s.time_1) {
     do {
@@ -158,6 +171,10 @@ __global__ void k_control(const hc_view c, hc_dev* d, hc_iter_handles hh) {
   }
   for (int n = 1; n <= p.rfnum; n++)  // calchydrograph :3718
     s.j_mean[n] = s.old_j_mean[n] + (((s.new_j_mean[n] - s.old_j_mean[n]) / 2) * (2 - (s.time_1 - s.cycle)));
+  if (arec) {
+    arec[HC_ADJ_T1] = s.time_1;
+    arec[HC_ADJ_T1 + 1] = s.cycle;
+  }
   double jmeanmax = 0;
   for (int n = 1; n <= p.rfnum; n++)
     if (s.j_mean[n] > jmeanmax) jmeanmax = s.j_mean[n];
@@ -178,6 +195,11 @@ __global__ void k_control(const hc_view c, hc_dev* d, hc_iter_handles hh) {
   if (recalc) d->pause |= HC_PAUSE_DRAINAGE;
 
   s.flow_timestep = flow_dt_of(p, s);
+  if (adj) {
+    if (d->adj_mode == 2) s.flow_timestep = arec[2];
+    else arec[2] = s.flow_timestep;
+    d->adj_i++;
+  }
   d->do_scan = ((long long)s.counter % p.scan_area_interval_iter) == 0;
   d->do_erode = !p.hydro_only && s.counter >= s.erode_call;
   d->erode_retry = d->do_erode;

@@ -252,3 +252,69 @@ int host_global_landsliding(const hc_params* p, const double* bedrock, double* e
   } while (total > 0 && inc < 200);
   return (int)inc;
 }
+
+// Derivatives of the TOPMODEL table (host_topmodel_table) with respect to the
+// rain table, by forward-mode differentiation of the same recurrence: for
+// table rows t < nsteps, zone n (1..rfnum) and rain row k < rows,
+//   d_old[(t*(rf+1) + n)*rows + k] = d old_j_mean[n] / d rain[k][n-1]
+//   d_new[...]                     = d new_j_mean[n] / d rain[k][n-1].
+// A rain value of 0 sits on the switch between the recession and the
+// infiltration formulas; its derivative is taken as 0.
+void host_topmodel_tangent(const hc_params* p, const float* rain, int rows, int cols, int nsteps,
+                           double* d_old, double* d_new) {
+  const int rf = p->rfnum;
+  const double M = p->M, fts = 60, a = fts / M;
+  const size_t R = (size_t)rows;
+  std::fill(d_old, d_old + (size_t)nsteps * (rf + 1) * R, 0.0);
+  std::fill(d_new, d_new + (size_t)nsteps * (rf + 1) * R, 0.0);
+  for (int n = 1; n <= rf; n++) {
+    double jv = 0.000000001, newm = 0.0;
+    std::vector<double> dj(R, 0.0), dnew(R, 0.0), dold(R, 0.0), djo(R, 0.0);
+    for (int t = 0; t < nsteps; t++) {
+      const double cyc = (t == 0) ? 1.0 : (double)t;
+      const int ts = (int)(cyc / p->rain_data_time_step);
+      dold = dnew;
+      djo = dj;
+      const double j0 = jv;
+      float v = 0.0f;
+      if (ts >= 0 && ts < rows && n - 1 < cols) v = rain[(size_t)ts * cols + (n - 1)];
+      double lrr = 0;
+      if (v > 0) lrr = p->rain_factor * ((v / 1000) / 3600);
+      const double dlrr = (v > 0) ? p->rain_factor / 3600000.0 : 0.0;  // d lrr / d v
+      if (lrr == 0) {
+        const double q = 1 + j0 * a;
+        jv = j0 / (1 + ((j0 * fts) / M));
+        newm = M / fts * std::log(1 + ((j0 * fts) / M));
+        for (size_t k = 0; k < R; k++) {
+          dj[k] = djo[k] / (q * q);
+          dnew[k] = djo[k] / q;
+        }
+      } else {
+        const double E = std::exp((0 - lrr) * fts / M);
+        const double u = ((lrr - j0) / j0) * E + 1;
+        const double eP = std::exp((lrr * fts) / M);
+        const double X = (lrr - j0) + j0 * eP;
+        jv = lrr / u;
+        newm = (M / fts) * std::log(X / lrr);
+        for (size_t k = 0; k < R; k++) {
+          const double dl = (k == (size_t)ts) ? dlrr : 0.0;
+          const double d0 = djo[k];
+          const double du = E * (dl / j0 - lrr / (j0 * j0) * d0) + (lrr / j0 - 1) * E * (-a * dl);
+          dj[k] = dl / u - lrr / (u * u) * du;
+          const double dX = dl - d0 + d0 * eP + j0 * eP * a * dl;
+          dnew[k] = (1 / a) * (dX / X - dl / lrr);
+        }
+      }
+      if (newm < 0) {
+        newm = 0;
+        std::fill(dnew.begin(), dnew.end(), 0.0);
+      }
+      double* ro = d_old + ((size_t)t * (rf + 1) + n) * R;
+      double* rn = d_new + ((size_t)t * (rf + 1) + n) * R;
+      for (size_t k = 0; k < R; k++) {
+        ro[k] = dold[k];
+        rn[k] = dnew[k];
+      }
+    }
+  }
+}

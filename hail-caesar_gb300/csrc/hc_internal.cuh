@@ -37,6 +37,14 @@
 
 #define HC_ERODE_PASSES 4     // entrainment passes captured per iteration
 
+// per-iteration record of an adjoint run: [0] time_step after
+// set_maximum_timestep, [1] the input points' dt, [2] the flow dt,
+// [3 .. 3+HC_MAX_RF] j_mean as the input points used it, then time_1 and
+// cycle as calchydrograph used them
+#define HC_ADJ_REC (3 + HC_MAX_RF + 1 + 2)
+#define HC_ADJ_T1 (3 + HC_MAX_RF + 1)
+static_assert(HC_ADJ_REC == HC_ADJ_RECORD, "record size of the C ABI");
+
 // Device-side control block.  One per context, in device memory; the single
 // thread control kernel owns the scalar logic of the reference's driver.
 struct hc_dev {
@@ -72,6 +80,8 @@ struct hc_dev {
   int do_drain;           // this iteration moved the baseflow threshold
   unsigned int drain_front, drain_done, drain_points, drain_levels;
   unsigned int drain_rf[HC_MAX_RF + 1];
+  int adj_mode;           // 0 off, 1 record the time steps, 2 impose them
+  int64_t adj_i, adj_n;   // next iteration, capacity of hc_view::adj_dt
   unsigned int xchains;   // chain starts of the +/-x apply pass (hc_view::chains)
   unsigned int ychains;   // chain starts of the +/-y apply pass
 };
@@ -131,6 +141,9 @@ struct hc_view {
   int32_t *drain_pend;
   double *drain_dt, *drain_snap;
   struct hc_drain_aux *drain_aux;
+  // adjoint runs (hc_adjoint.cu): per-iteration time steps, recorded or
+  // imposed (HC_ADJ_REC stride per iteration; see hc_dev::adj_mode)
+  double *adj_dt;
   unsigned long long *alloc_key; // N2: serial-order key of the first grain-record request
   int32_t *alloc_list;           // N2: cells allocated, in order
   int32_t *slide_list; int slide_cap;
@@ -337,8 +350,15 @@ hc_status run_drainage_device(hc_ctx* c, const double* el, bool area_valid,
                               const uint32_t* (*sort_order)(hc_ctx*, const double*),
                               bool* sorted);
 void launch_drain_snapshot(hc_ctx* c);
+hc_status ctx_pull(hc_ctx* c);   // control block device -> host mirror
+hc_status ctx_push(hc_ctx* c);   // host mirror -> device
+const float* ctx_rain(hc_ctx* c, int* rows, int* cols);  // host copy of the rain table
+hc_status hc_fail(hc_ctx* c, hc_status st, const char* fmt, ...);
+hc_status hc_cuda(hc_ctx* c, cudaError_t e, const char* what);
 void* host_drainage_cache_new();
 void host_drainage_cache_free(void* p);
 int host_global_landsliding(const hc_params* p, const double* bedrock, double* elev);
+void host_topmodel_tangent(const hc_params* p, const float* rain, int rows, int cols, int nsteps,
+                           double* d_old, double* d_new);
 void host_topmodel_table(const hc_params* p, const float* rain, int rows, int cols,
                          int nsteps, double* table /* [nsteps][2][rfnum+1] */);

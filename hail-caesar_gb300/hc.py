@@ -63,6 +63,9 @@ def load_library(path=LIB_PATH):
         "hc_bench_kernel": (C.c_int, [vp, C.c_char_p, C.c_int32, P(C.c_double), P(C.c_int64)]),
         "hc_get_counters": (C.c_int, [vp, P(C.c_int64), P(C.c_int64), P(C.c_int64)]),
         "hc_get_run_stats": (C.c_int, [vp, P(C.c_int64), P(C.c_double), C.c_int32]),
+        "hc_adj_forward": (C.c_int, [vp, C.c_int64, vp, vp, vp, C.c_int64, P(C.c_int64)]),
+        "hc_adj_gradient": (C.c_int, [vp, C.c_int64, C.c_int32, vp, C.c_int64, P(C.c_double),
+                                      vp, vp, vp]),
         "hc_profile_iteration": (C.c_int, [vp, C.c_int32, P(C.c_double)]),
     }
     for name, (res, args) in sig.items():
@@ -200,6 +203,40 @@ class Model:
         self._check(self.lib.hc_get_counters(self.h, C.byref(a), C.byref(b), C.byref(c)),
                     "counters")
         return a.value, b.value, c.value
+
+    # ---- adjoint (hydro-only)
+    ADJ_RECORD = 22
+
+    def adj_forward(self, n, fixed=None, max_samples=100000):
+        """Runs n iterations; returns (time-step record (n, 22), outlet Q at
+        the first iteration of every simulated minute).  `fixed`: a record to
+        impose instead of the adaptive time steps."""
+        rec = np.zeros((n, self.ADJ_RECORD), dtype=np.float64)
+        q = np.zeros(max_samples, dtype=np.float64)
+        ns = C.c_int64()
+        fx = None
+        if fixed is not None:
+            fx = np.ascontiguousarray(fixed, dtype=np.float64)
+            assert fx.shape == (n, self.ADJ_RECORD)
+        self._check(self.lib.hc_adj_forward(self.h, n, None if fx is None else fx.ctypes.data,
+                                            rec.ctypes.data, q.ctypes.data, max_samples,
+                                            C.byref(ns)), "adj_forward")
+        return rec, q[:min(ns.value, max_samples)].copy()
+
+    def adj_gradient(self, n, every, target):
+        """(loss, dL/dn per cell (imax+2, jmax+2), dL/drain (rain rows, cols),
+        [forward, reverse, total] ms) over n iterations from the current
+        state; checkpoints every `every` iterations."""
+        p = self.p
+        t = np.ascontiguousarray(target, dtype=np.float64)
+        gn = np.zeros((p.imax + 2, p.jmax + 2), dtype=np.float64)
+        gr = np.zeros(self.case.rain.shape, dtype=np.float64)
+        loss = C.c_double()
+        ms = (C.c_double * 3)()
+        self._check(self.lib.hc_adj_gradient(self.h, n, every, t.ctypes.data, len(t),
+                                             C.byref(loss), gn.ctypes.data, gr.ctypes.data, ms),
+                    "adj_gradient")
+        return loss.value, gn, gr, list(ms)
 
     RUN_STATS = ["chunks", "erode_retry", "lateral", "creep", "global_slide", "drainage",
                  "drainage_sort", "drainage_sweep", "drainage_levels", "idle_iters"]

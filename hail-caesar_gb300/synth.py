@@ -265,6 +265,32 @@ def flow_case(n=8192, DX=5.0, seed=3, hours=2, rain_mmh=30.0, jmax=None, relief=
     return Case("flow_%dx%d" % (imax, jmax), p, z, rain)
 
 
+def adjoint_case(n=1024, DX=10.0, seed=4, relief=200.0, rain_mmh=20.0, storm_h=3, hours=12,
+                 fill=True, n_seed=None):
+    """Hydro-only catchment for the adjoint: fractal DEM (`relief` m),
+    uniform rain `rain_mmh` for the first `storm_h` hours in 10-min steps,
+    Manning's n from a smooth seeded field in [0.03, 0.06] (n_seed: another
+    field, for a target run)."""
+    z = fractal_dem(n, n, relief, seed, fill=fill)
+    rng = np.random.default_rng((seed if n_seed is None else n_seed) + 1000)
+    nf = correlated_noise((n, n), 1.0, max(2.0, n / 20.0), rng)
+    nf = (nf - nf.min()) / max(1e-12, nf.max() - nf.min())
+    man = np.round(0.03 + 0.03 * nf, 6)
+    p = default_params(n, n, DX)
+    p.maxcycle = hours
+    p.max_time_step = 300
+    p.rain_data_time_step = 10
+    p.M = 0.01
+    p.spatially_var_mannings = 1
+    p.hydro_only = 1
+    p.edgeslope = 0.005
+    p.MIN_Q = 0.01
+    rows = int(hours * 60 / 10) + 200
+    rain = np.zeros((rows, 1), dtype=np.float32)
+    rain[: storm_h * 6] = rain_mmh
+    return Case("adjoint_%dx%d" % (n, n), p, z, rain, mannings=man, flags=0)
+
+
 def ensemble_member(k, seed=5, DX=10.0, hours=12, side_min=256, side_max=1536, fill=True):
     """Member k of the ensemble: sides U[side_min, side_max] per axis,
     relief U[100, 400] m, uniform rain U[5, 50] mm/h for the first 4 h, one

@@ -251,6 +251,29 @@ hc_status hc_run(hc_ctx* ctx, int64_t n, int32_t flags, hc_step_record* rec,
  * differ in size and parameters. */
 hc_status hc_run_ensemble(hc_ctx** ctxs, int32_t m, int64_t n, int32_t flags, int64_t* done);
 
+/* ---- adjoint of the hydraulic iteration (no counterpart in the reference)
+ * Hydro-only runs.  The outlet discharge Q (water_flux_out's sum) is
+ * sampled at the first iteration of every simulated minute.
+ *
+ * hc_adj_forward runs n iterations like hc_run and returns the Q samples.
+ * rec_out (optional, n*HC_ADJ_RECORD doubles) receives each iteration's
+ * time steps; passing such a record as `fixed` imposes those time steps
+ * instead of the adaptive ones (finite-difference runs of a perturbed model).
+ *
+ * hc_adj_gradient runs n iterations from the current state (checkpoints
+ * every `every` iterations), evaluates loss = mean over the samples of
+ * (Q - q_target)^2 and its gradient with respect to every cell's Manning's n
+ * (grad_n: (imax+2)(jmax+2) doubles) and every entry of the rain table
+ * (grad_rain: rows x cols as given to hc_set_rain).  Time steps, wet mask and
+ * input points are held at the run's values.  The model is left at the end
+ * of the n iterations.  ms (optional, 3 doubles): forward, reverse, total. */
+#define HC_ADJ_RECORD 22
+hc_status hc_adj_forward(hc_ctx* ctx, int64_t n, const double* fixed, double* rec_out,
+                         double* q_samples, int64_t q_cap, int64_t* n_samples);
+hc_status hc_adj_gradient(hc_ctx* ctx, int64_t n, int32_t every, const double* q_target,
+                          int64_t n_target, double* loss, double* grad_n, double* grad_rain,
+                          double* ms);
+
 /* What hc_run spent on the host (no counterpart in the reference): for
  * each kind below, how many times it ran and its host wall time in ms,
  * accumulated since hc_create.  Pauses leave the rest of a graph chunk as
