@@ -252,6 +252,21 @@ __global__ void __launch_bounds__(256) k_adj_gather(const hc_view c, AdjBufs b, 
   }
 }
 
+// the state an adjoint replay keeps: before the iteration's inputs
+__global__ void __launch_bounds__(256) k_adj_save(const hc_view c, const hc_dev* d) {
+  if (!d->it_active) return;
+  const int64_t k = d->adj_i - 1 - d->adj_slot_t0;  // k_control has counted this iteration
+  if (k < 0 || k >= d->adj_slot_n) return;
+  const size_t N2 = c.N2, off = (size_t)k * N2;
+  for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < N2;
+       q += (size_t)gridDim.x * blockDim.x) {
+    c.adj_sh[off + q] = c.h[q];
+    c.adj_sqx[off + q] = c.qx[q];
+    c.adj_sqy[off + q] = c.qy[q];
+    c.adj_smask[off + q] = c.mask[q];
+  }
+}
+
 __global__ void k_point_flags(const hc_view c, uint8_t* flags, int total) {
   for (int z = 1 + blockIdx.x * blockDim.x + threadIdx.x; z <= total;
        z += gridDim.x * blockDim.x)
@@ -315,7 +330,9 @@ hc_status load_state(hc_ctx* c, Checkpoint& k) {
 
 // switches the time-step recording on (mode 1) or imposes recorded steps
 // (mode 2) for the next iterations, from record index i0
-hc_status adj_mode(hc_ctx* c, double* buf, int64_t n, int mode, int64_t i0) {
+// (k_adj_save keeps the states of iterations slot_t0 .. slot_t0+slot_n-1)
+hc_status adj_mode(hc_ctx* c, double* buf, int64_t n, int mode, int64_t i0,
+                   int64_t slot_t0 = 0, int64_t slot_n = 0) {
   if (c->v.adj_dt != buf) {
     c->v.adj_dt = buf;
     c->graph_iters = 0;  // the graphs hold the view by value
@@ -324,7 +341,46 @@ hc_status adj_mode(hc_ctx* c, double* buf, int64_t n, int mode, int64_t i0) {
   c->hdev->adj_mode = buf ? mode : 0;
   c->hdev->adj_i = i0;
   c->hdev->adj_n = buf ? n : 0;
+  c->hdev->adj_slot_t0 = slot_t0;
+  c->hdev->adj_slot_n = slot_n;
   return ctx_push(c);
+}
+
+// input points of an adjoint replay: flag arrays, each valid from an
+// iteration on (the points change only when the baseflow threshold moves)
+struct PointsLog {
+  std::vector<int64_t> start;
+  std::vector<Dev*> flags;
+  std::vector<std::vector<double>> nact, cnt;  // the counters the inputs divide by
+  ~PointsLog() {
+    for (Dev* f : flags) delete f;
+  }
+  hc_status add(hc_ctx* c, int64_t from) {
+    Dev* f = new Dev();
+    flags.push_back(f);
+    start.push_back(from);
+    const hc_scalars& sc = c->hdev->s;
+    nact.emplace_back(sc.nActualGridCells, sc.nActualGridCells + HC_MAX_RF + 1);
+    cnt.emplace_back(sc.catchment_input_counter, sc.catchment_input_counter + HC_MAX_RF + 1);
+    if (dmalloc(*f, c->v.N2) != cudaSuccess) return hc_fail(c, HC_ERR_NOMEM, "adjoint points");
+    cudaMemsetAsync(f->p, 0, c->v.N2, c->s);
+    k_point_flags<<<152 * 4, 256, 0, c->s>>>(c->v, f->as<uint8_t>(),
+                                             (int)c->hdev->s.totalinputpoints);
+    return hc_cuda(c, cudaGetLastError(), "adjoint points");
+  }
+  size_t version(int64_t t) const {
+    size_t r = 0;
+    for (size_t k = 0; k < start.size(); k++)
+      if (start[k] <= t) r = k;
+    return r;
+  }
+  const uint8_t* at(int64_t t) const { return flags[version(t)]->as<uint8_t>(); }
+  const double* nact_at(int64_t t) const { return nact[version(t)].data(); }
+  const double* cnt_at(int64_t t) const { return cnt[version(t)].data(); }
+};
+
+void points_hook(hc_ctx* c, void* arg) {
+  ((PointsLog*)arg)->add(c, c->hdev->adj_i);
 }
 
 // sample rule: the first iteration whose cycle (minutes) passes a whole minute
@@ -380,13 +436,34 @@ extern "C" hc_status hc_adj_gradient(hc_ctx* c, int64_t n, int32_t every, const 
   const size_t N2 = v.N2;
   const int64_t nseg = (n + every - 1) / every;
   cudaStream_t s = c->s;
+  // replay slots, set in the view for the whole call (k_adj_save is part of
+  // the graphs while they are set)
+  Dev sh, sqx, sqy, smask;
+  if (dmalloc(sh, (size_t)every * N2 * 8) || dmalloc(sqx, (size_t)(every + 1) * N2 * 8) ||
+      dmalloc(sqy, (size_t)(every + 1) * N2 * 8) || dmalloc(smask, (size_t)every * N2))
+    return hc_fail(c, HC_ERR_NOMEM, "adjoint: out of device memory (segment of %d)", every);
+  struct SlotGuard {
+    hc_ctx* c;
+    ~SlotGuard() {
+      c->v.adj_sh = c->v.adj_sqx = c->v.adj_sqy = nullptr;
+      c->v.adj_smask = nullptr;
+      c->graph_iters = 0;
+      c->points_hook = nullptr;
+      c->points_hook_arg = nullptr;
+    }
+  } guard{c};
+  v.adj_sh = sh.as<double>();
+  v.adj_sqx = sqx.as<double>();
+  v.adj_sqy = sqy.as<double>();
+  v.adj_smask = smask.as<uint8_t>();
+  c->graph_iters = 0;
   // ---------------- forward, checkpointed, recording time steps and Q
   Dev dt;
   HC_CU(dmalloc(dt, (size_t)n * HC_ADJ_REC * 8), "adjoint record");
   std::vector<Checkpoint> cps((size_t)nseg + 1);
   HC_TRY(ctx_pull(c));
   const double cycle0 = c->hdev->s.cycle, time1_0 = c->hdev->s.time_1;
-  HC_TRY(adj_mode(c, dt.as<double>(), n, 1, 0));
+  HC_TRY(adj_mode(c, dt.as<double>(), n, 1, 0));  // no saves in the forward run
   std::vector<hc_step_record> rec((size_t)n);
   const auto t_fwd = std::chrono::steady_clock::now();
   int64_t done_all = 0;
@@ -422,15 +499,13 @@ extern "C" hc_status hc_adj_gradient(hc_ctx* c, int64_t n, int32_t every, const 
   // ---------------- reverse, one segment at a time
   const auto t_rev = std::chrono::steady_clock::now();
   const int64_t K = every;
-  Dev sh, sqx, sqy, smask, lam, mux, muy, lamd, p0x, p0y, p1x, p1y, gn, gj, pts;
-  if (dmalloc(sh, (size_t)K * N2 * 8) || dmalloc(sqx, (size_t)(K + 1) * N2 * 8) ||
-      dmalloc(sqy, (size_t)(K + 1) * N2 * 8) || dmalloc(smask, (size_t)K * N2) ||
-      dmalloc(lam, N2 * 8) || dmalloc(mux, N2 * 8) || dmalloc(muy, N2 * 8) ||
+  Dev lam, mux, muy, lamd, p0x, p0y, p1x, p1y, gn, gj;
+  if (dmalloc(lam, N2 * 8) || dmalloc(mux, N2 * 8) || dmalloc(muy, N2 * 8) ||
       dmalloc(lamd, N2 * 8) || dmalloc(p0x, N2 * 8) || dmalloc(p0y, N2 * 8) ||
       dmalloc(p1x, N2 * 8) || dmalloc(p1y, N2 * 8) || dmalloc(gn, N2 * 8) ||
-      dmalloc(gj, (size_t)n * (HC_MAX_RF + 1) * 8) || dmalloc(pts, (size_t)(K + 1) * N2)) {
+      dmalloc(gj, (size_t)n * (HC_MAX_RF + 1) * 8)) {
     adj_mode(c, nullptr, 0, 0, 0);
-    return hc_fail(c, HC_ERR_NOMEM, "adjoint: out of device memory (segment of %d)", every);
+    return hc_fail(c, HC_ERR_NOMEM, "adjoint: out of device memory");
   }
   for (Dev* d : {&lam, &mux, &muy, &lamd, &p0x, &p0y, &p1x, &p1y, &gn})
     cudaMemsetAsync(d->p, 0, N2 * 8, s);
@@ -439,28 +514,20 @@ extern "C" hc_status hc_adj_gradient(hc_ctx* c, int64_t n, int32_t every, const 
   for (int64_t g = nseg - 1; g >= 0; g--) {
     const int64_t t0 = g * K, len = std::min<int64_t>(K, n - t0);
     HC_TRY(load_state(c, cps[(size_t)g]));
-    HC_TRY(adj_mode(c, dt.as<double>(), n, 2, t0));
-    // replay: keep every iteration's state, its input points and the
-    // counters its inputs divide by
-    std::vector<double> nact((size_t)len * (HC_MAX_RF + 1)), cnt(nact.size());
-    for (int64_t k = 0; k < len; k++) {
-      for (int z = 0; z <= HC_MAX_RF; z++) {
-        nact[(size_t)k * (HC_MAX_RF + 1) + z] = c->hdev->s.nActualGridCells[z];
-        cnt[(size_t)k * (HC_MAX_RF + 1) + z] = c->hdev->s.catchment_input_counter[z];
-      }
-      cudaMemcpyAsync(sh.as<double>() + k * N2, v.h, N2 * 8, cudaMemcpyDeviceToDevice, s);
-      cudaMemcpyAsync(sqx.as<double>() + k * N2, v.qx, N2 * 8, cudaMemcpyDeviceToDevice, s);
-      cudaMemcpyAsync(sqy.as<double>() + k * N2, v.qy, N2 * 8, cudaMemcpyDeviceToDevice, s);
-      cudaMemcpyAsync(smask.as<uint8_t>() + k * N2, v.mask, N2, cudaMemcpyDeviceToDevice, s);
-      uint8_t* pf = pts.as<uint8_t>() + k * N2;
-      cudaMemsetAsync(pf, 0, N2, s);
-      const int total = (int)c->hdev->s.totalinputpoints;
-      k_point_flags<<<152 * 4, 256, 0, s>>>(v, pf, total);
-      int64_t done = 0;
-      HC_TRY(hc_run(c, 1, 0, nullptr, &done));
-    }
-    cudaMemcpyAsync(sqx.as<double>() + len * N2, v.qx, N2 * 8, cudaMemcpyDeviceToDevice, s);
-    cudaMemcpyAsync(sqy.as<double>() + len * N2, v.qy, N2 * 8, cudaMemcpyDeviceToDevice, s);
+    // replay as one graph run; k_adj_save keeps every iteration's state
+    HC_TRY(adj_mode(c, dt.as<double>(), n, 2, t0, t0, len));
+    PointsLog pts;
+    HC_TRY(pts.add(c, t0));
+    c->points_hook = points_hook;
+    c->points_hook_arg = &pts;
+    int64_t done = 0;
+    const hc_status rs = hc_run(c, len, 0, nullptr, &done);
+    c->points_hook = nullptr;
+    c->points_hook_arg = nullptr;
+    HC_TRY(rs);
+    HC_TRY(adj_mode(c, dt.as<double>(), n, 2, t0 + len));  // saves off
+    cudaMemcpyAsync(v.adj_sqx + (size_t)len * N2, v.qx, N2 * 8, cudaMemcpyDeviceToDevice, s);
+    cudaMemcpyAsync(v.adj_sqy + (size_t)len * N2, v.qy, N2 * 8, cudaMemcpyDeviceToDevice, s);
     // adjoint iterations, last first
     for (int64_t k = len - 1; k >= 0; k--) {
       const int64_t t = t0 + k;
@@ -472,13 +539,13 @@ extern "C" hc_status hc_adj_gradient(hc_ctx* c, int64_t n, int32_t every, const 
       st.ts = rec[(size_t)t].time_step;
       st.gQ = gQ[(size_t)t];
       AdjBufs bb;
-      bb.h0 = sh.as<double>() + k * N2;
-      bb.qx0 = sqx.as<double>() + k * N2;
-      bb.qy0 = sqy.as<double>() + k * N2;
-      bb.mask = smask.as<uint8_t>() + k * N2;
-      bb.qx1 = sqx.as<double>() + (k + 1) * N2;
-      bb.qy1 = sqy.as<double>() + (k + 1) * N2;
-      bb.point = pts.as<uint8_t>() + k * N2;
+      bb.h0 = v.adj_sh + (size_t)k * N2;
+      bb.qx0 = v.adj_sqx + (size_t)k * N2;
+      bb.qy0 = v.adj_sqy + (size_t)k * N2;
+      bb.mask = v.adj_smask + (size_t)k * N2;
+      bb.qx1 = v.adj_sqx + (size_t)(k + 1) * N2;
+      bb.qy1 = v.adj_sqy + (size_t)(k + 1) * N2;
+      bb.point = pts.at(t);
       bb.lam = lam.as<double>();
       bb.mux = mux.as<double>();
       bb.muy = muy.as<double>();
@@ -489,11 +556,11 @@ extern "C" hc_status hc_adj_gradient(hc_ctx* c, int64_t n, int32_t every, const 
       bb.p1y = p1y.as<double>();
       bb.gn = gn.as<double>();
       bb.gj = gj.as<double>() + (size_t)t * (HC_MAX_RF + 1);
+      const double* na = pts.nact_at(t);
+      const double* ct = pts.cnt_at(t);
       for (int z = 0; z <= v.p.rfnum && z <= HC_MAX_RF; z++) {
-        const double na = nact[(size_t)k * (HC_MAX_RF + 1) + z];
-        const double ct = cnt[(size_t)k * (HC_MAX_RF + 1) + z];
-        double a = (r[3 + z] * na) / (ct) * st.input_dt;
-        double da = na / ct * st.input_dt;
+        double a = (r[3 + z] * na[z]) / (ct[z]) * st.input_dt;
+        double da = na[z] / ct[z] * st.input_dt;
         if (a > v.p.ERODEFACTOR) a = v.p.ERODEFACTOR, da = 0;
         st.amt[z] = a;
         st.damt[z] = da;
@@ -503,6 +570,7 @@ extern "C" hc_status hc_adj_gradient(hc_ctx* c, int64_t n, int32_t every, const 
       k_adj_gather<<<gr, b, 0, s>>>(v, bb, st);
     }
     HC_CU(cudaGetLastError(), "adjoint kernels");
+    HC_CU(cudaStreamSynchronize(s), "adjoint");  // pts' buffers are freed next
   }
   HC_CU(cudaStreamSynchronize(s), "adjoint");
   const double ms_rev = ms_since(t_rev);
@@ -545,4 +613,9 @@ extern "C" hc_status hc_adj_gradient(hc_ctx* c, int64_t n, int32_t every, const 
     ms[2] = ms_since(t_all);
   }
   return HC_OK;
+}
+
+void launch_adj_save(hc_ctx* c) {
+  k_adj_save<<<152 * 4, 256, 0, c->cs>>>(c->v, c->dev);
+  count_launch(c, 1);
 }

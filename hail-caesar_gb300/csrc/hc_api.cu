@@ -733,6 +733,7 @@ static hc_status recompute_points(hc_ctx* c, bool snapshot) {
   HC_TRY(pull(c));
   if (c->hdev->pause & HC_PAUSE_ERROR) return device_error(c);
   if (!keep_area) c->stat_n[HC_STAT_DRAINAGE_LEVELS] += c->hdev->drain_levels;
+  if (c->points_hook) c->points_hook(c, c->points_hook_arg);
   return HC_OK;
 }
 
@@ -931,6 +932,7 @@ static hc_status capture_iteration(hc_ctx* c, int flags) {
   launch_control(c);
   H.has = 0;  // no other launch sets the iteration's conditions
   if (sed) launch_drain_snapshot(c);
+  if (c->v.adj_sh) launch_adj_save(c);
   launch_inputs(c);
   launch_flow_route(c, 1);
   launch_depth_update(c, 1);

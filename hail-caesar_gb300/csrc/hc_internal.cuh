@@ -82,6 +82,7 @@ struct hc_dev {
   unsigned int drain_rf[HC_MAX_RF + 1];
   int adj_mode;           // 0 off, 1 record the time steps, 2 impose them
   int64_t adj_i, adj_n;   // next iteration, capacity of hc_view::adj_dt
+  int64_t adj_slot_t0, adj_slot_n;  // iterations whose state k_adj_save keeps
   unsigned int xchains;   // chain starts of the +/-x apply pass (hc_view::chains)
   unsigned int ychains;   // chain starts of the +/-y apply pass
 };
@@ -144,6 +145,10 @@ struct hc_view {
   // adjoint runs (hc_adjoint.cu): per-iteration time steps, recorded or
   // imposed (HC_ADJ_REC stride per iteration; see hc_dev::adj_mode)
   double *adj_dt;
+  // adjoint replay: each iteration's state before it (slot = iteration -
+  // hc_dev::adj_slot_t0), saved by k_adj_save when these are set
+  double *adj_sh, *adj_sqx, *adj_sqy;
+  uint8_t *adj_smask;
   unsigned long long *alloc_key; // N2: serial-order key of the first grain-record request
   int32_t *alloc_list;           // N2: cells allocated, in order
   int32_t *slide_list; int slide_cap;
@@ -180,6 +185,9 @@ struct hc_ctx {
   int32_t *h_cin_x, *h_cin_y;
   void* drainage_cache;    // sweep order of the drainage area, reused while elev is unchanged
   bool area_valid;         // device area matches the cached sweep order
+  // called after every recomputation of the input points (adjoint replays)
+  void (*points_hook)(hc_ctx*, void*);
+  void* points_hook_arg;
   // CUDA graph of K iterations
   cudaGraphExec_t graph; int graph_iters; int graph_flags;
   int64_t graph_kernels;   // kernel nodes in the graph
@@ -350,6 +358,7 @@ hc_status run_drainage_device(hc_ctx* c, const double* el, bool area_valid,
                               const uint32_t* (*sort_order)(hc_ctx*, const double*),
                               bool* sorted);
 void launch_drain_snapshot(hc_ctx* c);
+void launch_adj_save(hc_ctx* c);         // adjoint replay: state before the iteration
 hc_status ctx_pull(hc_ctx* c);   // control block device -> host mirror
 hc_status ctx_push(hc_ctx* c);   // host mirror -> device
 const float* ctx_rain(hc_ctx* c, int* rows, int* cols);  // host copy of the rain table
