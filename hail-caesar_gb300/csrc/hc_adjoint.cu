@@ -44,11 +44,23 @@ struct DQ {
   double v, dq, dh0, dh1, dnn;
 };
 
+// Three-way test of A > B from float estimates (as the forward kernel's):
+// +1 surely, -1 surely not, 0 too close to call.
+__device__ __forceinline__ int decide(float a, float b) {
+  const float m = 1e-4f * (fabsf(a) + fabsf(b));
+  if (!(m >= 1e-34f) || !(m < 1e30f)) return 0;
+  const float dd = a - b;
+  if (dd > m) return 1;
+  if (dd < -m) return -1;
+  return 0;
+}
+
 // One face (:3096-3191), as the device evaluates it, with derivatives.
-// Branch decisions are the reference's expressions evaluated in FP64, the
-// same decisions the forward kernel takes.
+// The value and the branch decisions are the forward kernel's (exact FP64
+// where a branch is decided, float estimates first, as there); the
+// derivatives, which need no exact rounding, use reciprocals.
 __device__ DQ face_dq(double q, double e0, double h0, double e1, double h1, double nn, double dt,
-                      int es, const hc_params& p) {
+                      int es, const hc_params& p, double rDX) {
   const double DX = p.DX;
   DQ r = {0, 0, 0, 0, 0};
   const double a0 = e0 + h0, a1 = e1 + h1;
@@ -56,10 +68,11 @@ __device__ DQ face_dq(double q, double e0, double h0, double e1, double h1, doub
   const double hflow = smax(a0, a1) - smax(e1, e0);
   if (!(hflow > p.hflow_threshold)) return r;  // q = 0
   const double dhf0 = a1max ? 0.0 : 1.0, dhf1 = a1max ? 1.0 : 0.0;
-  double slope = (a1 - a0) / DX, ds0 = -1 / DX, ds1 = 1 / DX;
+  double slope = div_const(a1 - a0, DX, rDX), ds0 = -rDX, ds1 = rDX;
   if (es == 1) slope = p.edgeslope, ds0 = ds1 = 0;
   if (es == -1) slope = 0 - p.edgeslope, ds0 = ds1 = 0;
   const double ghd = kG * hflow * dt;
+  const double rhf = 1 / hflow;
   // qn and its derivatives with respect to q, hflow, slope, nn
   double qn, d_q, d_hf, d_s, d_nn;
   if (q == 0) {
@@ -73,35 +86,51 @@ __device__ DQ face_dq(double q, double e0, double h0, double e1, double h1, doub
     const double F = ghd * nn * fabs(q) / c3;
     const double D = 1 + F, N = q - (ghd * slope);
     qn = N / D;
-    const double dF_q = ghd * nn * (q > 0 ? 1.0 : -1.0) / c3;
-    const double dF_hf = -2 * F / hflow;
-    const double dF_nn = ghd * fabs(q) / c3;
-    d_q = 1 / D - qn * dF_q / D;
-    d_hf = (-kG * dt * slope) / D - qn * dF_hf / D;
-    d_s = -ghd / D;
-    d_nn = -qn * dF_nn / D;
+    const double rD = 1 / D, rc3 = 1 / c3;
+    const double dF_q = ghd * nn * (q > 0 ? 1.0 : -1.0) * rc3;
+    const double dF_hf = -2 * F * rhf;
+    const double dF_nn = ghd * fabs(q) * rc3;
+    d_q = rD - qn * dF_q * rD;
+    d_hf = (-kG * dt * slope) * rD - qn * dF_hf * rD;
+    d_s = -ghd * rD;
+    d_nn = -qn * dF_nn * rD;
   }
   double dh0 = d_hf * dhf0 + d_s * ds0, dh1 = d_hf * dhf1 + d_s * ds1;
-  // Froude limit (:3124-3134)
+  // Froude limit (:3124-3134): |q/hflow| / sqrt(g*hflow) > froude_limit
   const double fl = p.froude_limit;
-  if (qn > 0 && (qn / hflow) / sqrt(kG * hflow) > fl) {
-    qn = hflow * (sqrt(kG * hflow) * fl);
-    const double g = 1.5 * sqrt(kG * hflow) * fl;
-    d_q = 0, d_nn = 0, dh0 = g * dhf0, dh1 = g * dhf1;
+  if (qn != 0) {
+    const float hf = approx_abs_f(hflow);
+    int t = decide(approx_abs_f(qn) / (hf * sqrtf(9.81f * hf)), (float)fl);
+    if (t == 0) t = (fabs(qn / hflow) / sqrt(kG * hflow) > fl) ? 1 : -1;
+    if (t > 0) {
+      const double sg = sqrt(kG * hflow);
+      const double g = 1.5 * sg * fl;
+      if (qn > 0) {
+        qn = hflow * (sg * fl);
+        d_q = 0, d_nn = 0, dh0 = g * dhf0, dh1 = g * dhf1;
+      } else {
+        qn = 0 - (hflow * (sg * fl));
+        d_q = 0, d_nn = 0, dh0 = -g * dhf0, dh1 = -g * dhf1;
+      }
+    }
   }
-  if (qn < 0 && fabs(qn / hflow) / sqrt(kG * hflow) > fl) {
-    qn = 0 - (hflow * (sqrt(kG * hflow) * fl));
-    const double g = -1.5 * sqrt(kG * hflow) * fl;
-    d_q = 0, d_nn = 0, dh0 = g * dhf0, dh1 = g * dhf1;
+  // depth limits (:3138-3148), one after the other
+  const float dtf = approx_abs_f(dt), dxf = (float)DX;
+  if (qn > 0) {
+    int t = decide(approx_abs_f(qn) * dtf / dxf, approx_f(h0) * 0.25f);
+    if (t == 0) t = ((qn * dt / DX) > (h0 / 4)) ? 1 : -1;
+    if (t > 0) {
+      qn = ((h0 * DX) / 5) / dt;
+      d_q = 0, d_nn = 0, dh0 = DX / 5 / dt, dh1 = 0;
+    }
   }
-  // depth limits (:3138-3148)
-  if (qn > 0 && (qn * dt / DX) > (h0 / 4)) {
-    qn = ((h0 * DX) / 5) / dt;
-    d_q = 0, d_nn = 0, dh0 = DX / 5 / dt, dh1 = 0;
-  }
-  if (qn < 0 && fabs(qn * dt / DX) > (h1 / 4)) {
-    qn = 0 - ((h1 * DX) / 5) / dt;
-    d_q = 0, d_nn = 0, dh0 = 0, dh1 = -DX / 5 / dt;
+  if (qn < 0) {
+    int t = decide(approx_abs_f(qn) * dtf / dxf, approx_f(h1) * 0.25f);
+    if (t == 0) t = (fabs(qn * dt / DX) > (h1 / 4)) ? 1 : -1;
+    if (t > 0) {
+      qn = 0 - ((h1 * DX) / 5) / dt;
+      d_q = 0, d_nn = 0, dh0 = 0, dh1 = -DX / 5 / dt;
+    }
   }
   r.v = qn;
   r.dq = d_q;
@@ -189,7 +218,7 @@ __global__ void k_adj_flow(const hc_view c, AdjBufs b, AdjStep st) {
       const double h1 = hin(up), e1 = c.elev[up];
       if ((h0 > 0 || h1 > 0) && e1 > -9999) {
         const int es = (i == c.imax) ? 1 : ((i <= 2) ? -1 : 0);
-        const DQ r = face_dq(b.qx0[cell], e0, h0, e1, h1, nn, st.fdt, es, p);
+        const DQ r = face_dq(b.qx0[cell], e0, h0, e1, h1, nn, st.fdt, es, p, c.rDX);
         ox = r.dq * mux;
         p0x = r.dh0 * mux;
         p1x = r.dh1 * mux;
@@ -201,7 +230,7 @@ __global__ void k_adj_flow(const hc_view c, AdjBufs b, AdjStep st) {
       const double h1 = hin(lf), e1 = c.elev[lf];
       if ((h0 > 0 || h1 > 0) && e1 > -9999) {
         const int es = (j == c.jmax) ? 1 : ((j <= 2) ? -1 : 0);
-        const DQ r = face_dq(b.qy0[cell], e0, h0, e1, h1, nn, st.fdt, es, p);
+        const DQ r = face_dq(b.qy0[cell], e0, h0, e1, h1, nn, st.fdt, es, p, c.rDX);
         oy = r.dq * muy;
         p0y = r.dh0 * muy;
         p1y = r.dh1 * muy;

@@ -83,7 +83,7 @@ __global__ void __launch_bounds__(128) k_entrain(const hc_view c, hc_dev* d, int
       }
       c.ss[cell] = 0;
       const double h = c.h[cell];
-      if (h > thr) {
+      if (dgt(h, thr)) {
         const double DX = p.DX, rho = 1000.0;
         const double e0 = c.elev[cell];
         const unsigned long long pos = (unsigned long long)jy * (c.imax + 2) + ix;
@@ -101,13 +101,13 @@ __global__ void __launch_bounds__(128) k_entrain(const hc_view c, hc_dev* d, int
           const int pp = 1 + 2 * k;
           const int x2 = ix + kDXc[pp], y2 = jy + kDYc[pp];
           const size_t nb = (size_t)x2 * W + y2;
-          if (c.h[nb] > thr) {
+          if (dgt(c.h[nb], thr)) {
             const double edge2 = c.edge[EX(c, x2, y2)];
-            if (edge0 > edge2) temptot2 += (edge0 - edge2);
+            if (dgt(edge0, edge2)) temptot2 += (edge0 - edge2);
             const double vdir = c.vd[(size_t)k * N2 + cell];
-            if (vdir > 0) {
+            if (dgt0(vdir)) {
               vel = vdir;
-              if (vel > p.max_vel) vel = p.max_vel;
+              if (dgt(vel, p.max_vel)) vel = p.max_vel;
               tempdir[k] = vel * vel;
               veltot += tempdir[k];
               qtot += (vel * vel);
@@ -115,16 +115,16 @@ __global__ void __launch_bounds__(128) k_entrain(const hc_view c, hc_dev* d, int
             }
           }
         }
-        if (qtot > 0) {
+        if (dgt0(qtot)) {
           vel = (sqrt(qtot));
           c.vel[cell] = vel;
-          if (vel > p.max_vel) vel = p.max_vel;
+          if (dgt(vel, p.max_vel)) vel = p.max_vel;
           double ci = kG * (n_man * n_man) * pow(h, -0.33);
-          if (slopetot > 0) slopetot = 0;
+          if (dgt0(slopetot)) slopetot = 0;
           tau = 1000 * ci * vel * vel * (1 + (1 * (slopetot / vel)));
           c.tau[cell] = tau;
         }
-        if (tau > 0) {
+        if (dgt0(tau)) {
           double temp_dist[HC_G] = {0};
           double d_50 = 0, Fs = 0, graintot = 0;
           const double ts = d->s.time_step;
@@ -161,29 +161,29 @@ __global__ void __launch_bounds__(128) k_entrain(const hc_view c, hc_dev* d, int
               td = div_const(div_const(mts * (40 * cube_rn(1 / x)), c.einS[n], c.einRS[n]), DX,
                              c.rDX);
             }
-            if (td > GRN(c, cell, n)) td = GRN(c, cell, n);
+            if (dgt(td, GRN(c, cell, n))) td = GRN(c, cell, n);
             if (p.isSuspended[n] && n == 1) {
-              if ((td + c.vs[cell]) / h > p.Csuspmax) td = (h * p.Csuspmax) - c.vs[cell];
+              if (dgt((td + c.vs[cell]) / h, p.Csuspmax)) td = (h * p.Csuspmax) - c.vs[cell];
             }
-            if (td < 0) td = 0;
+            if (dlt0(td)) td = 0;
             temp_dist[n] = td;
             temptot1 += td;
           }
           const double bed = c.bed[cell];
-          if (e0 - temptot1 <= bed) {
+          if (!dgt(e0 - temptot1, bed)) {
             double elevdiff = e0 - bed;
             double temptot3 = temptot1;
             temptot1 = 0;
             for (int n = 1; n <= HC_G - 1; n++) {
-              if (e0 <= bed) {
+              if (!dgt(e0, bed)) {
                 temp_dist[n] = 0;
               } else {
                 temp_dist[n] = elevdiff * (temp_dist[n] / temptot3);
-                if (temp_dist[n] < 0) temp_dist[n] = 0;
+                if (dlt0(temp_dist[n])) temp_dist[n] = 0;
               }
               temptot1 += temp_dist[n];
             }
-            if (tau > p.bedrock_erosion_threshold) {
+            if (dgt(tau, p.bedrock_erosion_threshold)) {
               double amount = pow(p.bedrock_erosion_rate * tau, 1.5) * ts * mult * 0.000000317;
               c.bed[cell] = bed - amount;
               for (int n2 = 1; n2 <= HC_G - 1; n2++) GRN(c, cell, n2) += amount * p.dprop[n2];
@@ -192,22 +192,22 @@ __global__ void __launch_bounds__(128) k_entrain(const hc_view c, hc_dev* d, int
           // vegetation terms (:4459-4488) vanish: vegetation is not supported
           // (hc_create rejects vegetation_on) and veg stays zero.
           tb = temptot1;
-          if (temptot1 > 0) {
+          if (dgt0(temptot1)) {
             for (int k = 0; k < 4; k++) {
               const int pp = 1 + 2 * k;
               const int x2 = ix + kDXc[pp], y2 = jy + kDYc[pp];
               const size_t nb = (size_t)x2 * W + y2;
-              if (c.h[nb] > thr) {
+              if (dgt(c.h[nb], thr)) {
                 if (c.index[nb] < 1) {  // no final row number yet: ask
                   atomicMin(&c.alloc_key[nb], pos * 5 + 1 + k);
                   d->alloc_count = 1;
                 }
                 double factor = 0;
-                if (c.vd[(size_t)k * N2 + cell] > 0) factor += 0.75 * tempdir[k] / veltot;
+                if (dgt0(c.vd[(size_t)k * N2 + cell])) factor += 0.75 * tempdir[k] / veltot;
                 const double edge2 = c.edge[EX(c, x2, y2)];
-                if (edge0 > edge2) factor += 0.25 * ((edge0 - edge2) / temptot2);
+                if (dgt(edge0, edge2)) factor += 0.25 * ((edge0 - edge2) / temptot2);
                 for (int n = 1; n <= HC_G - 1; n++) {
-                  if (temp_dist[n] > 0) {
+                  if (dgt0(temp_dist[n])) {
                     if (n == 1 && p.isSuspended[n]) {
                       c.ss[cell] = temp_dist[n];
                     } else {
@@ -693,192 +693,338 @@ __global__ void __launch_bounds__(256) k_apply_gather(const hc_view c, hc_dev* d
   }
 }
 
-// A row's inputs to the walkers, staged in shared memory by asynchronous
-// copies (cp.async): a walker asks for row r+2 before it works on row r, so
-// the copies' latency hides behind that work.  One slot per thread.
-struct StagedRow {
-  double g[HC_G + 1];
-  double pre[HC_G + 1];
-  double elev, h, bed, edge, tau, ss, et3;
+// ---------------------------------------------------------------------------
+// The chain walkers.  One warp per chain: lane n holds fraction n of each
+// held row's grain record (lanes 0..HC_G), so the per-fraction arithmetic of
+// the gather, slide_GS and sort_active runs as one instruction for all
+// fractions instead of nine; the FP64 pipe, a few lanes per clock on this
+// GPU, is what a single walker waits on.  Sums keep the reference's order
+// (sequential over the fractions, every lane forming the same sum), so the
+// results are the serial loop's.  Rows r-1, r, r+1 are held (U, C, D) and
+// row r+2 is loaded while row r is worked on.
+// ---------------------------------------------------------------------------
+constexpr unsigned kFull = 0xffffffffu;
+
+struct WRow {
+  double g;  // grain plane `lane` (lanes 0..HC_G; 0 in the others)
+  double elev, h, bed, edge;
   int idx;
-  unsigned int mword;  // the aligned 4-byte word that holds mask[cell]
+  bool dirty;
 };
 
-__device__ __forceinline__ void cp_async(void* smem, const void* gmem, int bytes) {
-  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-  if (bytes == 8)
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
-  else
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() {
-  asm volatile("cp.async.commit_group;\n" ::: "memory");
-}
-__device__ __forceinline__ void cp_async_wait_all() {
-  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
-}
+// the rest of a row the x walker needs when it is the current row
+struct WExtra {
+  double pre;  // PRE plane `lane` (lanes 0..HC_G)
+  double tau, ss, et3;
+  bool mask;
+};
 
-__device__ __forceinline__ void stage_issue(const hc_view& c, StagedRow* st, size_t cell,
-                                            size_t ecell, bool with_pre) {
-  for (int n = 0; n <= HC_G; n++) cp_async(&st->g[n], &GRN(c, cell, n), 8);
-  if (with_pre)
-    for (int k = 0; k <= HC_G; k++) cp_async(&st->pre[k], &PRE(c, k, cell), 8);
-  cp_async(&st->elev, c.elev + cell, 8);
-  cp_async(&st->h, c.h + cell, 8);
-  cp_async(&st->bed, c.bed + cell, 8);
-  cp_async(&st->edge, c.edge + ecell, 8);
-  cp_async(&st->tau, c.tau + cell, 8);
-  cp_async(&st->ss, c.ss + cell, 8);
-  cp_async(&st->et3, c.erodetot3 + cell, 8);
-  cp_async(&st->idx, c.index + cell, 4);
-  cp_async(&st->mword, (const void*)((uintptr_t)(c.mask + cell) & ~(uintptr_t)3), 4);
-  cp_async_commit();
-}
+__device__ __forceinline__ int lane_id() { return (int)(threadIdx.x & 31); }
 
-// waits for the slot and moves it into registers
-__device__ __forceinline__ void stage_take(const StagedRow* st, size_t cell, ApplyRow& r,
-                                           double* pre, double& tau, double& ss, double& et3,
-                                           bool& mask) {
-  cp_async_wait_all();
-#pragma unroll
-  for (int n = 0; n <= HC_G; n++) r.g[n] = st->g[n];
-  if (pre)
-#pragma unroll
-    for (int k = 0; k <= HC_G; k++) pre[k] = st->pre[k];
-  r.elev = st->elev;
-  r.h = st->h;
-  r.bed = st->bed;
-  r.edge = st->edge;
-  r.idx = st->idx;
+__device__ __forceinline__ void wrow_load(const hc_view& c, size_t cell, size_t ecell, WRow& r) {
+  const int L = lane_id();
+  r.g = (L <= HC_G) ? GRN(c, cell, L) : 0.0;
+  r.elev = c.elev[cell];
+  r.h = c.h[cell];
+  r.bed = c.bed[cell];
+  r.edge = c.edge[ecell];
+  r.idx = c.index[cell];
   r.dirty = false;
-  tau = st->tau;
-  ss = st->ss;
-  et3 = st->et3;
-  mask = ((st->mword >> (8 * (unsigned)(cell & 3))) & 0xffu) != 0;
 }
 
-// chains along the columns, one per thread: rows r-1, r, r+1 held in U, C, D
+__device__ __forceinline__ void wextra_load(const hc_view& c, size_t cell, bool with_pre,
+                                            WExtra& x) {
+  const int L = lane_id();
+  x.pre = (with_pre && L <= HC_G) ? PRE(c, L, cell) : 0.0;
+  x.tau = c.tau[cell];
+  x.ss = c.ss[cell];
+  x.et3 = c.erodetot3[cell];
+  x.mask = c.mask[cell] != 0;
+}
+
+__device__ __forceinline__ void wrow_store(const hc_view& c, size_t cell, const WRow& r) {
+  if (!r.dirty) return;
+  const int L = lane_id();
+  if (L >= 1 && L <= HC_G - 1) GRN(c, cell, L) = r.g;
+  if (L == 0) c.elev[cell] = r.elev;
+}
+
+// sort_active on a held row, the warp together (same decisions as
+// sort_active_row; the float estimate's sum order does not matter, its
+// error bound holds for any order)
+__device__ void sort_active_w(const hc_view& c, hc_dev* d, size_t cell, WRow& r) {
+  const int L = lane_id();
+  if (r.idx == -9999) {
+    if (L == 0) {
+      d->err_code = 201;
+      d->pause |= HC_PAUSE_ERROR;
+    }
+    return;
+  }
+  const double active = c.p.active;
+  const float f = (L <= HC_G) ? approx_f(r.g) : 0.0f;
+  float sf = f, af = fabsf(f);
+  for (int o = 16; o > 0; o >>= 1) {
+    sf += __shfl_xor_sync(kFull, sf, o);
+    af += __shfl_xor_sync(kFull, af, o);
+  }
+  const float tol = 1e-5f * af + 1e-30f;
+  const float hi = (float)(active * 1.5), lo = (float)(active / 4);
+  const int dep = (sf > hi + tol) ? 1 : ((sf < hi - tol) ? -1 : 0);
+  const int ero = (sf < lo - tol) ? 1 : ((sf > lo + tol) ? -1 : 0);
+  if (dep == -1 && ero == -1) return;
+  double total = 0.0;  // in the reference's order, n = 0 .. HC_G
+  for (int n = 0; n <= HC_G; n++) total += __shfl_sync(kFull, r.g, n);
+  if (total > (active * 1.5)) {
+    if (L <= HC_G - 2)
+      for (int z = 9; z >= 1; z--) STR(c, cell, z, L) = STR(c, cell, z - 1, L);
+    __syncwarp();
+    const double coeff = active / total;
+    if (L >= 1 && L <= HC_G - 1 && r.g > 0.0) {
+      const double amount = coeff * (r.g);
+      STR(c, cell, 0, L - 1) = amount;
+      r.g = r.g - amount;
+    }
+    r.dirty = true;
+    __syncwarp();
+  }
+  if (total < (active / 4)) {
+    double s0 = 0;
+    if (L >= 1 && L <= HC_G - 1) s0 = STR(c, cell, 0, L - 1);
+    __syncwarp();
+    if (L <= HC_G - 2)
+      for (int z = 0; z <= 8; z++) STR(c, cell, z, L) = STR(c, cell, z + 1, L);
+    __syncwarp();
+    if (L >= 1 && L <= HC_G - 1) {
+      r.g += s0;
+      STR(c, cell, 9, L - 1) = active * c.p.dprop[L];
+    }
+    r.dirty = true;
+    __syncwarp();
+  }
+}
+
+// slide_GS(a -> b, amount) on held rows, the warp together
+__device__ void slide_GS_w(const hc_view& c, hc_dev* d, size_t a, WRow& A, double amount,
+                           size_t b, WRow& B) {
+  const int L = lane_id();
+  const bool fr = L >= 1 && L <= HC_G - 1;
+  const double dp = fr ? c.p.dprop[L] : 0.0;
+  const bool ha = A.idx != -9999, hb = B.idx != -9999;
+  if (ha && hb) {
+    double total = 0;  // positive fractions 1..9, in order
+    for (int n = 1; n <= HC_G - 1; n++) {
+      const double v = __shfl_sync(kFull, A.g, n);
+      if (v > 0) total += v;
+    }
+    if (amount > total) {
+      if (fr) B.g += (amount - total) * dp;
+      amount = total;
+    }
+    if (total > 0) {
+      const double rt = 1.0 / total;
+      if (fr) {
+        const double ga = A.g;
+        const double t = amount * div_const(ga, total, rt);
+        B.g += t;
+        double na = ga - t;
+        if (na < 0) na = 0;
+        A.g = na;
+      }
+    }
+    A.dirty = B.dirty = true;
+    sort_active_w(c, d, a, A);
+    sort_active_w(c, d, b, B);
+    return;
+  }
+  if (!ha && hb) {
+    if (fr) B.g += (amount)*dp;
+    B.dirty = true;
+    sort_active_w(c, d, b, B);
+    return;
+  }
+  if (ha && !hb && L == 0) {
+    d->err_code = 202;
+    d->pause |= HC_PAUSE_ERROR;
+  }
+}
+
+__device__ __forceinline__ bool lateral_amount_w(const hc_params& p, double mult, double ts,
+                                                 double tau0, double et3, const WRow& N,
+                                                 double e0, bool boundary, double& amt) {
+  const double DX = p.DX;
+  const double e_nb = N.elev;
+  amt = 0;
+  if (N.h < p.water_depth_erosion_threshold)
+    amt = mult * p.lateral_constant * tau0 * N.edge * ts / DX;
+  else
+    amt = p.chann_lateral_erosion * et3 * (e_nb - e0) / DX * 0.1;
+  if (!(amt > 0)) return false;
+  if ((e_nb - amt) < N.bed || boundary) amt = 0;
+  if (amt > p.ERODEFACTOR * 0.1) amt = p.ERODEFACTOR * 0.1;
+  return true;
+}
+
+__device__ __forceinline__ void lateral_step_w(const hc_view& c, hc_dev* d, double mult,
+                                               double ts, double tau0, double et3, size_t ccell,
+                                               WRow& C, double e0, size_t ncell, WRow& N,
+                                               bool boundary, double& elev_update) {
+  const double en = N.elev;
+  double amt;
+  if (en > e0 && lateral_amount_w(c.p, mult, ts, tau0, et3, N, e0, boundary, amt)) {
+    elev_update += amt;
+    N.elev = en - amt;
+    N.dirty = true;
+    slide_GS_w(c, d, ncell, N, amt, ccell, C);
+  }
+}
+
+// the gather of an active cell, the warp together
+__device__ __forceinline__ double gather_w(const hc_view& c, hc_dev* d, size_t cell, WRow& r,
+                                           const WExtra& x) {
+  const int L = lane_id();
+  const double pre0 = __shfl_sync(kFull, x.pre, 0);
+  const double erodetot = __shfl_sync(kFull, x.pre, HC_G);
+  if (L >= 1 && L <= HC_G - 1) {
+    if (L == 1 && c.p.isSuspended[1]) {
+      const double g = r.g - x.ss;
+      r.g = g + pre0;
+    } else {
+      r.g += x.pre;
+    }
+  }
+  const double e0 = r.elev + erodetot;
+  r.elev = e0;
+  r.dirty = true;
+  if (erodetot < 0) sort_active_w(c, d, cell, r);
+  return e0;
+}
+
+// chains along the columns, one warp per chain
 __global__ void __launch_bounds__(128) k_apply_xchains(const hc_view c, hc_dev* d) {
-  __shared__ StagedRow slots[128];
   if (!(d->it_active && d->rest_active && d->do_erode) || d->erode_retry) return;
-  StagedRow* st = &slots[threadIdx.x];
   const unsigned nch = d->xchains;
   const double mult = d->mult, ts = d->s.time_step;
   const double thr = c.p.water_depth_erosion_threshold;
   const size_t W = c.W;
-  auto active = [&](bool m, double h, int x) { return m && h > thr && x < c.imax && x > 1; };
-  for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < nch; k += gridDim.x * blockDim.x) {
+  const unsigned warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const unsigned nwarps = (gridDim.x * blockDim.x) >> 5;
+  auto active = [&](const WExtra& x, double h, int r) {
+    return x.mask && h > thr && r < c.imax && r > 1;
+  };
+  for (unsigned k = warp; k < nch; k += nwarps) {
     size_t cell = c.chains[k];
     const int y = (int)(cell % W);
     int r = (int)(cell / W);
-    ApplyRow U, C, D;
-    double Cpre[HC_G + 1], Dpre[HC_G + 1];
-    double Ctau, Css, Cet3, Dtau = 0, Dss = 0;
-    bool Cm, Dm;
+    WRow U, C, D, E;
+    WExtra Cx, Dx, Ex;
     bool hasU = false;
     size_t ucell = 0;
-    stage_issue(c, st, cell, EX(c, r, y), true);
-    stage_take(st, cell, C, Cpre, Ctau, Css, Cet3, Cm);
-    bool Cact = active(Cm, C.h, r);
-    if (r + 1 <= c.imax) stage_issue(c, st, cell + W, EX(c, r + 1, y), true);
+    wrow_load(c, cell, EX(c, r, y), C);
+    wextra_load(c, cell, true, Cx);
+    if (r + 1 <= c.imax) {
+      wrow_load(c, cell + W, EX(c, r + 1, y), D);
+      wextra_load(c, cell + W, true, Dx);
+    }
+    bool Cact = active(Cx, C.h, r);
     for (;;) {
       const bool hasD = r + 1 <= c.imax;
       const size_t dcell = cell + W;
-      double Det3 = 0;
-      bool Dact = false;
-      if (hasD) {
-        stage_take(st, dcell, D, Dpre, Dtau, Dss, Det3, Dm);
-        Dact = active(Dm, D.h, r + 1);
-        // row r+2 is copied while row r is worked on
-        if (r + 2 <= c.imax) stage_issue(c, st, dcell + W, EX(c, r + 2, y), true);
+      // row r+2, loaded while row r is worked on
+      const bool hasE = r + 2 <= c.imax;
+      if (hasE) {
+        wrow_load(c, dcell + W, EX(c, r + 2, y), E);
+        wextra_load(c, dcell + W, true, Ex);
       }
+      const double Det3 = hasD ? Dx.et3 : 0.0;
+      const bool Dact = hasD && active(Dx, D.h, r + 1);
       if (Cact) {
-        const double e0 = gather_row(c, d, cell, C, Cpre, Css);
-        if (Cet3 > 0) {
+        const double e0 = gather_w(c, d, cell, C, Cx);
+        if (Cx.et3 > 0) {
           double elev_update = 0;
           if (r > 2 && hasU)
-            lateral_step(c, d, mult, ts, Ctau, Cet3, cell, C, e0, ucell, U, r - 1 == 1,
-                         elev_update);
+            lateral_step_w(c, d, mult, ts, Cx.tau, Cx.et3, cell, C, e0, ucell, U, r - 1 == 1,
+                           elev_update);
           if (r < c.imax - 1 && hasD)
-            lateral_step(c, d, mult, ts, Ctau, Cet3, cell, C, e0, dcell, D, r + 1 == c.imax,
-                         elev_update);
+            lateral_step_w(c, d, mult, ts, Cx.tau, Cx.et3, cell, C, e0, dcell, D,
+                           r + 1 == c.imax, elev_update);
           C.elev = C.elev + elev_update;
         }
       }
-      if (hasU) row_store(c, ucell, U);  // row r-1 is final
-      if (!(Cet3 > 0 || Det3 > 0) || !hasD) {
-        row_store(c, cell, C);
-        if (hasD) row_store(c, dcell, D);
-        cp_async_wait_all();  // the slot is free for the next chain
+      if (hasU) wrow_store(c, ucell, U);  // row r-1 is final
+      if (!(Cx.et3 > 0 || Det3 > 0) || !hasD) {
+        wrow_store(c, cell, C);
+        if (hasD) wrow_store(c, dcell, D);
         break;
       }
       U = C;
       hasU = true;
       ucell = cell;
       C = D;
-#pragma unroll
-      for (int n = 0; n <= HC_G; n++) Cpre[n] = Dpre[n];
-      Ctau = Dtau;
-      Css = Dss;
-      Cet3 = Det3;
+      Cx = Dx;
       Cact = Dact;
+      D = E;
+      Dx = Ex;
       cell = dcell;
       r++;
     }
   }
 }
 
-// chains along the rows for the +/-y pass: columns q-1, q, q+1 held in
-// U, C, D
+// chains along the rows for the +/-y pass, one warp per chain: columns
+// q-1, q, q+1 held in U, C, D
 __global__ void __launch_bounds__(128) k_apply_ychains(const hc_view c, hc_dev* d) {
-  __shared__ StagedRow slots[128];
   if (!(d->it_active && d->rest_active && d->do_erode) || d->erode_retry) return;
-  StagedRow* st = &slots[threadIdx.x];
   const unsigned nch = d->ychains;
   const double mult = d->mult, ts = d->s.time_step;
   const size_t W = c.W;
-  for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < nch; k += gridDim.x * blockDim.x) {
+  const unsigned warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const unsigned nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (unsigned k = warp; k < nch; k += nwarps) {
     size_t cell = c.chains[c.N2 + k];
     const int x = (int)(cell / W);
     int q = (int)(cell % W);
-    auto lat = [&](int qq, bool m, double et3) { return qq >= 2 && qq <= c.jmax - 1 && m && et3 > 0; };
-    ApplyRow U, C, D;
-    double Ctau, Css, Cet3, Dtau, Dss, Det3, t0, t1, t2;
-    bool Cm, Dm, m0;
-    stage_issue(c, st, cell - 1, EX(c, x, q - 1), false);
-    stage_take(st, cell - 1, U, nullptr, t0, t1, t2, m0);
-    stage_issue(c, st, cell, EX(c, x, q), false);
-    stage_take(st, cell, C, nullptr, Ctau, Css, Cet3, Cm);
-    bool Clat = lat(q, Cm, Cet3);
-    stage_issue(c, st, cell + 1, EX(c, x, q + 1), false);  // q + 1 <= jmax
+    auto lat = [&](int qq, const WExtra& e) {
+      return qq >= 2 && qq <= c.jmax - 1 && e.mask && e.et3 > 0;
+    };
+    WRow U, C, D, E;
+    WExtra Cx, Dx, Ex;
+    wrow_load(c, cell - 1, EX(c, x, q - 1), U);
+    wrow_load(c, cell, EX(c, x, q), C);
+    wextra_load(c, cell, false, Cx);
+    wrow_load(c, cell + 1, EX(c, x, q + 1), D);  // q + 1 <= jmax
+    wextra_load(c, cell + 1, false, Dx);
+    bool Clat = lat(q, Cx);
     for (;;) {
       const size_t dcell = cell + 1;
-      stage_take(st, dcell, D, nullptr, Dtau, Dss, Det3, Dm);
-      const bool Dlat = lat(q + 1, Dm, Det3);
-      if (q + 2 <= c.jmax) stage_issue(c, st, dcell + 1, EX(c, x, q + 2), false);
+      const bool hasE = q + 2 <= c.jmax;
+      if (hasE) {
+        wrow_load(c, dcell + 1, EX(c, x, q + 2), E);
+        wextra_load(c, dcell + 1, false, Ex);
+      }
+      const bool Dlat = lat(q + 1, Dx);
       if (Clat) {
         const double e0 = C.elev;
         double elev_update = 0;
-        lateral_step(c, d, mult, ts, Ctau, Cet3, cell, C, e0, cell - 1, U, q - 1 == 1,
-                     elev_update);
-        lateral_step(c, d, mult, ts, Ctau, Cet3, cell, C, e0, dcell, D, q + 1 == c.jmax,
-                     elev_update);
+        lateral_step_w(c, d, mult, ts, Cx.tau, Cx.et3, cell, C, e0, cell - 1, U, q - 1 == 1,
+                       elev_update);
+        lateral_step_w(c, d, mult, ts, Cx.tau, Cx.et3, cell, C, e0, dcell, D, q + 1 == c.jmax,
+                       elev_update);
         C.elev = C.elev + elev_update;
         C.dirty = true;
       }
-      row_store(c, cell - 1, U);  // column q-1 is final
+      wrow_store(c, cell - 1, U);  // column q-1 is final
       if (!(Clat || Dlat) || q + 1 > c.jmax - 1) {
-        row_store(c, cell, C);
-        row_store(c, dcell, D);
-        cp_async_wait_all();
+        wrow_store(c, cell, C);
+        wrow_store(c, dcell, D);
         break;
       }
       U = C;
       C = D;
-      Ctau = Dtau;
-      Css = Dss;
-      Cet3 = Det3;
+      Cx = Dx;
       Clat = Dlat;
+      D = E;
+      Dx = Ex;
       cell = dcell;
       q++;
     }
