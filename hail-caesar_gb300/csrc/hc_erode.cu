@@ -693,6 +693,206 @@ __global__ void __launch_bounds__(256) k_apply_gather(const hc_view c, hc_dev* d
   }
 }
 
+// Chains are walked by one thread each when there are many (all of them in
+// flight at once), by one warp each when there are few (each one faster).
+constexpr unsigned kWalkBlocks = 152 * 8;            // blocks of 128 threads
+constexpr unsigned kWarpChains = kWalkBlocks * 4;    // warps in flight
+
+// A row's inputs to the walkers, staged in shared memory by asynchronous
+// copies (cp.async): a walker asks for row r+2 before it works on row r, so
+// the copies' latency hides behind that work.  One slot per thread.
+struct StagedRow {
+  double g[HC_G + 1];
+  double pre[HC_G + 1];
+  double elev, h, bed, edge, tau, ss, et3;
+  int idx;
+  unsigned int mword;  // the aligned 4-byte word that holds mask[cell]
+};
+
+__device__ __forceinline__ void cp_async(void* smem, const void* gmem, int bytes) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  if (bytes == 8)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+}
+
+__device__ __forceinline__ void stage_issue(const hc_view& c, StagedRow* st, size_t cell,
+                                            size_t ecell, bool with_pre) {
+  for (int n = 0; n <= HC_G; n++) cp_async(&st->g[n], &GRN(c, cell, n), 8);
+  if (with_pre)
+    for (int k = 0; k <= HC_G; k++) cp_async(&st->pre[k], &PRE(c, k, cell), 8);
+  cp_async(&st->elev, c.elev + cell, 8);
+  cp_async(&st->h, c.h + cell, 8);
+  cp_async(&st->bed, c.bed + cell, 8);
+  cp_async(&st->edge, c.edge + ecell, 8);
+  cp_async(&st->tau, c.tau + cell, 8);
+  cp_async(&st->ss, c.ss + cell, 8);
+  cp_async(&st->et3, c.erodetot3 + cell, 8);
+  cp_async(&st->idx, c.index + cell, 4);
+  cp_async(&st->mword, (const void*)((uintptr_t)(c.mask + cell) & ~(uintptr_t)3), 4);
+  cp_async_commit();
+}
+
+// waits for the slot and moves it into registers
+__device__ __forceinline__ void stage_take(const StagedRow* st, size_t cell, ApplyRow& r,
+                                           double* pre, double& tau, double& ss, double& et3,
+                                           bool& mask) {
+  cp_async_wait_all();
+#pragma unroll
+  for (int n = 0; n <= HC_G; n++) r.g[n] = st->g[n];
+  if (pre)
+#pragma unroll
+    for (int k = 0; k <= HC_G; k++) pre[k] = st->pre[k];
+  r.elev = st->elev;
+  r.h = st->h;
+  r.bed = st->bed;
+  r.edge = st->edge;
+  r.idx = st->idx;
+  r.dirty = false;
+  tau = st->tau;
+  ss = st->ss;
+  et3 = st->et3;
+  mask = ((st->mword >> (8 * (unsigned)(cell & 3))) & 0xffu) != 0;
+}
+
+// chains along the columns, one per thread (many chains): rows r-1, r, r+1
+// held in U, C, D
+__global__ void __launch_bounds__(128) k_apply_xchains_t(const hc_view c, hc_dev* d) {
+  __shared__ StagedRow slots[128];
+  if (!(d->it_active && d->rest_active && d->do_erode) || d->erode_retry) return;
+  if (d->xchains <= kWarpChains) return;  // few chains: the warp walker takes them
+  StagedRow* st = &slots[threadIdx.x];
+  const unsigned nch = d->xchains;
+  const double mult = d->mult, ts = d->s.time_step;
+  const double thr = c.p.water_depth_erosion_threshold;
+  const size_t W = c.W;
+  auto active = [&](bool m, double h, int x) { return m && h > thr && x < c.imax && x > 1; };
+  for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < nch; k += gridDim.x * blockDim.x) {
+    size_t cell = c.chains[k];
+    const int y = (int)(cell % W);
+    int r = (int)(cell / W);
+    ApplyRow U, C, D;
+    double Cpre[HC_G + 1], Dpre[HC_G + 1];
+    double Ctau, Css, Cet3, Dtau = 0, Dss = 0;
+    bool Cm, Dm;
+    bool hasU = false;
+    size_t ucell = 0;
+    stage_issue(c, st, cell, EX(c, r, y), true);
+    stage_take(st, cell, C, Cpre, Ctau, Css, Cet3, Cm);
+    bool Cact = active(Cm, C.h, r);
+    if (r + 1 <= c.imax) stage_issue(c, st, cell + W, EX(c, r + 1, y), true);
+    for (;;) {
+      const bool hasD = r + 1 <= c.imax;
+      const size_t dcell = cell + W;
+      double Det3 = 0;
+      bool Dact = false;
+      if (hasD) {
+        stage_take(st, dcell, D, Dpre, Dtau, Dss, Det3, Dm);
+        Dact = active(Dm, D.h, r + 1);
+        // row r+2 is copied while row r is worked on
+        if (r + 2 <= c.imax) stage_issue(c, st, dcell + W, EX(c, r + 2, y), true);
+      }
+      if (Cact) {
+        const double e0 = gather_row(c, d, cell, C, Cpre, Css);
+        if (Cet3 > 0) {
+          double elev_update = 0;
+          if (r > 2 && hasU)
+            lateral_step(c, d, mult, ts, Ctau, Cet3, cell, C, e0, ucell, U, r - 1 == 1,
+                         elev_update);
+          if (r < c.imax - 1 && hasD)
+            lateral_step(c, d, mult, ts, Ctau, Cet3, cell, C, e0, dcell, D, r + 1 == c.imax,
+                         elev_update);
+          C.elev = C.elev + elev_update;
+        }
+      }
+      if (hasU) row_store(c, ucell, U);  // row r-1 is final
+      if (!(Cet3 > 0 || Det3 > 0) || !hasD) {
+        row_store(c, cell, C);
+        if (hasD) row_store(c, dcell, D);
+        cp_async_wait_all();  // the slot is free for the next chain
+        break;
+      }
+      U = C;
+      hasU = true;
+      ucell = cell;
+      C = D;
+#pragma unroll
+      for (int n = 0; n <= HC_G; n++) Cpre[n] = Dpre[n];
+      Ctau = Dtau;
+      Css = Dss;
+      Cet3 = Det3;
+      Cact = Dact;
+      cell = dcell;
+      r++;
+    }
+  }
+}
+
+// chains along the rows for the +/-y pass: columns q-1, q, q+1 held in
+// U, C, D
+__global__ void __launch_bounds__(128) k_apply_ychains_t(const hc_view c, hc_dev* d) {
+  __shared__ StagedRow slots[128];
+  if (!(d->it_active && d->rest_active && d->do_erode) || d->erode_retry) return;
+  if (d->ychains <= kWarpChains) return;
+  StagedRow* st = &slots[threadIdx.x];
+  const unsigned nch = d->ychains;
+  const double mult = d->mult, ts = d->s.time_step;
+  const size_t W = c.W;
+  for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < nch; k += gridDim.x * blockDim.x) {
+    size_t cell = c.chains[c.N2 + k];
+    const int x = (int)(cell / W);
+    int q = (int)(cell % W);
+    auto lat = [&](int qq, bool m, double et3) { return qq >= 2 && qq <= c.jmax - 1 && m && et3 > 0; };
+    ApplyRow U, C, D;
+    double Ctau, Css, Cet3, Dtau, Dss, Det3, t0, t1, t2;
+    bool Cm, Dm, m0;
+    stage_issue(c, st, cell - 1, EX(c, x, q - 1), false);
+    stage_take(st, cell - 1, U, nullptr, t0, t1, t2, m0);
+    stage_issue(c, st, cell, EX(c, x, q), false);
+    stage_take(st, cell, C, nullptr, Ctau, Css, Cet3, Cm);
+    bool Clat = lat(q, Cm, Cet3);
+    stage_issue(c, st, cell + 1, EX(c, x, q + 1), false);  // q + 1 <= jmax
+    for (;;) {
+      const size_t dcell = cell + 1;
+      stage_take(st, dcell, D, nullptr, Dtau, Dss, Det3, Dm);
+      const bool Dlat = lat(q + 1, Dm, Det3);
+      if (q + 2 <= c.jmax) stage_issue(c, st, dcell + 1, EX(c, x, q + 2), false);
+      if (Clat) {
+        const double e0 = C.elev;
+        double elev_update = 0;
+        lateral_step(c, d, mult, ts, Ctau, Cet3, cell, C, e0, cell - 1, U, q - 1 == 1,
+                     elev_update);
+        lateral_step(c, d, mult, ts, Ctau, Cet3, cell, C, e0, dcell, D, q + 1 == c.jmax,
+                     elev_update);
+        C.elev = C.elev + elev_update;
+        C.dirty = true;
+      }
+      row_store(c, cell - 1, U);  // column q-1 is final
+      if (!(Clat || Dlat) || q + 1 > c.jmax - 1) {
+        row_store(c, cell, C);
+        row_store(c, dcell, D);
+        cp_async_wait_all();
+        break;
+      }
+      U = C;
+      C = D;
+      Ctau = Dtau;
+      Css = Dss;
+      Cet3 = Det3;
+      Clat = Dlat;
+      cell = dcell;
+      q++;
+    }
+  }
+}
+
 // ---------------------------------------------------------------------------
 // The chain walkers.  One warp per chain: lane n holds fraction n of each
 // held row's grain record (lanes 0..HC_G), so the per-fraction arithmetic of
@@ -901,9 +1101,10 @@ __device__ __forceinline__ double gather_w(const hc_view& c, hc_dev* d, size_t c
 }
 
 // chains along the columns, one warp per chain
-__global__ void __launch_bounds__(128) k_apply_xchains(const hc_view c, hc_dev* d) {
+__global__ void __launch_bounds__(128) k_apply_xchains_w(const hc_view c, hc_dev* d) {
   if (!(d->it_active && d->rest_active && d->do_erode) || d->erode_retry) return;
   const unsigned nch = d->xchains;
+  if (nch > kWarpChains) return;  // many chains: the thread walker takes them
   const double mult = d->mult, ts = d->s.time_step;
   const double thr = c.p.water_depth_erosion_threshold;
   const size_t W = c.W;
@@ -973,9 +1174,10 @@ __global__ void __launch_bounds__(128) k_apply_xchains(const hc_view c, hc_dev* 
 
 // chains along the rows for the +/-y pass, one warp per chain: columns
 // q-1, q, q+1 held in U, C, D
-__global__ void __launch_bounds__(128) k_apply_ychains(const hc_view c, hc_dev* d) {
+__global__ void __launch_bounds__(128) k_apply_ychains_w(const hc_view c, hc_dev* d) {
   if (!(d->it_active && d->rest_active && d->do_erode) || d->erode_retry) return;
   const unsigned nch = d->ychains;
+  if (nch > kWarpChains) return;
   const double mult = d->mult, ts = d->s.time_step;
   const size_t W = c.W;
   const unsigned warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -1233,18 +1435,17 @@ void launch_erode_pass(hc_ctx* c, int max_passes, cudaGraphConditionalHandle nex
   count_launch(c, 1);
 }
 
-// walkers: grid-stride over the chain lists, several blocks per SM
-constexpr int kWalkBlocks = 152 * 8;
-
 void launch_erode_finish(hc_ctx* c, int gated) {
   ErodeScratch s = scratch_of(c);
   dim3 b(32, 8);
   dim3 g((c->v.jmax - 2 + 31) / 32, (c->v.imax + 7) / 8);
   k_apply_pre<<<g, b, 0, c->cs>>>(c->v, c->dev);
   k_apply_gather<<<g, b, 0, c->cs>>>(c->v, c->dev);
-  k_apply_xchains<<<kWalkBlocks, 128, 0, c->cs>>>(c->v, c->dev);
-  k_apply_ychains<<<kWalkBlocks, 128, 0, c->cs>>>(c->v, c->dev);
-  count_launch(c, 4);
+  k_apply_xchains_t<<<kWalkBlocks, 128, 0, c->cs>>>(c->v, c->dev);
+  k_apply_xchains_w<<<kWalkBlocks, 128, 0, c->cs>>>(c->v, c->dev);
+  k_apply_ychains_t<<<kWalkBlocks, 128, 0, c->cs>>>(c->v, c->dev);
+  k_apply_ychains_w<<<kWalkBlocks, 128, 0, c->cs>>>(c->v, c->dev);
+  count_launch(c, 6);
   k_edge_out<<<1, 1024, 0, c->cs>>>(c->v, c->dev, s.contrib, nullptr);
   count_launch(c, 1);
   k_erode_post<<<1, 1, 0, c->cs>>>(c->v, c->dev, gated);
