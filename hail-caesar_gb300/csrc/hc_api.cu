@@ -365,6 +365,7 @@ static hc_status free_all(hc_ctx* c) {
   if (c->chunk_done) cudaEventDestroy(c->chunk_done);
   if (c->s) cudaStreamDestroy(c->s);
   if (c->s2) cudaStreamDestroy(c->s2);
+  if (c->s3) cudaStreamDestroy(c->s3);
   drop_extra(c);
   delete c;
   return HC_OK;
@@ -604,6 +605,53 @@ extern "C" hc_status hc_download(hc_ctx* c, hc_field f, void* host, size_t nbyte
       return hc_fail(c, HC_ERR_ARG, "field %d cannot be downloaded", (int)f);
   }
   return HC_OK;
+}
+
+// ------------------------------------------------------------------ snapshots
+// A field's copy taken in stream order (a device-to-device copy, so the run
+// can go on at once) and moved to pinned host memory on a side stream.
+struct hc_snapshot {
+  hc_ctx* c;
+  double* dev;
+  cudaEvent_t taken, done;
+};
+
+extern "C" hc_status hc_snapshot_begin(hc_ctx* c, hc_field f, void* host_pinned, size_t nbytes,
+                                       hc_snapshot** out) {
+  if (!c || !host_pinned || !out) return HC_ERR_ARG;
+  *out = nullptr;
+  double* src = plain_field(c, f);
+  if (!src) return hc_fail(c, HC_ERR_ARG, "field %d has no plain layout for a snapshot", (int)f);
+  HC_TRY(check_size(c, f, nbytes));
+  hc_snapshot* sn = new hc_snapshot();
+  sn->c = c;
+  if (cudaMalloc((void**)&sn->dev, nbytes) != cudaSuccess) {
+    cudaGetLastError();
+    delete sn;
+    return hc_fail(c, HC_ERR_NOMEM, "snapshot buffer");
+  }
+  cudaEventCreateWithFlags(&sn->taken, cudaEventDisableTiming);
+  cudaEventCreateWithFlags(&sn->done, cudaEventDisableTiming);
+  HC_CU(cudaMemcpyAsync(sn->dev, src, nbytes, cudaMemcpyDeviceToDevice, c->s), "snapshot");
+  if (!c->s3) HC_CU(cudaStreamCreateWithFlags(&c->s3, cudaStreamNonBlocking), "snapshot stream");
+  HC_CU(cudaEventRecord(sn->taken, c->s), "snapshot");
+  HC_CU(cudaStreamWaitEvent(c->s3, sn->taken, 0), "snapshot");
+  HC_CU(cudaMemcpyAsync(host_pinned, sn->dev, nbytes, cudaMemcpyDeviceToHost, c->s3), "snapshot");
+  HC_CU(cudaEventRecord(sn->done, c->s3), "snapshot");
+  c->d2h_bytes += nbytes;
+  *out = sn;
+  return HC_OK;
+}
+
+extern "C" hc_status hc_snapshot_end(hc_snapshot* sn) {
+  if (!sn) return HC_ERR_ARG;
+  hc_ctx* c = sn->c;
+  const cudaError_t e = cudaEventSynchronize(sn->done);
+  cudaEventDestroy(sn->taken);
+  cudaEventDestroy(sn->done);
+  cudaFree(sn->dev);
+  delete sn;
+  return hc_cuda(c, e, "snapshot");
 }
 
 // ------------------------------------------------------------------ series

@@ -227,7 +227,6 @@ __device__ __forceinline__ bool grid_barrier(DrainSync* g, unsigned nblocks) {
           ok = false;
           break;
         }
-        __nanosleep(20);
       }
     }
     __threadfence();
@@ -244,40 +243,41 @@ __device__ void drain_cell_g(const hc_view& c, const double* __restrict__ el, ui
   const int W = (int)c.W;
   const int i = (int)(cell / W), j = (int)(cell % W);
   const double e = el[cell];
-  double en[9];
-  for (int dx = -1, k = 0; dx <= 1; dx++)
-    for (int dy = -1; dy <= 1; dy++, k++) {
-      const int i2 = i + dx, j2 = j + dy;
-      en[k] = (i2 < 1 || i2 > c.imax || j2 < 1 || j2 > c.jmax) ? e : el[(size_t)i2 * W + j2];
-    }
-  if (c.drain_pos[cell] != 0) {
+  // every neighbour's elevation, sweep position, area and drop sum, loaded
+  // together (one round trip instead of three dependent ones)
+  double en[9], an[9], dn[9];
+  uint32_t pn[9];
+#pragma unroll
+  for (int k = 0; k < 9; k++) {
+    const int i2 = i + k / 3 - 1, j2 = j + k % 3 - 1;
+    const bool in = !(i2 < 1 || i2 > c.imax || j2 < 1 || j2 > c.jmax);
+    const size_t q = (size_t)i2 * W + j2;
+    en[k] = in ? __ldg(&el[q]) : e;
+    pn[k] = in ? __ldg(&c.drain_pos[q]) : 0u;
+    an[k] = in ? __ldcg(&c.area[q]) : 0.0;
+    dn[k] = in ? __ldg(&c.drain_dt[q]) : 0.0;
+  }
+  if (pn[4] != 0) {
     double a = (e == -9999) ? 0.0 : 1.0;
-    uint32_t nb[8], np[8];
-    double ne[8];
+    // higher neighbours the sweep reached, in sweep order: higher elevation
+    // first, equal elevations by sorted position (only in sorted runs)
+    int nb[8];
     int n = 0;
-    for (int dx = -1, kk = 0; dx <= 1; dx++)
-      for (int dy = -1; dy <= 1; dy++, kk++) {
-        if (dx == 0 && dy == 0) continue;
-        const double eq = en[kk];
-        if (!(eq > e)) continue;  // out-of-grid entries equal e
-        const uint32_t q = (uint32_t)((i + dx) * W + (j + dy));
-        const uint32_t pq = c.drain_pos[q];
-        if (pq == 0) continue;
-        int k = n++;
-        while (k > 0 && (ne[k - 1] < eq || (ne[k - 1] == eq && np[k - 1] < pq))) {
-          nb[k] = nb[k - 1];
-          np[k] = np[k - 1];
-          ne[k] = ne[k - 1];
-          k--;
-        }
-        nb[k] = q;
-        np[k] = pq;
-        ne[k] = eq;
+#pragma unroll
+    for (int kk = 0; kk < 9; kk++) {
+      if (kk == 4 || !(en[kk] > e) || pn[kk] == 0) continue;  // out-of-grid entries equal e
+      int k = n++;
+      while (k > 0 && (en[nb[k - 1]] < en[kk] ||
+                       (en[nb[k - 1]] == en[kk] && pn[nb[k - 1]] < pn[kk]))) {
+        nb[k] = nb[k - 1];
+        k--;
       }
+      nb[k] = kk;
+    }
     for (int k = 0; k < n; k++) {
-      const uint32_t q = nb[k];
-      const int iq = (int)(q / W), jq = (int)(q % W);
-      const double eq = ne[k], aq = __ldcg(&c.area[q]), dq = c.drain_dt[q];
+      const int kk = nb[k];
+      const int iq = i + kk / 3 - 1, jq = j + kk % 3 - 1;
+      const double eq = en[kk], aq = an[kk], dq = dn[kk];
       for (int dir = 1; dir <= 8; dir++) {
         const int i3 = clampi(iq + kDrX[dir], 1, c.imax), j3 = clampi(jq + kDrY[dir], 1, c.jmax);
         if (i3 != i || j3 != j) continue;

@@ -172,6 +172,7 @@ struct hc_ctx {
   cudaStream_t cs;        // stream launches go to (a side stream while a
                           // conditional node's body is captured)
   cudaStream_t s2;
+  cudaStream_t s3;         // snapshots to host memory (hc_snapshot_begin)
   hc_iter_handles hcur;   // handles of the iteration being captured
   int device;
   char err[512];

@@ -63,6 +63,8 @@ def load_library(path=LIB_PATH):
         "hc_bench_kernel": (C.c_int, [vp, C.c_char_p, C.c_int32, P(C.c_double), P(C.c_int64)]),
         "hc_get_counters": (C.c_int, [vp, P(C.c_int64), P(C.c_int64), P(C.c_int64)]),
         "hc_get_run_stats": (C.c_int, [vp, P(C.c_int64), P(C.c_double), C.c_int32]),
+        "hc_snapshot_begin": (C.c_int, [vp, C.c_int, vp, C.c_size_t, P(vp)]),
+        "hc_snapshot_end": (C.c_int, [vp]),
         "hc_adj_forward": (C.c_int, [vp, C.c_int64, vp, vp, vp, C.c_int64, P(C.c_int64)]),
         "hc_adj_gradient": (C.c_int, [vp, C.c_int64, C.c_int32, vp, C.c_int64, P(C.c_double),
                                       vp, vp, vp]),
@@ -203,6 +205,19 @@ class Model:
         self._check(self.lib.hc_get_counters(self.h, C.byref(a), C.byref(b), C.byref(c)),
                     "counters")
         return a.value, b.value, c.value
+
+    # ---- snapshots
+    def snapshot_begin(self, name, out):
+        """Starts copying field `name` into `out` (a page-locked numpy array of
+        the field's shape, e.g. from pinned_empty) while the run goes on;
+        returns a handle for snapshot_end."""
+        h = C.c_void_p()
+        self._check(self.lib.hc_snapshot_begin(self.h, FIELD_ID[name], out.ctypes.data,
+                                               out.nbytes, C.byref(h)), "snapshot_begin")
+        return h
+
+    def snapshot_end(self, handle):
+        self._check(self.lib.hc_snapshot_end(handle), "snapshot_end")
 
     # ---- adjoint (hydro-only)
     ADJ_RECORD = 22

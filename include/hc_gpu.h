@@ -244,6 +244,18 @@ hc_status hc_in_channel_landsliding(hc_ctx* ctx);
 hc_status hc_run(hc_ctx* ctx, int64_t n, int32_t flags, hc_step_record* rec,
                  int64_t* done);
 
+/* Raster output while the run goes on (no counterpart in the reference,
+ * which writes between iterations): hc_snapshot_begin copies a field with a
+ * plain layout (elev, water_depth, qx, qy, Vsusptot, Vel, Tau, bedrock,
+ * Manning's n, area, ss, edge) in stream order and moves the copy to
+ * `host_pinned` (page-locked memory of nbytes) on a side stream, so hc_run
+ * may be called again at once; hc_snapshot_end waits for the copy and frees
+ * the snapshot.  The host buffer must stay valid until then. */
+typedef struct hc_snapshot hc_snapshot;
+hc_status hc_snapshot_begin(hc_ctx* ctx, hc_field f, void* host_pinned, size_t nbytes,
+                            hc_snapshot** out);
+hc_status hc_snapshot_end(hc_snapshot* snap);
+
 /* Ensemble (no counterpart in the reference, which runs one catchment per
  * process): runs up to n iterations of each of m independent contexts at
  * once, each on its own stream with its own CUDA graph, adaptive dt and
