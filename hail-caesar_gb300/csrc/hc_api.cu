@@ -269,7 +269,7 @@ extern "C" hc_status hc_create(const hc_params* p, size_t max_bytes, hc_ctx** ou
   A(v.drain_aux, 1)
   if (sed) {
     A(v.sflux, 40 * N2) A(v.grain, 11 * N2) A(v.strata, 90 * N2) A(v.alloc_key, N2)
-    A(v.erodetot, N2) A(v.erodetot3, N2) A(v.pre, 11 * N2) A(v.chains, 2 * N2)
+    A(v.erodetot, N2) A(v.erodetot3, N2) A(v.pre, 11 * N2) A(v.chains, 4 * N2)
     A(v.drain_snap, N2)
   } else {
     A(v.erodetot, N2)

@@ -404,7 +404,7 @@ __global__ void k_alloc_finish(hc_dev* d, const int32_t* total) {
 
 // erodetot3 of every cell of the pass (0 where the cell is not processed)
 __device__ __forceinline__ bool apply_active(const hc_view& c, size_t cell, int x) {
-  return c.mask[cell] && c.h[cell] > c.p.water_depth_erosion_threshold && x < c.imax && x > 1;
+  return c.mask[cell] && dgt(c.h[cell], c.p.water_depth_erosion_threshold) && x < c.imax && x > 1;
 }
 
 // Per-cell terms of the apply pass that depend on the cell's own state and
@@ -423,6 +423,8 @@ __global__ void __launch_bounds__(256) k_apply_pre(const hc_view c, hc_dev* d) {
   if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0 && threadIdx.y == 0) {
     d->xchains = 0;  // the chain lists are rebuilt by k_apply_gather
     d->ychains = 0;
+    d->xresume = 0;
+    d->yresume = 0;
   }
   if (y > c.jmax - 1 || x > c.imax) return;
   const size_t cell = (size_t)x * c.W + y;
@@ -440,9 +442,9 @@ __global__ void __launch_bounds__(256) k_apply_pre(const hc_view c, hc_dev* d) {
         // inputpointsarray is all false in the reference (zero_values clears
         // it after the reach block), so settling applies everywhere
         double coeff = (p.fallVelocity[n] * ts) / c.h[cell];
-        if (coeff > 1) coeff = 1;
+        if (dgt(coeff, 1.0)) coeff = 1;
         double Vpdrop = coeff * vs;
-        if (Vpdrop > 0.001) Vpdrop = 0.001;
+        if (dgt(Vpdrop, 0.001)) Vpdrop = 0.001;
         erodetot += Vpdrop;
         vs -= Vpdrop;
         c.vs[cell] = vs;
@@ -548,13 +550,13 @@ __device__ void slide_GS_rows(const hc_view& c, hc_dev* d, size_t a, ApplyRow& A
     double total = 0;
 #pragma unroll
     for (int n = 1; n <= HC_G - 1; n++)
-      if (A.g[n] > 0) total += A.g[n];
-    if (amount > total) {
+      if (dgt0(A.g[n])) total += A.g[n];
+    if (dgt(amount, total)) {
 #pragma unroll
       for (int n = 1; n <= HC_G - 1; n++) B.g[n] += (amount - total) * dprop[n];
       amount = total;
     }
-    if (total > 0) {
+    if (dgt0(total)) {
       const double rt = 1.0 / total;
 #pragma unroll
       for (int n = 1; n <= HC_G - 1; n++) {
@@ -562,7 +564,7 @@ __device__ void slide_GS_rows(const hc_view& c, hc_dev* d, size_t a, ApplyRow& A
         const double t = amount * div_const(ga, total, rt);
         B.g[n] += t;
         double na = ga - t;
-        if (na < 0) na = 0;
+        if (dlt0(na)) na = 0;
         A.g[n] = na;
       }
     }
@@ -595,14 +597,14 @@ __device__ __forceinline__ bool lateral_amount(const hc_params& p, double mult, 
   const double DX = p.DX;
   const double e_nb = N.elev;
   amt = 0;
-  if (N.h < p.water_depth_erosion_threshold)
+  if (dlt(N.h, p.water_depth_erosion_threshold))
     amt = mult * p.lateral_constant * tau0 * N.edge * ts / DX;
   else
     amt = p.chann_lateral_erosion * et3 * (e_nb - e0) / DX * 0.1;
-  if (!(amt > 0)) return false;
+  if (!dgt0(amt)) return false;
   // amt *= 1 - veg * (1 - veg_lat_restriction): veg is zero (no vegetation)
-  if ((e_nb - amt) < N.bed || boundary) amt = 0;
-  if (amt > p.ERODEFACTOR * 0.1) amt = p.ERODEFACTOR * 0.1;
+  if (dlt(e_nb - amt, N.bed) || boundary) amt = 0;
+  if (dgt(amt, p.ERODEFACTOR * 0.1)) amt = p.ERODEFACTOR * 0.1;
   return true;
 }
 
@@ -613,7 +615,7 @@ __device__ __forceinline__ void lateral_step(const hc_view& c, hc_dev* d, double
                                              double& elev_update) {
   const double en = N.elev;
   double amt;
-  if (en > e0 && lateral_amount(c.p, mult, ts, tau0, et3, N, e0, boundary, amt)) {
+  if (dgt(en, e0) && lateral_amount(c.p, mult, ts, tau0, et3, N, e0, boundary, amt)) {
     elev_update += amt;
     N.elev = en - amt;
     N.dirty = true;
@@ -640,7 +642,7 @@ __device__ __forceinline__ double gather_row(const hc_view& c, hc_dev* d, size_t
   const double e0 = r.elev + erodetot;
   r.elev = e0;
   r.dirty = true;
-  if (erodetot < 0) sort_active_row(c, d, cell, r);
+  if (dlt0(erodetot)) sort_active_row(c, d, cell, r);
   return e0;
 }
 
@@ -664,9 +666,9 @@ __global__ void __launch_bounds__(256) k_apply_gather(const hc_view c, hc_dev* d
   const size_t W = c.W;
   const size_t cell = (size_t)x * W + y;
   const double* et3 = c.erodetot3;
-  const bool lat0 = et3[cell] > 0;
-  const bool latm = x - 1 >= 1 && et3[cell - W] > 0;
-  const bool latp = x + 1 <= c.imax && et3[cell + W] > 0;
+  const bool lat0 = dgt0(et3[cell]);
+  const bool latm = x - 1 >= 1 && dgt0(et3[cell - W]);
+  const bool latp = x + 1 <= c.imax && dgt0(et3[cell + W]);
   const bool link_prev = latm || lat0, link_next = lat0 || latp;
   if (!(link_prev && x > 1)) {
     if (link_next) {
@@ -683,7 +685,7 @@ __global__ void __launch_bounds__(256) k_apply_gather(const hc_view c, hc_dev* d
   }
   if (x >= 2 && x <= c.imax - 1) {
     auto lat = [&](int q) {
-      return q >= 2 && q <= c.jmax - 1 && c.mask[cell - y + q] && et3[cell - y + q] > 0;
+      return q >= 2 && q <= c.jmax - 1 && c.mask[cell - y + q] && dgt0(et3[cell - y + q]);
     };
     const bool l0 = lat(y);
     if (!((lat(y - 1) || l0) && y > 2) && (l0 || lat(y + 1))) {
@@ -695,8 +697,14 @@ __global__ void __launch_bounds__(256) k_apply_gather(const hc_view c, hc_dev* d
 
 // Chains are walked by one thread each when there are many (all of them in
 // flight at once), by one warp each when there are few (each one faster).
+// With many, a thread walks the first kHandOff rows of its chain and hands a
+// longer chain to the warp walkers: the rows it holds go back to memory and
+// the rest of the chain is listed as a resume point (bit 31: the row before
+// it is part of the chain).
 constexpr unsigned kWalkBlocks = 152 * 8;            // blocks of 128 threads
 constexpr unsigned kWarpChains = kWalkBlocks * 4;    // warps in flight
+constexpr int kHandOff = 32;
+constexpr uint32_t kResumeU = 0x80000000u;
 
 // A row's inputs to the walkers, staged in shared memory by asynchronous
 // copies (cp.async): a walker asks for row r+2 before it works on row r, so
@@ -773,7 +781,7 @@ __global__ void __launch_bounds__(128) k_apply_xchains_t(const hc_view c, hc_dev
   const double mult = d->mult, ts = d->s.time_step;
   const double thr = c.p.water_depth_erosion_threshold;
   const size_t W = c.W;
-  auto active = [&](bool m, double h, int x) { return m && h > thr && x < c.imax && x > 1; };
+  auto active = [&](bool m, double h, int x) { return m && dgt(h, thr) && x < c.imax && x > 1; };
   for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < nch; k += gridDim.x * blockDim.x) {
     size_t cell = c.chains[k];
     const int y = (int)(cell % W);
@@ -788,6 +796,7 @@ __global__ void __launch_bounds__(128) k_apply_xchains_t(const hc_view c, hc_dev
     stage_take(st, cell, C, Cpre, Ctau, Css, Cet3, Cm);
     bool Cact = active(Cm, C.h, r);
     if (r + 1 <= c.imax) stage_issue(c, st, cell + W, EX(c, r + 1, y), true);
+    int steps = 0;
     for (;;) {
       const bool hasD = r + 1 <= c.imax;
       const size_t dcell = cell + W;
@@ -801,7 +810,7 @@ __global__ void __launch_bounds__(128) k_apply_xchains_t(const hc_view c, hc_dev
       }
       if (Cact) {
         const double e0 = gather_row(c, d, cell, C, Cpre, Css);
-        if (Cet3 > 0) {
+        if (dgt0(Cet3)) {
           double elev_update = 0;
           if (r > 2 && hasU)
             lateral_step(c, d, mult, ts, Ctau, Cet3, cell, C, e0, ucell, U, r - 1 == 1,
@@ -813,10 +822,18 @@ __global__ void __launch_bounds__(128) k_apply_xchains_t(const hc_view c, hc_dev
         }
       }
       if (hasU) row_store(c, ucell, U);  // row r-1 is final
-      if (!(Cet3 > 0 || Det3 > 0) || !hasD) {
+      if (!(dgt0(Cet3) || dgt0(Det3)) || !hasD) {
         row_store(c, cell, C);
         if (hasD) row_store(c, dcell, D);
         cp_async_wait_all();  // the slot is free for the next chain
+        break;
+      }
+      if (++steps >= kHandOff) {  // a long chain: the warp walkers go on from row r+1
+        row_store(c, cell, C);
+        row_store(c, dcell, D);
+        cp_async_wait_all();
+        const unsigned m = atomicAdd(&d->xresume, 1u);
+        c.chains[2 * c.N2 + m] = (uint32_t)dcell | kResumeU;
         break;
       }
       U = C;
@@ -849,7 +866,7 @@ __global__ void __launch_bounds__(128) k_apply_ychains_t(const hc_view c, hc_dev
     size_t cell = c.chains[c.N2 + k];
     const int x = (int)(cell / W);
     int q = (int)(cell % W);
-    auto lat = [&](int qq, bool m, double et3) { return qq >= 2 && qq <= c.jmax - 1 && m && et3 > 0; };
+    auto lat = [&](int qq, bool m, double et3) { return qq >= 2 && qq <= c.jmax - 1 && m && dgt0(et3); };
     ApplyRow U, C, D;
     double Ctau, Css, Cet3, Dtau, Dss, Det3, t0, t1, t2;
     bool Cm, Dm, m0;
@@ -859,6 +876,7 @@ __global__ void __launch_bounds__(128) k_apply_ychains_t(const hc_view c, hc_dev
     stage_take(st, cell, C, nullptr, Ctau, Css, Cet3, Cm);
     bool Clat = lat(q, Cm, Cet3);
     stage_issue(c, st, cell + 1, EX(c, x, q + 1), false);  // q + 1 <= jmax
+    int steps = 0;
     for (;;) {
       const size_t dcell = cell + 1;
       stage_take(st, dcell, D, nullptr, Dtau, Dss, Det3, Dm);
@@ -879,6 +897,14 @@ __global__ void __launch_bounds__(128) k_apply_ychains_t(const hc_view c, hc_dev
         row_store(c, cell, C);
         row_store(c, dcell, D);
         cp_async_wait_all();
+        break;
+      }
+      if (++steps >= kHandOff) {  // a long chain: the warp walkers go on from column q+1
+        row_store(c, cell, C);
+        row_store(c, dcell, D);
+        cp_async_wait_all();
+        const unsigned m = atomicAdd(&d->yresume, 1u);
+        c.chains[3 * c.N2 + m] = (uint32_t)dcell;
         break;
       }
       U = C;
@@ -1015,20 +1041,20 @@ __device__ void slide_GS_w(const hc_view& c, hc_dev* d, size_t a, WRow& A, doubl
     double total = 0;  // positive fractions 1..9, in order
     for (int n = 1; n <= HC_G - 1; n++) {
       const double v = __shfl_sync(kFull, A.g, n);
-      if (v > 0) total += v;
+      if (dgt0(v)) total += v;
     }
-    if (amount > total) {
+    if (dgt(amount, total)) {
       if (fr) B.g += (amount - total) * dp;
       amount = total;
     }
-    if (total > 0) {
+    if (dgt0(total)) {
       const double rt = 1.0 / total;
       if (fr) {
         const double ga = A.g;
         const double t = amount * div_const(ga, total, rt);
         B.g += t;
         double na = ga - t;
-        if (na < 0) na = 0;
+        if (dlt0(na)) na = 0;
         A.g = na;
       }
     }
@@ -1055,13 +1081,13 @@ __device__ __forceinline__ bool lateral_amount_w(const hc_params& p, double mult
   const double DX = p.DX;
   const double e_nb = N.elev;
   amt = 0;
-  if (N.h < p.water_depth_erosion_threshold)
+  if (dlt(N.h, p.water_depth_erosion_threshold))
     amt = mult * p.lateral_constant * tau0 * N.edge * ts / DX;
   else
     amt = p.chann_lateral_erosion * et3 * (e_nb - e0) / DX * 0.1;
-  if (!(amt > 0)) return false;
-  if ((e_nb - amt) < N.bed || boundary) amt = 0;
-  if (amt > p.ERODEFACTOR * 0.1) amt = p.ERODEFACTOR * 0.1;
+  if (!dgt0(amt)) return false;
+  if (dlt(e_nb - amt, N.bed) || boundary) amt = 0;
+  if (dgt(amt, p.ERODEFACTOR * 0.1)) amt = p.ERODEFACTOR * 0.1;
   return true;
 }
 
@@ -1071,7 +1097,7 @@ __device__ __forceinline__ void lateral_step_w(const hc_view& c, hc_dev* d, doub
                                                bool boundary, double& elev_update) {
   const double en = N.elev;
   double amt;
-  if (en > e0 && lateral_amount_w(c.p, mult, ts, tau0, et3, N, e0, boundary, amt)) {
+  if (dgt(en, e0) && lateral_amount_w(c.p, mult, ts, tau0, et3, N, e0, boundary, amt)) {
     elev_update += amt;
     N.elev = en - amt;
     N.dirty = true;
@@ -1096,15 +1122,18 @@ __device__ __forceinline__ double gather_w(const hc_view& c, hc_dev* d, size_t c
   const double e0 = r.elev + erodetot;
   r.elev = e0;
   r.dirty = true;
-  if (erodetot < 0) sort_active_w(c, d, cell, r);
+  if (dlt0(erodetot)) sort_active_w(c, d, cell, r);
   return e0;
 }
 
 // chains along the columns, one warp per chain
 __global__ void __launch_bounds__(128) k_apply_xchains_w(const hc_view c, hc_dev* d) {
   if (!(d->it_active && d->rest_active && d->do_erode) || d->erode_retry) return;
-  const unsigned nch = d->xchains;
-  if (nch > kWarpChains) return;  // many chains: the thread walker takes them
+  // few chains: all of them from their starts; many: the long ones the
+  // thread walker handed over
+  const bool few = d->xchains <= kWarpChains;
+  const unsigned nch = few ? d->xchains : d->xresume;
+  const uint32_t* list = c.chains + (few ? 0 : 2 * c.N2);
   const double mult = d->mult, ts = d->s.time_step;
   const double thr = c.p.water_depth_erosion_threshold;
   const size_t W = c.W;
@@ -1114,13 +1143,15 @@ __global__ void __launch_bounds__(128) k_apply_xchains_w(const hc_view c, hc_dev
     return x.mask && h > thr && r < c.imax && r > 1;
   };
   for (unsigned k = warp; k < nch; k += nwarps) {
-    size_t cell = c.chains[k];
+    const uint32_t rec = list[k];
+    size_t cell = rec & ~kResumeU;
     const int y = (int)(cell % W);
     int r = (int)(cell / W);
     WRow U, C, D, E;
     WExtra Cx, Dx, Ex;
-    bool hasU = false;
-    size_t ucell = 0;
+    bool hasU = (rec & kResumeU) != 0;
+    size_t ucell = cell - W;
+    if (hasU) wrow_load(c, ucell, EX(c, r - 1, y), U);
     wrow_load(c, cell, EX(c, r, y), C);
     wextra_load(c, cell, true, Cx);
     if (r + 1 <= c.imax) {
@@ -1176,14 +1207,15 @@ __global__ void __launch_bounds__(128) k_apply_xchains_w(const hc_view c, hc_dev
 // q-1, q, q+1 held in U, C, D
 __global__ void __launch_bounds__(128) k_apply_ychains_w(const hc_view c, hc_dev* d) {
   if (!(d->it_active && d->rest_active && d->do_erode) || d->erode_retry) return;
-  const unsigned nch = d->ychains;
-  if (nch > kWarpChains) return;
+  const bool few = d->ychains <= kWarpChains;
+  const unsigned nch = few ? d->ychains : d->yresume;
+  const uint32_t* list = c.chains + (few ? 1 : 3) * c.N2;
   const double mult = d->mult, ts = d->s.time_step;
   const size_t W = c.W;
   const unsigned warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const unsigned nwarps = (gridDim.x * blockDim.x) >> 5;
   for (unsigned k = warp; k < nch; k += nwarps) {
-    size_t cell = c.chains[c.N2 + k];
+    size_t cell = list[k];
     const int x = (int)(cell / W);
     int q = (int)(cell % W);
     auto lat = [&](int qq, const WExtra& e) {

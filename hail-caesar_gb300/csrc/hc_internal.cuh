@@ -85,6 +85,7 @@ struct hc_dev {
   int64_t adj_slot_t0, adj_slot_n;  // iterations whose state k_adj_save keeps
   unsigned int xchains;   // chain starts of the +/-x apply pass (hc_view::chains)
   unsigned int ychains;   // chain starts of the +/-y apply pass
+  unsigned int xresume, yresume;  // long chains handed from the thread to the warp walkers
 };
 
 // Working state of a drainage recomputation (hc_drain.cu): the radix
@@ -135,7 +136,8 @@ struct hc_view {
   // scratch
   double *erodetot, *erodetot3;  // N2 each
   double *pre;                   // 11 * N2: per-cell apply-pass terms (see hc_erode.cu)
-  uint32_t *chains;              // 2 * N2: apply-pass chain starts (x pass, then y pass)
+  uint32_t *chains;              // 4 * N2: apply-pass chain starts (x pass, y pass), then
+                                 // the resume points of long chains (x, y)
   // drainage area (hc_drain.cu): sweep position, sum of drops, higher
   // neighbours pending, two frontiers, and the elevation snapshot
   uint32_t *drain_pos, *drain_f0, *drain_f1;
