@@ -19,7 +19,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-std=c++17", "--fmad=false", "-lineinfo", "-Xcompiler", "-fPIC",
            "-Xcompiler", "-ffp-contract=off", "-Xptxas", "-warn-spills"]
 SOURCES = ["hc_api.cu", "hc_flow.cu", "hc_erode.cu", "hc_slide.cu", "hc_lateral.cu",
-           "hc_host.cpp", "hc_drain.cu", "hc_adjoint.cu", "hc_noalloc.cu"]
+           "hc_host.cpp", "hc_drain.cu", "hc_adjoint.cu", "hc_noalloc.cu",
+           "hc_sort.cu"]
 
 
 def nvcc():

@@ -229,6 +229,8 @@ extern "C" hc_status hc_create(const hc_params* p, size_t max_bytes, hc_ctx** ou
   v.rDX = 1.0 / p->DX;
   v.DXf = (float)p->DX;
   v.flf = (float)p->froude_limit;
+  v.act_hi = (float)(p->active * 1.5);
+  v.act_lo = (float)(p->active / 4);
   {
     long long b;
     std::memcpy(&b, &p->hflow_threshold, 8);
@@ -359,6 +361,7 @@ static hc_status free_all(hc_ctx* c) {
   if (c->hdev) cudaFreeHost(c->hdev);
   if (c->h_elev) cudaFreeHost(c->h_elev);
   if (c->drainage_cache) host_drainage_cache_free(c->drainage_cache);
+  sort_work_free(c->sort_work);
   free(extra(c).h_rain);
   if (c->graph) cudaGraphExecDestroy(c->graph);
   if (c->graph1) cudaGraphExecDestroy(c->graph1);
@@ -752,16 +755,24 @@ struct StatTimer {
 };
 }  // namespace
 
-// the drainage sweep order from the host sort, when the device needs it
-static const uint32_t* drainage_sort(hc_ctx* c, const double* del) {
+// the drainage sweep order, sorted on the device; the host's exact sort
+// when the device declines (depth budget exhausted, NaN elevations)
+static hc_status drainage_sort(hc_ctx* c, const double* del, uint32_t* order_dev) {
+  StatTimer st(c, HC_STAT_DRAINAGE_SORT);
+  bool fallback = false;
+  HC_CU(device_drainage_order(c, del, order_dev, &fallback), "drainage sort");
+  if (!fallback) return HC_OK;
+  StatTimer hs(c, HC_STAT_DRAINAGE_HOST_SORT);
   const size_t N2 = c->v.N2;
   std::vector<double> elev(N2);
-  if (cudaMemcpy(elev.data(), del, N2 * 8, cudaMemcpyDeviceToHost) != cudaSuccess) return nullptr;
+  HC_CU(cudaMemcpy(elev.data(), del, N2 * 8, cudaMemcpyDeviceToHost), "drainage sort");
   c->d2h_bytes += N2 * 8;
   if (!c->drainage_cache) c->drainage_cache = host_drainage_cache_new();
-  StatTimer st(c, HC_STAT_DRAINAGE_SORT);
   bool reused = false;
-  return host_drainage_order(&c->v.p, elev.data(), c->drainage_cache, &reused);
+  const uint32_t* order = host_drainage_order(&c->v.p, elev.data(), c->drainage_cache, &reused);
+  HC_CU(cudaMemcpy(order_dev, order, N2 * 4, cudaMemcpyHostToDevice), "drainage sort");
+  c->h2d_bytes += N2 * 4;
+  return HC_OK;
 }
 
 // zero_and_calc_drainage_area + get_catchment_input_points (hc_drain.cu).

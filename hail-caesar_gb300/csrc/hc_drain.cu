@@ -4,7 +4,7 @@
 // get_catchment_input_points :3741-3767.
 //
 // The reference sweeps all cells once from the highest to the lowest (an
-// order fixed by a sort, host_drainage_order) and pushes each cell's area to
+// order fixed by a sort, hc_sort.cu) and pushes each cell's area to
 // its lower neighbours.  A cell's final area is therefore its initial value
 // plus the pushes of its higher neighbours, added in the order those were
 // swept.  Here the same sums are pulled instead: a cell is ready once all
@@ -22,7 +22,8 @@
 // or the last reached position.  The device checks for those (a radix
 // selection finds the last reached position); when none occurs, "reached" is
 // a threshold on the elevation, the pushes are ordered by elevation, and no
-// sort runs at all.  Otherwise the host sorts (host_drainage_order).
+// sort runs at all.  Otherwise the device sorts (hc_sort.cu; the host's
+// exact sort where that declines).
 //
 // The elevations are those at the start of the iteration that moved the
 // threshold (k_drain_snapshot copies them before the iteration's erosion).
@@ -448,7 +449,7 @@ void launch_drain_snapshot(hc_ctx* c) {
 // among equal elevations can show (see the top of the file).  Returns HC_OK,
 // or HC_ERR_CUDA; *sorted tells which way it went.
 hc_status run_drainage_device(hc_ctx* c, const double* el, bool area_valid,
-                              const uint32_t* (*sort_order)(hc_ctx*, const double*),
+                              hc_status (*sort_order)(hc_ctx*, const double*, uint32_t*),
                               bool* sorted) {
   hc_view& v = c->v;
   const size_t N2 = v.N2;
@@ -482,12 +483,8 @@ hc_status run_drainage_device(hc_ctx* c, const double* el, bool area_valid,
     const bool bottom_ok =
         a.min_u > kZeroKey || (a.min_u < kZeroKey && (a.min_count == 1 || !a.min_matters));
     if (a.contrib_tie || !top_ok || !bottom_ok) {
-      const uint32_t* order = sort_order(c, el);
-      if (!order) return HC_ERR_CUDA;
-      c->h2d_bytes += N2 * 4;
-      if (cudaMemcpyAsync(v.drain_f1, order, N2 * 4, cudaMemcpyHostToDevice, s) != cudaSuccess ||
-          cudaMemsetAsync(v.drain_pos, 0, N2 * 4, s) != cudaSuccess)
-        return HC_ERR_CUDA;
+      if (sort_order(c, el, v.drain_f1) != HC_OK) return HC_ERR_CUDA;
+      if (cudaMemsetAsync(v.drain_pos, 0, N2 * 4, s) != cudaSuccess) return HC_ERR_CUDA;
       k_drain_pos<<<152 * 4, 256, 0, s>>>(v, v.drain_f1);
       c->launches += 1;
       *sorted = true;

@@ -509,7 +509,7 @@ __device__ void sort_active_row(const hc_view& c, hc_dev* d, size_t cell, ApplyR
     af += fabsf(f);
   }
   const float tol = 1e-5f * af + 1e-30f;
-  const float hi = (float)(active * 1.5), lo = (float)(active / 4);
+  const float hi = c.act_hi, lo = c.act_lo;
   const int dep = (sf > hi + tol) ? 1 : ((sf < hi - tol) ? -1 : 0);
   const int ero = (sf < lo - tol) ? 1 : ((sf > lo + tol) ? -1 : 0);
   if (dep == -1 && ero == -1) return;
@@ -591,16 +591,17 @@ __device__ void slide_GS_rows(const hc_view& c, hc_dev* d, size_t a, ApplyRow& A
 // false when the raw amount is not positive; otherwise the (possibly zeroed
 // or capped) amount, which the caller applies and hands to slide_GS even
 // when it is zero, as the reference does.
-__device__ __forceinline__ bool lateral_amount(const hc_params& p, double mult, double ts,
-                                               double tau0, double et3, const ApplyRow& N,
-                                               double e0, bool boundary, double& amt) {
+__device__ __forceinline__ bool lateral_amount(const hc_params& p, double rDX, double mult,
+                                               double ts, double tau0, double et3,
+                                               const ApplyRow& N, double e0, bool boundary,
+                                               double& amt) {
   const double DX = p.DX;
   const double e_nb = N.elev;
   amt = 0;
   if (dlt(N.h, p.water_depth_erosion_threshold))
-    amt = mult * p.lateral_constant * tau0 * N.edge * ts / DX;
+    amt = div_const(mult * p.lateral_constant * tau0 * N.edge * ts, DX, rDX);
   else
-    amt = p.chann_lateral_erosion * et3 * (e_nb - e0) / DX * 0.1;
+    amt = div_const(p.chann_lateral_erosion * et3 * (e_nb - e0), DX, rDX) * 0.1;
   if (!dgt0(amt)) return false;
   // amt *= 1 - veg * (1 - veg_lat_restriction): veg is zero (no vegetation)
   if (dlt(e_nb - amt, N.bed) || boundary) amt = 0;
@@ -615,7 +616,7 @@ __device__ __forceinline__ void lateral_step(const hc_view& c, hc_dev* d, double
                                              double& elev_update) {
   const double en = N.elev;
   double amt;
-  if (dgt(en, e0) && lateral_amount(c.p, mult, ts, tau0, et3, N, e0, boundary, amt)) {
+  if (dgt(en, e0) && lateral_amount(c.p, c.rDX, mult, ts, tau0, et3, N, e0, boundary, amt)) {
     elev_update += amt;
     N.elev = en - amt;
     N.dirty = true;
@@ -995,7 +996,7 @@ __device__ void sort_active_w(const hc_view& c, hc_dev* d, size_t cell, WRow& r)
     af += __shfl_xor_sync(kFull, af, o);
   }
   const float tol = 1e-5f * af + 1e-30f;
-  const float hi = (float)(active * 1.5), lo = (float)(active / 4);
+  const float hi = c.act_hi, lo = c.act_lo;
   const int dep = (sf > hi + tol) ? 1 : ((sf < hi - tol) ? -1 : 0);
   const int ero = (sf < lo - tol) ? 1 : ((sf > lo + tol) ? -1 : 0);
   if (dep == -1 && ero == -1) return;
@@ -1075,16 +1076,17 @@ __device__ void slide_GS_w(const hc_view& c, hc_dev* d, size_t a, WRow& A, doubl
   }
 }
 
-__device__ __forceinline__ bool lateral_amount_w(const hc_params& p, double mult, double ts,
-                                                 double tau0, double et3, const WRow& N,
-                                                 double e0, bool boundary, double& amt) {
+__device__ __forceinline__ bool lateral_amount_w(const hc_params& p, double rDX, double mult,
+                                                 double ts, double tau0, double et3,
+                                                 const WRow& N, double e0, bool boundary,
+                                                 double& amt) {
   const double DX = p.DX;
   const double e_nb = N.elev;
   amt = 0;
   if (dlt(N.h, p.water_depth_erosion_threshold))
-    amt = mult * p.lateral_constant * tau0 * N.edge * ts / DX;
+    amt = div_const(mult * p.lateral_constant * tau0 * N.edge * ts, DX, rDX);
   else
-    amt = p.chann_lateral_erosion * et3 * (e_nb - e0) / DX * 0.1;
+    amt = div_const(p.chann_lateral_erosion * et3 * (e_nb - e0), DX, rDX) * 0.1;
   if (!dgt0(amt)) return false;
   if (dlt(e_nb - amt, N.bed) || boundary) amt = 0;
   if (dgt(amt, p.ERODEFACTOR * 0.1)) amt = p.ERODEFACTOR * 0.1;
@@ -1097,7 +1099,7 @@ __device__ __forceinline__ void lateral_step_w(const hc_view& c, hc_dev* d, doub
                                                bool boundary, double& elev_update) {
   const double en = N.elev;
   double amt;
-  if (dgt(en, e0) && lateral_amount_w(c.p, mult, ts, tau0, et3, N, e0, boundary, amt)) {
+  if (dgt(en, e0) && lateral_amount_w(c.p, c.rDX, mult, ts, tau0, et3, N, e0, boundary, amt)) {
     elev_update += amt;
     N.elev = en - amt;
     N.dirty = true;

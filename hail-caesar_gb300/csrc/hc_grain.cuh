@@ -46,7 +46,7 @@ HC_DEV void sort_active_dev(const hc_view& c, hc_dev* d, size_t cell, bool may_a
     af += fabsf(f);
   }
   const float tol = 1e-5f * af + 1e-30f;
-  const float hi = (float)(active * 1.5), lo = (float)(active / 4);
+  const float hi = c.act_hi, lo = c.act_lo;
   int dep = (sf > hi + tol) ? 1 : ((sf < hi - tol) ? -1 : 0);
   int ero = (sf < lo - tol) ? 1 : ((sf > lo + tol) ? -1 : 0);
   if (dep == -1 && ero == -1) return;

@@ -19,6 +19,8 @@
 #include <stdint.h>
 #include <stddef.h>
 
+#include <utility>
+
 #include "../../include/hc_gpu.h"
 
 #define HC_G 10               // G_MAX
@@ -103,6 +105,7 @@ struct hc_view {
   hc_params p;
   double rDX;             // RN(1/DX), for div_const
   float DXf, flf;         // DX and froude_limit as floats (estimates only)
+  float act_hi, act_lo;   // (float)(active*1.5), (float)(active/4): sort_active's estimates
   long long thr_key;      // dkey(hflow_threshold)
   int imax, jmax;
   size_t W, N2, E2;       // pitch, padded cells, edge-array cells
@@ -187,6 +190,7 @@ struct hc_ctx {
   // the reference keeps its vector)
   int32_t *h_cin_x, *h_cin_y;
   void* drainage_cache;    // sweep order of the drainage area, reused while elev is unchanged
+  struct hc_sort_work* sort_work;  // device sort of the elevations (hc_sort.cu)
   bool area_valid;         // device area matches the cached sweep order
   // called after every recomputation of the input points (adjoint replays)
   void (*points_hook)(hc_ctx*, void*);
@@ -357,9 +361,19 @@ size_t slide_scratch_bytes(size_t N2);
 // the elevations are unchanged (*reused)
 const uint32_t* host_drainage_order(const hc_params* p, const double* elev, void* cache,
                                     bool* reused);
+// sort_order(c, el, order): the sweep order for the elevations el (device)
+// into order (device, N2 entries)
 hc_status run_drainage_device(hc_ctx* c, const double* el, bool area_valid,
-                              const uint32_t* (*sort_order)(hc_ctx*, const double*),
+                              hc_status (*sort_order)(hc_ctx*, const double*, uint32_t*),
                               bool* sorted);
+// device sort (hc_sort.cu): std::sort's permutation of the drainage pairs
+// (or of n values); *fallback when the host's exact sort must run instead
+struct hc_sort_work* sort_work_new();
+void sort_work_free(struct hc_sort_work* w);
+cudaError_t device_drainage_order(hc_ctx* c, const double* el, uint32_t* order, bool* fallback);
+cudaError_t device_sort_values(struct hc_sort_work* w, const double* v, size_t n, uint32_t* perm,
+                               cudaStream_t s, bool* fallback, int64_t* launches);
+void host_sort_exact(std::pair<double, double>* a, size_t n, int threads);
 void launch_drain_snapshot(hc_ctx* c);
 void launch_adj_save(hc_ctx* c);         // adjoint replay: state before the iteration
 hc_status ctx_pull(hc_ctx* c);   // control block device -> host mirror

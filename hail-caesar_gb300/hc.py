@@ -69,6 +69,7 @@ def load_library(path=LIB_PATH):
         "hc_adj_gradient": (C.c_int, [vp, C.c_int64, C.c_int32, vp, C.c_int64, P(C.c_double),
                                       vp, vp, vp]),
         "hc_profile_iteration": (C.c_int, [vp, C.c_int32, P(C.c_double)]),
+        "hc_drainage_sort": (C.c_int, [vp, C.c_uint64, vp, P(C.c_int32)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -76,6 +77,20 @@ def load_library(path=LIB_PATH):
         f.argtypes = args
     _lib = lib
     return lib
+
+
+def drainage_sort(values):
+    """(perm, on_device): the permutation std::sort gives (index, value)
+    pairs compared by value, as drainage_area_D8 sorts its elevations;
+    on_device False when the host's exact sort ran instead."""
+    lib = load_library()
+    v = np.ascontiguousarray(values, dtype=np.float64)
+    perm = np.empty(v.size, dtype=np.uint32)
+    dev = C.c_int32(1)
+    st = lib.hc_drainage_sort(v.ctypes.data, v.size, perm.ctypes.data, C.byref(dev))
+    if st != 0:
+        raise HCError("drainage_sort failed: %s" % STATUS.get(st, st))
+    return perm, bool(dev.value)
 
 
 class Model:
@@ -254,7 +269,8 @@ class Model:
         return loss.value, gn, gr, list(ms)
 
     RUN_STATS = ["chunks", "erode_retry", "lateral", "creep", "global_slide", "drainage",
-                 "drainage_sort", "drainage_sweep", "drainage_levels", "idle_iters"]
+                 "drainage_sort", "drainage_sweep", "drainage_levels", "idle_iters",
+                 "drainage_host_sort"]
 
     def run_stats(self):
         """{kind: (count, host ms)} of hc_run's host-side work so far."""

@@ -222,6 +222,14 @@ hc_status hc_depth_update_noalloc(int32_t imax, int32_t jmax, double DX, double 
                                   const double* qx, const double* qy, const double* qxs,
                                   const double* qys, double* water_depth, double* Vsusptot,
                                   double* maxdepth, void* stream, char* err, size_t err_len);
+/* The order drainage_area_D8 sweeps the cells in (:2091-2180): the
+ * permutation std::sort (GCC's introsort) gives (key, value) pairs compared
+ * by value only, equal values in std::sort's own order.  perm[k] receives the
+ * index of the value at sorted position k; hc_run calls the same sort with
+ * the reference's padded pair vector.  Runs on the current device;
+ * *on_device (optional) is 0 when the host's exact sort ran instead (an
+ * input that exhausts the introsort's depth budget, or a NaN). */
+hc_status hc_drainage_sort(const double* values, uint64_t n, uint32_t* perm, int32_t* on_device);
 /* scan_area :3821-3849 */
 hc_status hc_scan_area(hc_ctx* ctx);
 /* water_flux_out :3005-3047 */
@@ -297,10 +305,11 @@ enum {
   HC_STAT_CREEP,           /* slope creep */
   HC_STAT_GLOBAL_SLIDE,    /* global landsliding */
   HC_STAT_DRAINAGE,        /* drainage area + input points (baseflow change) */
-  HC_STAT_DRAINAGE_SORT,   /* of those, host sorts (equal elevations that matter) */
+  HC_STAT_DRAINAGE_SORT,   /* of those, sorts of the elevations (equal elevations that matter) */
   HC_STAT_DRAINAGE_SWEEP,  /* device accumulation (ms: device time) */
   HC_STAT_DRAINAGE_LEVELS, /* frontiers the accumulations went through (count) */
   HC_STAT_IDLE_ITERS,      /* captured iterations skipped after a pause */
+  HC_STAT_DRAINAGE_HOST_SORT, /* of the sorts, those the host finished (see hc_drainage_sort) */
   HC_STAT_COUNT
 };
 hc_status hc_get_run_stats(hc_ctx* ctx, int64_t* counts, double* host_ms, int32_t n);

@@ -204,6 +204,19 @@ extern "C" double hco_get_flow_timestep(hco_model* m) {  // :1913-1923
 // ---------------------------------------------------------------------------
 // drainage area and catchment input points :2055-2271, :3741-3767
 // ---------------------------------------------------------------------------
+// The permutation the reference's sort of (key, elevation) pairs applies
+// (:2143-2180, std::sort with LSDUtils::sort_pair_second): perm[k] = the
+// index of the value at sorted position k.  The same library call.
+extern "C" void hco_sort_perm(const double* v, int64_t n, uint32_t* perm) {
+  std::vector<std::pair<double, double>> pr((size_t)n);
+  for (int64_t k = 0; k < n; k++) pr[(size_t)k] = std::make_pair((double)k, v[k]);
+  std::sort(pr.begin(), pr.end(), [](const std::pair<double, double>& a,
+                                     const std::pair<double, double>& b) {
+    return a.second < b.second;
+  });
+  for (int64_t k = 0; k < n; k++) perm[k] = (uint32_t)pr[(size_t)k].first;
+}
+
 static void drainage_area_D8(hco_model* m) {  // :2091-2271
   const unsigned imax = m->imax, jmax = m->jmax;
   const size_t N2 = m->N2;

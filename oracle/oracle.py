@@ -83,6 +83,7 @@ def _lib(omp=False):
                   "hco_set_maximum_timestep"):
             getattr(lib, f).argtypes = [C.c_void_p]
         lib.hco_creep.argtypes = [C.c_void_p, C.c_double]
+        lib.hco_sort_perm.argtypes = [C.c_void_p, C.c_int64, C.c_void_p]
         lib.hco_get_flow_timestep.restype = C.c_double
         lib.hco_get_flow_timestep.argtypes = [C.c_void_p]
         _LIBS[name] = lib
