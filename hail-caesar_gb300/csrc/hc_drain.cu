@@ -237,10 +237,11 @@ __device__ __forceinline__ bool grid_barrier(DrainSync* g, unsigned nblocks) {
 }
 
 // One ready cell: pull the pushes of its higher neighbours in sweep order,
-// then release its lower neighbours into the next frontier.  Values written
-// by other blocks in earlier frontiers are read past L1.
-__device__ void drain_cell_g(const hc_view& c, const double* __restrict__ el, uint32_t cell,
-                             uint32_t* fout, unsigned* n_out) {
+// then count down its lower neighbours.  Returns the neighbours (bit
+// k = 3*(di+1) + (dj+1)) this released into the next frontier.  Values
+// written by other blocks in earlier frontiers are read past L1.
+__device__ unsigned drain_cell_g(const hc_view& c, const double* __restrict__ el,
+                                 uint32_t cell) {
   const int W = (int)c.W;
   const int i = (int)(cell / W), j = (int)(cell % W);
   const double e = el[cell];
@@ -298,12 +299,10 @@ __device__ void drain_cell_g(const hc_view& c, const double* __restrict__ el, ui
     const int dx = kk / 3 - 1, dy = kk % 3 - 1;
     old[kk] = (kk != 4 && en[kk] < e) ? atomicSub(&c.drain_pend[(i + dx) * W + (j + dy)], 1) : 0;
   }
+  unsigned released = 0;
 #pragma unroll
-  for (int kk = 0; kk < 9; kk++) {
-    if (old[kk] != 1) continue;
-    const unsigned m = atomicAdd(n_out, 1u);
-    __stcg(&fout[m], (uint32_t)((i + kk / 3 - 1) * W + (j + kk % 3 - 1)));
-  }
+  for (int kk = 0; kk < 9; kk++) released |= (old[kk] == 1 ? 1u : 0u) << kk;
+  return released;
 }
 
 // All frontiers in one cooperative launch, one grid barrier between
@@ -315,6 +314,7 @@ __global__ void __launch_bounds__(512) k_drain_sweep(const hc_view c, hc_dev* d,
   const unsigned nblocks = gridDim.x;
   const unsigned gtid = blockIdx.x * blockDim.x + threadIdx.x;
   const unsigned gsize = nblocks * blockDim.x;
+  const unsigned lane = threadIdx.x & 31;
   const unsigned long long M = (unsigned long long)c.imax * c.jmax;
   unsigned long long done = 0;
   unsigned level = 0;
@@ -325,8 +325,33 @@ __global__ void __launch_bounds__(512) k_drain_sweep(const hc_view c, hc_dev* d,
     if (n_in == 0) break;
     const uint32_t* fin = fr[level & 1];
     uint32_t* fout = fr[(level + 1) & 1];
-    for (unsigned k = gtid; k < n_in; k += gsize)
-      drain_cell_g(c, el, __ldcg(&fin[k]), fout, &g->count[nxt]);
+    // a warp's released cells are appended with one atomic
+    for (unsigned k0 = gtid - lane; k0 < n_in; k0 += gsize) {
+      const unsigned k = k0 + lane;
+      uint32_t cell = 0;
+      unsigned rel = 0;
+      if (k < n_in) {
+        cell = __ldcg(&fin[k]);
+        rel = drain_cell_g(c, el, cell);
+      }
+      const unsigned cnt = __popc(rel);
+      unsigned incl = cnt;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const unsigned y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+      }
+      unsigned base = 0;
+      if (lane == 31 && incl) base = atomicAdd(&g->count[nxt], incl);
+      base = __shfl_sync(0xffffffffu, base, 31);
+      unsigned m = base + incl - cnt;
+      const int W = (int)c.W;
+      while (rel) {
+        const int kk = __ffs(rel) - 1;
+        rel &= rel - 1;
+        __stcg(&fout[m++], (uint32_t)((int)cell + (kk / 3 - 1) * W + (kk % 3 - 1)));
+      }
+    }
     if (gtid == 0) g->count[(level + 2) % 3] = 0;  // read two frontiers ago
     done += n_in;
     level++;

@@ -2,7 +2,8 @@
 //
 // Structure on the device:
 //   k_erode_begin    time_step *= 1.5 (:4219), open the retry loop
-//   k_entrain        the entrainment pass (:4236-4548), one thread per cell;
+//   k_entrain_tau, k_entrain  the entrainment pass (:4236-4548): shear stress
+//                    per cell, then the transport of the cells with tau > 0;
 //                    its last block evaluates the retry test (:4550-4565)
 //   k_alloc_*        grain records requested during the pass get the
 //                    reference's row numbers in the reference's serial order
@@ -40,6 +41,9 @@ __device__ __forceinline__ size_t EX(const hc_view& c, int x, int y) {
   return (size_t)x * (c.jmax + 1) + y;
 }
 
+// blocks of 128 threads of the transport kernel (grid-stride over its list)
+constexpr unsigned kEntrainBlocks = 152 * 8;
+
 __global__ void k_erode_begin(const hc_view c, hc_dev* d, int gated, double mult_override) {
   if (gated) {
     if (!(d->it_active && d->do_erode)) return;
@@ -58,20 +62,23 @@ __global__ void k_erode_begin(const hc_view c, hc_dev* d, int gated, double mult
 // ---------------------------------------------------------------------------
 // entrainment pass
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(128) k_entrain(const hc_view c, hc_dev* d, int max_passes,
-                                                  cudaGraphConditionalHandle next, int has_next) {
-  __shared__ double wmax[4];
-  __shared__ bool last;
+// Two kernels.  k_entrain_tau, one thread per cell, clears the pass's
+// outputs, makes the records of cells that ask for one, computes the flow
+// velocity and shear stress, and lists the cells whose tau is positive
+// (one atomic per warp).  k_entrain runs the transport of the listed cells
+// only, so its warps are full: in a storm, a third or less of the lanes of a
+// row of cells has tau > 0, and the transport is FP64-pipe bound.
+__global__ void __launch_bounds__(128) k_entrain_tau(const hc_view c, hc_dev* d) {
   if (!(d->it_active && d->erode_retry)) return;
   const hc_params& p = c.p;
   const int jy = 1 + blockIdx.x * blockDim.x + threadIdx.x;  // column y
   const int ix = 1 + blockIdx.y * blockDim.y + threadIdx.y;  // row x
   const size_t W = c.W, N2 = c.N2;
   const double thr = p.water_depth_erosion_threshold;
-  const double mult = d->mult;
-  double tb = 0;
+  bool listed = false;
+  size_t cell = 0;
   if (ix <= c.imax && jy <= c.jmax - 1) {
-    const size_t cell = (size_t)ix * W + jy;
+    cell = (size_t)ix * W + jy;
     if (c.mask[cell]) {
       c.vel[cell] = 0;
       c.tau[cell] = 0;
@@ -84,7 +91,7 @@ __global__ void __launch_bounds__(128) k_entrain(const hc_view c, hc_dev* d, int
       c.ss[cell] = 0;
       const double h = c.h[cell];
       if (dgt(h, thr)) {
-        const double DX = p.DX, rho = 1000.0;
+        const double DX = p.DX;
         const double e0 = c.elev[cell];
         const unsigned long long pos = (unsigned long long)jy * (c.imax + 2) + ix;
         double n_man = p.spatially_var_mannings ? c.man[cell] : p.mannings;
@@ -94,22 +101,16 @@ __global__ void __launch_bounds__(128) k_entrain(const hc_view c, hc_dev* d, int
           atomicMin(&c.alloc_key[cell], pos * 5);
           d->alloc_count = 1;
         }
-        double temptot2 = 0, veltot = 0, vel = 0, qtot = 0, tau = 0, slopetot = 0;
-        double tempdir[4] = {0, 0, 0, 0};
-        const double edge0 = c.edge[EX(c, ix, jy)];
+        double vel = 0, qtot = 0, tau = 0, slopetot = 0;
         for (int k = 0; k < 4; k++) {
           const int pp = 1 + 2 * k;
           const int x2 = ix + kDXc[pp], y2 = jy + kDYc[pp];
           const size_t nb = (size_t)x2 * W + y2;
           if (dgt(c.h[nb], thr)) {
-            const double edge2 = c.edge[EX(c, x2, y2)];
-            if (dgt(edge0, edge2)) temptot2 += (edge0 - edge2);
             const double vdir = c.vd[(size_t)k * N2 + cell];
             if (dgt0(vdir)) {
               vel = vdir;
               if (dgt(vel, p.max_vel)) vel = p.max_vel;
-              tempdir[k] = vel * vel;
-              veltot += tempdir[k];
               qtot += (vel * vel);
               slopetot += ((e0 - c.elev[nb]) / DX) * vel;
             }
@@ -124,121 +125,176 @@ __global__ void __launch_bounds__(128) k_entrain(const hc_view c, hc_dev* d, int
           tau = 1000 * ci * vel * vel * (1 + (1 * (slopetot / vel)));
           c.tau[cell] = tau;
         }
-        if (dgt0(tau)) {
-          double temp_dist[HC_G] = {0};
-          double d_50 = 0, Fs = 0, graintot = 0;
-          const double ts = d->s.time_step;
-          if (p.wilcock) {
-            d_50 = d50_dev(c, cell);
-            if (d_50 < p.d[1]) d_50 = p.d[1];
-            Fs = sand_fraction_dev(c, cell);
-            for (int n = 1; n <= HC_G; n++) graintot += GRN(c, cell, n);
-          }
-          double temptot1 = 0;
-          const double mts = mult * ts;
-          // Einstein: 1 / ((1650 Di) / (tau/g)); the nine quotients by tau/g
-          // share one reciprocal (div_const, exact)
-          const double Bq = tau / kG, rB = 1.0 / Bq;
-          for (int n = 1; n <= HC_G - 1; n++) {
-            const double Di = p.d[n];
-            double td = 0;
-            if (p.wilcock) {
-              double tau_ri = (0.021 + (0.015 * exp(-20 * Fs))) * (rho * kG * d_50) *
-                              pow((Di / d_50), (0.67 / (1 + exp(1.5 - (Di / d_50)))));
-              // pow(tau / rho, 0.5): the square root, correctly rounded
-              double U_star = sqrt(tau / rho);
-              double Fi = GRN(c, cell, n) / graintot;
-              double Wi_star;
-              if ((tau / tau_ri) < 1.35)
-                Wi_star = 0.002 * pow(tau / tau_ri, 7.5);
-              else
-                Wi_star = 14 * pow(1 - (0.894 / sqrt(tau / tau_ri)), 4.5);
-              td = div_const(mts * ((Fi * (U_star * U_star * U_star)) / ((2.65 - 1) * kG)) * Wi_star,
-                             DX, c.rDX);
-            }
-            if (p.einstein) {
-              const double x = div_const(c.einA[n], Bq, rB);
-              td = div_const(div_const(mts * (40 * cube_rn(1 / x)), c.einS[n], c.einRS[n]), DX,
-                             c.rDX);
-            }
-            if (dgt(td, GRN(c, cell, n))) td = GRN(c, cell, n);
-            if (p.isSuspended[n] && n == 1) {
-              if (dgt((td + c.vs[cell]) / h, p.Csuspmax)) td = (h * p.Csuspmax) - c.vs[cell];
-            }
-            if (dlt0(td)) td = 0;
-            temp_dist[n] = td;
-            temptot1 += td;
-          }
-          const double bed = c.bed[cell];
-          if (!dgt(e0 - temptot1, bed)) {
-            double elevdiff = e0 - bed;
-            double temptot3 = temptot1;
-            temptot1 = 0;
-            for (int n = 1; n <= HC_G - 1; n++) {
-              if (!dgt(e0, bed)) {
-                temp_dist[n] = 0;
-              } else {
-                temp_dist[n] = elevdiff * (temp_dist[n] / temptot3);
-                if (dlt0(temp_dist[n])) temp_dist[n] = 0;
-              }
-              temptot1 += temp_dist[n];
-            }
-            if (dgt(tau, p.bedrock_erosion_threshold)) {
-              double amount = pow(p.bedrock_erosion_rate * tau, 1.5) * ts * mult * 0.000000317;
-              c.bed[cell] = bed - amount;
-              for (int n2 = 1; n2 <= HC_G - 1; n2++) GRN(c, cell, n2) += amount * p.dprop[n2];
-            }
-          }
-          // vegetation terms (:4459-4488) vanish: vegetation is not supported
-          // (hc_create rejects vegetation_on) and veg stays zero.
-          tb = temptot1;
-          if (dgt0(temptot1)) {
-            for (int k = 0; k < 4; k++) {
-              const int pp = 1 + 2 * k;
-              const int x2 = ix + kDXc[pp], y2 = jy + kDYc[pp];
-              const size_t nb = (size_t)x2 * W + y2;
-              if (dgt(c.h[nb], thr)) {
-                if (c.index[nb] < 1) {  // no final row number yet: ask
-                  atomicMin(&c.alloc_key[nb], pos * 5 + 1 + k);
-                  d->alloc_count = 1;
-                }
-                double factor = 0;
-                if (dgt0(c.vd[(size_t)k * N2 + cell])) factor += 0.75 * tempdir[k] / veltot;
-                const double edge2 = c.edge[EX(c, x2, y2)];
-                if (dgt(edge0, edge2)) factor += 0.25 * ((edge0 - edge2) / temptot2);
-                for (int n = 1; n <= HC_G - 1; n++) {
-                  if (dgt0(temp_dist[n])) {
-                    if (n == 1 && p.isSuspended[n]) {
-                      c.ss[cell] = temp_dist[n];
-                    } else {
-                      SF(c, k, n, cell) = temp_dist[n] * factor;
-                    }
-                  }
-                }
-              }
+        listed = dgt0(tau);
+      }
+    }
+  }
+  // blockDim.x == 32: a warp is one run of columns
+  const unsigned lane = threadIdx.x;
+  const unsigned b = __ballot_sync(0xffffffffu, listed);
+  if (b) {
+    unsigned base = 0;
+    if (lane == 0) base = atomicAdd(&d->ent_n, (unsigned)__popc(b));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (listed) c.ent_list[base + __popc(b & ((1u << lane) - 1))] = (uint32_t)cell;
+  }
+}
+
+// The transport of one listed cell (:4388-4548); returns temptot1.
+__device__ double entrain_cell(const hc_view& c, hc_dev* d, size_t cell, double mult,
+                               double ts) {
+  const hc_params& p = c.p;
+  const size_t W = c.W, N2 = c.N2;
+  const int ix = (int)(cell / W), jy = (int)(cell % W);
+  const double thr = p.water_depth_erosion_threshold;
+  const double h = c.h[cell], tau = c.tau[cell];
+  const double DX = p.DX, rho = 1000.0;
+  const double e0 = c.elev[cell];
+  const unsigned long long pos = (unsigned long long)jy * (c.imax + 2) + ix;
+  // the direction weights of the velocity pass (:4250-4289), again
+  double temptot2 = 0, veltot = 0;
+  double tempdir[4] = {0, 0, 0, 0};
+  const double edge0 = c.edge[EX(c, ix, jy)];
+  for (int k = 0; k < 4; k++) {
+    const int pp = 1 + 2 * k;
+    const int x2 = ix + kDXc[pp], y2 = jy + kDYc[pp];
+    const size_t nb = (size_t)x2 * W + y2;
+    if (dgt(c.h[nb], thr)) {
+      const double edge2 = c.edge[EX(c, x2, y2)];
+      if (dgt(edge0, edge2)) temptot2 += (edge0 - edge2);
+      const double vdir = c.vd[(size_t)k * N2 + cell];
+      if (dgt0(vdir)) {
+        double vel = vdir;
+        if (dgt(vel, p.max_vel)) vel = p.max_vel;
+        tempdir[k] = vel * vel;
+        veltot += tempdir[k];
+      }
+    }
+  }
+  double temp_dist[HC_G] = {0};
+  double d_50 = 0, Fs = 0, graintot = 0;
+  if (p.wilcock) {
+    d_50 = d50_dev(c, cell);
+    if (d_50 < p.d[1]) d_50 = p.d[1];
+    Fs = sand_fraction_dev(c, cell);
+    for (int n = 1; n <= HC_G; n++) graintot += GRN(c, cell, n);
+  }
+  double temptot1 = 0;
+  const double mts = mult * ts;
+  // Einstein: 1 / ((1650 Di) / (tau/g)); the nine quotients by tau/g
+  // share one reciprocal (div_const, exact)
+  const double Bq = tau / kG, rB = 1.0 / Bq;
+  for (int n = 1; n <= HC_G - 1; n++) {
+    const double Di = p.d[n];
+    double td = 0;
+    if (p.wilcock) {
+      double tau_ri = (0.021 + (0.015 * exp(-20 * Fs))) * (rho * kG * d_50) *
+                      pow((Di / d_50), (0.67 / (1 + exp(1.5 - (Di / d_50)))));
+      // pow(tau / rho, 0.5): the square root, correctly rounded
+      double U_star = sqrt(tau / rho);
+      double Fi = GRN(c, cell, n) / graintot;
+      double Wi_star;
+      if ((tau / tau_ri) < 1.35)
+        Wi_star = 0.002 * pow(tau / tau_ri, 7.5);
+      else
+        Wi_star = 14 * pow(1 - (0.894 / sqrt(tau / tau_ri)), 4.5);
+      td = div_const(mts * ((Fi * (U_star * U_star * U_star)) / ((2.65 - 1) * kG)) * Wi_star,
+                     DX, c.rDX);
+    }
+    if (p.einstein) {
+      const double x = div_const(c.einA[n], Bq, rB);
+      td = div_const(div_const(mts * (40 * cube_rn(1 / x)), c.einS[n], c.einRS[n]), DX,
+                     c.rDX);
+    }
+    if (dgt(td, GRN(c, cell, n))) td = GRN(c, cell, n);
+    if (p.isSuspended[n] && n == 1) {
+      if (dgt((td + c.vs[cell]) / h, p.Csuspmax)) td = (h * p.Csuspmax) - c.vs[cell];
+    }
+    if (dlt0(td)) td = 0;
+    temp_dist[n] = td;
+    temptot1 += td;
+  }
+  const double bed = c.bed[cell];
+  if (!dgt(e0 - temptot1, bed)) {
+    double elevdiff = e0 - bed;
+    double temptot3 = temptot1;
+    temptot1 = 0;
+    for (int n = 1; n <= HC_G - 1; n++) {
+      if (!dgt(e0, bed)) {
+        temp_dist[n] = 0;
+      } else {
+        temp_dist[n] = elevdiff * (temp_dist[n] / temptot3);
+        if (dlt0(temp_dist[n])) temp_dist[n] = 0;
+      }
+      temptot1 += temp_dist[n];
+    }
+    if (dgt(tau, p.bedrock_erosion_threshold)) {
+      double amount = pow(p.bedrock_erosion_rate * tau, 1.5) * ts * mult * 0.000000317;
+      c.bed[cell] = bed - amount;
+      for (int n2 = 1; n2 <= HC_G - 1; n2++) GRN(c, cell, n2) += amount * p.dprop[n2];
+    }
+  }
+  // vegetation terms (:4459-4488) vanish: vegetation is not supported
+  // (hc_create rejects vegetation_on) and veg stays zero.
+  if (dgt0(temptot1)) {
+    for (int k = 0; k < 4; k++) {
+      const int pp = 1 + 2 * k;
+      const int x2 = ix + kDXc[pp], y2 = jy + kDYc[pp];
+      const size_t nb = (size_t)x2 * W + y2;
+      if (dgt(c.h[nb], thr)) {
+        if (c.index[nb] < 1) {  // no final row number yet: ask
+          atomicMin(&c.alloc_key[nb], pos * 5 + 1 + k);
+          d->alloc_count = 1;
+        }
+        double factor = 0;
+        if (dgt0(c.vd[(size_t)k * N2 + cell])) factor += 0.75 * tempdir[k] / veltot;
+        const double edge2 = c.edge[EX(c, x2, y2)];
+        if (dgt(edge0, edge2)) factor += 0.25 * ((edge0 - edge2) / temptot2);
+        for (int n = 1; n <= HC_G - 1; n++) {
+          if (dgt0(temp_dist[n])) {
+            if (n == 1 && p.isSuspended[n]) {
+              c.ss[cell] = temp_dist[n];
+            } else {
+              SF(c, k, n, cell) = temp_dist[n] * factor;
             }
           }
         }
       }
     }
   }
+  return temptot1;
+}
+
+__global__ void __launch_bounds__(128) k_entrain(const hc_view c, hc_dev* d, int max_passes,
+                                                  cudaGraphConditionalHandle next, int has_next) {
+  __shared__ double wmax[4];
+  __shared__ bool last;
+  if (!(d->it_active && d->erode_retry)) return;
+  const hc_params& p = c.p;
+  const double mult = d->mult, ts = d->s.time_step;
+  const unsigned n_list = *(volatile unsigned*)&d->ent_n;
+  double tb = 0;
+  for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < n_list;
+       k += gridDim.x * blockDim.x)
+    tb = smax(tb, entrain_cell(c, d, c.ent_list[k], mult, ts));
   // tempbmax: max over the pass (warp shuffle, block, grid via last block)
   for (int o = 16; o > 0; o >>= 1) tb = smax(tb, __shfl_xor_sync(0xffffffffu, tb, o));
-  const int t = threadIdx.y * blockDim.x + threadIdx.x;
+  const int t = threadIdx.x;
   if ((t & 31) == 0) wmax[t >> 5] = tb;
   __syncthreads();
   if (t == 0) {
     double b = 0;
-    for (int w = 0; w < (int)(blockDim.x * blockDim.y) / 32; w++) b = smax(b, wmax[w]);
+    for (int w = 0; w < (int)blockDim.x / 32; w++) b = smax(b, wmax[w]);
     if (b > 0) atomic_max_pos(&d->tempbmax_bits, b);
     __threadfence();
-    last = (atomicAdd(&d->pass_done, 1u) == gridDim.x * gridDim.y - 1);
+    last = (atomicAdd(&d->pass_done, 1u) == gridDim.x - 1);
   }
   __syncthreads();
   if (last && t == 0) {
     __threadfence();
     const double tempbmax = __longlong_as_double((long long)atomicExch(&d->tempbmax_bits, 0ull));
     d->pass_done = 0;
+    d->ent_n = 0;
     d->erode_passes++;
     const double EF = p.ERODEFACTOR;
     if (tempbmax > EF) {
@@ -253,7 +309,7 @@ __global__ void __launch_bounds__(128) k_entrain(const hc_view c, hc_dev* d, int
     }
     if (has_next) {
       cudaGraphSetConditional(next, d->erode_retry ? 1u : 0u);
-      if (d->erode_retry) d->body_kernels += 6;  // the next pass's kernels
+      if (d->erode_retry) d->body_kernels += 7;  // the next pass's kernels
     }
     d->s.tempbmax = tempbmax;  // tempbmax of the last pass
   }
@@ -1452,8 +1508,9 @@ void launch_erode_pass(hc_ctx* c, int max_passes, cudaGraphConditionalHandle nex
   dim3 b(32, 4);
   dim3 g((c->v.jmax - 1 + b.x - 1) / b.x, (c->v.imax + b.y - 1) / b.y);
   if (g.x < 1) g.x = 1;
-  k_entrain<<<g, b, 0, c->cs>>>(c->v, c->dev, max_passes, next, has_next);
-  count_launch(c, 1);
+  k_entrain_tau<<<g, b, 0, c->cs>>>(c->v, c->dev);
+  k_entrain<<<kEntrainBlocks, 128, 0, c->cs>>>(c->v, c->dev, max_passes, next, has_next);
+  count_launch(c, 2);
   size_t nwords = c->v.N2 / 4 + 1;
   int nb = (int)((c->v.N2 + 255) / 256);
   k_alloc_mark<<<nb, 256, 0, c->cs>>>(c->v, c->dev, s.bits);

@@ -205,8 +205,8 @@ __global__ void k_control(const hc_view c, hc_dev* d, hc_iter_handles hh) {
   d->erode_retry = d->do_erode;
   d->do_slide = !p.hydro_only && ((long long)s.counter % p.in_channel_landslide_iter_interval) == 0;
   if (hh.has) {
-    // kernels inside the bodies enabled here: scan 4, erosion 7 + 8, slide_3 5
-    d->body_kernels += (d->do_scan ? 4 : 0) + (d->do_erode && !p.hydro_only ? 15 : 0) +
+    // kernels inside the bodies enabled here: scan 4, erosion 8 + 8, slide_3 5
+    d->body_kernels += (d->do_scan ? 4 : 0) + (d->do_erode && !p.hydro_only ? 16 : 0) +
                        (d->do_slide ? 5 : 0);
     cudaGraphSetConditional(hh.scan, d->do_scan ? 1u : 0u);
     if (!p.hydro_only) {

@@ -88,6 +88,7 @@ struct hc_dev {
   unsigned int xchains;   // chain starts of the +/-x apply pass (hc_view::chains)
   unsigned int ychains;   // chain starts of the +/-y apply pass
   unsigned int xresume, yresume;  // long chains handed from the thread to the warp walkers
+  unsigned int ent_n;     // cells listed for the transport of an entrainment pass
 };
 
 // Working state of a drainage recomputation (hc_drain.cu): the radix
@@ -124,6 +125,7 @@ struct hc_view {
   int32_t *wet;                // cells of the wet mask, ascending (the down_scan
                                // lists as one array); length in hc_dev::wet_count
   int32_t *wet_sums;           // per-block counts for building it
+  uint32_t *ent_list;          // cells with tau > 0 in an entrainment pass (N2)
   int cin_cap;
 
   // time series
@@ -278,6 +280,80 @@ HC_DEV double div_const(double x, double y, double r) {
   const double q = __dmul_rn(x, r);
   const double e = fma(-q, y, x);
   return fma(e, r, q);
+}
+
+// RN(a / b), the IEEE quotient, computed on the integer pipe.  On this GPU
+// the FP64 pipe retires two lanes per clock per SM, an IEEE division takes
+// about nine of its instructions, and a warp's integer multiply-add costs a
+// thirtieth of one FP64 instruction; the stencils are FP64-pipe bound.
+//
+// Significands ma (normalised so that mb <= ma < 2 mb) and mb (53 bits):
+// the quotient's significand is q = floor(ma 2^52 / mb), exact remainder
+// r = ma 2^52 - q mb, rounded up when 2r > mb (2r == mb cannot occur for a
+// quotient of 53-bit significands, and is rounded to even regardless).
+// q comes from a 64-bit reciprocal V of mb: a float estimate (rcp.approx,
+// relative error below 2^-21 after truncating mb to 24 bits), then two
+// Newton-Raphson steps x + x (1 - mb x) in fixed point, each of which stays
+// below 2^116/mb; the second leaves V within two units of it, so
+// floor(ma V / 2^64) is q or q - 1, and the remainder settles it.  Operands
+// that are zero, subnormal, infinite or NaN, and quotients that would leave
+// the normal range, take the hardware division.
+HC_DEV double ddiv_rn(double a, double b) {
+  const unsigned long long A = (unsigned long long)__double_as_longlong(a);
+  const unsigned long long B = (unsigned long long)__double_as_longlong(b);
+  const unsigned long long M52 = (1ull << 52) - 1, H52 = 1ull << 52;
+  const int ea = (int)(A >> 52) & 0x7ff, eb = (int)(B >> 52) & 0x7ff;
+  unsigned long long ma = (A & M52) | H52;
+  const unsigned long long mb = (B & M52) | H52;
+  int er = ea - eb + 1023;
+  if (ma < mb) {
+    ma <<= 1;
+    er--;
+  }
+  if (ea == 0 || ea == 0x7ff || eb == 0 || eb == 0x7ff || er < 1 || er > 2045)
+    return __ddiv_rn(a, b);
+  unsigned long long q, r;
+  if (mb == H52) {  // b a power of two: exact
+    q = ma;
+    r = 0;
+  } else {
+    // float estimate of 2^83/mb from the top 24 bits of mb, as an integer
+    const float fm = __uint_as_float(0x3f800000u | (unsigned)((mb >> 29) & 0x7fffffu));
+    float rf;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(rf) : "f"(fm));
+    const unsigned rb = __float_as_uint(rf);  // rf in (0.5, 1]
+    const unsigned long long R0 = (unsigned long long)((rb & 0x7fffffu) | 0x800000u)
+                                  << ((int)(rb >> 23) - 119);
+    // Newton step at 2^83: E = 2^83 - mb R0, |E| < 2^62 (low 64 bits suffice)
+    const long long E = (long long)(0ull - mb * R0);
+    const unsigned long long plo = R0 * (unsigned long long)E;
+    const unsigned long long phi = (unsigned long long)__mul64hi((long long)R0, E);
+    unsigned long long V = (R0 << 33) + ((phi << 14) | (plo >> 50));  // ~2^116/mb
+    // Newton step at 2^116: E2 = 2^116 - mb V in [0, 2^74), kept as E2 / 2^20
+    const unsigned long long qlo = mb * V, qhi = __umul64hi(mb, V);
+    const unsigned long long e_lo = 0ull - qlo;
+    const unsigned long long e_hi = H52 - qhi - (qlo != 0 ? 1ull : 0ull);
+    const unsigned long long e_s = (e_hi << 44) | (e_lo >> 20);
+    V += __umul64hi(V, e_s) >> 32;
+    q = __umul64hi(ma, V);
+    r = (ma << 52) - q * mb;
+    if (r >= mb) {
+      r -= mb;
+      q++;
+    }
+    if (r >= mb) {
+      r -= mb;
+      q++;
+    }
+  }
+  const unsigned long long r2 = r << 1;
+  if (r2 > mb || (r2 == mb && (q & 1))) q++;
+  if (q == (H52 << 1)) {
+    q = H52;
+    er++;
+  }
+  const unsigned long long sgn = (A ^ B) & 0x8000000000000000ull;
+  return __longlong_as_double((long long)(sgn | ((unsigned long long)er << 52) | (q & M52)));
 }
 
 // A float within a relative 2^-20 of |x| (or 0 / +inf when |x| is outside
