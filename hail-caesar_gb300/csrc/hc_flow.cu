@@ -299,7 +299,7 @@ __device__ __forceinline__ void inertial_face(double& q, double& qs, double& vel
     // (0 - ghd*slope) / (1 + (ghd*nn*0)/h^3) = (0 - ghd*slope) / 1
     qn = q - (ghd * slope);
   } else {
-    qn = ((q - (ghd * slope)) / (1 + ghd * nn * fabs(q) / cube_rn(hflow)));
+    qn = ddiv_rn(q - (ghd * slope), 1 + ddiv_rn(ghd * nn * fabs(q), cube_rn(hflow)));
   }
   const float hf = approx_abs_f(hflow);
   const float dtf = approx_abs_f(dt);
@@ -311,7 +311,7 @@ __device__ __forceinline__ void inertial_face(double& q, double& qs, double& vel
   if (!deq0(qn)) {
     float fr;
     if (kVel) {
-      qoh = qn / hflow;
+      qoh = ddiv_rn(qn, hflow);
       qoh_valid = true;
       fr = approx_abs_f(qoh) / sqrtf(9.81f * hf);
     } else {
@@ -319,7 +319,7 @@ __device__ __forceinline__ void inertial_face(double& q, double& qs, double& vel
     }
     int t = decide_gt(fr, c.flf);
     if (t == 0) {
-      if (!qoh_valid) qoh = qn / hflow;
+      if (!qoh_valid) qoh = ddiv_rn(qn, hflow);
       t = (fabs(qoh) / sqrt(kG * hflow) > p.froude_limit) ? 1 : -1;
     }
     if (t > 0) {
@@ -334,7 +334,7 @@ __device__ __forceinline__ void inertial_face(double& q, double& qs, double& vel
     int t = decide_gt(approx_abs_f(qn) * dtf / c.DXf, approx_f(h0) * 0.25f);
     if (t == 0) t = ((qn * dt / DX) > (h0 / 4)) ? 1 : -1;
     if (t > 0) {
-      qn = ((h0 * DX) / 5) / dt;
+      qn = ddiv_rn(ddiv_rn(h0 * DX, 5.0), dt);
       qoh_valid = false;
     }
   }
@@ -342,7 +342,7 @@ __device__ __forceinline__ void inertial_face(double& q, double& qs, double& vel
     int t = decide_gt(approx_abs_f(qn) * dtf / c.DXf, approx_f(h1) * 0.25f);
     if (t == 0) t = (fabs(qn * dt / DX) > (h1 / 4)) ? 1 : -1;
     if (t > 0) {
-      qn = zero_minus(((h1 * DX) / 5) / dt);
+      qn = zero_minus(ddiv_rn(ddiv_rn(h1 * DX, 5.0), dt));
       qoh_valid = false;
     }
   }
@@ -350,22 +350,22 @@ __device__ __forceinline__ void inertial_face(double& q, double& qs, double& vel
   if (kSusp) {
     // qs = q * (V/h) of the giving cell; V = 0 gives 0 * q (a signed zero)
     if (qpos) qs = qn * c0;
-    if (qneg) qs = qn * (deq0(v1) ? v1 : v1 / h1);  // h1 > 0 here, as h0 above
+    if (qneg) qs = qn * (deq0(v1) ? v1 : ddiv_rn(v1, h1));  // h1 > 0 here, as h0 above
     // qs*dt > V*DX/4 (giving cell) caps the sediment flux
     if (dgt0(qs)) {
       int t = decide_gt(approx_abs_f(qs) * dtf, approx_f(v0) * c.DXf * 0.25f);
       if (t == 0) t = (qs * dt > (v0 * DX) / 4) ? 1 : -1;
-      if (t > 0) qs = ((v0 * DX) / 5) / dt;
+      if (t > 0) qs = ddiv_rn(ddiv_rn(v0 * DX, 5.0), dt);
     }
     if (dlt0(qs)) {
       int t = decide_gt(approx_abs_f(qs) * dtf, approx_f(v1) * c.DXf * 0.25f);
       if (t == 0) t = (fabs(qs * dt) > (v1 * DX) / 4) ? 1 : -1;
-      if (t > 0) qs = zero_minus(((v1 * DX) / 5) / dt);
+      if (t > 0) qs = zero_minus(ddiv_rn(ddiv_rn(v1 * DX, 5.0), dt));
     }
   }
   if (kVel) {
     // (0 - q)/hflow = -(q/hflow) exactly: division rounds symmetrically
-    if ((qpos || qneg) && !qoh_valid) qoh = qn / hflow;
+    if ((qpos || qneg) && !qoh_valid) qoh = ddiv_rn(qn, hflow);
     if (qpos) {
       vel_out = qoh;
       vdir = 1;
@@ -398,7 +398,7 @@ __device__ __forceinline__ void flow_cell(const hc_view& c, const hc_dev* __rest
   // V/h of this cell, shared by both faces.  Only used where q > 0 after
   // the depth limit, which implies h > 0, so a zero V gives V itself (with
   // its sign) without the division.
-  const double c0 = (susp && !deq0(v0)) ? v0 / h0 : v0;
+  const double c0 = (susp && !deq0(v0)) ? ddiv_rn(v0, h0) : v0;
   const bool wet0 = dgt0(h0);
   // x face (rows i-1, i)
   {

@@ -1,0 +1,145 @@
+// Test driver: the library's integer-pipe division (ddiv_rn in
+// hc_internal.cuh) against the hardware's IEEE division, bit for bit, over
+// several input families; and the throughput of both.  Built by
+// test_gpu_arith.py with the library's own compiler flags.
+#include <cstdint>
+
+#include "../hail-caesar_gb300/csrc/hc_internal.cuh"
+
+namespace {
+
+__device__ __forceinline__ unsigned long long mix(unsigned long long x) {  // splitmix64
+  x += 0x9e3779b97f4a7c15ull;
+  x = (x ^ (x >> 30)) * 0xbf58476d1ce4e5b9ull;
+  x = (x ^ (x >> 27)) * 0x94d049bb133111ebull;
+  return x ^ (x >> 31);
+}
+
+__device__ __forceinline__ double mk(unsigned long long sign, int e, unsigned long long m) {
+  return __longlong_as_double(
+      (long long)((sign << 63) | ((unsigned long long)(e & 0x7ff) << 52) | (m & ((1ull << 52) - 1))));
+}
+
+__device__ void pair(int mode, unsigned long long k, double& a, double& b) {
+  const unsigned long long r1 = mix(k), r2 = mix(k ^ 0xabcdef12345ull), r3 = mix(k * 7 + 3);
+  switch (mode) {
+    case 0:  // any bit patterns: zeros, subnormals, infinities, NaNs included
+      a = __longlong_as_double((long long)r1);
+      b = __longlong_as_double((long long)r2);
+      break;
+    case 1:  // normal operands, quotients across the whole normal range
+      a = mk(r3 & 1, 1 + (int)(r1 >> 53) % 2046, r1);
+      b = mk((r3 >> 1) & 1, 1 + (int)(r2 >> 53) % 2046, r2);
+      break;
+    case 2: {  // significands at the ends of their range
+      const unsigned long long ma = (r3 & 4) ? (r1 & 0xffff) : ((1ull << 52) - 1 - (r1 & 0xffff));
+      const unsigned long long mb = (r3 & 8) ? (r2 & 0xffff) : ((1ull << 52) - 1 - (r2 & 0xffff));
+      a = mk(r3 & 1, 1023 + (int)(r1 >> 58) - 32, ma);
+      b = mk((r3 >> 1) & 1, 1023 + (int)(r2 >> 58) - 32, mb);
+      break;
+    }
+    case 3: {  // quotients at or next to small integers and simple fractions
+      b = mk(0, 1000 + (int)(r2 >> 58), r2);
+      const double m = (double)(1 + (r1 >> 56));
+      const double p = b * m;
+      const long long d = (long long)(r3 % 5) - 2;
+      a = __longlong_as_double(__double_as_longlong(p) + d);
+      break;
+    }
+    case 4: {  // quotients at the edges of the normal range
+      const int eb = 1 + (int)(r2 >> 53) % 2046;
+      const int t = (int)(r3 % 8);
+      const int target = (t < 4) ? (t - 1) : (2044 + (t - 4));  // -1..2, 2044..2047
+      int ea = target + eb - 1023;
+      if (ea < 1) ea = 1;
+      if (ea > 2046) ea = 2046;
+      a = mk(r3 >> 63, ea, r1);
+      b = mk(0, eb, r2);
+      break;
+    }
+    default: {  // the model's magnitudes: depths, discharges, volumes
+      a = mk(r3 & 1, 1023 - 30 + (int)(r1 >> 59), r1);
+      b = mk(0, 1023 - 20 + (int)(r2 >> 59), r2);
+    }
+  }
+}
+
+__global__ void k_check(unsigned long long n, unsigned long long seed, int mode,
+                        unsigned long long* bad, double* first) {
+  for (unsigned long long k = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; k < n;
+       k += (unsigned long long)gridDim.x * blockDim.x) {
+    double a, b;
+    pair(mode, k + seed * 0x100000000ull, a, b);
+    const double x = ddiv_rn(a, b), y = __ddiv_rn(a, b);
+    const bool same = __double_as_longlong(x) == __double_as_longlong(y) ||
+                      (disnan(x) && disnan(y));
+    if (!same && atomicAdd(bad, 1ull) == 0) {
+      first[0] = a;
+      first[1] = b;
+      first[2] = x;
+      first[3] = y;
+    }
+  }
+}
+
+// throughput: each thread divides independent operands kIter times
+template <bool kInt>
+__global__ void k_time(const double* in, double* out, int iters) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  double a = in[t & 1023] + t * 1e-9, b = in[(t + 7) & 1023] + 1.5;
+  double acc = 0;
+  for (int k = 0; k < iters; k++) {
+    const double q = kInt ? ddiv_rn(a, b) : __ddiv_rn(a, b);
+    acc = acc + q;
+    a = q + 1.25;  // the next quotient depends on this one
+  }
+  out[t] = acc;
+}
+
+}  // namespace
+
+extern "C" int arith_check(unsigned long long n, unsigned long long seed, int mode,
+                           unsigned long long* bad, double* first) {
+  unsigned long long* d_bad;
+  double* d_first;
+  if (cudaMalloc(&d_bad, 8) != cudaSuccess || cudaMalloc(&d_first, 32) != cudaSuccess) return 1;
+  cudaMemset(d_bad, 0, 8);
+  cudaMemset(d_first, 0, 32);
+  k_check<<<152 * 16, 256>>>(n, seed, mode, d_bad, d_first);
+  cudaMemcpy(bad, d_bad, 8, cudaMemcpyDeviceToHost);
+  cudaMemcpy(first, d_first, 32, cudaMemcpyDeviceToHost);
+  const cudaError_t e = cudaGetLastError();
+  cudaFree(d_bad);
+  cudaFree(d_first);
+  return e == cudaSuccess ? 0 : 2;
+}
+
+// divisions per second of each kind (ms for `iters` divisions per thread)
+extern "C" int arith_time(int iters, float* ms_native, float* ms_int) {
+  const int blocks = 152 * 8, threads = 256;
+  double *in, *out;
+  if (cudaMalloc(&in, 1024 * 8) != cudaSuccess ||
+      cudaMalloc(&out, (size_t)blocks * threads * 8) != cudaSuccess)
+    return 1;
+  double h[1024];
+  for (int k = 0; k < 1024; k++) h[k] = 0.1 + k * 0.37;
+  cudaMemcpy(in, h, sizeof h, cudaMemcpyHostToDevice);
+  cudaEvent_t e0, e1, e2;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventCreate(&e2);
+  k_time<false><<<blocks, threads>>>(in, out, 16);  // warm-up
+  k_time<true><<<blocks, threads>>>(in, out, 16);
+  cudaEventRecord(e0);
+  k_time<false><<<blocks, threads>>>(in, out, iters);
+  cudaEventRecord(e1);
+  k_time<true><<<blocks, threads>>>(in, out, iters);
+  cudaEventRecord(e2);
+  cudaEventSynchronize(e2);
+  cudaEventElapsedTime(ms_native, e0, e1);
+  cudaEventElapsedTime(ms_int, e1, e2);
+  const cudaError_t e = cudaGetLastError();
+  cudaFree(in);
+  cudaFree(out);
+  return e == cudaSuccess ? 0 : 2;
+}

@@ -1,0 +1,45 @@
+"""The integer-pipe IEEE division of the kernels (ddiv_rn in
+hc_internal.cuh) against the hardware's division, bit for bit: 2^30
+quotients per input family (arbitrary bit patterns, normal operands, edge
+significands, near-integer quotients, edges of the normal range, the
+model's magnitudes); and the throughput of both, printed."""
+import ctypes as C
+import os
+import subprocess
+
+import pytest
+
+pytestmark = pytest.mark.gpu
+HERE = os.path.dirname(os.path.abspath(__file__))
+FAMILIES = ["bit patterns", "normal", "edge significands", "near-integer quotients",
+            "range edges", "model magnitudes"]
+
+
+@pytest.fixture(scope="module")
+def arith(tmp_path_factory):
+    import build as hcbuild
+    so = str(tmp_path_factory.mktemp("arith") / "arith_check.so")
+    cmd = [hcbuild.nvcc()] + hcbuild.ARCH + hcbuild.NVFLAGS + \
+        ["-shared", "-o", so, os.path.join(HERE, "arith_check.cu")]
+    subprocess.run(cmd, check=True, capture_output=True)
+    lib = C.CDLL(so)
+    lib.arith_check.argtypes = [C.c_uint64, C.c_uint64, C.c_int, C.POINTER(C.c_uint64),
+                                C.POINTER(C.c_double)]
+    lib.arith_time.argtypes = [C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float)]
+    return lib
+
+
+@pytest.mark.parametrize("mode", range(len(FAMILIES)), ids=FAMILIES)
+def test_division_matches_hardware(arith, mode):
+    bad = C.c_uint64(0)
+    first = (C.c_double * 4)()
+    assert arith.arith_check(1 << 30, 1 + mode, mode, C.byref(bad), first) == 0
+    assert bad.value == 0, "%d mismatches; first a=%r b=%r got %r want %r" % (
+        bad.value, first[0], first[1], first[2], first[3])
+
+
+def test_division_throughput(arith):
+    tn, ti = C.c_float(0), C.c_float(0)
+    assert arith.arith_time(2000, C.byref(tn), C.byref(ti)) == 0
+    print("divisions: hardware %.3f ms, integer pipe %.3f ms (%.2fx)" %
+          (tn.value, ti.value, tn.value / ti.value))
