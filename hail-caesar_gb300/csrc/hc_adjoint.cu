@@ -60,7 +60,7 @@ __device__ __forceinline__ int decide(float a, float b) {
 // where a branch is decided, float estimates first, as there); the
 // derivatives, which need no exact rounding, use reciprocals.
 __device__ DQ face_dq(double q, double e0, double h0, double e1, double h1, double nn, double dt,
-                      int es, const hc_params& p, double rDX) {
+                      int es, const hc_params& p, double rDX, const hc_divisor& dxd) {
   const double DX = p.DX;
   DQ r = {0, 0, 0, 0, 0};
   const double a0 = e0 + h0, a1 = e1 + h1;
@@ -68,11 +68,11 @@ __device__ DQ face_dq(double q, double e0, double h0, double e1, double h1, doub
   const double hflow = smax(a0, a1) - smax(e1, e0);
   if (!(hflow > p.hflow_threshold)) return r;  // q = 0
   const double dhf0 = a1max ? 0.0 : 1.0, dhf1 = a1max ? 1.0 : 0.0;
-  double slope = div_const(a1 - a0, DX, rDX), ds0 = -rDX, ds1 = rDX;
+  double slope = ddiv_by(a1 - a0, dxd), ds0 = -rDX, ds1 = rDX;
   if (es == 1) slope = p.edgeslope, ds0 = ds1 = 0;
   if (es == -1) slope = 0 - p.edgeslope, ds0 = ds1 = 0;
   const double ghd = kG * hflow * dt;
-  const double rhf = 1 / hflow;
+  const double rhf = ddiv_rn(1.0, hflow);
   // qn and its derivatives with respect to q, hflow, slope, nn
   double qn, d_q, d_hf, d_s, d_nn;
   if (q == 0) {
@@ -83,10 +83,10 @@ __device__ DQ face_dq(double q, double e0, double h0, double e1, double h1, doub
     d_nn = 0;
   } else {
     const double c3 = cube_rn(hflow);
-    const double F = ghd * nn * fabs(q) / c3;
+    const double F = ddiv_rn(ghd * nn * fabs(q), c3);
     const double D = 1 + F, N = q - (ghd * slope);
-    qn = N / D;
-    const double rD = 1 / D, rc3 = 1 / c3;
+    qn = ddiv_rn(N, D);
+    const double rD = ddiv_rn(1.0, D), rc3 = ddiv_rn(1.0, c3);
     const double dF_q = ghd * nn * (q > 0 ? 1.0 : -1.0) * rc3;
     const double dF_hf = -2 * F * rhf;
     const double dF_nn = ghd * fabs(q) * rc3;
@@ -120,16 +120,16 @@ __device__ DQ face_dq(double q, double e0, double h0, double e1, double h1, doub
     int t = decide(approx_abs_f(qn) * dtf / dxf, approx_f(h0) * 0.25f);
     if (t == 0) t = ((qn * dt / DX) > (h0 / 4)) ? 1 : -1;
     if (t > 0) {
-      qn = ((h0 * DX) / 5) / dt;
-      d_q = 0, d_nn = 0, dh0 = DX / 5 / dt, dh1 = 0;
+      qn = ddiv_rn(ddiv_rn(h0 * DX, 5.0), dt);
+      d_q = 0, d_nn = 0, dh0 = ddiv_rn(ddiv_rn(DX, 5.0), dt), dh1 = 0;
     }
   }
   if (qn < 0) {
     int t = decide(approx_abs_f(qn) * dtf / dxf, approx_f(h1) * 0.25f);
     if (t == 0) t = (fabs(qn * dt / DX) > (h1 / 4)) ? 1 : -1;
     if (t > 0) {
-      qn = 0 - ((h1 * DX) / 5) / dt;
-      d_q = 0, d_nn = 0, dh0 = 0, dh1 = -DX / 5 / dt;
+      qn = 0 - ddiv_rn(ddiv_rn(h1 * DX, 5.0), dt);
+      d_q = 0, d_nn = 0, dh0 = 0, dh1 = -ddiv_rn(ddiv_rn(DX, 5.0), dt);
     }
   }
   r.v = qn;
@@ -176,7 +176,8 @@ __global__ void k_adj_depth(const hc_view c, AdjBufs b, AdjStep st) {
   double hd = ha;
   bool zeroed = false;
   if (b.mask[cell]) {
-    hd += st.fdt * (b.qx1[cell + W] - b.qx1[cell] + b.qy1[cell + 1] - b.qy1[cell]) / c.p.DX;
+    hd += ddiv_by(st.fdt * (b.qx1[cell + W] - b.qx1[cell] + b.qy1[cell + 1] - b.qy1[cell]),
+                  c.dxd);
     if (hd > 0 && c.elev[cell] == -9999) zeroed = true;
   }
   double lam = b.lam[cell];
@@ -218,7 +219,7 @@ __global__ void k_adj_flow(const hc_view c, AdjBufs b, AdjStep st) {
       const double h1 = hin(up), e1 = c.elev[up];
       if ((h0 > 0 || h1 > 0) && e1 > -9999) {
         const int es = (i == c.imax) ? 1 : ((i <= 2) ? -1 : 0);
-        const DQ r = face_dq(b.qx0[cell], e0, h0, e1, h1, nn, st.fdt, es, p, c.rDX);
+        const DQ r = face_dq(b.qx0[cell], e0, h0, e1, h1, nn, st.fdt, es, p, c.rDX, c.dxd);
         ox = r.dq * mux;
         p0x = r.dh0 * mux;
         p1x = r.dh1 * mux;
@@ -230,7 +231,7 @@ __global__ void k_adj_flow(const hc_view c, AdjBufs b, AdjStep st) {
       const double h1 = hin(lf), e1 = c.elev[lf];
       if ((h0 > 0 || h1 > 0) && e1 > -9999) {
         const int es = (j == c.jmax) ? 1 : ((j <= 2) ? -1 : 0);
-        const DQ r = face_dq(b.qy0[cell], e0, h0, e1, h1, nn, st.fdt, es, p, c.rDX);
+        const DQ r = face_dq(b.qy0[cell], e0, h0, e1, h1, nn, st.fdt, es, p, c.rDX, c.dxd);
         oy = r.dq * muy;
         p0y = r.dh0 * muy;
         p1y = r.dh1 * muy;

@@ -211,6 +211,19 @@ extern "C" void* hc_stream(hc_ctx* c) { return c ? (void*)c->s : nullptr; }
 // ------------------------------------------------------------------ create
 static hc_status free_all(hc_ctx* c);
 
+hc_divisor host_divisor(double b) {
+  unsigned long long B;
+  std::memcpy(&B, &b, 8);
+  const unsigned long long H52 = 1ull << 52;
+  hc_divisor d;
+  d.b = b;
+  d.eb = (int)(B >> 52) & 0x7ff;
+  d.ok = d.eb != 0 && d.eb != 0x7ff;
+  d.mb = (B & (H52 - 1)) | H52;
+  d.V = (d.mb == H52) ? 0 : (unsigned long long)(((unsigned __int128)1 << 116) / d.mb);
+  return d;
+}
+
 extern "C" hc_status hc_create(const hc_params* p, size_t max_bytes, hc_ctx** out) {
   if (!p || !out) return HC_ERR_ARG;
   *out = nullptr;
@@ -227,6 +240,7 @@ extern "C" hc_status hc_create(const hc_params* p, size_t max_bytes, hc_ctx** ou
   hc_view& v = c->v;
   v.p = *p;
   v.rDX = 1.0 / p->DX;
+  v.dxd = host_divisor(p->DX);
   v.DXf = (float)p->DX;
   v.flf = (float)p->froude_limit;
   v.act_hi = (float)(p->active * 1.5);
@@ -242,6 +256,7 @@ extern "C" hc_status hc_create(const hc_params* p, size_t max_bytes, hc_ctx** ou
     v.einA[n] = (2650 - 1000) * Di;
     v.einS[n] = std::sqrt(1000 / ((2250 - 1000) * g * (Di * Di * Di)));
     v.einRS[n] = 1.0 / v.einS[n];
+    v.einSd[n] = host_divisor(v.einS[n]);
   }
   v.imax = p->imax;
   v.jmax = p->jmax;

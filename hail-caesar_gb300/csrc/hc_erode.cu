@@ -91,7 +91,6 @@ __global__ void __launch_bounds__(128) k_entrain_tau(const hc_view c, hc_dev* d)
       c.ss[cell] = 0;
       const double h = c.h[cell];
       if (dgt(h, thr)) {
-        const double DX = p.DX;
         const double e0 = c.elev[cell];
         const unsigned long long pos = (unsigned long long)jy * (c.imax + 2) + ix;
         double n_man = p.spatially_var_mannings ? c.man[cell] : p.mannings;
@@ -112,7 +111,7 @@ __global__ void __launch_bounds__(128) k_entrain_tau(const hc_view c, hc_dev* d)
               vel = vdir;
               if (dgt(vel, p.max_vel)) vel = p.max_vel;
               qtot += (vel * vel);
-              slopetot += ((e0 - c.elev[nb]) / DX) * vel;
+              slopetot += ddiv_by(e0 - c.elev[nb], c.dxd) * vel;
             }
           }
         }
@@ -122,7 +121,7 @@ __global__ void __launch_bounds__(128) k_entrain_tau(const hc_view c, hc_dev* d)
           if (dgt(vel, p.max_vel)) vel = p.max_vel;
           double ci = kG * (n_man * n_man) * pow(h, -0.33);
           if (dgt0(slopetot)) slopetot = 0;
-          tau = 1000 * ci * vel * vel * (1 + (1 * (slopetot / vel)));
+          tau = 1000 * ci * vel * vel * (1 + (1 * ddiv_rn(slopetot, vel)));
           c.tau[cell] = tau;
         }
         listed = dgt0(tau);
@@ -148,7 +147,7 @@ __device__ double entrain_cell(const hc_view& c, hc_dev* d, size_t cell, double 
   const int ix = (int)(cell / W), jy = (int)(cell % W);
   const double thr = p.water_depth_erosion_threshold;
   const double h = c.h[cell], tau = c.tau[cell];
-  const double DX = p.DX, rho = 1000.0;
+  const double rho = 1000.0;
   const double e0 = c.elev[cell];
   const unsigned long long pos = (unsigned long long)jy * (c.imax + 2) + ix;
   // the direction weights of the velocity pass (:4250-4289), again
@@ -182,8 +181,9 @@ __device__ double entrain_cell(const hc_view& c, hc_dev* d, size_t cell, double 
   double temptot1 = 0;
   const double mts = mult * ts;
   // Einstein: 1 / ((1650 Di) / (tau/g)); the nine quotients by tau/g
-  // share one reciprocal (div_const, exact)
-  const double Bq = tau / kG, rB = 1.0 / Bq;
+  // share one prepared divisor
+  const double Bq = ddiv_rn(tau, kG);
+  const hc_divisor Bd = ddiv_prep(Bq);
   for (int n = 1; n <= HC_G - 1; n++) {
     const double Di = p.d[n];
     double td = 0;
@@ -198,13 +198,12 @@ __device__ double entrain_cell(const hc_view& c, hc_dev* d, size_t cell, double 
         Wi_star = 0.002 * pow(tau / tau_ri, 7.5);
       else
         Wi_star = 14 * pow(1 - (0.894 / sqrt(tau / tau_ri)), 4.5);
-      td = div_const(mts * ((Fi * (U_star * U_star * U_star)) / ((2.65 - 1) * kG)) * Wi_star,
-                     DX, c.rDX);
+      td = ddiv_by(mts * ((Fi * (U_star * U_star * U_star)) / ((2.65 - 1) * kG)) * Wi_star,
+                   c.dxd);
     }
     if (p.einstein) {
-      const double x = div_const(c.einA[n], Bq, rB);
-      td = div_const(div_const(mts * (40 * cube_rn(1 / x)), c.einS[n], c.einRS[n]), DX,
-                     c.rDX);
+      const double x = ddiv_by(c.einA[n], Bd);
+      td = ddiv_by(ddiv_by(mts * (40 * cube_rn(ddiv_rn(1.0, x))), c.einSd[n]), c.dxd);
     }
     if (dgt(td, GRN(c, cell, n))) td = GRN(c, cell, n);
     if (p.isSuspended[n] && n == 1) {
@@ -223,7 +222,7 @@ __device__ double entrain_cell(const hc_view& c, hc_dev* d, size_t cell, double 
       if (!dgt(e0, bed)) {
         temp_dist[n] = 0;
       } else {
-        temp_dist[n] = elevdiff * (temp_dist[n] / temptot3);
+        temp_dist[n] = elevdiff * ddiv_rn(temp_dist[n], temptot3);
         if (dlt0(temp_dist[n])) temp_dist[n] = 0;
       }
       temptot1 += temp_dist[n];
@@ -247,9 +246,9 @@ __device__ double entrain_cell(const hc_view& c, hc_dev* d, size_t cell, double 
           d->alloc_count = 1;
         }
         double factor = 0;
-        if (dgt0(c.vd[(size_t)k * N2 + cell])) factor += 0.75 * tempdir[k] / veltot;
+        if (dgt0(c.vd[(size_t)k * N2 + cell])) factor += ddiv_rn(0.75 * tempdir[k], veltot);
         const double edge2 = c.edge[EX(c, x2, y2)];
-        if (dgt(edge0, edge2)) factor += 0.25 * ((edge0 - edge2) / temptot2);
+        if (dgt(edge0, edge2)) factor += 0.25 * ddiv_rn(edge0 - edge2, temptot2);
         for (int n = 1; n <= HC_G - 1; n++) {
           if (dgt0(temp_dist[n])) {
             if (n == 1 && p.isSuspended[n]) {
@@ -613,11 +612,11 @@ __device__ void slide_GS_rows(const hc_view& c, hc_dev* d, size_t a, ApplyRow& A
       amount = total;
     }
     if (dgt0(total)) {
-      const double rt = 1.0 / total;
+      const hc_divisor td = ddiv_prep(total);
 #pragma unroll
       for (int n = 1; n <= HC_G - 1; n++) {
         const double ga = A.g[n];
-        const double t = amount * div_const(ga, total, rt);
+        const double t = amount * ddiv_by(ga, td);
         B.g[n] += t;
         double na = ga - t;
         if (dlt0(na)) na = 0;
@@ -647,17 +646,17 @@ __device__ void slide_GS_rows(const hc_view& c, hc_dev* d, size_t a, ApplyRow& A
 // false when the raw amount is not positive; otherwise the (possibly zeroed
 // or capped) amount, which the caller applies and hands to slide_GS even
 // when it is zero, as the reference does.
-__device__ __forceinline__ bool lateral_amount(const hc_params& p, double rDX, double mult,
+__device__ __forceinline__ bool lateral_amount(const hc_params& p, const hc_divisor& dxd,
+                                               double mult,
                                                double ts, double tau0, double et3,
                                                const ApplyRow& N, double e0, bool boundary,
                                                double& amt) {
-  const double DX = p.DX;
   const double e_nb = N.elev;
   amt = 0;
   if (dlt(N.h, p.water_depth_erosion_threshold))
-    amt = div_const(mult * p.lateral_constant * tau0 * N.edge * ts, DX, rDX);
+    amt = ddiv_by(mult * p.lateral_constant * tau0 * N.edge * ts, dxd);
   else
-    amt = div_const(p.chann_lateral_erosion * et3 * (e_nb - e0), DX, rDX) * 0.1;
+    amt = ddiv_by(p.chann_lateral_erosion * et3 * (e_nb - e0), dxd) * 0.1;
   if (!dgt0(amt)) return false;
   // amt *= 1 - veg * (1 - veg_lat_restriction): veg is zero (no vegetation)
   if (dlt(e_nb - amt, N.bed) || boundary) amt = 0;
@@ -672,7 +671,7 @@ __device__ __forceinline__ void lateral_step(const hc_view& c, hc_dev* d, double
                                              double& elev_update) {
   const double en = N.elev;
   double amt;
-  if (dgt(en, e0) && lateral_amount(c.p, c.rDX, mult, ts, tau0, et3, N, e0, boundary, amt)) {
+  if (dgt(en, e0) && lateral_amount(c.p, c.dxd, mult, ts, tau0, et3, N, e0, boundary, amt)) {
     elev_update += amt;
     N.elev = en - amt;
     N.dirty = true;
@@ -1105,10 +1104,9 @@ __device__ void slide_GS_w(const hc_view& c, hc_dev* d, size_t a, WRow& A, doubl
       amount = total;
     }
     if (dgt0(total)) {
-      const double rt = 1.0 / total;
       if (fr) {
         const double ga = A.g;
-        const double t = amount * div_const(ga, total, rt);
+        const double t = amount * ddiv_rn(ga, total);
         B.g += t;
         double na = ga - t;
         if (dlt0(na)) na = 0;
@@ -1132,17 +1130,17 @@ __device__ void slide_GS_w(const hc_view& c, hc_dev* d, size_t a, WRow& A, doubl
   }
 }
 
-__device__ __forceinline__ bool lateral_amount_w(const hc_params& p, double rDX, double mult,
+__device__ __forceinline__ bool lateral_amount_w(const hc_params& p, const hc_divisor& dxd,
+                                                 double mult,
                                                  double ts, double tau0, double et3,
                                                  const WRow& N, double e0, bool boundary,
                                                  double& amt) {
-  const double DX = p.DX;
   const double e_nb = N.elev;
   amt = 0;
   if (dlt(N.h, p.water_depth_erosion_threshold))
-    amt = div_const(mult * p.lateral_constant * tau0 * N.edge * ts, DX, rDX);
+    amt = ddiv_by(mult * p.lateral_constant * tau0 * N.edge * ts, dxd);
   else
-    amt = div_const(p.chann_lateral_erosion * et3 * (e_nb - e0), DX, rDX) * 0.1;
+    amt = ddiv_by(p.chann_lateral_erosion * et3 * (e_nb - e0), dxd) * 0.1;
   if (!dgt0(amt)) return false;
   if (dlt(e_nb - amt, N.bed) || boundary) amt = 0;
   if (dgt(amt, p.ERODEFACTOR * 0.1)) amt = p.ERODEFACTOR * 0.1;
@@ -1155,7 +1153,7 @@ __device__ __forceinline__ void lateral_step_w(const hc_view& c, hc_dev* d, doub
                                                bool boundary, double& elev_update) {
   const double en = N.elev;
   double amt;
-  if (dgt(en, e0) && lateral_amount_w(c.p, c.rDX, mult, ts, tau0, et3, N, e0, boundary, amt)) {
+  if (dgt(en, e0) && lateral_amount_w(c.p, c.dxd, mult, ts, tau0, et3, N, e0, boundary, amt)) {
     elev_update += amt;
     N.elev = en - amt;
     N.dirty = true;

@@ -290,7 +290,7 @@ __device__ __forceinline__ void inertial_face(double& q, double& qs, double& vel
     qs = 0;
     return;
   }
-  double slope = div_const(a1 - a0, DX, c.rDX);
+  double slope = ddiv_by(a1 - a0, c.dxd);
   if (edge_slope == 1) slope = p.edgeslope;
   if (edge_slope == -1) slope = zero_minus(p.edgeslope);
   const double ghd = kG * hflow * dt;
@@ -468,7 +468,7 @@ __global__ void __launch_bounds__(256) k_depth_update(const hc_view c, hc_dev* d
   __shared__ bool last;
   if (gated && !d->it_active) return;
   const size_t W = c.W;
-  const double dt = d->s.flow_timestep, DX = c.p.DX, rDX = c.rDX;
+  const double dt = d->s.flow_timestep;
   const bool susp = c.p.isSuspended[1] && !c.p.hydro_only;
   const int nw = d->wet_count;
   // the running maximum is kept as the bits of a non-negative double, which
@@ -478,11 +478,11 @@ __global__ void __launch_bounds__(256) k_depth_update(const hc_view c, hc_dev* d
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nw; k += gridDim.x * blockDim.x) {
     const size_t cell = (size_t)c.wet[k];
     double h = c.h[cell];
-    h += div_const(dt * (c.qx[cell + W] - c.qx[cell] + c.qy[cell + 1] - c.qy[cell]), DX, rDX);
+    h += ddiv_by(dt * (c.qx[cell + W] - c.qx[cell] + c.qy[cell + 1] - c.qy[cell]), c.dxd);
     // hydro-only runs keep Vsusptot at zero (no sediment source exists)
     if (susp)
-      c.vs[cell] += div_const(dt * (c.qxs[cell + W] - c.qxs[cell] + c.qys[cell + 1] - c.qys[cell]),
-                              DX, rDX);
+      c.vs[cell] += ddiv_by(dt * (c.qxs[cell + W] - c.qxs[cell] + c.qys[cell + 1] - c.qys[cell]),
+                            c.dxd);
     nonfinite |= disnan(h);
     if (dgt0(h)) {
       if (dbits(c.elev[cell]) == kNoDataBits) h = 0;

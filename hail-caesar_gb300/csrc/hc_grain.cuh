@@ -115,12 +115,12 @@ HC_DEV void slide_GS_dev(const hc_view& c, hc_dev* d, size_t a, double amount, s
       amount = total;
     }
     if (total > 0) {
-      // grain/total for the nine fractions: one reciprocal, then the exact
-      // quotient of each (div_const)
-      const double rt = 1.0 / total;
+      // grain/total for the nine fractions: one prepared divisor, then the
+      // exact quotient of each (ddiv_by)
+      const hc_divisor td = ddiv_prep(total);
       for (int n = 1; n <= HC_G - 1; n++) {
         const double ga = GRN(c, a, n);
-        double t = amount * div_const(ga, total, rt);
+        double t = amount * ddiv_by(ga, td);
         GRN(c, b, n) += t;
         double na = ga - t;
         if (na < 0) na = 0;
@@ -150,10 +150,10 @@ HC_DEV void slide_GS_dev(const hc_view& c, hc_dev* d, size_t a, double amount, s
     for (int n = 1; n <= HC_G - 1; n++)
       if (GRN(c, a, n) > 0) total += GRN(c, a, n);
     if (total > 0) {
-      const double rt = 1.0 / total;
+      const hc_divisor td = ddiv_prep(total);
       for (int n = 1; n <= HC_G - 1; n++) {
         const double ga = GRN(c, a, n);
-        const double t = amount * div_const(ga, total, rt);
+        const double t = amount * ddiv_by(ga, td);
         GRN(c, b, n) += t;
         double na = ga;
         if (na > 0.0001) na -= t;

@@ -101,10 +101,20 @@ struct hc_drain_aux {
   unsigned int hist[256];
 };
 
+// A divisor prepared for ddiv_by (below): its significand, exponent and a
+// 64-bit reciprocal of the significand.
+struct hc_divisor {
+  unsigned long long mb, V;  // significand of b, ~2^116/mb (unused when mb == 2^52)
+  double b;
+  int eb;                    // biased exponent of b
+  int ok;                    // b normal and finite
+};
+
 // Everything a kernel needs, passed by value (device pointers + parameters).
 struct hc_view {
   hc_params p;
   double rDX;             // RN(1/DX), for div_const
+  hc_divisor dxd;         // DX as a divisor (ddiv_by)
   float DXf, flf;         // DX and froude_limit as floats (estimates only)
   float act_hi, act_lo;   // (float)(active*1.5), (float)(active/4): sort_active's estimates
   long long thr_key;      // dkey(hflow_threshold)
@@ -137,6 +147,7 @@ struct hc_view {
   // reference's expressions (:4393-4394): (2650-1000)*Di, the square root
   // sqrt(1000/((2250-1000)*g*Di^3)) and its reciprocal
   double einA[HC_G], einS[HC_G], einRS[HC_G];
+  hc_divisor einSd[HC_G];  // the einS as divisors
 
   // scratch
   double *erodetot, *erodetot3;  // N2 each
@@ -298,25 +309,21 @@ HC_DEV double div_const(double x, double y, double r) {
 // floor(ma V / 2^64) is q or q - 1, and the remainder settles it.  Operands
 // that are zero, subnormal, infinite or NaN, and quotients that would leave
 // the normal range, take the hardware division.
-HC_DEV double ddiv_rn(double a, double b) {
-  const unsigned long long A = (unsigned long long)__double_as_longlong(a);
+//
+// An hc_divisor holds the divisor's part (V), so quotients by one divisor
+// share it: ddiv_prep(b) once, then ddiv_by(a, d) per dividend.  Divisors
+// fixed for a run are prepared on the host (host_divisor, exact V).
+HC_DEV hc_divisor ddiv_prep(double b) {
   const unsigned long long B = (unsigned long long)__double_as_longlong(b);
   const unsigned long long M52 = (1ull << 52) - 1, H52 = 1ull << 52;
-  const int ea = (int)(A >> 52) & 0x7ff, eb = (int)(B >> 52) & 0x7ff;
-  unsigned long long ma = (A & M52) | H52;
+  hc_divisor d;
+  d.b = b;
+  d.eb = (int)(B >> 52) & 0x7ff;
+  d.ok = d.eb != 0 && d.eb != 0x7ff;
   const unsigned long long mb = (B & M52) | H52;
-  int er = ea - eb + 1023;
-  if (ma < mb) {
-    ma <<= 1;
-    er--;
-  }
-  if (ea == 0 || ea == 0x7ff || eb == 0 || eb == 0x7ff || er < 1 || er > 2045)
-    return __ddiv_rn(a, b);
-  unsigned long long q, r;
-  if (mb == H52) {  // b a power of two: exact
-    q = ma;
-    r = 0;
-  } else {
+  d.mb = mb;
+  d.V = 0;
+  if (mb != H52) {
     // float estimate of 2^83/mb from the top 24 bits of mb, as an integer
     const float fm = __uint_as_float(0x3f800000u | (unsigned)((mb >> 29) & 0x7fffffu));
     float rf;
@@ -334,8 +341,29 @@ HC_DEV double ddiv_rn(double a, double b) {
     const unsigned long long e_lo = 0ull - qlo;
     const unsigned long long e_hi = H52 - qhi - (qlo != 0 ? 1ull : 0ull);
     const unsigned long long e_s = (e_hi << 44) | (e_lo >> 20);
-    V += __umul64hi(V, e_s) >> 32;
-    q = __umul64hi(ma, V);
+    d.V = V + (__umul64hi(V, e_s) >> 32);
+  }
+  return d;
+}
+
+HC_DEV double ddiv_by(double a, const hc_divisor& d) {
+  const unsigned long long A = (unsigned long long)__double_as_longlong(a);
+  const unsigned long long M52 = (1ull << 52) - 1, H52 = 1ull << 52;
+  const int ea = (int)(A >> 52) & 0x7ff;
+  unsigned long long ma = (A & M52) | H52;
+  const unsigned long long mb = d.mb;
+  int er = ea - d.eb + 1023;
+  if (ma < mb) {
+    ma <<= 1;
+    er--;
+  }
+  if (!d.ok || ea == 0 || ea == 0x7ff || er < 1 || er > 2045) return __ddiv_rn(a, d.b);
+  unsigned long long q, r;
+  if (mb == H52) {  // b a power of two: exact
+    q = ma;
+    r = 0;
+  } else {
+    q = __umul64hi(ma, d.V);
     r = (ma << 52) - q * mb;
     if (r >= mb) {
       r -= mb;
@@ -352,9 +380,15 @@ HC_DEV double ddiv_rn(double a, double b) {
     q = H52;
     er++;
   }
-  const unsigned long long sgn = (A ^ B) & 0x8000000000000000ull;
+  const unsigned long long sgn = (A ^ (unsigned long long)__double_as_longlong(d.b)) &
+                                 0x8000000000000000ull;
   return __longlong_as_double((long long)(sgn | ((unsigned long long)er << 52) | (q & M52)));
 }
+
+HC_DEV double ddiv_rn(double a, double b) { return ddiv_by(a, ddiv_prep(b)); }
+
+// hc_divisor for a divisor fixed for the run, V exact (floor(2^116/mb))
+hc_divisor host_divisor(double b);
 
 // A float within a relative 2^-20 of |x| (or 0 / +inf when |x| is outside
 // the float normal range), built with integer operations only: the FP64

@@ -1,8 +1,10 @@
-// Test driver: the library's integer-pipe division (ddiv_rn in
+// Test driver: the library's integer-pipe division (ddiv_rn, ddiv_by in
 // hc_internal.cuh) against the hardware's IEEE division, bit for bit, over
-// several input families; and the throughput of both.  Built by
+// several input families, with divisors prepared on the device and on the
+// host; and the throughput of both.  Built by
 // test_gpu_arith.py with the library's own compiler flags.
 #include <cstdint>
+#include <cstring>
 
 #include "../hail-caesar_gb300/csrc/hc_internal.cuh"
 
@@ -82,6 +84,29 @@ __global__ void k_check(unsigned long long n, unsigned long long seed, int mode,
   }
 }
 
+// quotients by divisors prepared on the host (exact reciprocal), as the
+// library prepares DX and the Einstein constants
+__global__ void k_check_prepared(unsigned long long n, unsigned long long seed,
+                                 const hc_divisor* tab, int ntab, unsigned long long* bad,
+                                 double* first) {
+  for (unsigned long long k = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; k < n;
+       k += (unsigned long long)gridDim.x * blockDim.x) {
+    const unsigned long long r1 = mix(k + seed * 0x100000000ull);
+    const hc_divisor& d = tab[(r1 >> 40) % ntab];
+    const double a = ((r1 & 7) == 0) ? __longlong_as_double((long long)mix(r1))
+                                     : mk(r1 >> 63, 1023 - 60 + (int)((r1 >> 52) & 127), mix(r1));
+    const double x = ddiv_by(a, d), y = __ddiv_rn(a, d.b);
+    const bool same = __double_as_longlong(x) == __double_as_longlong(y) ||
+                      (disnan(x) && disnan(y));
+    if (!same && atomicAdd(bad, 1ull) == 0) {
+      first[0] = a;
+      first[1] = d.b;
+      first[2] = x;
+      first[3] = y;
+    }
+  }
+}
+
 // throughput: each thread divides independent operands kIter times
 template <bool kInt>
 __global__ void k_time(const double* in, double* out, int iters) {
@@ -111,6 +136,59 @@ extern "C" int arith_check(unsigned long long n, unsigned long long seed, int mo
   const cudaError_t e = cudaGetLastError();
   cudaFree(d_bad);
   cudaFree(d_first);
+  return e == cudaSuccess ? 0 : 2;
+}
+
+// the host preparation of a divisor (exact floor(2^116/mb))
+static hc_divisor prepare(double b) {
+  unsigned long long B;
+  memcpy(&B, &b, 8);
+  const unsigned long long H52 = 1ull << 52;
+  hc_divisor d;
+  d.b = b;
+  d.eb = (int)(B >> 52) & 0x7ff;
+  d.ok = d.eb != 0 && d.eb != 0x7ff;
+  d.mb = (B & (H52 - 1)) | H52;
+  d.V = (d.mb == H52) ? 0 : (unsigned long long)(((unsigned __int128)1 << 116) / d.mb);
+  return d;
+}
+
+extern "C" int arith_check_prepared(unsigned long long n, unsigned long long seed,
+                                    unsigned long long* bad, double* first) {
+  const int ntab = 4099;
+  hc_divisor* h = new hc_divisor[ntab];
+  unsigned long long x = seed;
+  for (int k = 0; k < ntab; k++) {
+    x = x * 6364136223846793005ull + 1442695040888963407ull;
+    double b;
+    if (k < 8) {
+      const double fixed[8] = {1.0, 2.0, 10.0, 20.0, 9.81, 0.5, 3.0, 1e-3};
+      b = fixed[k];
+    } else {
+      const unsigned long long e = 1023 - 40 + ((x >> 33) % 80);
+      const unsigned long long m = (k % 5 == 0) ? ((x >> 11) & 0xff) : (x >> 12);
+      const unsigned long long bits = (e << 52) | (m & ((1ull << 52) - 1));
+      memcpy(&b, &bits, 8);
+    }
+    h[k] = prepare(b);
+  }
+  hc_divisor* tab;
+  unsigned long long* d_bad;
+  double* d_first;
+  if (cudaMalloc(&tab, ntab * sizeof(hc_divisor)) != cudaSuccess ||
+      cudaMalloc(&d_bad, 8) != cudaSuccess || cudaMalloc(&d_first, 32) != cudaSuccess)
+    return 1;
+  cudaMemcpy(tab, h, ntab * sizeof(hc_divisor), cudaMemcpyHostToDevice);
+  cudaMemset(d_bad, 0, 8);
+  cudaMemset(d_first, 0, 32);
+  k_check_prepared<<<152 * 16, 256>>>(n, seed, tab, ntab, d_bad, d_first);
+  cudaMemcpy(bad, d_bad, 8, cudaMemcpyDeviceToHost);
+  cudaMemcpy(first, d_first, 32, cudaMemcpyDeviceToHost);
+  const cudaError_t e = cudaGetLastError();
+  cudaFree(tab);
+  cudaFree(d_bad);
+  cudaFree(d_first);
+  delete[] h;
   return e == cudaSuccess ? 0 : 2;
 }
 

@@ -25,6 +25,8 @@ def arith(tmp_path_factory):
     lib = C.CDLL(so)
     lib.arith_check.argtypes = [C.c_uint64, C.c_uint64, C.c_int, C.POINTER(C.c_uint64),
                                 C.POINTER(C.c_double)]
+    lib.arith_check_prepared.argtypes = [C.c_uint64, C.c_uint64, C.POINTER(C.c_uint64),
+                                         C.POINTER(C.c_double)]
     lib.arith_time.argtypes = [C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float)]
     return lib
 
@@ -34,6 +36,16 @@ def test_division_matches_hardware(arith, mode):
     bad = C.c_uint64(0)
     first = (C.c_double * 4)()
     assert arith.arith_check(1 << 30, 1 + mode, mode, C.byref(bad), first) == 0
+    assert bad.value == 0, "%d mismatches; first a=%r b=%r got %r want %r" % (
+        bad.value, first[0], first[1], first[2], first[3])
+
+
+def test_division_by_prepared_divisors(arith):
+    """Divisors prepared on the host (exact reciprocal), as DX and the
+    Einstein constants are."""
+    bad = C.c_uint64(0)
+    first = (C.c_double * 4)()
+    assert arith.arith_check_prepared(1 << 30, 99, C.byref(bad), first) == 0
     assert bad.value == 0, "%d mismatches; first a=%r b=%r got %r want %r" % (
         bad.value, first[0], first[1], first[2], first[3])
 
