@@ -480,6 +480,8 @@ __global__ void __launch_bounds__(256) k_apply_pre(const hc_view c, hc_dev* d) {
     d->ychains = 0;
     d->xresume = 0;
     d->yresume = 0;
+    d->xtake = 0;
+    d->ytake = 0;
   }
   if (y > c.jmax - 1 || x > c.imax) return;
   const size_t cell = (size_t)x * c.W + y;
@@ -826,8 +828,24 @@ __device__ __forceinline__ void stage_take(const StagedRow* st, size_t cell, App
   mask = ((st->mword >> (8 * (unsigned)(cell & 3))) & 0xffu) != 0;
 }
 
+// The next chain for the lanes of a warp that need one (one atomic per
+// warp): the chains are taken in list order as lanes free up, so a lane
+// whose chain ended does not wait for the longest chain of its warp.
+// Returns the chain number (>= nch: none left).
+__device__ __forceinline__ unsigned take_chain(unsigned* counter, bool need) {
+  const unsigned lane = threadIdx.x & 31;
+  const unsigned b = __ballot_sync(0xffffffffu, need);
+  if (!b) return ~0u;
+  const unsigned leader = __ffs(b) - 1;
+  unsigned base = 0;
+  if (lane == leader) base = atomicAdd(counter, (unsigned)__popc(b));
+  base = __shfl_sync(0xffffffffu, base, leader);
+  return base + __popc(b & ((1u << lane) - 1));
+}
+
 // chains along the columns, one per thread (many chains): rows r-1, r, r+1
-// held in U, C, D
+// held in U, C, D; one row per turn of the loop, a new chain as soon as the
+// lane's chain ends
 __global__ void __launch_bounds__(128) k_apply_xchains_t(const hc_view c, hc_dev* d) {
   __shared__ StagedRow slots[128];
   if (!(d->it_active && d->rest_active && d->do_erode) || d->erode_retry) return;
@@ -838,78 +856,91 @@ __global__ void __launch_bounds__(128) k_apply_xchains_t(const hc_view c, hc_dev
   const double thr = c.p.water_depth_erosion_threshold;
   const size_t W = c.W;
   auto active = [&](bool m, double h, int x) { return m && dgt(h, thr) && x < c.imax && x > 1; };
-  for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < nch; k += gridDim.x * blockDim.x) {
-    size_t cell = c.chains[k];
-    const int y = (int)(cell % W);
-    int r = (int)(cell / W);
-    ApplyRow U, C, D;
-    double Cpre[HC_G + 1], Dpre[HC_G + 1];
-    double Ctau, Css, Cet3, Dtau = 0, Dss = 0;
-    bool Cm, Dm;
-    bool hasU = false;
-    size_t ucell = 0;
-    stage_issue(c, st, cell, EX(c, r, y), true);
-    stage_take(st, cell, C, Cpre, Ctau, Css, Cet3, Cm);
-    bool Cact = active(Cm, C.h, r);
-    if (r + 1 <= c.imax) stage_issue(c, st, cell + W, EX(c, r + 1, y), true);
-    int steps = 0;
-    for (;;) {
-      const bool hasD = r + 1 <= c.imax;
-      const size_t dcell = cell + W;
-      double Det3 = 0;
-      bool Dact = false;
-      if (hasD) {
-        stage_take(st, dcell, D, Dpre, Dtau, Dss, Det3, Dm);
-        Dact = active(Dm, D.h, r + 1);
-        // row r+2 is copied while row r is worked on
-        if (r + 2 <= c.imax) stage_issue(c, st, dcell + W, EX(c, r + 2, y), true);
+  ApplyRow U, C, D;
+  double Cpre[HC_G + 1], Dpre[HC_G + 1];
+  double Ctau = 0, Css = 0, Cet3 = 0;
+  bool Cm, Dm, Cact = false, hasU = false;
+  size_t cell = 0, ucell = 0;
+  int y = 0, r = 0, steps = 0;
+  bool live = false, done = false;
+  for (;;) {
+    const unsigned k = take_chain(&d->xtake, !live && !done);
+    if (!live && !done) {
+      if (k < nch) {
+        cell = c.chains[k];
+        y = (int)(cell % W);
+        r = (int)(cell / W);
+        stage_issue(c, st, cell, EX(c, r, y), true);
+        stage_take(st, cell, C, Cpre, Ctau, Css, Cet3, Cm);
+        Cact = active(Cm, C.h, r);
+        if (r + 1 <= c.imax) stage_issue(c, st, cell + W, EX(c, r + 1, y), true);
+        steps = 0;
+        hasU = false;
+        live = true;
+      } else {
+        done = true;
       }
-      if (Cact) {
-        const double e0 = gather_row(c, d, cell, C, Cpre, Css);
-        if (dgt0(Cet3)) {
-          double elev_update = 0;
-          if (r > 2 && hasU)
-            lateral_step(c, d, mult, ts, Ctau, Cet3, cell, C, e0, ucell, U, r - 1 == 1,
-                         elev_update);
-          if (r < c.imax - 1 && hasD)
-            lateral_step(c, d, mult, ts, Ctau, Cet3, cell, C, e0, dcell, D, r + 1 == c.imax,
-                         elev_update);
-          C.elev = C.elev + elev_update;
-        }
-      }
-      if (hasU) row_store(c, ucell, U);  // row r-1 is final
-      if (!(dgt0(Cet3) || dgt0(Det3)) || !hasD) {
-        row_store(c, cell, C);
-        if (hasD) row_store(c, dcell, D);
-        cp_async_wait_all();  // the slot is free for the next chain
-        break;
-      }
-      if (++steps >= kHandOff) {  // a long chain: the warp walkers go on from row r+1
-        row_store(c, cell, C);
-        row_store(c, dcell, D);
-        cp_async_wait_all();
-        const unsigned m = atomicAdd(&d->xresume, 1u);
-        c.chains[2 * c.N2 + m] = (uint32_t)dcell | kResumeU;
-        break;
-      }
-      U = C;
-      hasU = true;
-      ucell = cell;
-      C = D;
-#pragma unroll
-      for (int n = 0; n <= HC_G; n++) Cpre[n] = Dpre[n];
-      Ctau = Dtau;
-      Css = Dss;
-      Cet3 = Det3;
-      Cact = Dact;
-      cell = dcell;
-      r++;
     }
+    if (!__any_sync(0xffffffffu, live)) break;
+    if (!live) continue;
+    const bool hasD = r + 1 <= c.imax;
+    const size_t dcell = cell + W;
+    double Det3 = 0, Dtau = 0, Dss = 0;
+    bool Dact = false;
+    if (hasD) {
+      stage_take(st, dcell, D, Dpre, Dtau, Dss, Det3, Dm);
+      Dact = active(Dm, D.h, r + 1);
+      // row r+2 is copied while row r is worked on
+      if (r + 2 <= c.imax) stage_issue(c, st, dcell + W, EX(c, r + 2, y), true);
+    }
+    if (Cact) {
+      const double e0 = gather_row(c, d, cell, C, Cpre, Css);
+      if (dgt0(Cet3)) {
+        double elev_update = 0;
+        if (r > 2 && hasU)
+          lateral_step(c, d, mult, ts, Ctau, Cet3, cell, C, e0, ucell, U, r - 1 == 1,
+                       elev_update);
+        if (r < c.imax - 1 && hasD)
+          lateral_step(c, d, mult, ts, Ctau, Cet3, cell, C, e0, dcell, D, r + 1 == c.imax,
+                       elev_update);
+        C.elev = C.elev + elev_update;
+      }
+    }
+    if (hasU) row_store(c, ucell, U);  // row r-1 is final
+    if (!(dgt0(Cet3) || dgt0(Det3)) || !hasD) {
+      row_store(c, cell, C);
+      if (hasD) row_store(c, dcell, D);
+      cp_async_wait_all();  // the slot is free for the next chain
+      live = false;
+      continue;
+    }
+    if (++steps >= kHandOff) {  // a long chain: the warp walkers go on from row r+1
+      row_store(c, cell, C);
+      row_store(c, dcell, D);
+      cp_async_wait_all();
+      const unsigned m = atomicAdd(&d->xresume, 1u);
+      c.chains[2 * c.N2 + m] = (uint32_t)dcell | kResumeU;
+      live = false;
+      continue;
+    }
+    U = C;
+    hasU = true;
+    ucell = cell;
+    C = D;
+#pragma unroll
+    for (int n = 0; n <= HC_G; n++) Cpre[n] = Dpre[n];
+    Ctau = Dtau;
+    Css = Dss;
+    Cet3 = Det3;
+    Cact = Dact;
+    cell = dcell;
+    r++;
   }
 }
 
 // chains along the rows for the +/-y pass: columns q-1, q, q+1 held in
-// U, C, D
+// U, C, D; one column per turn of the loop, a new chain as soon as the
+// lane's chain ends
 __global__ void __launch_bounds__(128) k_apply_ychains_t(const hc_view c, hc_dev* d) {
   __shared__ StagedRow slots[128];
   if (!(d->it_active && d->rest_active && d->do_erode) || d->erode_retry) return;
@@ -918,60 +949,74 @@ __global__ void __launch_bounds__(128) k_apply_ychains_t(const hc_view c, hc_dev
   const unsigned nch = d->ychains;
   const double mult = d->mult, ts = d->s.time_step;
   const size_t W = c.W;
-  for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < nch; k += gridDim.x * blockDim.x) {
-    size_t cell = c.chains[c.N2 + k];
-    const int x = (int)(cell / W);
-    int q = (int)(cell % W);
-    auto lat = [&](int qq, bool m, double et3) { return qq >= 2 && qq <= c.jmax - 1 && m && dgt0(et3); };
-    ApplyRow U, C, D;
-    double Ctau, Css, Cet3, Dtau, Dss, Det3, t0, t1, t2;
-    bool Cm, Dm, m0;
-    stage_issue(c, st, cell - 1, EX(c, x, q - 1), false);
-    stage_take(st, cell - 1, U, nullptr, t0, t1, t2, m0);
-    stage_issue(c, st, cell, EX(c, x, q), false);
-    stage_take(st, cell, C, nullptr, Ctau, Css, Cet3, Cm);
-    bool Clat = lat(q, Cm, Cet3);
-    stage_issue(c, st, cell + 1, EX(c, x, q + 1), false);  // q + 1 <= jmax
-    int steps = 0;
-    for (;;) {
-      const size_t dcell = cell + 1;
-      stage_take(st, dcell, D, nullptr, Dtau, Dss, Det3, Dm);
-      const bool Dlat = lat(q + 1, Dm, Det3);
-      if (q + 2 <= c.jmax) stage_issue(c, st, dcell + 1, EX(c, x, q + 2), false);
-      if (Clat) {
-        const double e0 = C.elev;
-        double elev_update = 0;
-        lateral_step(c, d, mult, ts, Ctau, Cet3, cell, C, e0, cell - 1, U, q - 1 == 1,
-                     elev_update);
-        lateral_step(c, d, mult, ts, Ctau, Cet3, cell, C, e0, dcell, D, q + 1 == c.jmax,
-                     elev_update);
-        C.elev = C.elev + elev_update;
-        C.dirty = true;
+  auto lat = [&](int qq, bool m, double et3) { return qq >= 2 && qq <= c.jmax - 1 && m && dgt0(et3); };
+  ApplyRow U, C, D;
+  double Ctau = 0, Css = 0, Cet3 = 0, t0, t1, t2;
+  bool Cm, Dm, m0, Clat = false;
+  size_t cell = 0;
+  int x = 0, q = 0, steps = 0;
+  bool live = false, done = false;
+  for (;;) {
+    const unsigned k = take_chain(&d->ytake, !live && !done);
+    if (!live && !done) {
+      if (k < nch) {
+        cell = c.chains[c.N2 + k];
+        x = (int)(cell / W);
+        q = (int)(cell % W);
+        stage_issue(c, st, cell - 1, EX(c, x, q - 1), false);
+        stage_take(st, cell - 1, U, nullptr, t0, t1, t2, m0);
+        stage_issue(c, st, cell, EX(c, x, q), false);
+        stage_take(st, cell, C, nullptr, Ctau, Css, Cet3, Cm);
+        Clat = lat(q, Cm, Cet3);
+        stage_issue(c, st, cell + 1, EX(c, x, q + 1), false);  // q + 1 <= jmax
+        steps = 0;
+        live = true;
+      } else {
+        done = true;
       }
-      row_store(c, cell - 1, U);  // column q-1 is final
-      if (!(Clat || Dlat) || q + 1 > c.jmax - 1) {
-        row_store(c, cell, C);
-        row_store(c, dcell, D);
-        cp_async_wait_all();
-        break;
-      }
-      if (++steps >= kHandOff) {  // a long chain: the warp walkers go on from column q+1
-        row_store(c, cell, C);
-        row_store(c, dcell, D);
-        cp_async_wait_all();
-        const unsigned m = atomicAdd(&d->yresume, 1u);
-        c.chains[3 * c.N2 + m] = (uint32_t)dcell;
-        break;
-      }
-      U = C;
-      C = D;
-      Ctau = Dtau;
-      Css = Dss;
-      Cet3 = Det3;
-      Clat = Dlat;
-      cell = dcell;
-      q++;
     }
+    if (!__any_sync(0xffffffffu, live)) break;
+    if (!live) continue;
+    const size_t dcell = cell + 1;
+    double Dtau, Dss, Det3;
+    stage_take(st, dcell, D, nullptr, Dtau, Dss, Det3, Dm);
+    const bool Dlat = lat(q + 1, Dm, Det3);
+    if (q + 2 <= c.jmax) stage_issue(c, st, dcell + 1, EX(c, x, q + 2), false);
+    if (Clat) {
+      const double e0 = C.elev;
+      double elev_update = 0;
+      lateral_step(c, d, mult, ts, Ctau, Cet3, cell, C, e0, cell - 1, U, q - 1 == 1,
+                   elev_update);
+      lateral_step(c, d, mult, ts, Ctau, Cet3, cell, C, e0, dcell, D, q + 1 == c.jmax,
+                   elev_update);
+      C.elev = C.elev + elev_update;
+      C.dirty = true;
+    }
+    row_store(c, cell - 1, U);  // column q-1 is final
+    if (!(Clat || Dlat) || q + 1 > c.jmax - 1) {
+      row_store(c, cell, C);
+      row_store(c, dcell, D);
+      cp_async_wait_all();
+      live = false;
+      continue;
+    }
+    if (++steps >= kHandOff) {  // a long chain: the warp walkers go on from column q+1
+      row_store(c, cell, C);
+      row_store(c, dcell, D);
+      cp_async_wait_all();
+      const unsigned m = atomicAdd(&d->yresume, 1u);
+      c.chains[3 * c.N2 + m] = (uint32_t)dcell;
+      live = false;
+      continue;
+    }
+    U = C;
+    C = D;
+    Ctau = Dtau;
+    Css = Dss;
+    Cet3 = Det3;
+    Clat = Dlat;
+    cell = dcell;
+    q++;
   }
 }
 

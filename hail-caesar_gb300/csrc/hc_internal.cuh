@@ -88,6 +88,7 @@ struct hc_dev {
   unsigned int xchains;   // chain starts of the +/-x apply pass (hc_view::chains)
   unsigned int ychains;   // chain starts of the +/-y apply pass
   unsigned int xresume, yresume;  // long chains handed from the thread to the warp walkers
+  unsigned int xtake, ytake;      // chains taken so far by the thread walkers
   unsigned int ent_n;     // cells listed for the transport of an entrainment pass
 };
 
