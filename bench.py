@@ -233,7 +233,7 @@ def run_gpu(args, rank, world, dist):
     out["phases_ms"]["iterations_profiled"] = nprof
     # end-to-end through the public API: one hc_run call per step with the
     # step's record read back to host memory (the drop-in call pattern)
-    e2e_steps = max(3, min(args.steps, 50))
+    e2e_steps = max(3, min(args.steps, 200))
     _, h0, d0 = model.counters()
     t0 = time.perf_counter()
     e0.record(stream)

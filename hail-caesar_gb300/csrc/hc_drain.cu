@@ -207,7 +207,16 @@ struct DrainSync {
   unsigned int gen;
   unsigned int err;
   unsigned int count[3];  // frontier lengths, rotating by level
+  unsigned int solo_level;            // level at which block 0 left its last solo run
+  unsigned int pad;
+  unsigned long long solo_done;       // cells done by then
 };
+
+// Frontiers of at most this many cells are swept by block 0 alone, level
+// after level with block barriers, while the other blocks wait: most
+// frontiers of a catchment hold a few hundred cells, and a grid barrier per
+// level costs more than the work.
+constexpr unsigned kSoloMax = 2048;
 
 __device__ __forceinline__ bool grid_barrier(DrainSync* g, unsigned nblocks) {
   __shared__ bool ok;
@@ -261,28 +270,51 @@ __device__ unsigned drain_cell_g(const hc_view& c, const double* __restrict__ el
   }
   if (pn[4] != 0) {
     double a = (e == -9999) ? 0.0 : 1.0;
-    // higher neighbours the sweep reached, in sweep order: higher elevation
-    // first, equal elevations by sorted position (only in sorted runs)
-    int nb[8];
-    int n = 0;
+    // higher neighbours the sweep reached, taken in sweep order: higher
+    // elevation first, equal elevations by sorted position (only in sorted
+    // runs).  Each is picked by a scan with constant indices, so the
+    // neighbour values stay in registers (indexed arrays went to local
+    // memory, which at this block size lives in L2).
+    long long ek[9];
+    unsigned left = 0;
 #pragma unroll
     for (int kk = 0; kk < 9; kk++) {
-      if (kk == 4 || !(en[kk] > e) || pn[kk] == 0) continue;  // out-of-grid entries equal e
-      int k = n++;
-      while (k > 0 && (en[nb[k - 1]] < en[kk] ||
-                       (en[nb[k - 1]] == en[kk] && pn[nb[k - 1]] < pn[kk]))) {
-        nb[k] = nb[k - 1];
-        k--;
-      }
-      nb[k] = kk;
+      ek[kk] = dkey(en[kk]);
+      if (kk != 4 && ek[kk] > dkey(e) && pn[kk] != 0) left |= 1u << kk;  // out-of-grid: e
     }
-    for (int k = 0; k < n; k++) {
-      const int kk = nb[k];
-      const int iq = i + kk / 3 - 1, jq = j + kk % 3 - 1;
-      const double eq = en[kk], aq = an[kk], dq = dn[kk];
+#pragma unroll 1
+    while (left) {
+      int best = -1;
+      long long bk = 0;
+      unsigned bp = 0;
+      double eq = 0, aq = 0, dq = 1;
+#pragma unroll
+      for (int kk = 0; kk < 9; kk++) {
+        if (!((left >> kk) & 1u)) continue;
+        if (best < 0 || ek[kk] > bk || (ek[kk] == bk && pn[kk] > bp)) {
+          best = kk;
+          bk = ek[kk];
+          bp = pn[kk];
+          eq = en[kk];
+          aq = an[kk];
+          dq = dn[kk];
+        }
+      }
+      left &= ~(1u << best);
+      const int iq = i + best / 3 - 1, jq = j + best % 3 - 1;
+      // the directions of q whose (clamped) step lands here, in order: one
+      // for an interior q, possibly more at the edges; found with integer
+      // tests first, so that the divisions run once per term and not once
+      // per direction of the warp's slowest lane
+      unsigned dirs = 0;
+#pragma unroll 1
       for (int dir = 1; dir <= 8; dir++) {
         const int i3 = clampi(iq + kDrX[dir], 1, c.imax), j3 = clampi(jq + kDrY[dir], 1, c.jmax);
-        if (i3 != i || j3 != j) continue;
+        if (i3 == i && j3 == j) dirs |= 1u << dir;
+      }
+      while (dirs) {
+        const int dir = __ffs(dirs) - 1;
+        dirs &= dirs - 1;
         if (dir % 2 != 0)
           a += aq * ((eq - e) / dq);
         else
@@ -291,13 +323,16 @@ __device__ unsigned drain_cell_g(const hc_view& c, const double* __restrict__ el
     }
     if (a > 0) __stcg(&c.area[cell], a);
   }
-  __threadfence();  // the area is visible before any lower neighbour is released
+  // No fence here: the area is read by the lower neighbours in a later
+  // frontier, after a block barrier (block 0 alone) or a grid barrier, which
+  // order it before those reads.
   // the eight decrements do not depend on one another: issue them together
   int old[9];
 #pragma unroll
   for (int kk = 0; kk < 9; kk++) {
     const int dx = kk / 3 - 1, dy = kk % 3 - 1;
-    old[kk] = (kk != 4 && en[kk] < e) ? atomicSub(&c.drain_pend[(i + dx) * W + (j + dy)], 1) : 0;
+    old[kk] = (kk != 4 && dlt(en[kk], e)) ? atomicSub(&c.drain_pend[(i + dx) * W + (j + dy)], 1)
+                                          : 0;
   }
   unsigned released = 0;
 #pragma unroll
@@ -305,16 +340,53 @@ __device__ unsigned drain_cell_g(const hc_view& c, const double* __restrict__ el
   return released;
 }
 
+// Sweeps one frontier, the threads of [start, start + stride) taking cells
+// start, start + stride, ...; released cells go to fout, counted in *n_out
+// (one atomic per warp).
+__device__ __forceinline__ void drain_frontier(const hc_view& c, const double* __restrict__ el,
+                                               const uint32_t* fin, unsigned n_in,
+                                               uint32_t* fout, unsigned* n_out, unsigned start,
+                                               unsigned stride) {
+  const unsigned lane = threadIdx.x & 31;
+  for (unsigned k0 = start - lane; k0 < n_in; k0 += stride) {
+    const unsigned k = k0 + lane;
+    uint32_t cell = 0;
+    unsigned rel = 0;
+    if (k < n_in) {
+      cell = __ldcg(&fin[k]);
+      rel = drain_cell_g(c, el, cell);
+    }
+    const unsigned cnt = __popc(rel);
+    unsigned incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    unsigned base = 0;
+    if (lane == 31 && incl) base = atomicAdd(n_out, incl);
+    base = __shfl_sync(0xffffffffu, base, 31);
+    unsigned m = base + incl - cnt;
+    const int W = (int)c.W;
+    while (rel) {
+      const int kk = __ffs(rel) - 1;
+      rel &= rel - 1;
+      __stcg(&fout[m++], (uint32_t)((int)cell + (kk / 3 - 1) * W + (kk % 3 - 1)));
+    }
+  }
+}
+
 // All frontiers in one cooperative launch, one grid barrier between
-// frontiers.  Each cell enters exactly one frontier, so at most imax*jmax
-// cells are processed.
-__global__ void __launch_bounds__(512) k_drain_sweep(const hc_view c, hc_dev* d,
+// frontiers, or block 0 alone while they are small.  Each cell enters
+// exactly one frontier, so at most imax*jmax cells are processed.
+__global__ void __launch_bounds__(512, 1) k_drain_sweep(const hc_view c, hc_dev* d,
                                                       const double* __restrict__ el,
                                                       DrainSync* g) {
+  __shared__ unsigned s_cnt;
+  __shared__ bool s_ok;
   const unsigned nblocks = gridDim.x;
   const unsigned gtid = blockIdx.x * blockDim.x + threadIdx.x;
   const unsigned gsize = nblocks * blockDim.x;
-  const unsigned lane = threadIdx.x & 31;
   const unsigned long long M = (unsigned long long)c.imax * c.jmax;
   unsigned long long done = 0;
   unsigned level = 0;
@@ -322,36 +394,57 @@ __global__ void __launch_bounds__(512) k_drain_sweep(const hc_view c, hc_dev* d,
   for (;;) {
     const unsigned cur = level % 3, nxt = (level + 1) % 3;
     const unsigned n_in = *(volatile unsigned*)&g->count[cur];
-    if (n_in == 0) break;
-    const uint32_t* fin = fr[level & 1];
-    uint32_t* fout = fr[(level + 1) & 1];
-    // a warp's released cells are appended with one atomic
-    for (unsigned k0 = gtid - lane; k0 < n_in; k0 += gsize) {
-      const unsigned k = k0 + lane;
-      uint32_t cell = 0;
-      unsigned rel = 0;
-      if (k < n_in) {
-        cell = __ldcg(&fin[k]);
-        rel = drain_cell_g(c, el, cell);
+    if (n_in == 0 || *(volatile unsigned*)&g->err) break;
+    if (n_in <= kSoloMax) {
+      if (blockIdx.x == 0) {
+        unsigned n = n_in;
+        for (;;) {
+          if (threadIdx.x == 0) s_cnt = 0;
+          __syncthreads();
+          drain_frontier(c, el, fr[level & 1], n, fr[(level + 1) & 1], &s_cnt, threadIdx.x,
+                         blockDim.x);
+          __syncthreads();
+          const unsigned nn = s_cnt;
+          __syncthreads();  // all have read s_cnt before it is cleared
+          done += n;
+          level++;
+          n = nn;
+          if (done > M) {  // cannot happen: "higher than" has no cycles
+            if (threadIdx.x == 0) atomicExch(&g->err, 2u);
+            break;
+          }
+          if (n == 0 || n > kSoloMax) break;
+        }
+        if (threadIdx.x == 0) {
+          g->count[level % 3] = n;
+          g->count[(level + 1) % 3] = 0;
+          g->solo_done = done;
+          __threadfence();
+          atomicExch(&g->solo_level, level);  // the other blocks go on from here
+        }
+        __syncthreads();
+      } else {
+        if (threadIdx.x == 0) {
+          s_ok = true;
+          long spins = 0;
+          while (*(volatile unsigned*)&g->solo_level <= level) {
+            if (++spins > (1L << 24) || *(volatile unsigned*)&g->err) {
+              atomicExch(&g->err, 1u);
+              s_ok = false;
+              break;
+            }
+            __nanosleep(256);
+          }
+          __threadfence();
+        }
+        __syncthreads();
+        if (!s_ok) break;
+        level = *(volatile unsigned*)&g->solo_level;
+        done = *(volatile unsigned long long*)&g->solo_done;
       }
-      const unsigned cnt = __popc(rel);
-      unsigned incl = cnt;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const unsigned y = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) incl += y;
-      }
-      unsigned base = 0;
-      if (lane == 31 && incl) base = atomicAdd(&g->count[nxt], incl);
-      base = __shfl_sync(0xffffffffu, base, 31);
-      unsigned m = base + incl - cnt;
-      const int W = (int)c.W;
-      while (rel) {
-        const int kk = __ffs(rel) - 1;
-        rel &= rel - 1;
-        __stcg(&fout[m++], (uint32_t)((int)cell + (kk / 3 - 1) * W + (kk % 3 - 1)));
-      }
+      continue;
     }
+    drain_frontier(c, el, fr[level & 1], n_in, fr[(level + 1) & 1], &g->count[nxt], gtid, gsize);
     if (gtid == 0) g->count[(level + 2) % 3] = 0;  // read two frontiers ago
     done += n_in;
     level++;

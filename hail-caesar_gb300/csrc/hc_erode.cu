@@ -1369,7 +1369,8 @@ __global__ void __launch_bounds__(128) k_apply_ychains_w(const hc_view c, hc_dev
 // ---------------------------------------------------------------------------
 // sediment leaving the edges :4750-4841.  The reference accumulates gtot2 in
 // float, entry by entry in its loop order: the contributions are laid out in
-// that order and each fraction's float sum is run in order by its own thread.
+// that order, one plane per fraction, and each fraction's float sum is run in
+// order by its own warp.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(1024) k_edge_out(const hc_view c, hc_dev* d, double* contrib,
                                                     int32_t* list) {
@@ -1382,6 +1383,7 @@ __global__ void __launch_bounds__(1024) k_edge_out(const hc_view c, hc_dev* d, d
   const int nA = (jmax - 2 > 0) ? 2 * (jmax - 2) : 0;   // y = 2..jmax-1: (imax,y), (1,y)
   const int nB = (imax - 2 > 0) ? 2 * (imax - 2) : 0;   // x = 2..imax-1: (x,jmax), (x,1)
   const int ntot = nA + nB;
+  const size_t cap = (size_t)(2 * (imax + jmax) + 8);  // entries per fraction plane
   // entries handled by this thread: a contiguous chunk, so the block scan
   // below keeps the loop order
   const int per = (ntot + blockDim.x - 1) / blockDim.x;
@@ -1439,7 +1441,7 @@ __global__ void __launch_bounds__(1024) k_edge_out(const hc_view c, hc_dev* d, d
       } else {
         v = SF(c, dir, n, src);
       }
-      contrib[(size_t)o * HC_G + n] = v;
+      contrib[(size_t)n * cap + o] = v;
     }
     o++;
   }
@@ -1465,11 +1467,18 @@ __global__ void __launch_bounds__(1024) k_edge_out(const hc_view c, hc_dev* d, d
   }
   __syncthreads();
   const int total = d->misc_done;
-  if (threadIdx.x >= 1 && threadIdx.x <= HC_G - 1) {
-    const int n = threadIdx.x;
+  // fraction n's sum, by warp n: the warp loads 32 contributions at a time
+  // and every lane adds them in order from registers
+  const int wn = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (wn >= 1 && wn <= HC_G - 1) {
+    const double* cn = contrib + (size_t)wn * cap;
     float g = 0.0f;
-    for (int e = 0; e < total; e++) g = (float)((double)g + contrib[(size_t)e * HC_G + n]);
-    gsum[n] = g;
+    for (int e0 = 0; e0 < total; e0 += 32) {
+      const double v = (e0 + lane < total) ? cn[e0 + lane] : 0.0;
+      const int m = min(32, total - e0);
+      for (int k = 0; k < m; k++) g = (float)((double)g + __shfl_sync(0xffffffffu, v, k));
+    }
+    if (lane == 0) gsum[wn] = g;
   }
   if (threadIdx.x == 0) gsum[0] = 0.0f, gsum[HC_G] = 0.0f;
   __syncthreads();

@@ -154,6 +154,13 @@ __global__ void k_control(const hc_view c, hc_dev* d, hc_iter_handles hh) {
   if (arec)
     for (int i = 0; i <= HC_MAX_RF; i++) arec[3 + i] = (i <= p.rfnum) ? s.j_mean[i] : 0.0;
   d->input_dt = fdt2;
+  // what each input point of a zone receives (:3463-3477), the same for all
+  // points of the zone
+  for (int z = 0; z <= p.rfnum && z <= HC_MAX_RF; z++) {
+    double amt = (d->j_mean_in[z] * s.nActualGridCells[z]) / (s.catchment_input_counter[z]) * fdt2;
+    if (amt > p.ERODEFACTOR) amt = p.ERODEFACTOR;
+    d->input_amt[z] = amt;
+  }
   if (s.cycle >= s.time_1) {
     do {
       s.time_1++;
@@ -226,11 +233,7 @@ __global__ void k_inputs(const hc_view c, hc_dev* d) {
        z += gridDim.x * blockDim.x) {
     const int i = c.cin_x[z], j = c.cin_y[z];
     const size_t cell = (size_t)i * c.W + j;
-    const int rf = c.rfarea[cell];
-    double amt = (d->j_mean_in[rf] * s.nActualGridCells[rf]) / (s.catchment_input_counter[rf]) *
-                 d->input_dt;
-    if (amt > c.p.ERODEFACTOR) amt = c.p.ERODEFACTOR;
-    c.h[cell] += amt;
+    c.h[cell] += d->input_amt[c.rfarea[cell]];
   }
 }
 

@@ -68,6 +68,7 @@ struct hc_dev {
   double reach_dt;        // flow dt used by the water inputs this iteration
   double j_mean_in[HC_MAX_RF + 1];  // j_mean used by the input points
   double input_dt;        // flow dt used by the catchment input points
+  double input_amt[HC_MAX_RF + 1];  // water each input point of a zone receives
   double mult;            // mult_factor of the current erode() call
   unsigned long long maxdepth_bits;  // atomic max of h (positive doubles)
   unsigned long long tempbmax_bits;  // atomic max of temptot1

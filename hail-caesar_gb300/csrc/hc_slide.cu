@@ -93,6 +93,58 @@ __device__ bool slide_visit(const hc_view& c, hc_dev* d, int x, int y, double fa
   return any;
 }
 
+// The visit as the serial replay makes it: the eight neighbours' elevations
+// are loaded together (one round trip instead of eight dependent ones), a
+// diagonal test is first decided on a float estimate and its FP64 division
+// evaluated only near the threshold, and moves update the held values.  The
+// tests, moves and their order are slide_visit's; returns the moved
+// directions.
+__device__ int slide_visit_held(const hc_view& c, hc_dev* d, int x, int y, double factor,
+                                bool global, double* total) {
+  constexpr int dxs[8] = {1, 0, -1, -1, -1, 0, 1, 1};
+  constexpr int dys[8] = {1, 1, 1, 0, -1, -1, -1, 0};
+  const size_t W = c.W;
+  const size_t cell = (size_t)x * W + y;
+  const double active = c.p.active;
+  double en[8];
+#pragma unroll
+  for (int k = 0; k < 8; k++) en[k] = c.elev[(size_t)(x + dxs[k]) * W + (y + dys[k])];
+  double e = c.elev[cell];
+  const double floor_e = c.bed[cell] + active;
+  double wet_factor = factor;
+  if (e <= floor_e) wet_factor = global ? 10 * c.p.DX : 10000;
+  const float wf = approx_f(wet_factor);
+  int moved = 0;
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    const bool diag = dxs[k] != 0 && dys[k] != 0;
+    const double e2 = en[k];
+    if (!(dkey(e2) > kNoDataKey)) continue;  // e2 > -9999
+    double drop;
+    if (diag) {
+      const float est = approx_f(e - e2) * (1.0f / 1.41f);
+      const float m = 1e-4f * (fabsf(est) + fabsf(wf));
+      if (m >= 1e-34f && m < 1e30f && est - wf < -m) continue;  // surely not above
+      drop = (e - e2) / 1.41;
+    } else {
+      drop = e - e2;
+    }
+    if (!dgt(drop, wet_factor)) continue;
+    double diff = drop - wet_factor;
+    if ((e - diff) < floor_e) diff = (e - floor_e);
+    if (global && diff > c.p.ERODEFACTOR) diff = c.p.ERODEFACTOR;
+    const size_t nb = (size_t)(x + dxs[k]) * W + (y + dys[k]);
+    e = e - diff;
+    en[k] = e2 + diff;
+    c.elev[cell] = e;
+    c.elev[nb] = en[k];
+    if (global) *total += diff;
+    else slide_GS_dev(c, d, cell, diff, nb, true);
+    moved |= 1 << k;
+  }
+  return moved;
+}
+
 // Phase 1: flag every loop position whose visit would move something now.
 __global__ void k_slide_probe(const hc_view c, const hc_dev* d, uint8_t* flag, int global,
                               double factor, int gated) {
@@ -277,8 +329,7 @@ __global__ void k_slide_replay(const hc_view c, hc_dev* d, const int32_t* list, 
       if (xc == c.imax) xc = c.imax - 1;
       if (xc == 1) xc = 2;
     }
-    int moved = 0;
-    slide_visit(c, d, xc, y, factor, global != 0, false, &total, &moved);
+    const int moved = slide_visit_held(c, d, xc, y, factor, global != 0, &total);
     if (moved) push_affected(c, d, o, xc, y, cand, global != 0, heap, hn, heap_cap);
     if (d->err_code == 301 && err0 != 301) {
       // heap overflow: finish the sweep visiting every later position
@@ -289,7 +340,7 @@ __global__ void k_slide_replay(const hc_view c, hc_dev* d, const int32_t* list, 
         if (global) {
           if (xx > c.imax - 1) break;
           if (yy < 2 || yy > c.jmax - 1 || xx < 2) continue;
-          slide_visit(c, d, xx, yy, factor, true, false, &total, nullptr);
+          slide_visit_held(c, d, xx, yy, factor, true, &total);
         } else {
           if (yy > c.jmax - 1) break;
           if (xx < 1 || xx > c.imax || yy < 2) continue;
@@ -297,7 +348,7 @@ __global__ void k_slide_replay(const hc_view c, hc_dev* d, const int32_t* list, 
           int x3 = xx;
           if (x3 == c.imax) x3 = c.imax - 1;
           if (x3 == 1) x3 = 2;
-          slide_visit(c, d, x3, yy, factor, false, false, &total, nullptr);
+          slide_visit_held(c, d, x3, yy, factor, false, &total);
         }
       }
       break;
