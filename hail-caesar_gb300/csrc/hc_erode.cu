@@ -681,6 +681,25 @@ __device__ __forceinline__ void lateral_step(const hc_view& c, hc_dev* d, double
   }
 }
 
+// The lateral steps of C toward U, then toward D, through one copy of the
+// step's code (the side's row goes through N): the walkers are bound by
+// latency and instruction fetch, not by registers moves.
+__device__ __forceinline__ void lateral_both(const hc_view& c, hc_dev* d, double mult, double ts,
+                                             double tau0, double et3, size_t ccell, ApplyRow& C,
+                                             double e0, bool doU, size_t ucell, ApplyRow& U,
+                                             bool bU, bool doD, size_t dcell, ApplyRow& D,
+                                             bool bD, double& elev_update) {
+#pragma unroll 1
+  for (int side = 0; side < 2; side++) {
+    if (!(side == 0 ? doU : doD)) continue;
+    ApplyRow N = (side == 0) ? U : D;
+    lateral_step(c, d, mult, ts, tau0, et3, ccell, C, e0, side == 0 ? ucell : dcell, N,
+                 side == 0 ? bU : bD, elev_update);
+    if (side == 0) U = N;
+    else D = N;
+  }
+}
+
 // the gather of an active cell (:4579-4628): grain += incoming - outgoing,
 // elev += erodetot, sort_active when the cell lost material.  Returns the
 // new elevation.
@@ -897,12 +916,9 @@ __global__ void __launch_bounds__(128) k_apply_xchains_t(const hc_view c, hc_dev
       const double e0 = gather_row(c, d, cell, C, Cpre, Css);
       if (dgt0(Cet3)) {
         double elev_update = 0;
-        if (r > 2 && hasU)
-          lateral_step(c, d, mult, ts, Ctau, Cet3, cell, C, e0, ucell, U, r - 1 == 1,
-                       elev_update);
-        if (r < c.imax - 1 && hasD)
-          lateral_step(c, d, mult, ts, Ctau, Cet3, cell, C, e0, dcell, D, r + 1 == c.imax,
-                       elev_update);
+        lateral_both(c, d, mult, ts, Ctau, Cet3, cell, C, e0, r > 2 && hasU, ucell, U,
+                     r - 1 == 1, r < c.imax - 1 && hasD, dcell, D, r + 1 == c.imax,
+                     elev_update);
         C.elev = C.elev + elev_update;
       }
     }
@@ -985,10 +1001,8 @@ __global__ void __launch_bounds__(128) k_apply_ychains_t(const hc_view c, hc_dev
     if (Clat) {
       const double e0 = C.elev;
       double elev_update = 0;
-      lateral_step(c, d, mult, ts, Ctau, Cet3, cell, C, e0, cell - 1, U, q - 1 == 1,
-                   elev_update);
-      lateral_step(c, d, mult, ts, Ctau, Cet3, cell, C, e0, dcell, D, q + 1 == c.jmax,
-                   elev_update);
+      lateral_both(c, d, mult, ts, Ctau, Cet3, cell, C, e0, true, cell - 1, U, q - 1 == 1, true,
+                   dcell, D, q + 1 == c.jmax, elev_update);
       C.elev = C.elev + elev_update;
       C.dirty = true;
     }
