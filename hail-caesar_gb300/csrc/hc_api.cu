@@ -283,6 +283,7 @@ extern "C" hc_status hc_create(const hc_params* p, size_t max_bytes, hc_ctx** ou
   A(v.cin_x, (size_t)p->imax * p->jmax + 2) A(v.cin_y, (size_t)p->imax * p->jmax + 2)
   A(v.wet, N2) A(v.wet_sums, (N2 + 1023) / 1024 + 1)
   A(v.drain_pos, N2) A(v.drain_f0, N2) A(v.drain_f1, N2) A(v.drain_pend, N2) A(v.drain_dt, N2)
+  A(v.drain_frac, 9 * N2) A(v.drain_multi, N2)
   A(v.drain_aux, 1)
   if (sed) {
     A(v.sflux, 40 * N2) A(v.grain, 11 * N2) A(v.strata, 90 * N2) A(v.alloc_key, N2)
@@ -367,7 +368,7 @@ static hc_status free_all(hc_ctx* c) {
   void* ptrs[] = {v.elev, v.h, v.qx, v.qy, v.qxs, v.qys, v.vs, v.vel, v.tau, v.bed, v.man,
                   v.area, v.ss, v.vd, v.sflux, v.grain, v.strata, v.index, v.mask, v.rfarea,
                   v.edge, v.edge2, v.veg, v.cin_x, v.cin_y, v.erodetot, v.erodetot3, v.pre,
-                  v.chains, v.ent_list, v.drain_pos, v.drain_f0, v.drain_f1, v.drain_pend, v.drain_dt,
+                  v.chains, v.ent_list, v.drain_pos, v.drain_f0, v.drain_f1, v.drain_pend, v.drain_dt, v.drain_frac, v.drain_multi,
                   v.drain_snap, v.drain_aux, v.alloc_key, v.red, v.touched, v.topm, v.rain, v.rec, c->dev, v.wet,
                   v.wet_sums,
                   v.reach[0], v.reach[1], v.reach[2], extra(c).lateral};

@@ -199,6 +199,44 @@ __global__ void k_drain_init(const hc_view c, hc_dev* d, const double* __restric
   }
 }
 
+// The share of each higher neighbour's area that reaches this cell, before
+// the sweep: the reference's term (e_q - e)/difftot_q, or its diagonal form
+// ((e_q - e)/1.414)/difftot_q, for the first direction of q whose (clamped)
+// step lands here; neighbours with more than one such direction (at the
+// edges) are marked and summed term by term in the sweep.  The sweep then
+// adds aq * share, the reference's operations on the same values, and its
+// critical path has no division (about 600 cycles each on this GPU's FP64
+// pipe, against 128 for a multiply and an add).
+__global__ void k_drain_frac(const hc_view c, const double* __restrict__ el) {
+  int i, j;
+  if (!interior_ij(c, i, j)) return;
+  const size_t W = c.W, N2 = c.N2;
+  const size_t cell = (size_t)i * W + j;
+  const double e = el[cell];
+  unsigned multi = 0;
+  for (int kk = 0; kk < 9; kk++) {
+    double g = 0;
+    const int iq = i + kk / 3 - 1, jq = j + kk % 3 - 1;
+    if (kk != 4 && iq >= 1 && iq <= c.imax && jq >= 1 && jq <= c.jmax) {
+      const size_t q = (size_t)iq * W + jq;
+      const double eq = el[q];
+      if (eq > e) {
+        const double dq = c.drain_dt[q];
+        int found = 0;
+        for (int dir = 1; dir <= 8; dir++) {
+          const int i3 = clampi(iq + kDrX[dir], 1, c.imax), j3 = clampi(jq + kDrY[dir], 1, c.jmax);
+          if (i3 != i || j3 != j) continue;
+          if (found == 0) g = (dir % 2 != 0) ? ((eq - e) / dq) : (((eq - e) / 1.414) / dq);
+          found++;
+        }
+        if (found > 1) multi |= 1u << kk;
+      }
+    }
+    c.drain_frac[(size_t)kk * N2 + cell] = g;
+  }
+  c.drain_multi[cell] = (uint16_t)multi;
+}
+
 // Grid-wide barrier for k_drain_sweep, which is launched cooperatively (all
 // blocks resident).  Sense by generation count; every wait is bounded: a
 // block that gives up raises err and the sweep ends with an error status.
@@ -254,20 +292,24 @@ __device__ unsigned drain_cell_g(const hc_view& c, const double* __restrict__ el
   const int W = (int)c.W;
   const int i = (int)(cell / W), j = (int)(cell % W);
   const double e = el[cell];
-  // every neighbour's elevation, sweep position, area and drop sum, loaded
-  // together (one round trip instead of three dependent ones)
-  double en[9], an[9], dn[9];
+  // every neighbour's elevation, sweep position, area and share of its
+  // area that comes here, loaded together (one round trip)
+  // (elevations as their integer keys: out-of-grid entries take e's)
+  const long long ke = dkey(e);
+  long long ek[9];
+  double an[9], gn[9];
   uint32_t pn[9];
 #pragma unroll
   for (int k = 0; k < 9; k++) {
     const int i2 = i + k / 3 - 1, j2 = j + k % 3 - 1;
     const bool in = !(i2 < 1 || i2 > c.imax || j2 < 1 || j2 > c.jmax);
     const size_t q = (size_t)i2 * W + j2;
-    en[k] = in ? __ldg(&el[q]) : e;
+    ek[k] = in ? dkey(__ldg(&el[q])) : ke;
     pn[k] = in ? __ldg(&c.drain_pos[q]) : 0u;
     an[k] = in ? __ldcg(&c.area[q]) : 0.0;
-    dn[k] = in ? __ldg(&c.drain_dt[q]) : 0.0;
+    gn[k] = __ldg(&c.drain_frac[(size_t)k * c.N2 + cell]);
   }
+  const unsigned multi = __ldg(&c.drain_multi[cell]);
   if (pn[4] != 0) {
     double a = (e == -9999) ? 0.0 : 1.0;
     // higher neighbours the sweep reached, taken in sweep order: higher
@@ -275,19 +317,16 @@ __device__ unsigned drain_cell_g(const hc_view& c, const double* __restrict__ el
     // runs).  Each is picked by a scan with constant indices, so the
     // neighbour values stay in registers (indexed arrays went to local
     // memory, which at this block size lives in L2).
-    long long ek[9];
     unsigned left = 0;
 #pragma unroll
-    for (int kk = 0; kk < 9; kk++) {
-      ek[kk] = dkey(en[kk]);
-      if (kk != 4 && ek[kk] > dkey(e) && pn[kk] != 0) left |= 1u << kk;  // out-of-grid: e
-    }
+    for (int kk = 0; kk < 9; kk++)
+      if (kk != 4 && ek[kk] > ke && pn[kk] != 0) left |= 1u << kk;
 #pragma unroll 1
     while (left) {
       int best = -1;
       long long bk = 0;
       unsigned bp = 0;
-      double eq = 0, aq = 0, dq = 1;
+      double aq = 0, gq = 0;
 #pragma unroll
       for (int kk = 0; kk < 9; kk++) {
         if (!((left >> kk) & 1u)) continue;
@@ -295,13 +334,17 @@ __device__ unsigned drain_cell_g(const hc_view& c, const double* __restrict__ el
           best = kk;
           bk = ek[kk];
           bp = pn[kk];
-          eq = en[kk];
           aq = an[kk];
-          dq = dn[kk];
+          gq = gn[kk];
         }
       }
       left &= ~(1u << best);
+      if (!((multi >> best) & 1u)) {  // one direction of q lands here
+        a += aq * gq;
+        continue;
+      }
       const int iq = i + best / 3 - 1, jq = j + best % 3 - 1;
+      const double dq = c.drain_dt[(size_t)iq * W + jq], eq = el[(size_t)iq * W + jq];
       // the directions of q whose (clamped) step lands here, in order: one
       // for an interior q, possibly more at the edges; found with integer
       // tests first, so that the divisions run once per term and not once
@@ -331,8 +374,7 @@ __device__ unsigned drain_cell_g(const hc_view& c, const double* __restrict__ el
 #pragma unroll
   for (int kk = 0; kk < 9; kk++) {
     const int dx = kk / 3 - 1, dy = kk % 3 - 1;
-    old[kk] = (kk != 4 && dlt(en[kk], e)) ? atomicSub(&c.drain_pend[(i + dx) * W + (j + dy)], 1)
-                                          : 0;
+    old[kk] = (kk != 4 && ek[kk] < ke) ? atomicSub(&c.drain_pend[(i + dx) * W + (j + dy)], 1) : 0;
   }
   unsigned released = 0;
 #pragma unroll
@@ -591,7 +633,8 @@ hc_status run_drainage_device(hc_ctx* c, const double* el, bool area_valid,
       k_sel_pick<<<1, 1, 0, s>>>(v, shift, P);
     }
     k_drain_init<<<g, b, 0, s>>>(v, c->dev, el);
-    c->launches += 19;
+    k_drain_frac<<<g, b, 0, s>>>(v, el);
+    c->launches += 20;
     hc_drain_aux a;
     if (cudaMemcpyAsync(&a, v.drain_aux, sizeof a, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
         cudaStreamSynchronize(s) != cudaSuccess)

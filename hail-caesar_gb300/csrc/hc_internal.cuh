@@ -161,6 +161,8 @@ struct hc_view {
   uint32_t *drain_pos, *drain_f0, *drain_f1;
   int32_t *drain_pend;
   double *drain_dt, *drain_snap;
+  double *drain_frac;     // 9*N2: share of neighbour k's area pushed here (plane k)
+  uint16_t *drain_multi;  // N2: neighbours (bit k) that push here in more than one direction
   struct hc_drain_aux *drain_aux;
   // adjoint runs (hc_adjoint.cu): per-iteration time steps, recorded or
   // imposed (HC_ADJ_REC stride per iteration; see hc_dev::adj_mode)
