@@ -82,7 +82,7 @@ __device__ DQ face_dq(double q, double e0, double h0, double e1, double h1, doub
     d_s = -ghd;
     d_nn = 0;
   } else {
-    const double c3 = cube_rn(hflow);
+    const double c3 = icube_rn(hflow);
     const double F = ddiv_rn(ghd * nn * fabs(q), c3);
     const double D = 1 + F, N = q - (ghd * slope);
     qn = ddiv_rn(N, D);

@@ -203,7 +203,7 @@ __device__ double entrain_cell(const hc_view& c, hc_dev* d, size_t cell, double 
     }
     if (p.einstein) {
       const double x = ddiv_by(c.einA[n], Bd);
-      td = ddiv_by(ddiv_by(mts * (40 * cube_rn(ddiv_rn(1.0, x))), c.einSd[n]), c.dxd);
+      td = ddiv_by(ddiv_by(mts * (40 * icube_rn(ddiv_rn(1.0, x))), c.einSd[n]), c.dxd);
     }
     if (dgt(td, GRN(c, cell, n))) td = GRN(c, cell, n);
     if (p.isSuspended[n] && n == 1) {
@@ -1487,10 +1487,17 @@ __global__ void __launch_bounds__(1024) k_edge_out(const hc_view c, hc_dev* d, d
   if (wn >= 1 && wn <= HC_G - 1) {
     const double* cn = contrib + (size_t)wn * cap;
     float g = 0.0f;
+    // a zero contribution leaves g unchanged ((double)g + 0 == (double)g,
+    // and g, starting at +0 with nothing to cancel to -0, is never -0), so
+    // only the nonzero ones enter the chain of roundings
     for (int e0 = 0; e0 < total; e0 += 32) {
       const double v = (e0 + lane < total) ? cn[e0 + lane] : 0.0;
-      const int m = min(32, total - e0);
-      for (int k = 0; k < m; k++) g = (float)((double)g + __shfl_sync(0xffffffffu, v, k));
+      unsigned nz = __ballot_sync(0xffffffffu, !deq0(v));
+      while (nz) {
+        const int k = __ffs(nz) - 1;
+        nz &= nz - 1;
+        g = (float)((double)g + __shfl_sync(0xffffffffu, v, k));
+      }
     }
     if (lane == 0) gsum[wn] = g;
   }

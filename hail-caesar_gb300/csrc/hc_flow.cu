@@ -302,7 +302,7 @@ __device__ __forceinline__ void inertial_face(double& q, double& qs, double& vel
     // (0 - ghd*slope) / (1 + (ghd*nn*0)/h^3) = (0 - ghd*slope) / 1
     qn = q - (ghd * slope);
   } else {
-    qn = ddiv_rn(q - (ghd * slope), 1 + ddiv_rn(ghd * nn * fabs(q), cube_rn(hflow)));
+    qn = ddiv_rn(q - (ghd * slope), 1 + ddiv_rn(ghd * nn * fabs(q), icube_rn(hflow)));
   }
   const float hf = approx_abs_f(hflow);
   const float dtf = approx_abs_f(dt);

@@ -283,6 +283,43 @@ HC_DEV double cube_rn(double h) {
   return __dadd_rn(q, c);
 }
 
+// h^3 rounded to nearest-even, computed exactly on the integer pipe: the
+// cube of the 53-bit significand m (159 bits, from two 64x64 products) is
+// rounded at its 53rd bit with the round bit and a sticky bit, the exponent
+// is 3E plus the normalisation shift.  Five FP64 instructions (cube_rn)
+// occupy this GPU's FP64 pipe for as long as about 150 integer ones; this
+// takes about 45.  Zero, subnormal, infinite or NaN h, and cubes outside
+// the normal range, take cube_rn.
+HC_DEV double icube_rn(double h) {
+  const unsigned long long H = (unsigned long long)__double_as_longlong(h);
+  const int eh = (int)(H >> 52) & 0x7ff;
+  // the cube's biased exponent is 3 eh - 2046 + k (k = 0..2) before
+  // rounding: keep it within [1, 2045]
+  if (eh < 683 || eh > 1363) return cube_rn(h);
+  const unsigned long long M52 = (1ull << 52) - 1;
+  const unsigned long long m = (H & M52) | (1ull << 52);
+  const unsigned long long a0 = m * m, a1 = __umul64hi(m, m);  // m^2 < 2^106
+  const unsigned long long t0 = a0 * m, t1 = __umul64hi(a0, m);
+  const unsigned long long u0 = a1 * m, u1 = __umul64hi(a1, m);
+  const unsigned long long w1 = t1 + u0;
+  const unsigned long long w2 = u1 + (w1 < t1 ? 1ull : 0ull);  // m^3 = w2:w1:t0, w2 < 2^31
+  // top bit of m^3 at 156 + k
+  const int k = (w2 >> 30) ? 2 : ((w2 >> 29) ? 1 : 0);
+  const int sh = 104 + k;               // significand = m^3 >> sh (53 bits)
+  const int r1 = sh - 64;               // 40..42: the shift within w2:w1
+  unsigned long long sig = (w2 << (64 - r1)) | (w1 >> r1);
+  const bool rbit = (w1 >> (r1 - 1)) & 1ull;
+  const bool sticky = (w1 & ((1ull << (r1 - 1)) - 1)) != 0 || t0 != 0;
+  int er = sh + 3 * (eh - 1075) + 1075;
+  if (rbit && (sticky || (sig & 1ull))) sig++;
+  if (sig == (1ull << 53)) {
+    sig >>= 1;
+    er++;
+  }
+  const unsigned long long sgn = H & 0x8000000000000000ull;
+  return __longlong_as_double((long long)(sgn | ((unsigned long long)er << 52) | (sig & M52)));
+}
+
 // RN(x / y) for a divisor fixed for the run, with r = RN(1/y) precomputed:
 // q = RN(x*r) is within one ulp of x/y, the remainder x - q*y is exact in
 // one FMA, and RN(q + rem*r) is the correctly rounded quotient (Markstein's

@@ -107,6 +107,32 @@ __global__ void k_check_prepared(unsigned long long n, unsigned long long seed,
   }
 }
 
+// the integer-pipe cube against the FP64 one; the first 64 arguments where
+// they differ are kept with both results (the caller decides which one is
+// correctly rounded)
+__global__ void k_check_cube(unsigned long long n, unsigned long long seed, int mode,
+                             unsigned long long* bad, double* keep) {
+  for (unsigned long long k = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; k < n;
+       k += (unsigned long long)gridDim.x * blockDim.x) {
+    const unsigned long long r = mix(k + seed * 0x100000000ull);
+    double h;
+    if (mode == 0) h = __longlong_as_double((long long)r);               // any bit pattern
+    else if (mode == 1) h = mk(0, 1023 - 40 + (int)((r >> 52) % 48), r);  // depths
+    else h = mk(0, 1023 - 20 + (int)((r >> 52) % 30), (r >> 35) << 35);   // short significands
+    const double x = icube_rn(h), y = cube_rn(h);
+    const bool same = __double_as_longlong(x) == __double_as_longlong(y) ||
+                      (disnan(x) && disnan(y));
+    if (!same) {
+      const unsigned long long i = atomicAdd(bad, 1ull);
+      if (i < 64) {
+        keep[3 * i] = h;
+        keep[3 * i + 1] = x;
+        keep[3 * i + 2] = y;
+      }
+    }
+  }
+}
+
 // throughput: each thread divides independent operands kIter times
 template <bool kInt>
 __global__ void k_time(const double* in, double* out, int iters) {
@@ -136,6 +162,23 @@ extern "C" int arith_check(unsigned long long n, unsigned long long seed, int mo
   const cudaError_t e = cudaGetLastError();
   cudaFree(d_bad);
   cudaFree(d_first);
+  return e == cudaSuccess ? 0 : 2;
+}
+
+extern "C" int arith_check_cube(unsigned long long n, unsigned long long seed, int mode,
+                                unsigned long long* bad, double* keep) {
+  unsigned long long* d_bad;
+  double* d_keep;
+  if (cudaMalloc(&d_bad, 8) != cudaSuccess || cudaMalloc(&d_keep, 3 * 64 * 8) != cudaSuccess)
+    return 1;
+  cudaMemset(d_bad, 0, 8);
+  cudaMemset(d_keep, 0, 3 * 64 * 8);
+  k_check_cube<<<152 * 16, 256>>>(n, seed, mode, d_bad, d_keep);
+  cudaMemcpy(bad, d_bad, 8, cudaMemcpyDeviceToHost);
+  cudaMemcpy(keep, d_keep, 3 * 64 * 8, cudaMemcpyDeviceToHost);
+  const cudaError_t e = cudaGetLastError();
+  cudaFree(d_bad);
+  cudaFree(d_keep);
   return e == cudaSuccess ? 0 : 2;
 }
 

@@ -27,6 +27,8 @@ def arith(tmp_path_factory):
                                 C.POINTER(C.c_double)]
     lib.arith_check_prepared.argtypes = [C.c_uint64, C.c_uint64, C.POINTER(C.c_uint64),
                                          C.POINTER(C.c_double)]
+    lib.arith_check_cube.argtypes = [C.c_uint64, C.c_uint64, C.c_int, C.POINTER(C.c_uint64),
+                                     C.POINTER(C.c_double)]
     lib.arith_time.argtypes = [C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float)]
     return lib
 
@@ -48,6 +50,23 @@ def test_division_by_prepared_divisors(arith):
     assert arith.arith_check_prepared(1 << 30, 99, C.byref(bad), first) == 0
     assert bad.value == 0, "%d mismatches; first a=%r b=%r got %r want %r" % (
         bad.value, first[0], first[1], first[2], first[3])
+
+
+@pytest.mark.parametrize("mode", range(3), ids=["bit patterns", "depths", "short significands"])
+def test_cube_on_integer_pipe(arith, mode):
+    """icube_rn (the friction term's h^3 on the integer pipe) against the
+    FP64 cube_rn over 2^30 arguments; where they differ, the exact cube
+    decides, and it must be icube_rn's."""
+    from fractions import Fraction
+    import math
+    bad = C.c_uint64(0)
+    keep = (C.c_double * (3 * 64))()
+    assert arith.arith_check_cube(1 << 30, 7 + mode, mode, C.byref(bad), keep) == 0
+    for i in range(min(64, bad.value)):
+        h, x, y = keep[3 * i], keep[3 * i + 1], keep[3 * i + 2]
+        exact = Fraction(h) ** 3
+        want = float(exact) if abs(exact) < Fraction(2) ** 1023 else math.copysign(math.inf, h)
+        assert x == want, "h=%r: icube %r, cube_rn %r, exact %r" % (h, x, y, want)
 
 
 def test_division_throughput(arith):
