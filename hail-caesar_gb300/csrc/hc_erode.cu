@@ -599,15 +599,23 @@ __device__ void sort_active_row(const hc_view& c, hc_dev* d, size_t cell, ApplyR
 
 // slide_GS(a -> b, amount) on held rows (records exist: allocated before the
 // pass).  Same arithmetic as slide_GS_dev.
+// The sum of A's positive fractions, in order: slide_GS's `total`.
+__device__ __forceinline__ double positive_total(const ApplyRow& A) {
+  double total = 0;
+#pragma unroll
+  for (int n = 1; n <= HC_G - 1; n++)
+    if (dgt0(A.g[n])) total += A.g[n];
+  return total;
+}
+
+// total_a: positive_total(A), which the caller may have formed ahead (the
+// sum is a chain of nine dependent FP64 additions)
 __device__ void slide_GS_rows(const hc_view& c, hc_dev* d, size_t a, ApplyRow& A, double amount,
-                              size_t b, ApplyRow& B) {
+                              size_t b, ApplyRow& B, double total_a) {
   const double* dprop = c.p.dprop;
   const bool ha = A.idx != -9999, hb = B.idx != -9999;
   if (ha && hb) {
-    double total = 0;
-#pragma unroll
-    for (int n = 1; n <= HC_G - 1; n++)
-      if (dgt0(A.g[n])) total += A.g[n];
+    const double total = total_a;
     if (dgt(amount, total)) {
 #pragma unroll
       for (int n = 1; n <= HC_G - 1; n++) B.g[n] += (amount - total) * dprop[n];
@@ -670,14 +678,14 @@ __device__ __forceinline__ bool lateral_amount(const hc_params& p, const hc_divi
 __device__ __forceinline__ void lateral_step(const hc_view& c, hc_dev* d, double mult, double ts,
                                              double tau0, double et3, size_t ccell, ApplyRow& C,
                                              double e0, size_t ncell, ApplyRow& N, bool boundary,
-                                             double& elev_update) {
+                                             double& elev_update, double totN) {
   const double en = N.elev;
   double amt;
   if (dgt(en, e0) && lateral_amount(c.p, c.dxd, mult, ts, tau0, et3, N, e0, boundary, amt)) {
     elev_update += amt;
     N.elev = en - amt;
     N.dirty = true;
-    slide_GS_rows(c, d, ncell, N, amt, ccell, C);
+    slide_GS_rows(c, d, ncell, N, amt, ccell, C, totN);
   }
 }
 
@@ -689,12 +697,16 @@ __device__ __forceinline__ void lateral_both(const hc_view& c, hc_dev* d, double
                                              double e0, bool doU, size_t ucell, ApplyRow& U,
                                              bool bU, bool doD, size_t dcell, ApplyRow& D,
                                              bool bD, double& elev_update) {
+  // both rows' slide_GS totals, formed ahead and side by side (the slide
+  // toward C changes neither U's nor D's fractions before its own slide)
+  const double totU = doU ? positive_total(U) : 0.0;
+  const double totD = doD ? positive_total(D) : 0.0;
 #pragma unroll 1
   for (int side = 0; side < 2; side++) {
     if (!(side == 0 ? doU : doD)) continue;
     ApplyRow N = (side == 0) ? U : D;
     lateral_step(c, d, mult, ts, tau0, et3, ccell, C, e0, side == 0 ? ucell : dcell, N,
-                 side == 0 ? bU : bD, elev_update);
+                 side == 0 ? bU : bD, elev_update, side == 0 ? totU : totD);
     if (side == 0) U = N;
     else D = N;
   }
@@ -1496,7 +1508,7 @@ __global__ void __launch_bounds__(1024) k_edge_out(const hc_view c, hc_dev* d, d
       while (nz) {
         const int k = __ffs(nz) - 1;
         nz &= nz - 1;
-        g = (float)((double)g + __shfl_sync(0xffffffffu, v, k));
+        g = d2f_i(f2d_i(g) + __shfl_sync(0xffffffffu, v, k));
       }
     }
     if (lane == 0) gsum[wn] = g;

@@ -290,12 +290,16 @@ HC_DEV double cube_rn(double h) {
 // occupy this GPU's FP64 pipe for as long as about 150 integer ones; this
 // takes about 45.  Zero, subnormal, infinite or NaN h, and cubes outside
 // the normal range, take cube_rn.
+// (a call, so that the compiler does not if-convert it: predicated-off FP64
+// instructions still take their issue slots on the FP64 pipe)
+static __device__ __noinline__ double cube_rn_call(double h) { return cube_rn(h); }
+
 HC_DEV double icube_rn(double h) {
   const unsigned long long H = (unsigned long long)__double_as_longlong(h);
   const int eh = (int)(H >> 52) & 0x7ff;
   // the cube's biased exponent is 3 eh - 2046 + k (k = 0..2) before
   // rounding: keep it within [1, 2045]
-  if (eh < 683 || eh > 1363) return cube_rn(h);
+  if (eh < 683 || eh > 1363) return cube_rn_call(h);
   const unsigned long long M52 = (1ull << 52) - 1;
   const unsigned long long m = (H & M52) | (1ull << 52);
   const unsigned long long a0 = m * m, a1 = __umul64hi(m, m);  // m^2 < 2^106
@@ -430,6 +434,43 @@ HC_DEV double ddiv_rn(double a, double b) { return ddiv_by(a, ddiv_prep(b)); }
 
 // hc_divisor for a divisor fixed for the run, V exact (floor(2^116/mb))
 hc_divisor host_divisor(double b);
+
+// (double)f on the integer pipe for normal floats and zeros, the conversion
+// instruction (an FP64-pipe operation) otherwise.
+HC_DEV double f2d_i(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned ex = (u >> 23) & 0xffu;
+  if (ex == 0 || ex == 0xffu) {
+    if ((u & 0x7fffffffu) == 0)
+      return __longlong_as_double((long long)((unsigned long long)(u & 0x80000000u) << 32));
+    return (double)f;
+  }
+  return __longlong_as_double((long long)(((unsigned long long)(u & 0x80000000u) << 32) |
+                                          ((unsigned long long)(ex - 127 + 1023) << 52) |
+                                          ((unsigned long long)(u & 0x7fffffu) << 29)));
+}
+
+// (float)x, rounded to nearest-even, on the integer pipe for results in the
+// float normal range and zeros, the conversion instruction otherwise.
+HC_DEV float d2f_i(double x) {
+  const unsigned long long X = (unsigned long long)__double_as_longlong(x);
+  const unsigned sgn = (unsigned)(X >> 32) & 0x80000000u;
+  const int ef = ((int)(X >> 52) & 0x7ff) - 1023 + 127;
+  if (ef < 1 || ef > 253) {
+    if ((X << 1) == 0) return __uint_as_float(sgn);
+    return (float)x;
+  }
+  const unsigned long long mant = X & ((1ull << 52) - 1);
+  unsigned m = (unsigned)(mant >> 29), e = (unsigned)ef;
+  const unsigned long long rem = mant & ((1ull << 29) - 1), half = 1ull << 28;
+  if (rem > half || (rem == half && (m & 1u))) {
+    if (++m == (1u << 23)) {
+      m = 0;
+      e++;
+    }
+  }
+  return __uint_as_float(sgn | (e << 23) | m);
+}
 
 // A float within a relative 2^-20 of |x| (or 0 / +inf when |x| is outside
 // the float normal range), built with integer operations only: the FP64

@@ -133,6 +133,27 @@ __global__ void k_check_cube(unsigned long long n, unsigned long long seed, int 
   }
 }
 
+// the integer-pipe float <-> double conversions against the instructions
+__global__ void k_check_conv(unsigned long long n, unsigned long long seed,
+                             unsigned long long* bad, double* first) {
+  for (unsigned long long k = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; k < n;
+       k += (unsigned long long)gridDim.x * blockDim.x) {
+    const unsigned long long r = mix(k + seed * 0x100000000ull);
+    // doubles: any bits, and values near the float range and its roundings
+    const double x = (k & 1) ? __longlong_as_double((long long)r)
+                             : mk(r >> 63, 1023 - 130 + (int)((r >> 52) % 260), r);
+    const float a = d2f_i(x), b = __double2float_rn(x);
+    const float f = __uint_as_float((unsigned)(r >> 17));
+    const double p = f2d_i(f), q = (double)f;
+    const bool same1 = __float_as_uint(a) == __float_as_uint(b) || (a != a && b != b);
+    const bool same2 = __double_as_longlong(p) == __double_as_longlong(q) || (p != p && q != q);
+    if (!(same1 && same2) && atomicAdd(bad, 1ull) == 0) {
+      first[0] = x;
+      first[1] = (double)f;
+    }
+  }
+}
+
 // throughput: each thread divides independent operands kIter times
 template <bool kInt>
 __global__ void k_time(const double* in, double* out, int iters) {
@@ -179,6 +200,22 @@ extern "C" int arith_check_cube(unsigned long long n, unsigned long long seed, i
   const cudaError_t e = cudaGetLastError();
   cudaFree(d_bad);
   cudaFree(d_keep);
+  return e == cudaSuccess ? 0 : 2;
+}
+
+extern "C" int arith_check_conv(unsigned long long n, unsigned long long seed,
+                                unsigned long long* bad, double* first) {
+  unsigned long long* d_bad;
+  double* d_first;
+  if (cudaMalloc(&d_bad, 8) != cudaSuccess || cudaMalloc(&d_first, 32) != cudaSuccess) return 1;
+  cudaMemset(d_bad, 0, 8);
+  cudaMemset(d_first, 0, 32);
+  k_check_conv<<<152 * 16, 256>>>(n, seed, d_bad, d_first);
+  cudaMemcpy(bad, d_bad, 8, cudaMemcpyDeviceToHost);
+  cudaMemcpy(first, d_first, 32, cudaMemcpyDeviceToHost);
+  const cudaError_t e = cudaGetLastError();
+  cudaFree(d_bad);
+  cudaFree(d_first);
   return e == cudaSuccess ? 0 : 2;
 }
 

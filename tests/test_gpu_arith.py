@@ -29,6 +29,8 @@ def arith(tmp_path_factory):
                                          C.POINTER(C.c_double)]
     lib.arith_check_cube.argtypes = [C.c_uint64, C.c_uint64, C.c_int, C.POINTER(C.c_uint64),
                                      C.POINTER(C.c_double)]
+    lib.arith_check_conv.argtypes = [C.c_uint64, C.c_uint64, C.POINTER(C.c_uint64),
+                                     C.POINTER(C.c_double)]
     lib.arith_time.argtypes = [C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float)]
     return lib
 
@@ -67,6 +69,15 @@ def test_cube_on_integer_pipe(arith, mode):
         exact = Fraction(h) ** 3
         want = float(exact) if abs(exact) < Fraction(2) ** 1023 else math.copysign(math.inf, h)
         assert x == want, "h=%r: icube %r, cube_rn %r, exact %r" % (h, x, y, want)
+
+
+def test_float_conversions_on_integer_pipe(arith):
+    """d2f_i / f2d_i (the edge output's float sums) against the conversion
+    instructions, over 2^30 values each."""
+    bad = C.c_uint64(0)
+    first = (C.c_double * 4)()
+    assert arith.arith_check_conv(1 << 30, 5, C.byref(bad), first) == 0
+    assert bad.value == 0, "%d mismatches; first x=%r f=%r" % (bad.value, first[0], first[1])
 
 
 def test_division_throughput(arith):
