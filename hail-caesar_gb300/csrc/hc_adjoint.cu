@@ -428,6 +428,8 @@ extern "C" hc_status hc_adj_forward(hc_ctx* c, int64_t n, const double* fixed, d
                                     double* q_samples, int64_t q_cap, int64_t* n_samples) {
   if (!c || n <= 0) return HC_ERR_ARG;
   if (!c->v.p.hydro_only) return hc_fail(c, HC_ERR_UNSUPPORTED, "adjoint runs are hydro-only");
+  if (c->v.p.spatially_complex_rainfall)
+    return hc_fail(c, HC_ERR_UNSUPPORTED, "adjoint runs use the zoned rainfall inputs");
   if (!c->prepared) return hc_fail(c, HC_ERR_STATE, "hc_prepare must come before the run");
   Dev dt;
   const size_t nrec = (size_t)n * HC_ADJ_REC;
@@ -461,6 +463,8 @@ extern "C" hc_status hc_adj_gradient(hc_ctx* c, int64_t n, int32_t every, const 
   if (!c || n <= 0 || every <= 0 || !q_target || n_target < 0) return HC_ERR_ARG;
   hc_view& v = c->v;
   if (!v.p.hydro_only) return hc_fail(c, HC_ERR_UNSUPPORTED, "adjoint runs are hydro-only");
+  if (v.p.spatially_complex_rainfall)
+    return hc_fail(c, HC_ERR_UNSUPPORTED, "adjoint runs use the zoned rainfall inputs");
   if (!c->prepared) return hc_fail(c, HC_ERR_STATE, "hc_prepare must come before the run");
   const auto t_all = std::chrono::steady_clock::now();
   const size_t N2 = v.N2;

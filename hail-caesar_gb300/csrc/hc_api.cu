@@ -846,13 +846,31 @@ extern "C" hc_status hc_prepare(hc_ctx* c) {
   HC_TRY(dalloc(c, &v.topm, table.size()));
   HC_CU(cudaMemcpy(v.topm, table.data(), table.size() * 8, cudaMemcpyHostToDevice), "prepare");
   v.topm_rows = rows;
-  for (int n = 1; n <= p.rfnum; n++) {
+  for (int n = p.spatially_complex_rainfall ? 0 : 1; n <= p.rfnum; n++) {
     s.old_j_mean[n] = table[n];
     s.new_j_mean[n] = table[(p.rfnum + 1) + n];
   }
   for (int n = 1; n <= 9; n++) v.dlog[n] = std::log(p.d[n]);
-  HC_TRY(push(c));
-  HC_TRY(recompute_points(c, false));
+  if (p.spatially_complex_rainfall) {
+    // distributed runoff: the computed cells (rows 1 .. imax-1, columns
+    // 1 .. jmax-1, above no-data) per rain state; initialise_drainage_area
+    // skips the drainage area and the input points in this mode (:2055-2070)
+    for (int z = 0; z <= HC_MAX_RF; z++) v.runoff_count[z] = 0;
+    v.runoff_present = 0;
+    for (int i = 1; i < p.imax; i++)
+      for (int j = 1; j < p.jmax; j++) {
+        const size_t cell = (size_t)i * v.W + j;
+        if (!(elev[cell] > -9999)) continue;
+        const int r = rf[cell];
+        const int z = (p.rfnum == 1) ? 1 : ((r >= 1 && r <= p.rfnum - 1) ? r : 0);
+        v.runoff_count[z] += 1;
+        v.runoff_present |= 1u << z;
+      }
+    HC_TRY(push(c));
+  } else {
+    HC_TRY(push(c));
+    HC_TRY(recompute_points(c, false));
+  }
   c->prepared = true;
   c->graph_iters = 0;  // parameters of the view changed: rebuild the graph
   return HC_OK;

@@ -46,7 +46,7 @@ __device__ void topmodel_step(hc_dev* d, const hc_params& p, const double* topm,
     return;
   }
   const double* row = topm + (size_t)t * 2 * (rf + 1);
-  for (int n = 1; n <= rf; n++) {
+  for (int n = p.spatially_complex_rainfall ? 0 : 1; n <= rf; n++) {
     d->s.old_j_mean[n] = row[n];
     d->s.new_j_mean[n] = row[(rf + 1) + n];
   }
@@ -149,57 +149,98 @@ __global__ void k_control(const hc_view c, hc_dev* d, hc_iter_handles hh) {
     if (d->adj_mode == 2) fdt2 = arec[1];
     else arec[1] = fdt2;
   }
-  for (int i = 1; i <= p.rfnum; i++) s.waterinput += s.j_mean[i] * s.nActualGridCells[i] * DX * DX;
-  for (int i = 0; i <= p.rfnum; i++) d->j_mean_in[i] = s.j_mean[i];
-  if (arec)
-    for (int i = 0; i <= HC_MAX_RF; i++) arec[3 + i] = (i <= p.rfnum) ? s.j_mean[i] : 0.0;
-  d->input_dt = fdt2;
-  // what each input point of a zone receives (:3463-3477), the same for all
-  // points of the zone
-  for (int z = 0; z <= p.rfnum && z <= HC_MAX_RF; z++) {
-    double amt = (d->j_mean_in[z] * s.nActualGridCells[z]) / (s.catchment_input_counter[z]) * fdt2;
-    if (amt > p.ERODEFACTOR) amt = p.ERODEFACTOR;
-    d->input_amt[z] = amt;
-  }
-  if (s.cycle >= s.time_1) {
-    do {
-      s.time_1++;
-      topmodel_step(d, p, c.topm, c.topm_rows);
-      if (s.time_step > p.max_time_step) {
-        double jmm = 0;
-        for (int n = 1; n <= p.rfnum; n++)
-          if (s.new_j_mean[n] > jmm) jmm = s.new_j_mean[n];
-        if (jmm > (0.2 / ((unsigned)p.imax * (unsigned)p.jmax * DX * DX))) {
+  if (p.spatially_complex_rainfall) {
+    // catchment_water_input_and_hydrology(flow_timestep, runoff) :3544-3607.
+    // A cell's runoff recurrence (runoffGrid::calculate_runoff) depends only
+    // on its rain, i.e. on its rain state: the zone (zones 1 .. rfnum-1, or
+    // column 0 for all cells when rfnum is 1) or none (state 0: zone rfnum
+    // and others get no rain, rainGrid::create, LSDRainfallRunoff.cpp:33-66),
+    // so every cell of a state holds the
+    // same values; the host tabulates them per state with glibc.
+    const int rf = p.rfnum;
+    for (int z = 0; z <= rf; z++) {
+      double amt = s.j_mean[z] * fdt2;
+      if (amt > p.ERODEFACTOR) amt = p.ERODEFACTOR;
+      d->input_amt[z] = amt;
+      d->j_mean_in[z] = s.j_mean[z];
+    }
+    // the two sums over the cells (:3547-3571), formed state by state
+    for (int z = 0; z <= rf; z++) s.waterinput += c.runoff_count[z] * (s.j_mean[z] * DX * DX);
+    for (int z = 0; z <= rf; z++)
+      s.waterinput += c.runoff_count[z] * ((d->input_amt[z] / fdt2) * DX * DX);
+    d->input_dt = fdt2;
+    // new_jmeanmax (:3575-3586), over the states that hold a computed cell
+    double jmm = 0;
+    for (int z = 0; z <= rf; z++)
+      if (((c.runoff_present >> z) & 1u) && s.new_j_mean[z] > jmm) jmm = s.new_j_mean[z];
+    if (s.cycle >= s.time_1) {
+      do {
+        s.time_1++;
+        topmodel_step(d, p, c.topm, c.topm_rows);
+        if (s.time_step > p.max_time_step &&
+            jmm > (0.2 / ((unsigned)p.jmax * (unsigned)p.imax * DX * DX))) {
           s.cycle = s.time_1 + (p.max_time_step / 60);
           s.time_step = p.max_time_step;
         }
-      }
-    } while (s.time_1 < s.cycle && !(d->pause & HC_PAUSE_ERROR));
+      } while (s.time_1 < s.cycle && !(d->pause & HC_PAUSE_ERROR));
+    }
+    for (int z = 0; z <= rf; z++)  // calchydrograph(time, runoff) :3728-3740
+      s.j_mean[z] = s.old_j_mean[z] + (((s.new_j_mean[z] - s.old_j_mean[z]) / 2) *
+                                       (2 - (s.time_1 - s.cycle)));
+    d->do_drain = 0;  // no drainage area or input points in this mode
+  } else {
+    for (int i = 1; i <= p.rfnum; i++) s.waterinput += s.j_mean[i] * s.nActualGridCells[i] * DX * DX;
+    for (int i = 0; i <= p.rfnum; i++) d->j_mean_in[i] = s.j_mean[i];
+    if (arec)
+      for (int i = 0; i <= HC_MAX_RF; i++) arec[3 + i] = (i <= p.rfnum) ? s.j_mean[i] : 0.0;
+    d->input_dt = fdt2;
+    // what each input point of a zone receives (:3463-3477), the same for all
+    // points of the zone
+    for (int z = 0; z <= p.rfnum && z <= HC_MAX_RF; z++) {
+      double amt = (d->j_mean_in[z] * s.nActualGridCells[z]) / (s.catchment_input_counter[z]) * fdt2;
+      if (amt > p.ERODEFACTOR) amt = p.ERODEFACTOR;
+      d->input_amt[z] = amt;
+    }
+    if (s.cycle >= s.time_1) {
+      do {
+        s.time_1++;
+        topmodel_step(d, p, c.topm, c.topm_rows);
+        if (s.time_step > p.max_time_step) {
+          double jmm = 0;
+          for (int n = 1; n <= p.rfnum; n++)
+            if (s.new_j_mean[n] > jmm) jmm = s.new_j_mean[n];
+          if (jmm > (0.2 / ((unsigned)p.imax * (unsigned)p.jmax * DX * DX))) {
+            s.cycle = s.time_1 + (p.max_time_step / 60);
+            s.time_step = p.max_time_step;
+          }
+        }
+      } while (s.time_1 < s.cycle && !(d->pause & HC_PAUSE_ERROR));
+    }
+    for (int n = 1; n <= p.rfnum; n++)  // calchydrograph :3718
+      s.j_mean[n] = s.old_j_mean[n] + (((s.new_j_mean[n] - s.old_j_mean[n]) / 2) * (2 - (s.time_1 - s.cycle)));
+    if (arec) {
+      arec[HC_ADJ_T1] = s.time_1;
+      arec[HC_ADJ_T1 + 1] = s.cycle;
+    }
+    double jmeanmax = 0;
+    for (int n = 1; n <= p.rfnum; n++)
+      if (s.j_mean[n] > jmeanmax) jmeanmax = s.j_mean[n];
+    bool recalc = false;
+    if (jmeanmax >= s.baseflow) {
+      s.baseflow = s.baseflow * 3;
+      recalc = true;
+    }
+    if (s.baseflow > (jmeanmax * 3) && s.baseflow > 0.000001) {
+      s.baseflow = jmeanmax * 1.25;
+      recalc = true;
+    }
+    // The drainage area and the input-point list are recomputed before the
+    // next iteration (the host sorts the elevations, hc_drain.cu does the
+    // rest), from the elevations as they are now (k_drain_snapshot); the
+    // reference, too, applies the new list from the next iteration on.
+    d->do_drain = recalc;
+    if (recalc) d->pause |= HC_PAUSE_DRAINAGE;
   }
-  for (int n = 1; n <= p.rfnum; n++)  // calchydrograph :3718
-    s.j_mean[n] = s.old_j_mean[n] + (((s.new_j_mean[n] - s.old_j_mean[n]) / 2) * (2 - (s.time_1 - s.cycle)));
-  if (arec) {
-    arec[HC_ADJ_T1] = s.time_1;
-    arec[HC_ADJ_T1 + 1] = s.cycle;
-  }
-  double jmeanmax = 0;
-  for (int n = 1; n <= p.rfnum; n++)
-    if (s.j_mean[n] > jmeanmax) jmeanmax = s.j_mean[n];
-  bool recalc = false;
-  if (jmeanmax >= s.baseflow) {
-    s.baseflow = s.baseflow * 3;
-    recalc = true;
-  }
-  if (s.baseflow > (jmeanmax * 3) && s.baseflow > 0.000001) {
-    s.baseflow = jmeanmax * 1.25;
-    recalc = true;
-  }
-  // The drainage area and the input-point list are recomputed before the
-  // next iteration (the host sorts the elevations, hc_drain.cu does the
-  // rest), from the elevations as they are now (k_drain_snapshot); the
-  // reference, too, applies the new list from the next iteration on.
-  d->do_drain = recalc;
-  if (recalc) d->pause |= HC_PAUSE_DRAINAGE;
 
   s.flow_timestep = flow_dt_of(p, s);
   if (adj) {
@@ -235,6 +276,20 @@ __global__ void k_inputs(const hc_view c, hc_dev* d) {
     const size_t cell = (size_t)i * c.W + j;
     c.h[cell] += d->input_amt[c.rfarea[cell]];
   }
+}
+
+// Distributed runoff (:3560-3573): every computed cell (rows 1 .. imax-1,
+// columns 1 .. jmax-1, elevation above no-data) takes its state's amount.
+__global__ void k_runoff_inputs(const hc_view c, hc_dev* d) {
+  if (!d->it_active) return;
+  const int j = 1 + blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = 1 + blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= c.imax || j >= c.jmax) return;
+  const size_t cell = (size_t)i * c.W + j;
+  if (!(dkey(c.elev[cell]) > kNoDataKey)) return;  // j_mean stays 0 there
+  const int rf = c.p.rfnum, r = c.rfarea[cell];
+  const int z = (rf == 1) ? 1 : ((r >= 1 && r <= rf - 1) ? r : 0);
+  c.h[cell] += d->input_amt[z];
 }
 
 __global__ void k_flow_dt(const hc_view c, hc_dev* d) {
@@ -692,6 +747,12 @@ void launch_control(hc_ctx* c) {
 }
 
 void launch_inputs(hc_ctx* c) {
+  if (c->v.p.spatially_complex_rainfall) {
+    dim3 b(32, 8), g((c->v.jmax + 31) / 32, (c->v.imax + 7) / 8);
+    k_runoff_inputs<<<g, b, 0, c->cs>>>(c->v, c->dev);
+    count_launch(c, 1);
+    return;
+  }
   // grid-stride over the current list (its length lives on the device)
   int n = c->v.cin_cap;
   int blocks = std::min((n + 255) / 256, 152 * 4);

@@ -181,16 +181,29 @@ void host_topmodel_table(const hc_params* p, const float* rain, int rows, int co
   std::vector<double> jv(rf + 1, 0.000000001), jo(rf + 1, 0.000000001);
   std::vector<double> oldm(rf + 1, 0.0), newm(rf + 1, 0.0);
   const double M = p->M;
+  const bool grid = p->spatially_complex_rainfall != 0;
+  auto rain_at = [&](int ts, int col) {
+    return (ts >= 0 && ts < rows && col >= 0 && col < cols) ? rain[(size_t)ts * cols + col] : 0.0f;
+  };
   auto step = [&](double cyc) {
     const int ts = (int)(cyc / p->rain_data_time_step);
-    for (int n = 1; n <= rf; n++) {
+    for (int n = grid ? 0 : 1; n <= rf; n++) {
       double lrr = 0;
       const double fts = 60;
       oldm[n] = newm[n];
       jo[n] = jv[n];
-      float v = 0.0f;
-      if (ts >= 0 && ts < rows && n - 1 < cols) v = rain[(size_t)ts * cols + (n - 1)];
-      if (v > 0) lrr = p->rain_factor * ((v / 1000) / 3600);
+      if (grid) {
+        // runoffGrid::calculate_runoff (LSDRainfallRunoff.cpp:175-241) for
+        // rain state n: the grid holds the rain as a double, rain_factor is
+        // passed as an int; state 0 gets no rain (rainGrid::create :33-66)
+        double g = 0;
+        if (rf == 1) g = (n == 1) ? (double)rain_at(ts, 0) : 0.0;
+        else if (n >= 1 && n <= rf - 1) g = (double)rain_at(ts, n - 1);
+        if (g > 0) lrr = (int)p->rain_factor * ((g / 1000) / 3600);
+      } else {
+        const float v = rain_at(ts, n - 1);
+        if (v > 0) lrr = p->rain_factor * ((v / 1000) / 3600);
+      }
       const double j0 = jo[n];
       if (lrr == 0) {
         jv[n] = j0 / (1 + ((j0 * fts) / M));

@@ -148,6 +148,8 @@ struct hc_view {
   // Einstein per-fraction constants, evaluated on the host with the
   // reference's expressions (:4393-4394): (2650-1000)*Di, the square root
   // sqrt(1000/((2250-1000)*g*Di^3)) and its reciprocal
+  double runoff_count[HC_MAX_RF + 1];  // distributed runoff: computed cells per rain state
+  unsigned runoff_present;             // bit z: rain state z holds a computed cell
   double einA[HC_G], einS[HC_G], einRS[HC_G];
   hc_divisor einSd[HC_G];  // the einS as divisors
 

@@ -48,6 +48,7 @@ class hc_params(C.Structure):
         ("in_channel_landslide_iter_interval", C.c_int32),
         ("creep_time_interval", C.c_int32), ("global_landsliding_interval", C.c_int32),
         ("creep_coeff", C.c_double), ("LIMIT", C.c_int32),
+        ("spatially_complex_rainfall", C.c_int32),
     ]
 
 

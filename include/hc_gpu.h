@@ -100,6 +100,12 @@ typedef struct hc_params {
   int32_t global_landsliding_interval;
   double creep_coeff;
   int32_t LIMIT;
+  /* distributed TOPMODEL rainfall-runoff: every cell of the grid takes its
+   * own runoff (catchment_water_input_and_hydrology(flow_timestep, runoff)
+   * :3544-3607, runoffGrid::calculate_runoff LSDRainfallRunoff.cpp:175-241,
+   * key spatially_complex_rainfall_on :1355); 0: zoned TOPMODEL through the
+   * catchment input points */
+  int32_t spatially_complex_rainfall;
 } hc_params;
 
 /* Scalar state of the model object (members of LSDCatchmentModel that the

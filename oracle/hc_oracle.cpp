@@ -80,6 +80,9 @@ struct hco_model {
   int grain_array_tot = 1;
   int totalinputpoints = 0;
   std::vector<double> sum_grain, jv, jo, j_mean, old_j_mean, new_j_mean;
+  // runoffGrid (LSDRainfallRunoff.cpp:120-133), per cell, for the
+  // distributed TOPMODEL (spatially_complex_rainfall)
+  std::vector<double> rj, rjo, rjm, rold, rnew;
   std::vector<int> nActualGridCells, cin_counter;
 
   inline size_t ix(unsigned i, unsigned j) const { return (size_t)i * W + j; }
@@ -159,6 +162,13 @@ extern "C" hco_model* hco_create(const hc_params* prm) {
   m->old_j_mean.assign(rf + 1, 0.0);
   m->new_j_mean.assign(rf + 1, 0.0);
   m->nActualGridCells.assign(rf + 1, 0);
+  if (prm->spatially_complex_rainfall) {
+    m->rj.assign(m->N2, 0.000000001);
+    m->rjo.assign(m->N2, 0.000000001);
+    m->rjm.assign(m->N2, 0.0);
+    m->rold.assign(m->N2, 0.0);
+    m->rnew.assign(m->N2, 0.0);
+  }
   m->cin_counter.assign(rf + 1, 0);
   // The reach block of initialise_arrays marks the input cells in
   // inputpointsarray (:1770), but zero_values (:2905), called at the end of
@@ -351,6 +361,91 @@ static void topmodel_runoff(hco_model* m, double cyc) {  // :3649-3715
 static void calchydrograph(hco_model* m, double t) {  // :3718-3724
   for (int n = 1; n <= m->p.rfnum; n++)
     m->j_mean[n] = m->old_j_mean[n] + (((m->new_j_mean[n] - m->old_j_mean[n]) / 2) * (2 - t));
+}
+
+// Distributed TOPMODEL (spatially_complex_rainfall).  rainGrid::create
+// (LSDRainfallRunoff.cpp:33-66): one zone: every cell (padding included)
+// takes column 0; otherwise the cells of zones 1 .. rfnum-1 take their
+// column and the others none (the loop stops before rfnum).
+static void rain_grid(hco_model* m, int ts, std::vector<double>& g) {
+  g.assign(m->N2, 0.0);
+  const int rf = m->p.rfnum;
+  if (rf == 1) {
+    std::fill(g.begin(), g.end(), (double)rain_at(m, ts, 0));
+    return;
+  }
+  for (unsigned i = 1; i < m->imax; i++)
+    for (unsigned j = 1; j < m->jmax; j++)
+      for (int z = 1; z < rf; z++)
+        if (m->rfarea[m->ix(i, j)] == z) g[m->ix(i, j)] = rain_at(m, ts, z - 1);
+}
+
+// topmodel_runoff(cycle, runoff) :3610-3628 -> runoffGrid::calculate_runoff
+// (LSDRainfallRunoff.cpp:175-241), which takes rain_factor as an int
+static void topmodel_runoff_grid(hco_model* m, double cyc) {
+  const int ts = (int)(cyc / m->p.rain_data_time_step);
+  std::vector<double> g;
+  rain_grid(m, ts, g);
+  const int rain_factor = (int)m->p.rain_factor;
+  const double M = m->p.M;
+  for (unsigned a = 1; a < m->imax; a++)
+    for (unsigned b = 1; b < m->jmax; b++) {
+      const size_t c = m->ix(a, b);
+      if (!(m->E(a, b) > -9999)) continue;
+      double lrr = 0;
+      const double lts = 60;
+      m->rold[c] = m->rnew[c];
+      m->rjo[c] = m->rj[c];
+      if (g[c] > 0) lrr = rain_factor * ((g[c] / 1000) / 3600);
+      const double jo = m->rjo[c];
+      if (lrr == 0) {
+        m->rj[c] = jo / (1 + ((jo * lts) / M));
+        m->rnew[c] = M / lts * std::log(1 + ((jo * lts) / M));
+      }
+      if (lrr > 0) {
+        m->rj[c] = lrr / (((lrr - jo) / jo) * std::exp((0 - lrr) * lts / M) + 1);
+        m->rnew[c] = (M / lts) * std::log(((lrr - jo) + jo * std::exp((lrr * lts) / M)) / lrr);
+      }
+      if (m->rnew[c] < 0) m->rnew[c] = 0;
+    }
+}
+
+static void calchydrograph_grid(hco_model* m, double t) {  // :3728-3740
+  for (unsigned a = 1; a <= m->imax; a++)
+    for (unsigned b = 1; b <= m->jmax; b++) {
+      const size_t c = m->ix(a, b);
+      m->rjm[c] = m->rold[c] + (((m->rnew[c] - m->rold[c]) / 2) * (2 - t));
+    }
+}
+
+// catchment_water_input_and_hydrology(flow_timestep, runoff) :3544-3607
+static void catchment_water_input_grid(hco_model* m, double fdt) {
+  const double DX = m->DX;
+  for (unsigned i = 1; i < m->imax; i++)
+    for (unsigned j = 1; j < m->jmax; j++) m->waterinput += m->rjm[m->ix(i, j)] * DX * DX;
+  for (unsigned i = 1; i < m->imax; i++)
+    for (unsigned j = 1; j < m->jmax; j++) {
+      double amt = m->rjm[m->ix(i, j)] * fdt;
+      if (amt > m->p.ERODEFACTOR) amt = m->p.ERODEFACTOR;
+      m->waterinput += (amt / fdt) * DX * DX;
+      m->H(i, j) += amt;
+    }
+  double new_jmeanmax = 0;
+  for (unsigned a = 1; a <= m->imax; a++)
+    for (unsigned b = 1; b <= m->jmax; b++)
+      if (m->rnew[m->ix(a, b)] > new_jmeanmax) new_jmeanmax = m->rnew[m->ix(a, b)];
+  if (m->cycle >= m->time_1) {
+    do {
+      m->time_1++;
+      topmodel_runoff_grid(m, m->time_1);
+      if (m->time_step > m->p.max_time_step &&
+          new_jmeanmax > (0.2 / (m->jmax * m->imax * DX * DX))) {
+        m->cycle = m->time_1 + (m->p.max_time_step / 60);
+        m->time_step = m->p.max_time_step;
+      }
+    } while (m->time_1 < m->cycle);
+  }
+  calchydrograph_grid(m, m->time_1 - m->cycle);
 }
 
 static void catchment_water_input_and_hydrology(hco_model* m, double fdt) {  // :3455-3541
@@ -1437,6 +1532,10 @@ extern "C" void hco_prepare(hco_model* m) {
     for (unsigned j = 1; j < m->jmax; j++)
       if (m->E(i, j) > -9999) m->nActualGridCells[m->rfarea[m->ix(i, j)]]++;
   m->creep_time = m->creep_time2 = m->time_1 = m->cycle;  // set_time_counters :1862
+  if (m->p.spatially_complex_rainfall) {
+    topmodel_runoff_grid(m, 1.0);  // initialise_rainfall_runoff :2041-2053
+    return;                        // initialise_drainage_area skips both :2055-2070
+  }
   topmodel_runoff(m, 1.0);                                 // initialise_rainfall_runoff
   zero_and_calc_drainage_area(m);                          // initialise_drainage_area
   get_catchment_input_points(m);
@@ -1453,7 +1552,10 @@ extern "C" long hco_iterate(hco_model* m, long n, int flags, hco_step_record* re
     m->cycle += m->time_step / 60;
     reach_water_and_sediment_input(m);
     m->waterinput = 0;                            // catchment_waterinputs :2027
-    catchment_water_input_and_hydrology(m, hco_get_flow_timestep(m));
+    if (p.spatially_complex_rainfall)
+      catchment_water_input_grid(m, hco_get_flow_timestep(m));
+    else
+      catchment_water_input_and_hydrology(m, hco_get_flow_timestep(m));
     hco_flow_route(m);
     hco_depth_update(m);
     const double md = m->maxdepth;
@@ -1584,6 +1686,18 @@ extern "C" void hco_resume(hco_model* m) {
     for (unsigned j = 1; j < m->jmax; j++)
       if (m->E(i, j) > -9999) m->nActualGridCells[m->rfarea[m->ix(i, j)]]++;
   const int rf = m->p.rfnum;
+  if (m->p.spatially_complex_rainfall) {
+    // the runoff grid from its start: every cell's recurrence depends only
+    // on the rain table and its own elevation's no-data test
+    std::fill(m->rj.begin(), m->rj.end(), 0.000000001);
+    std::fill(m->rjo.begin(), m->rjo.end(), 0.000000001);
+    std::fill(m->rold.begin(), m->rold.end(), 0.0);
+    std::fill(m->rnew.begin(), m->rnew.end(), 0.0);
+    topmodel_runoff_grid(m, 1.0);
+    for (int t = 1; t <= (int)m->time_1; t++) topmodel_runoff_grid(m, (double)t);
+    calchydrograph_grid(m, m->time_1 - m->cycle);
+    return;
+  }
   std::vector<double> keep(m->j_mean);
   for (int n = 0; n <= rf; n++) {
     m->jv[n] = m->jo[n] = 0.000000001;

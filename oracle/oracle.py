@@ -238,7 +238,7 @@ def write_reference_inputs(case, d):
         ("rainfall_data_on", "yes" if rain_on else "no"),
         ("rain_data_time_step", _fmt(p.rain_data_time_step)),
         ("spatial_var_rain", "no"), ("num_unique_rain_cells", str(p.rfnum)),
-        ("spatially_complex_rainfall_on", "no"),
+        ("spatially_complex_rainfall_on", "yes" if p.spatially_complex_rainfall else "no"),
         ("vegetation_on", "no"), ("grass_grow_rate", "0.0"),
         ("vegetation_crit_shear", _fmt(p.vegTauCrit)),
         ("veg_erosion_prop", _fmt(p.veg_lat_restriction)),

@@ -114,13 +114,19 @@ def _have_ref(oracle_mod):
     return os.path.exists(oracle_mod.REF_HARNESS)
 
 
-@pytest.mark.parametrize("kind", ["reach", "catchment"])
+@pytest.mark.parametrize("kind", ["reach", "catchment", "runoff"])
 def test_oracle_matches_live_reference(oracle_mod, kind):
     if not _have_ref(oracle_mod):
         pytest.skip("reference harness not built (no reference checkout)")
     if kind == "reach":
         case = synth.reach_case(imax=48, jmax=20, DX=10.0, hours=24, seed=11)
         n = 3000
+    elif kind == "runoff":
+        # distributed TOPMODEL: every cell takes its own runoff
+        case = synth.catchment_case(n=30, DX=20.0, hours=72, relief=80.0, seed=13,
+                                    lateral=False, storm_start_h=0.5)
+        case.params.spatially_complex_rainfall = 1
+        n = 6000
     else:
         case = synth.catchment_case(n=30, DX=20.0, hours=72, relief=80.0, seed=12, lateral=True)
         n = 15000
