@@ -139,7 +139,7 @@ def log(msg):
 # qx, qy written (48 B); + Manning's n (8 B) when spatially variable;
 # + suspended load (Vsusptot read, qxs, qys written: 24 B) and the two
 # vel_dir entries erosion consumes (16 B) when erosion is on.
-TRAFFIC_SED_FLOW = 121.5  # B per wet cell, profiles/k_flow_route_catchment1400.md
+TRAFFIC_SED_FLOW = 121.6  # B per wet cell, profiles/k_flow_route_catchment1400.md
 
 
 def flow_bytes_per_cell(p):
@@ -270,7 +270,7 @@ def run_gpu(args, rank, world, dist):
                        "traffic": None if traffic_per_cell is None else traffic_per_cell * wet,
                        "peak_kind": kind, "bytes_per_wet_cell": per_cell, "wet_cells": wet,
                        "launch_ms": ms_flow,
-                       "limiter": "FP64 pipe (ncu: 85 % busy, HBM 4 %)"}
+                       "limiter": "FP64 pipe (ncu: 78 % of its issue slots, DRAM 7 %)"}
     return out, model, case
 
 

@@ -101,9 +101,9 @@ __device__ DQ face_dq(double q, double e0, double h0, double e1, double h1, doub
   if (qn != 0) {
     const float hf = approx_abs_f(hflow);
     int t = decide(approx_abs_f(qn) / (hf * sqrtf(9.81f * hf)), (float)fl);
-    if (t == 0) t = (fabs(qn / hflow) / sqrt(kG * hflow) > fl) ? 1 : -1;
+    if (t == 0) t = dgt(ddiv_rn(fabs(ddiv_rn(qn, hflow)), isqrt_rn(kG * hflow)), fl) ? 1 : -1;
     if (t > 0) {
-      const double sg = sqrt(kG * hflow);
+      const double sg = isqrt_rn(kG * hflow);
       const double g = 1.5 * sg * fl;
       if (qn > 0) {
         qn = hflow * (sg * fl);

@@ -116,7 +116,7 @@ __global__ void __launch_bounds__(128) k_entrain_tau(const hc_view c, hc_dev* d)
           }
         }
         if (dgt0(qtot)) {
-          vel = (sqrt(qtot));
+          vel = isqrt_rn(qtot);
           c.vel[cell] = vel;
           if (dgt(vel, p.max_vel)) vel = p.max_vel;
           double ci = kG * (n_man * n_man) * pow(h, -0.33);
@@ -191,7 +191,7 @@ __device__ double entrain_cell(const hc_view& c, hc_dev* d, size_t cell, double 
       double tau_ri = (0.021 + (0.015 * exp(-20 * Fs))) * (rho * kG * d_50) *
                       pow((Di / d_50), (0.67 / (1 + exp(1.5 - (Di / d_50)))));
       // pow(tau / rho, 0.5): the square root, correctly rounded
-      double U_star = sqrt(tau / rho);
+      double U_star = isqrt_rn(tau / rho);
       double Fi = GRN(c, cell, n) / graintot;
       double Wi_star;
       if ((tau / tau_ri) < 1.35)

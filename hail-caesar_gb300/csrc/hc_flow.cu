@@ -378,10 +378,10 @@ __device__ __forceinline__ void inertial_face(double& q, double& qs, double& vel
     int t = decide_gt(fr, c.flf);
     if (t == 0) {
       if (!qoh_valid) qoh = ddiv_rn(qn, hflow);
-      t = (fabs(qoh) / sqrt(kG * hflow) > p.froude_limit) ? 1 : -1;
+      t = dgt(ddiv_rn(fabs(qoh), isqrt_rn(kG * hflow)), p.froude_limit) ? 1 : -1;
     }
     if (t > 0) {
-      const double lim = hflow * (sqrt(kG * hflow) * p.froude_limit);
+      const double lim = hflow * (isqrt_rn(kG * hflow) * p.froude_limit);
       qn = dgt0(qn) ? lim : zero_minus(lim);
       qoh_valid = false;
     }

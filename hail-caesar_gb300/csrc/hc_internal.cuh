@@ -326,6 +326,68 @@ HC_DEV double icube_rn(double h) {
   return __longlong_as_double((long long)(sgn | ((unsigned long long)er << 52) | (sig & M52)));
 }
 
+// sqrt(x) rounded to nearest, on the integer pipe, for positive normal x:
+// x = m' 2^E' with E' even and m' in [2^52, 2^54); s = floor(sqrt(m' 2^52))
+// (53 bits) from a 64-bit reciprocal square root of m' (a float rsqrt.approx
+// estimate, then two Newton-Raphson steps y (3 - u y^2) / 2 in fixed point),
+// settled by the exact remainder r = m' 2^52 - s^2 and rounded up when
+// r > s (a square root never falls on a midpoint).  Other x take the
+// hardware square root through a call (kept out of line so that its FP64
+// instructions are not predicated into the caller).
+static __device__ __noinline__ double sqrt_call(double x) { return sqrt(x); }
+
+HC_DEV double isqrt_rn(double x) {
+  const unsigned long long X = (unsigned long long)__double_as_longlong(x);
+  const int ex = (int)(X >> 52) & 0x7ff;
+  if ((X >> 63) || ex == 0 || ex == 0x7ff) return sqrt_call(x);
+  const unsigned long long m = (X & ((1ull << 52) - 1)) | (1ull << 52);
+  const int E = ex - 1075;
+  const int odd = E & 1;
+  const unsigned long long mp = m << odd;  // [2^52, 2^54)
+  const int big = (mp >> 53) ? 1 : 0;
+  const float uf =
+      __uint_as_float((unsigned)((127 + big) << 23) | (unsigned)((mp >> (29 + big)) & 0x7fffffu));
+  float r0;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r0) : "f"(uf));
+  const unsigned rb = __float_as_uint(r0);  // r0 in (0.5, 1]
+  unsigned long long Y = (unsigned long long)((rb & 0x7fffffu) | 0x800000u) << ((int)(rb >> 23) - 87);
+#pragma unroll
+  for (int k = 0; k < 2; k++) {  // Y ~ 2^63 / sqrt(m' / 2^52)
+    const unsigned long long P_hi = __umul64hi(Y, Y);
+    const unsigned long long lo = mp * P_hi, hi = __umul64hi(mp, P_hi);
+    const unsigned long long W = (hi << 12) | (lo >> 52);  // ~2^62 u y^2
+    const long long E0 = (long long)((1ull << 62) - W);  // ~2^62 (1 - u y^2), small
+    const unsigned long long aE = (E0 < 0) ? (unsigned long long)(-E0) : (unsigned long long)E0;
+    const unsigned long long c = (__umul64hi(Y, aE) << 1) | ((Y * aE) >> 63);  // Y |E0| / 2^63
+    Y = (E0 < 0) ? Y - c : Y + c;
+  }
+  unsigned long long s = (__umul64hi(mp, Y) << 1) | ((mp * Y) >> 63);
+  long long r = (long long)((mp << 52) - s * s);  // exact: |r| < 2^63
+  if (r < 0) {
+    s--;
+    r += (long long)(2 * s + 1);
+  }
+  if (r < 0) {
+    s--;
+    r += (long long)(2 * s + 1);
+  }
+  if (r > (long long)(2 * s)) {
+    r -= (long long)(2 * s + 1);
+    s++;
+  }
+  if (r > (long long)(2 * s)) {
+    r -= (long long)(2 * s + 1);
+    s++;
+  }
+  int er = (E - odd - 52) / 2 + 1075;
+  if (r > (long long)s) s++;
+  if (s == (1ull << 53)) {
+    s >>= 1;
+    er++;
+  }
+  return __longlong_as_double((long long)(((unsigned long long)er << 52) | (s & ((1ull << 52) - 1))));
+}
+
 // RN(x / y) for a divisor fixed for the run, with r = RN(1/y) precomputed:
 // q = RN(x*r) is within one ulp of x/y, the remainder x - q*y is exact in
 // one FMA, and RN(q + rem*r) is the correctly rounded quotient (Markstein's
@@ -353,9 +415,10 @@ HC_DEV double div_const(double x, double y, double r) {
 // relative error below 2^-21 after truncating mb to 24 bits), then two
 // Newton-Raphson steps x + x (1 - mb x) in fixed point, each of which stays
 // below 2^116/mb; the second leaves V within two units of it, so
-// floor(ma V / 2^64) is q or q - 1, and the remainder settles it.  Operands
-// that are zero, subnormal, infinite or NaN, and quotients that would leave
-// the normal range, take the hardware division.
+// floor(ma V / 2^64) is q or q - 1, and the remainder settles it.  A zero
+// dividend gives the signed zero; other operands that are zero, subnormal,
+// infinite or NaN, and quotients that would leave the normal range, take the
+// hardware division.
 //
 // An hc_divisor holds the divisor's part (V), so quotients by one divisor
 // share it: ddiv_prep(b) once, then ddiv_by(a, d) per dividend.  Divisors
@@ -404,7 +467,14 @@ HC_DEV double ddiv_by(double a, const hc_divisor& d) {
     ma <<= 1;
     er--;
   }
-  if (!d.ok || ea == 0 || ea == 0x7ff || er < 1 || er > 2045) return __ddiv_rn(a, d.b);
+  if (!d.ok || ea == 0 || ea == 0x7ff || er < 1 || er > 2045) {
+    // a zero dividend (frequent: flat water surfaces, cells with no net
+    // flux) gives the signed zero here rather than in the hardware division
+    if (d.ok && (A << 1) == 0)
+      return __longlong_as_double(
+          (long long)((A ^ (unsigned long long)__double_as_longlong(d.b)) & 0x8000000000000000ull));
+    return __ddiv_rn(a, d.b);
+  }
   unsigned long long q, r;
   if (mb == H52) {  // b a power of two: exact
     q = ma;

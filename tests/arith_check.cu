@@ -59,9 +59,14 @@ __device__ void pair(int mode, unsigned long long k, double& a, double& b) {
       b = mk(0, eb, r2);
       break;
     }
-    default: {  // the model's magnitudes: depths, discharges, volumes
+    case 5: {  // the model's magnitudes: depths, discharges, volumes
       a = mk(r3 & 1, 1023 - 30 + (int)(r1 >> 59), r1);
       b = mk(0, 1023 - 20 + (int)(r2 >> 59), r2);
+      break;
+    }
+    default: {  // signed zero and subnormal dividends, any divisors
+      a = mk(r3 & 1, 0, (r3 & 2) ? 0ull : r1);
+      b = (r3 & 4) ? __longlong_as_double((long long)r2) : mk(r2 >> 63, 1 + (int)(r2 >> 53) % 2046, r2);
     }
   }
 }
@@ -93,8 +98,9 @@ __global__ void k_check_prepared(unsigned long long n, unsigned long long seed,
        k += (unsigned long long)gridDim.x * blockDim.x) {
     const unsigned long long r1 = mix(k + seed * 0x100000000ull);
     const hc_divisor& d = tab[(r1 >> 40) % ntab];
-    const double a = ((r1 & 7) == 0) ? __longlong_as_double((long long)mix(r1))
-                                     : mk(r1 >> 63, 1023 - 60 + (int)((r1 >> 52) & 127), mix(r1));
+    const double a = ((r1 & 7) == 0)   ? __longlong_as_double((long long)mix(r1))
+                     : ((r1 & 15) == 1) ? mk(r1 >> 63, 0, 0)  // signed zeros
+                                        : mk(r1 >> 63, 1023 - 60 + (int)((r1 >> 52) & 127), mix(r1));
     const double x = ddiv_by(a, d), y = __ddiv_rn(a, d.b);
     const bool same = __double_as_longlong(x) == __double_as_longlong(y) ||
                       (disnan(x) && disnan(y));
@@ -150,6 +156,29 @@ __global__ void k_check_conv(unsigned long long n, unsigned long long seed,
     if (!(same1 && same2) && atomicAdd(bad, 1ull) == 0) {
       first[0] = x;
       first[1] = (double)f;
+    }
+  }
+}
+
+// the integer-pipe square root against the hardware's
+__global__ void k_check_sqrt(unsigned long long n, unsigned long long seed, int mode,
+                             unsigned long long* bad, double* first) {
+  for (unsigned long long k = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; k < n;
+       k += (unsigned long long)gridDim.x * blockDim.x) {
+    const unsigned long long r = mix(k + seed * 0x100000000ull);
+    double x;
+    if (mode == 0) x = __longlong_as_double((long long)r);            // any bit pattern
+    else if (mode == 1) x = mk(0, 1 + (int)((r >> 52) % 2046), r);    // positive normal
+    else {                                                            // squares and neighbours
+      const double q = (double)(r >> 40) + 1.0;
+      x = __longlong_as_double(__double_as_longlong(q * q) + (long long)(r & 3) - 1);
+    }
+    const double a = isqrt_rn(x), b = sqrt(x);
+    const bool same = __double_as_longlong(a) == __double_as_longlong(b) || (disnan(a) && disnan(b));
+    if (!same && atomicAdd(bad, 1ull) == 0) {
+      first[0] = x;
+      first[1] = a;
+      first[2] = b;
     }
   }
 }
@@ -211,6 +240,22 @@ extern "C" int arith_check_conv(unsigned long long n, unsigned long long seed,
   cudaMemset(d_bad, 0, 8);
   cudaMemset(d_first, 0, 32);
   k_check_conv<<<152 * 16, 256>>>(n, seed, d_bad, d_first);
+  cudaMemcpy(bad, d_bad, 8, cudaMemcpyDeviceToHost);
+  cudaMemcpy(first, d_first, 32, cudaMemcpyDeviceToHost);
+  const cudaError_t e = cudaGetLastError();
+  cudaFree(d_bad);
+  cudaFree(d_first);
+  return e == cudaSuccess ? 0 : 2;
+}
+
+extern "C" int arith_check_sqrt(unsigned long long n, unsigned long long seed, int mode,
+                                unsigned long long* bad, double* first) {
+  unsigned long long* d_bad;
+  double* d_first;
+  if (cudaMalloc(&d_bad, 8) != cudaSuccess || cudaMalloc(&d_first, 32) != cudaSuccess) return 1;
+  cudaMemset(d_bad, 0, 8);
+  cudaMemset(d_first, 0, 32);
+  k_check_sqrt<<<152 * 16, 256>>>(n, seed, mode, d_bad, d_first);
   cudaMemcpy(bad, d_bad, 8, cudaMemcpyDeviceToHost);
   cudaMemcpy(first, d_first, 32, cudaMemcpyDeviceToHost);
   const cudaError_t e = cudaGetLastError();

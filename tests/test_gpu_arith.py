@@ -2,7 +2,8 @@
 hc_internal.cuh) against the hardware's division, bit for bit: 2^30
 quotients per input family (arbitrary bit patterns, normal operands, edge
 significands, near-integer quotients, edges of the normal range, the
-model's magnitudes); and the throughput of both, printed."""
+model's magnitudes, signed zero and subnormal dividends); and the
+throughput of both, printed."""
 import ctypes as C
 import os
 import subprocess
@@ -12,7 +13,7 @@ import pytest
 pytestmark = pytest.mark.gpu
 HERE = os.path.dirname(os.path.abspath(__file__))
 FAMILIES = ["bit patterns", "normal", "edge significands", "near-integer quotients",
-            "range edges", "model magnitudes"]
+            "range edges", "model magnitudes", "zero and subnormal dividends"]
 
 
 @pytest.fixture(scope="module")
@@ -30,6 +31,8 @@ def arith(tmp_path_factory):
     lib.arith_check_cube.argtypes = [C.c_uint64, C.c_uint64, C.c_int, C.POINTER(C.c_uint64),
                                      C.POINTER(C.c_double)]
     lib.arith_check_conv.argtypes = [C.c_uint64, C.c_uint64, C.POINTER(C.c_uint64),
+                                     C.POINTER(C.c_double)]
+    lib.arith_check_sqrt.argtypes = [C.c_uint64, C.c_uint64, C.c_int, C.POINTER(C.c_uint64),
                                      C.POINTER(C.c_double)]
     lib.arith_time.argtypes = [C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float)]
     return lib
@@ -69,6 +72,17 @@ def test_cube_on_integer_pipe(arith, mode):
         exact = Fraction(h) ** 3
         want = float(exact) if abs(exact) < Fraction(2) ** 1023 else math.copysign(math.inf, h)
         assert x == want, "h=%r: icube %r, cube_rn %r, exact %r" % (h, x, y, want)
+
+
+@pytest.mark.parametrize("mode", range(3), ids=["bit patterns", "positive normal", "squares"])
+def test_sqrt_on_integer_pipe(arith, mode):
+    """isqrt_rn (the Froude limiter's and the flow velocity's square roots)
+    against the hardware square root, 2^30 arguments per family."""
+    bad = C.c_uint64(0)
+    first = (C.c_double * 4)()
+    assert arith.arith_check_sqrt(1 << 30, 11 + mode, mode, C.byref(bad), first) == 0
+    assert bad.value == 0, "%d mismatches; first x=%r got %r want %r" % (
+        bad.value, first[0], first[1], first[2])
 
 
 def test_float_conversions_on_integer_pipe(arith):
