@@ -522,135 +522,6 @@ __global__ void __launch_bounds__(256) k_apply_pre(const hc_view c, hc_dev* d) {
   c.erodetot3[cell] = et3;
 }
 
-// A cell as the apply walkers hold it.
-struct ApplyRow {
-  double g[HC_G + 1];  // grain record, planes 0..HC_G
-  double elev, h, bed, edge;
-  int idx;             // index[] (-9999: no record)
-  bool dirty;          // g[1..9] or elev changed
-};
-
-__device__ __forceinline__ void row_load(const hc_view& c, size_t cell, size_t ecell,
-                                         ApplyRow& r) {
-#pragma unroll
-  for (int n = 0; n <= HC_G; n++) r.g[n] = GRN(c, cell, n);
-  r.elev = c.elev[cell];
-  r.h = c.h[cell];
-  r.bed = c.bed[cell];
-  r.edge = c.edge[ecell];
-  r.idx = c.index[cell];
-  r.dirty = false;
-}
-
-__device__ __forceinline__ void row_store(const hc_view& c, size_t cell, const ApplyRow& r) {
-  if (!r.dirty) return;
-#pragma unroll
-  for (int n = 1; n <= HC_G - 1; n++) GRN(c, cell, n) = r.g[n];
-  c.elev[cell] = r.elev;
-}
-
-// sort_active on a held row; the strata stay in memory (they move only when
-// the record crosses a threshold).  Same decisions as sort_active_dev.
-__device__ void sort_active_row(const hc_view& c, hc_dev* d, size_t cell, ApplyRow& r) {
-  if (r.idx == -9999) {
-    d->err_code = 201;  // records were allocated before the pass (cannot happen)
-    d->pause |= HC_PAUSE_ERROR;
-    return;
-  }
-  const double active = c.p.active;
-  float sf = 0.0f, af = 0.0f;
-#pragma unroll
-  for (int n = 0; n <= HC_G; n++) {
-    const float f = approx_f(r.g[n]);
-    sf += f;
-    af += fabsf(f);
-  }
-  const float tol = 1e-5f * af + 1e-30f;
-  const float hi = c.act_hi, lo = c.act_lo;
-  const int dep = (sf > hi + tol) ? 1 : ((sf < hi - tol) ? -1 : 0);
-  const int ero = (sf < lo - tol) ? 1 : ((sf > lo + tol) ? -1 : 0);
-  if (dep == -1 && ero == -1) return;
-  double total = 0.0;
-#pragma unroll
-  for (int n = 0; n <= HC_G; n++) total += r.g[n];
-  if (total > (active * 1.5)) {
-    for (int z = 9; z >= 1; z--)
-      for (int n = 0; n <= HC_G - 2; n++) STR(c, cell, z, n) = STR(c, cell, z - 1, n);
-    const double coeff = active / total;
-#pragma unroll
-    for (int n = 1; n <= HC_G - 1; n++) {
-      if (r.g[n] > 0.0) {
-        const double amount = coeff * (r.g[n]);
-        STR(c, cell, 0, n - 1) = amount;
-        r.g[n] = r.g[n] - amount;
-      }
-    }
-    r.dirty = true;
-  }
-  if (total < (active / 4)) {
-#pragma unroll
-    for (int n = 1; n <= HC_G - 1; n++) r.g[n] += STR(c, cell, 0, n - 1);
-    for (int z = 0; z <= 8; z++)
-      for (int n = 0; n <= HC_G - 2; n++) STR(c, cell, z, n) = STR(c, cell, z + 1, n);
-    for (int n = 1; n <= HC_G - 1; n++) STR(c, cell, 9, n - 1) = active * c.p.dprop[n];
-    r.dirty = true;
-  }
-}
-
-// slide_GS(a -> b, amount) on held rows (records exist: allocated before the
-// pass).  Same arithmetic as slide_GS_dev.
-// The sum of A's positive fractions, in order: slide_GS's `total`.
-__device__ __forceinline__ double positive_total(const ApplyRow& A) {
-  double total = 0;
-#pragma unroll
-  for (int n = 1; n <= HC_G - 1; n++)
-    if (dgt0(A.g[n])) total += A.g[n];
-  return total;
-}
-
-// total_a: positive_total(A), which the caller may have formed ahead (the
-// sum is a chain of nine dependent FP64 additions)
-__device__ void slide_GS_rows(const hc_view& c, hc_dev* d, size_t a, ApplyRow& A, double amount,
-                              size_t b, ApplyRow& B, double total_a) {
-  const double* dprop = c.p.dprop;
-  const bool ha = A.idx != -9999, hb = B.idx != -9999;
-  if (ha && hb) {
-    const double total = total_a;
-    if (dgt(amount, total)) {
-#pragma unroll
-      for (int n = 1; n <= HC_G - 1; n++) B.g[n] += (amount - total) * dprop[n];
-      amount = total;
-    }
-    if (dgt0(total)) {
-      const hc_divisor td = ddiv_prep(total);
-#pragma unroll
-      for (int n = 1; n <= HC_G - 1; n++) {
-        const double ga = A.g[n];
-        const double t = amount * ddiv_by(ga, td);
-        B.g[n] += t;
-        double na = ga - t;
-        if (dlt0(na)) na = 0;
-        A.g[n] = na;
-      }
-    }
-    A.dirty = B.dirty = true;
-    sort_active_row(c, d, a, A);
-    sort_active_row(c, d, b, B);
-    return;
-  }
-  if (!ha && hb) {
-#pragma unroll
-    for (int n = 1; n <= HC_G - 1; n++) B.g[n] += (amount)*dprop[n];
-    B.dirty = true;
-    sort_active_row(c, d, b, B);
-    return;
-  }
-  if (ha && !hb) {
-    d->err_code = 202;  // receiver without a record outside a serial context
-    d->pause |= HC_PAUSE_ERROR;
-  }
-}
-
 // One lateral step of the apply passes (:4630-4677, :4690-4744) from a cell
 // at elevation e0 (tau0, erodetot3 et3) toward its neighbour N.  Returns
 // false when the raw amount is not positive; otherwise the (possibly zeroed

@@ -93,6 +93,24 @@ __device__ bool slide_visit(const hc_view& c, hc_dev* d, int x, int y, double fa
   return any;
 }
 
+// slide_GS for a move of the replay.  When both records exist, on the
+// records held in registers (all loads issued together: the serial replay
+// waits on latency); out of line, so that the eight tests of a visit share
+// one copy of it.
+static __device__ __noinline__ void replay_slide_GS(const hc_view& c, hc_dev* d, size_t cell,
+                                                    double diff, size_t nb) {
+  if (c.index[cell] != -9999 && c.index[nb] != -9999) {
+    ApplyRow A, B;
+    row_load(c, cell, 0, A);
+    row_load(c, nb, 0, B);
+    slide_GS_rows(c, d, cell, A, diff, nb, B, positive_total(A));
+    row_store(c, cell, A);
+    row_store(c, nb, B);
+  } else {
+    slide_GS_dev(c, d, cell, diff, nb, true);
+  }
+}
+
 // The visit as the serial replay makes it: the eight neighbours' elevations
 // are loaded together (one round trip instead of eight dependent ones), a
 // diagonal test is first decided on a float estimate and its FP64 division
@@ -138,8 +156,11 @@ __device__ int slide_visit_held(const hc_view& c, hc_dev* d, int x, int y, doubl
     en[k] = e2 + diff;
     c.elev[cell] = e;
     c.elev[nb] = en[k];
-    if (global) *total += diff;
-    else slide_GS_dev(c, d, cell, diff, nb, true);
+    if (global) {
+      *total += diff;
+    } else {
+      replay_slide_GS(c, d, cell, diff, nb);
+    }
     moved |= 1 << k;
   }
   return moved;
