@@ -288,7 +288,7 @@ extern "C" hc_status hc_create(const hc_params* p, size_t max_bytes, hc_ctx** ou
   if (sed) {
     A(v.sflux, 40 * N2) A(v.grain, 11 * N2) A(v.strata, 90 * N2) A(v.alloc_key, N2)
     A(v.erodetot, N2) A(v.erodetot3, N2) A(v.pre, 11 * N2) A(v.chains, 4 * N2)
-    A(v.drain_snap, N2) A(v.ent_list, N2)
+    A(v.drain_snap, N2) A(v.ent_list, N2) A(v.ent_qs, 2 * N2)
   } else {
     A(v.erodetot, N2)
   }
@@ -368,7 +368,7 @@ static hc_status free_all(hc_ctx* c) {
   void* ptrs[] = {v.elev, v.h, v.qx, v.qy, v.qxs, v.qys, v.vs, v.vel, v.tau, v.bed, v.man,
                   v.area, v.ss, v.vd, v.sflux, v.grain, v.strata, v.index, v.mask, v.rfarea,
                   v.edge, v.edge2, v.veg, v.cin_x, v.cin_y, v.erodetot, v.erodetot3, v.pre,
-                  v.chains, v.ent_list, v.drain_pos, v.drain_f0, v.drain_f1, v.drain_pend, v.drain_dt, v.drain_frac, v.drain_multi,
+                  v.chains, v.ent_list, v.ent_qs, v.drain_pos, v.drain_f0, v.drain_f1, v.drain_pend, v.drain_dt, v.drain_frac, v.drain_multi,
                   v.drain_snap, v.drain_aux, v.alloc_key, v.red, v.touched, v.topm, v.rain, v.rec, c->dev, v.wet,
                   v.wet_sums,
                   v.reach[0], v.reach[1], v.reach[2], extra(c).lateral};

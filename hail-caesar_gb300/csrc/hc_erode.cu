@@ -63,11 +63,12 @@ __global__ void k_erode_begin(const hc_view c, hc_dev* d, int gated, double mult
 // entrainment pass
 // ---------------------------------------------------------------------------
 // Two kernels.  k_entrain_tau, one thread per cell, clears the pass's
-// outputs, makes the records of cells that ask for one, computes the flow
-// velocity and shear stress, and lists the cells whose tau is positive
-// (one atomic per warp).  k_entrain runs the transport of the listed cells
-// only, so its warps are full: in a storm, a third or less of the lanes of a
-// row of cells has tau > 0, and the transport is FP64-pipe bound.
+// outputs, makes the records of cells that ask for one, sums the squared
+// velocities and slopes, and lists the cells with flow (qtot > 0; one
+// atomic per warp).  k_entrain computes the shear stress and the transport
+// of the listed cells only, so its warps are full: in a storm, a third or
+// less of the lanes of a row of cells has flow, and these terms (pow, the
+// Einstein or Wilcock sums) are FP64-pipe bound.
 __global__ void __launch_bounds__(128) k_entrain_tau(const hc_view c, hc_dev* d) {
   if (!(d->it_active && d->erode_retry)) return;
   const hc_params& p = c.p;
@@ -77,6 +78,7 @@ __global__ void __launch_bounds__(128) k_entrain_tau(const hc_view c, hc_dev* d)
   const double thr = p.water_depth_erosion_threshold;
   bool listed = false;
   size_t cell = 0;
+  double qtot = 0, slopetot = 0;
   if (ix <= c.imax && jy <= c.jmax - 1) {
     cell = (size_t)ix * W + jy;
     if (c.mask[cell]) {
@@ -93,14 +95,13 @@ __global__ void __launch_bounds__(128) k_entrain_tau(const hc_view c, hc_dev* d)
       if (dgt(h, thr)) {
         const double e0 = c.elev[cell];
         const unsigned long long pos = (unsigned long long)jy * (c.imax + 2) + ix;
-        double n_man = p.spatially_var_mannings ? c.man[cell] : p.mannings;
         if (c.index[cell] == -9999) {  // addGS(x, y)
           grain_record_init(c, cell, e0, c.bed[cell]);
           c.index[cell] = -2;  // record made, row number pending
           atomicMin(&c.alloc_key[cell], pos * 5);
           d->alloc_count = 1;
         }
-        double vel = 0, qtot = 0, tau = 0, slopetot = 0;
+        double vel = 0;
         for (int k = 0; k < 4; k++) {
           const int pp = 1 + 2 * k;
           const int x2 = ix + kDXc[pp], y2 = jy + kDYc[pp];
@@ -115,16 +116,9 @@ __global__ void __launch_bounds__(128) k_entrain_tau(const hc_view c, hc_dev* d)
             }
           }
         }
-        if (dgt0(qtot)) {
-          vel = isqrt_rn(qtot);
-          c.vel[cell] = vel;
-          if (dgt(vel, p.max_vel)) vel = p.max_vel;
-          double ci = kG * (n_man * n_man) * pow(h, -0.33);
-          if (dgt0(slopetot)) slopetot = 0;
-          tau = 1000 * ci * vel * vel * (1 + (1 * ddiv_rn(slopetot, vel)));
-          c.tau[cell] = tau;
-        }
-        listed = dgt0(tau);
+        // the shear stress itself (:4316-4333: sqrt, pow(h, -0.33)) is
+        // evaluated by k_entrain for the listed cells, whose warps are full
+        listed = dgt0(qtot);
       }
     }
   }
@@ -135,18 +129,36 @@ __global__ void __launch_bounds__(128) k_entrain_tau(const hc_view c, hc_dev* d)
     unsigned base = 0;
     if (lane == 0) base = atomicAdd(&d->ent_n, (unsigned)__popc(b));
     base = __shfl_sync(0xffffffffu, base, 0);
-    if (listed) c.ent_list[base + __popc(b & ((1u << lane) - 1))] = (uint32_t)cell;
+    if (listed) {
+      const unsigned k = base + __popc(b & ((1u << lane) - 1));
+      c.ent_list[k] = (uint32_t)cell;
+      c.ent_qs[2 * (size_t)k] = qtot;
+      c.ent_qs[2 * (size_t)k + 1] = slopetot;
+    }
   }
 }
 
-// The transport of one listed cell (:4388-4548); returns temptot1.
+// The shear stress (:4316-4333) and the transport (:4388-4548) of one
+// listed cell (qtot > 0); returns temptot1.
 __device__ double entrain_cell(const hc_view& c, hc_dev* d, size_t cell, double mult,
-                               double ts) {
+                               double ts, double qtot, double slopetot) {
   const hc_params& p = c.p;
   const size_t W = c.W, N2 = c.N2;
   const int ix = (int)(cell / W), jy = (int)(cell % W);
   const double thr = p.water_depth_erosion_threshold;
-  const double h = c.h[cell], tau = c.tau[cell];
+  const double h = c.h[cell];
+  double tau;
+  {
+    double vel = isqrt_rn(qtot);
+    c.vel[cell] = vel;
+    if (dgt(vel, p.max_vel)) vel = p.max_vel;
+    const double n_man = p.spatially_var_mannings ? c.man[cell] : p.mannings;
+    const double ci = kG * (n_man * n_man) * pow(h, -0.33);
+    if (dgt0(slopetot)) slopetot = 0;
+    tau = 1000 * ci * vel * vel * (1 + (1 * ddiv_rn(slopetot, vel)));
+    c.tau[cell] = tau;
+    if (!dgt0(tau)) return 0;  // no transport from this cell
+  }
   const double rho = 1000.0;
   const double e0 = c.elev[cell];
   const unsigned long long pos = (unsigned long long)jy * (c.imax + 2) + ix;
@@ -275,7 +287,8 @@ __global__ void __launch_bounds__(128) k_entrain(const hc_view c, hc_dev* d, int
   double tb = 0;
   for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < n_list;
        k += gridDim.x * blockDim.x)
-    tb = smax(tb, entrain_cell(c, d, c.ent_list[k], mult, ts));
+    tb = smax(tb, entrain_cell(c, d, c.ent_list[k], mult, ts, c.ent_qs[2 * (size_t)k],
+                               c.ent_qs[2 * (size_t)k + 1]));
   // tempbmax: max over the pass (warp shuffle, block, grid via last block)
   for (int o = 16; o > 0; o >>= 1) tb = smax(tb, __shfl_xor_sync(0xffffffffu, tb, o));
   const int t = threadIdx.x;
@@ -1287,16 +1300,14 @@ __global__ void __launch_bounds__(1024) k_edge_out(const hc_view c, hc_dev* d, d
   const int k0 = threadIdx.x * per, k1 = min(ntot, k0 + per);
   int mine = 0;
   for (int k = k0; k < k1; k++) {
-    int x, y, srcx, srcy, dir;
+    int x, y;  // the sources: sr[imax-1][y], sl[2][y], sd[x][jmax-1], su[x][2]
     if (k < nA) {
       y = 2 + k / 2;
-      if ((k & 1) == 0) { x = imax; srcx = imax - 1; srcy = y; dir = 1; }  // sr[imax-1][y]
-      else { x = 1; srcx = 2; srcy = y; dir = 3; }                          // sl[2][y]
+      x = ((k & 1) == 0) ? imax : 1;
     } else {
       const int kk = k - nA;
       x = 2 + kk / 2;
-      if ((kk & 1) == 0) { y = jmax; srcx = x; srcy = jmax - 1; dir = 2; }  // sd[x][jmax-1]
-      else { y = 1; srcx = x; srcy = 2; dir = 0; }                          // su[x][2]
+      y = ((kk & 1) == 0) ? jmax : 1;
     }
     const size_t cell = (size_t)x * c.W + y;
     if (c.h[cell] > thr || c.vs[cell] > 0) mine++;

@@ -137,7 +137,8 @@ struct hc_view {
   int32_t *wet;                // cells of the wet mask, ascending (the down_scan
                                // lists as one array); length in hc_dev::wet_count
   int32_t *wet_sums;           // per-block counts for building it
-  uint32_t *ent_list;          // cells with tau > 0 in an entrainment pass (N2)
+  uint32_t *ent_list;          // cells with flow in an entrainment pass (N2)
+  double *ent_qs;              // their qtot and slope sum (2 per entry)
   int cin_cap;
 
   // time series
