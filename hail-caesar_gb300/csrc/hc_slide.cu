@@ -291,12 +291,24 @@ __device__ int32_t heap_pop(int32_t* h, int& n) {
   return top;
 }
 
-// Queue the later loop positions whose visit reads a cell within one of
-// (x, y) - i.e. visits of cells within two.
-__device__ void push_affected(const hc_view& c, hc_dev* d, const Order& o, int x, int y,
+// Queue the later loop positions whose visit reads a cell changed by the
+// moves of a visit at (x, y): the visited cell and each moved-to neighbour
+// (bit k of `moved`).  A visit reads the 3x3 block around its cell, so
+// these are the positions whose cell lies within one of a changed cell;
+// every other later position still sees the elevations the probe tested.
+__device__ void push_affected(const hc_view& c, hc_dev* d, const Order& o, int x, int y, int moved,
                               long long Pcur, bool global, int32_t* heap, int& hn, int cap) {
+  // cells of the 5x5 block around (x, y) within one of a changed cell
+  unsigned need = 0;  // bit (dx+2)*5 + (dy+2)
+  for (int k = -1; k < 8; k++) {
+    if (k >= 0 && !((moved >> k) & 1)) continue;
+    const int cx = (k < 0) ? 0 : kSx[k], cy = (k < 0) ? 0 : kSy[k];
+    for (int dx = -1; dx <= 1; dx++)
+      for (int dy = -1; dy <= 1; dy++) need |= 1u << ((cx + dx + 2) * 5 + (cy + dy + 2));
+  }
   for (int dx = -2; dx <= 2; dx++)
     for (int dy = -2; dy <= 2; dy++) {
+      if (!((need >> ((dx + 2) * 5 + (dy + 2))) & 1u)) continue;
       const int xx = x + dx, yy = y + dy;
       if (xx < 2 || xx > c.imax - 1 || yy < 2 || yy > c.jmax - 1) continue;
       if (global) {
@@ -351,7 +363,7 @@ __global__ void k_slide_replay(const hc_view c, hc_dev* d, const int32_t* list, 
       if (xc == 1) xc = 2;
     }
     const int moved = slide_visit_held(c, d, xc, y, factor, global != 0, &total);
-    if (moved) push_affected(c, d, o, xc, y, cand, global != 0, heap, hn, heap_cap);
+    if (moved) push_affected(c, d, o, xc, y, moved, cand, global != 0, heap, hn, heap_cap);
     if (d->err_code == 301 && err0 != 301) {
       // heap overflow: finish the sweep visiting every later position
       d->err_code = err0;
