@@ -270,7 +270,7 @@ def run_gpu(args, rank, world, dist):
                        "traffic": None if traffic_per_cell is None else traffic_per_cell * wet,
                        "peak_kind": kind, "bytes_per_wet_cell": per_cell, "wet_cells": wet,
                        "launch_ms": ms_flow,
-                       "limiter": "FP64 pipe (ncu: 78 % of its issue slots, DRAM 7 %)"}
+                       "limiter": "FP64 pipe (ncu: 67 % of its issue slots, ALU 42 %, DRAM 9 %)"}
     return out, model, case
 
 

@@ -255,7 +255,6 @@ extern "C" hc_status hc_create(const hc_params* p, size_t max_bytes, hc_ctx** ou
     const double Di = p->d[n], g = 9.81;
     v.einA[n] = (2650 - 1000) * Di;
     v.einS[n] = std::sqrt(1000 / ((2250 - 1000) * g * (Di * Di * Di)));
-    v.einRS[n] = 1.0 / v.einS[n];
     v.einSd[n] = host_divisor(v.einS[n]);
   }
   v.imax = p->imax;

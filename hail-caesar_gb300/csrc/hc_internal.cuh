@@ -115,7 +115,7 @@ struct hc_divisor {
 // Everything a kernel needs, passed by value (device pointers + parameters).
 struct hc_view {
   hc_params p;
-  double rDX;             // RN(1/DX), for div_const
+  double rDX;             // RN(1/DX) (the adjoint's slope derivatives)
   hc_divisor dxd;         // DX as a divisor (ddiv_by)
   float DXf, flf;         // DX and froude_limit as floats (estimates only)
   float act_hi, act_lo;   // (float)(active*1.5), (float)(active/4): sort_active's estimates
@@ -151,7 +151,7 @@ struct hc_view {
   // sqrt(1000/((2250-1000)*g*Di^3)) and its reciprocal
   double runoff_count[HC_MAX_RF + 1];  // distributed runoff: computed cells per rain state
   unsigned runoff_present;             // bit z: rain state z holds a computed cell
-  double einA[HC_G], einS[HC_G], einRS[HC_G];
+  double einA[HC_G], einS[HC_G];
   hc_divisor einSd[HC_G];  // the einS as divisors
 
   // scratch
@@ -387,20 +387,6 @@ HC_DEV double isqrt_rn(double x) {
     er++;
   }
   return __longlong_as_double((long long)(((unsigned long long)er << 52) | (s & ((1ull << 52) - 1))));
-}
-
-// RN(x / y) for a divisor fixed for the run, with r = RN(1/y) precomputed:
-// q = RN(x*r) is within one ulp of x/y, the remainder x - q*y is exact in
-// one FMA, and RN(q + rem*r) is the correctly rounded quotient (Markstein's
-// theorem, Handbook of Floating-Point Arithmetic, 2nd ed., sec. 4.7).  Valid
-// away from underflow/overflow, so x outside [2^-900, 2^900] in magnitude
-// takes the ordinary division.  Three FP64 operations instead of a division.
-HC_DEV double div_const(double x, double y, double r) {
-  const int ex = (__double2hiint(x) >> 20) & 0x7ff;
-  if (ex < 1023 - 900 || ex > 1023 + 900) return __ddiv_rn(x, y);
-  const double q = __dmul_rn(x, r);
-  const double e = fma(-q, y, x);
-  return fma(e, r, q);
 }
 
 // RN(a / b), the IEEE quotient, computed on the integer pipe.  On this GPU

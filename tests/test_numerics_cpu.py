@@ -3,7 +3,8 @@
 cube_rn (the friction term's h^3) is correctly rounded; glibc's
 pow(h, 3.0), which the reference calls, is not always (about 0.08 % of
 arguments), which is why hydraulic parity is to rounding level rather than
-bitwise.  div_const (division by the cell size) equals IEEE division."""
+bitwise.  (The integer-pipe division, cube and square root are checked
+against the GPU's own instructions in test_gpu_arith.py.)"""
 import ctypes as C
 import os
 import subprocess
@@ -25,10 +26,6 @@ def numlib():
     lib = C.CDLL(so)
     lib.cube_rn.restype = C.c_double
     lib.cube_rn.argtypes = [C.c_double]
-    lib.div_const.restype = C.c_double
-    lib.div_const.argtypes = [C.c_double, C.c_double, C.c_double]
-    lib.div_mismatches.restype = C.c_long
-    lib.div_mismatches.argtypes = [C.c_double, C.c_long, C.c_uint64]
     return lib
 
 
@@ -49,11 +46,6 @@ def test_glibc_pow_cube_is_not_always_correctly_rounded(numlib):
     libm.pow.argtypes = [C.c_double, C.c_double]
     diff = sum(1 for h in hs if libm.pow(float(h), 3.0) != numlib.cube_rn(float(h)))
     assert diff < 0.01 * len(hs)
-
-
-@pytest.mark.parametrize("y", [5.0, 10.0, 20.0, 50.0, 12.5, 9.81, 3.0, 100.0])
-def test_div_const_equals_division(numlib, y):
-    assert numlib.div_mismatches(y, 400000, 1234) == 0
 
 
 def test_exact_sort_matches_std_sort(tmp_path):
