@@ -4,16 +4,18 @@
 //                          core, hc_host.cpp)
 //   creep                  :5293-5427 (host-driven, every 10 days)
 //
-// slide_3 and global landsliding are sequential relaxations: every test sees
-// the elevations left by the moves before it, in the reference's loop order.
-// Moves are rare (a drop steeper than the failure angle over one cell), so
-// the device first tests every cell against the elevations at the start of
-// the sweep, in parallel.  If no test passes, the serial sweep would move
-// nothing either and the sweep is over.  Otherwise one thread replays the
-// sweep in loop order, visiting only (a) the cells whose test passed and
-// (b) cells later in the loop whose 3x3 neighbourhood a move has changed -
-// every other cell would evaluate its tests on unchanged elevations, where
-// they failed.  The result is the serial sweep's, move for move.
+// slide_3 is a sequential relaxation: every test sees the elevations left by
+// the moves before it, in the reference's loop order.  Moves are rare (a
+// drop steeper than the failure angle over one cell), so the device first
+// tests every cell against the elevations at the start of the sweep, in
+// parallel.  If no test passes, the serial sweep would move nothing either
+// and the sweep is over.  Otherwise one thread replays the sweep in loop
+// order, visiting only (a) the cells whose test passed and (b) cells later
+// in the loop whose 3x3 neighbourhood a move has changed - every other cell
+// would evaluate its tests on unchanged elevations, where they failed.  The
+// result is the serial sweep's, move for move.  Tests are decided on float
+// estimates built with integer operations, and formed in FP64 only near the
+// threshold: the FP64 pipe is this GPU's scarce unit.
 
 #include "hc_grain.cuh"
 
@@ -24,73 +26,83 @@
 
 namespace {
 
-// neighbour order of the eight tests (:5457-5522 and :5561-5641)
-__constant__ int kSx[8] = {1, 0, -1, -1, -1, 0, 1, 1};
-__constant__ int kSy[8] = {1, 1, 1, 0, -1, -1, -1, 0};
-
 struct SlideScratch {
   uint8_t* flag;        // N2 bytes, one per loop position
   int32_t* list;        // positions whose test passed, in loop order
   int32_t* block_sums;
   int32_t* count;
-  int32_t* heap;        // pending re-tests
+  int32_t* heap;        // pending re-tests, once the shared-memory heap is full
   int heap_cap;
-  double* total;        // global landsliding: sum of moves of the sweep
 };
 
-// Loop position of a cell.  slide_3 walks columns (y outer, the wet rows of
-// down_scan inner); global landsliding walks rows (x outer, y inner).
+// pending re-tests the replay holds in shared memory before it moves its heap
+// to device memory
+constexpr int kSharedHeap = 8192;
+
+// Loop position of a cell: slide_3 walks columns (y outer, the wet rows of
+// down_scan inner), P = y*(imax+2) + x.  Positions fit 32 bits, as the
+// grid's cell count does.
 struct Order {
-  int col_major;  // 1: P = y*(imax+2) + x ; 0: P = x*(jmax+2) + y
-  int imax, jmax;
-  __device__ __forceinline__ long long pos(int x, int y) const {
-    return col_major ? (long long)y * (imax + 2) + x : (long long)x * (jmax + 2) + y;
-  }
-  __device__ __forceinline__ void cell(long long P, int& x, int& y) const {
-    if (col_major) {
-      y = (int)(P / (imax + 2));
-      x = (int)(P % (imax + 2));
-    } else {
-      x = (int)(P / (jmax + 2));
-      y = (int)(P % (jmax + 2));
-    }
+  int H;  // imax + 2
+  __device__ __forceinline__ int pos(int x, int y) const { return y * H + x; }
+  __device__ __forceinline__ void cell(int P, int& x, int& y) const {
+    y = P / H;
+    x = P - y * H;
   }
 };
 
-// The eight tests of one visit.  slide3: the cell is the clamped row of a
-// down_scan entry, failure at tan(angle)*DX or 10000 when at the bedrock
-// floor, moves go through slide_GS.  global: cap at ERODEFACTOR, floor factor
-// 10*DX, no grain bookkeeping.  `probe`: test only, no moves.
-__device__ bool slide_visit(const hc_view& c, hc_dev* d, int x, int y, double factor, bool global,
-                            bool probe, double* total, int* moved_dirs) {
+// One test of a visit (:5457-5522): drop > w with drop = (e - e2)/1.41 on a
+// diagonal, e - e2 otherwise.  Decided first on the estimates fe, fe2, fw of
+// e, e2, w (approx_f: integer operations, within a relative 2^-20): the
+// estimated drop is within 1.1 * 2^-20 * (|fe| + |fe2| + |fw|) (+ 2^-125
+// for values below the float range) of (drop - w), and the margin m is eight
+// times that.  Returns 0 when drop <= w surely, 1 when drop > w surely, 2
+// when the FP64 test must decide (non-finite estimates give an infinite or
+// NaN margin, and so 2).
+__device__ __forceinline__ int drop_above_est(float fe, float fe2, float fw, bool diag) {
+  float est = fe - fe2;
+  if (diag) est *= (1.0f / 1.41f);
+  const float m = 0x1p-17f * (fabsf(fe) + fabsf(fe2) + fabsf(fw)) + 1e-30f;
+  const float t = est - fw;
+  if (t < -m) return 0;
+  if (t > m) return 1;
+  return 2;
+}
+
+// the test in FP64, as the reference writes it (:5457-5522); out of line, so
+// that the probe's eight call sites issue no FP64 work when they skip it
+static __device__ __noinline__ bool drop_above_exact(double e, double e2, double w, bool diag) {
+  const double drop = diag ? ((e - e2) / 1.41) : (e - e2);
+  return drop > w && e2 > -9999;
+}
+
+// Whether the visit of the cell at (x, y) would move anything now.  Before a
+// move all eight tests read the same elevations, so any passing test decides.
+__device__ bool slide_probe_cell(const hc_view& c, int x, int y, double factor) {
+  constexpr int dxs[8] = {1, 0, -1, -1, -1, 0, 1, 1};
+  constexpr int dys[8] = {1, 1, 1, 0, -1, -1, -1, 0};
   const size_t W = c.W;
   const size_t cell = (size_t)x * W + y;
-  const double active = c.p.active;
-  double wet_factor = factor;
-  if (c.elev[cell] <= (c.bed[cell] + active)) wet_factor = global ? 10 * c.p.DX : 10000;
-  bool any = false;
-  int moved = 0;
+  double en[8];
+#pragma unroll
+  for (int k = 0; k < 8; k++) en[k] = c.elev[(size_t)(x + dxs[k]) * W + (y + dys[k])];
+  const double e = c.elev[cell];
+  const double wet_factor = (e <= (c.bed[cell] + c.p.active)) ? 10000.0 : factor;
+  const float fe = approx_f(e), fw = approx_f(wet_factor);
+  int undecided = 0;
+#pragma unroll
   for (int k = 0; k < 8; k++) {
-    const int x2 = x + kSx[k], y2 = y + kSy[k];
-    const size_t nb = (size_t)x2 * W + y2;
-    const bool diag = (kSx[k] != 0 && kSy[k] != 0);
-    const double e = c.elev[cell], e2 = c.elev[nb];
-    const double drop = diag ? ((e - e2) / 1.41) : (e - e2);
-    if (drop > wet_factor && e2 > -9999) {
-      any = true;
-      if (probe) return true;
-      double diff = (diag ? ((e - e2) / 1.41) : (e - e2)) - wet_factor;
-      if ((e - diff) < (c.bed[cell] + active)) diff = (e - (c.bed[cell] + active));
-      if (global && diff > c.p.ERODEFACTOR) diff = c.p.ERODEFACTOR;
-      c.elev[cell] = e - diff;
-      c.elev[nb] = e2 + diff;
-      if (global) *total += diff;
-      else slide_GS_dev(c, d, cell, diff, nb, true);
-      moved |= 1 << k;
-    }
+    const int r = drop_above_est(fe, approx_f(en[k]), fw, dxs[k] != 0 && dys[k] != 0);
+    // r == 1: the estimates are finite, so the key compare is e2 > -9999
+    if (r == 1 && dkey(en[k]) > kNoDataKey) return true;
+    if (r == 2) undecided |= 1 << k;
   }
-  if (moved_dirs) *moved_dirs = moved;
-  return any;
+  if (!undecided) return false;
+#pragma unroll
+  for (int k = 0; k < 8; k++)
+    if (((undecided >> k) & 1) && drop_above_exact(e, en[k], wet_factor, dxs[k] != 0 && dys[k] != 0))
+      return true;
+  return false;
 }
 
 // slide_GS for a move of the replay.  When both records exist, on the
@@ -111,81 +123,62 @@ static __device__ __noinline__ void replay_slide_GS(const hc_view& c, hc_dev* d,
   }
 }
 
-// The visit as the serial replay makes it: the eight neighbours' elevations
-// are loaded together (one round trip instead of eight dependent ones), a
-// diagonal test is first decided on a float estimate and its FP64 division
-// evaluated only near the threshold, and moves update the held values.  The
-// tests, moves and their order are slide_visit's; returns the moved
-// directions.
-__device__ int slide_visit_held(const hc_view& c, hc_dev* d, int x, int y, double factor,
-                                bool global, double* total) {
+// The visit as the serial replay makes it (:5445-5525): the eight
+// neighbours' elevations are loaded together (one round trip instead of
+// eight dependent ones), each test is first decided on estimates
+// (drop_above_est) and formed in FP64 only when it may pass, and moves update
+// the held values.  The tests, moves and their order are the reference's;
+// returns the moved directions (bit k: neighbour k).
+__device__ int slide_visit_held(const hc_view& c, hc_dev* d, int x, int y, double factor) {
   constexpr int dxs[8] = {1, 0, -1, -1, -1, 0, 1, 1};
   constexpr int dys[8] = {1, 1, 1, 0, -1, -1, -1, 0};
   const size_t W = c.W;
   const size_t cell = (size_t)x * W + y;
-  const double active = c.p.active;
   double en[8];
 #pragma unroll
   for (int k = 0; k < 8; k++) en[k] = c.elev[(size_t)(x + dxs[k]) * W + (y + dys[k])];
   double e = c.elev[cell];
-  const double floor_e = c.bed[cell] + active;
-  double wet_factor = factor;
-  if (e <= floor_e) wet_factor = global ? 10 * c.p.DX : 10000;
-  const float wf = approx_f(wet_factor);
+  const double floor_e = c.bed[cell] + c.p.active;
+  const double wet_factor = (e <= floor_e) ? 10000.0 : factor;
+  const float fw = approx_f(wet_factor);
   int moved = 0;
 #pragma unroll
   for (int k = 0; k < 8; k++) {
     const bool diag = dxs[k] != 0 && dys[k] != 0;
     const double e2 = en[k];
-    if (!(dkey(e2) > kNoDataKey)) continue;  // e2 > -9999
-    double drop;
-    if (diag) {
-      const float est = approx_f(e - e2) * (1.0f / 1.41f);
-      const float m = 1e-4f * (fabsf(est) + fabsf(wf));
-      if (m >= 1e-34f && m < 1e30f && est - wf < -m) continue;  // surely not above
-      drop = (e - e2) / 1.41;
-    } else {
-      drop = e - e2;
-    }
-    if (!dgt(drop, wet_factor)) continue;
+    if (drop_above_est(approx_f(e), approx_f(e2), fw, diag) == 0) continue;
+    const double drop = diag ? ((e - e2) / 1.41) : (e - e2);
+    if (!(drop > wet_factor && e2 > -9999)) continue;
     double diff = drop - wet_factor;
     if ((e - diff) < floor_e) diff = (e - floor_e);
-    if (global && diff > c.p.ERODEFACTOR) diff = c.p.ERODEFACTOR;
     const size_t nb = (size_t)(x + dxs[k]) * W + (y + dys[k]);
     e = e - diff;
     en[k] = e2 + diff;
     c.elev[cell] = e;
     c.elev[nb] = en[k];
-    if (global) {
-      *total += diff;
-    } else {
-      replay_slide_GS(c, d, cell, diff, nb);
-    }
+    replay_slide_GS(c, d, cell, diff, nb);
     moved |= 1 << k;
   }
   return moved;
 }
 
 // Phase 1: flag every loop position whose visit would move something now.
-__global__ void k_slide_probe(const hc_view c, const hc_dev* d, uint8_t* flag, int global,
-                              double factor, int gated) {
+// Positions follow down_scan's rows, whose first and last wet rows visit the
+// clamped rows 2 and imax-1 (:5436-5440).
+__global__ void k_slide_probe(const hc_view c, const hc_dev* d, uint8_t* flag, double factor,
+                              int gated) {
   if (gated && !(d->it_active && d->rest_active && d->do_slide)) return;
   const int y = 1 + blockIdx.x * blockDim.x + threadIdx.x;
   const int x = 1 + blockIdx.y * blockDim.y + threadIdx.y;
   if (x > c.imax || y > c.jmax) return;
-  const size_t cell = (size_t)x * c.W + y;
   uint8_t f = 0;
-  if (global) {
-    if (x >= 2 && x <= c.imax - 1 && y >= 2 && y <= c.jmax - 1)
-      f = slide_visit(c, nullptr, x, y, factor, true, true, nullptr, nullptr) ? 1 : 0;
-  } else if (y >= 2 && y <= c.jmax - 1 && c.mask[cell]) {
+  if (y >= 2 && y <= c.jmax - 1 && c.mask[(size_t)x * c.W + y]) {
     int xc = x;
     if (xc == c.imax) xc = c.imax - 1;
     if (xc == 1) xc = 2;
-    f = slide_visit(c, nullptr, xc, y, factor, false, true, nullptr, nullptr) ? 1 : 0;
+    f = slide_probe_cell(c, xc, y, factor) ? 1 : 0;
   }
-  // flags are indexed by loop position
-  Order o{global ? 0 : 1, c.imax, c.jmax};
+  const Order o{c.imax + 2};
   flag[o.pos(x, y)] = f;
 }
 
@@ -258,11 +251,8 @@ __global__ void k_flag_compact(const uint8_t* flag, size_t n, const int32_t* blo
 }
 
 // ---- the serial replay -----------------------------------------------------
-__device__ void heap_push(int32_t* h, int& n, int cap, int32_t v, hc_dev* d) {
-  if (n >= cap) {
-    d->err_code = 301;  // overflow: caught by the caller, which rescans
-    return;
-  }
+// A binary min-heap of positions, in shared or device memory.
+__device__ void heap_push(int32_t* h, int& n, int32_t v) {
   int i = n++;
   h[i] = v;
   while (i > 0) {
@@ -274,8 +264,7 @@ __device__ void heap_push(int32_t* h, int& n, int cap, int32_t v, hc_dev* d) {
     i = p;
   }
 }
-__device__ int32_t heap_pop(int32_t* h, int& n) {
-  int32_t top = h[0];
+__device__ void heap_pop(int32_t* h, int& n) {
   h[0] = h[--n];
   int i = 0;
   for (;;) {
@@ -288,107 +277,125 @@ __device__ int32_t heap_pop(int32_t* h, int& n) {
     h[i] = t;
     i = m;
   }
-  return top;
 }
+
+// The replay's pending re-tests: a heap in shared memory that moves to
+// device memory (gheap, gcap entries) when it fills.
+struct Pending {
+  int32_t* h;
+  int n, cap;
+  int32_t* gheap;
+  int gcap;
+  // false when the device-memory heap is full too
+  __device__ bool push(int32_t v) {
+    if (n == cap) {
+      if (h == gheap || gcap <= cap) return false;
+      for (int i = 0; i < n; i++) gheap[i] = h[i];
+      h = gheap;
+      cap = gcap;
+    }
+    heap_push(h, n, v);
+    return true;
+  }
+};
 
 // Queue the later loop positions whose visit reads a cell changed by the
 // moves of a visit at (x, y): the visited cell and each moved-to neighbour
 // (bit k of `moved`).  A visit reads the 3x3 block around its cell, so
 // these are the positions whose cell lies within one of a changed cell;
 // every other later position still sees the elevations the probe tested.
-__device__ void push_affected(const hc_view& c, hc_dev* d, const Order& o, int x, int y, int moved,
-                              long long Pcur, bool global, int32_t* heap, int& hn, int cap) {
-  // cells of the 5x5 block around (x, y) within one of a changed cell
-  unsigned need = 0;  // bit (dx+2)*5 + (dy+2)
+// The down_scan entries that visit row xx of column yy are xx itself and
+// the clamped entries 1 -> 2 and imax -> imax-1.  All masks are loaded
+// before the first push.  Returns false when the queue is full.
+__device__ bool push_affected(const hc_view& c, const Order& o, int x, int y, int moved, int Pcur,
+                              Pending& q) {
+  constexpr int dxs[8] = {1, 0, -1, -1, -1, 0, 1, 1};
+  constexpr int dys[8] = {1, 1, 1, 0, -1, -1, -1, 0};
+  // cells of the 5x5 block around (x, y) within one of a changed cell:
+  // bit (dx+2)*5 + (dy+2)
+  unsigned need = 0;
+#pragma unroll
   for (int k = -1; k < 8; k++) {
     if (k >= 0 && !((moved >> k) & 1)) continue;
-    const int cx = (k < 0) ? 0 : kSx[k], cy = (k < 0) ? 0 : kSy[k];
+    const int cx = (k < 0) ? 0 : dxs[k], cy = (k < 0) ? 0 : dys[k];
+#pragma unroll
     for (int dx = -1; dx <= 1; dx++)
+#pragma unroll
       for (int dy = -1; dy <= 1; dy++) need |= 1u << ((cx + dx + 2) * 5 + (cy + dy + 2));
   }
-  for (int dx = -2; dx <= 2; dx++)
-    for (int dy = -2; dy <= 2; dy++) {
-      if (!((need >> ((dx + 2) * 5 + (dy + 2))) & 1u)) continue;
-      const int xx = x + dx, yy = y + dy;
-      if (xx < 2 || xx > c.imax - 1 || yy < 2 || yy > c.jmax - 1) continue;
-      if (global) {
-        long long P = o.pos(xx, yy);
-        if (P > Pcur) heap_push(heap, hn, cap, (int32_t)P, d);
-      } else {
-        // down_scan entries that visit row xx of column yy: xx itself, and the
-        // clamped entries 1 -> 2 and imax -> imax-1
-        const size_t W = c.W;
-        if (c.mask[(size_t)xx * W + yy]) {
-          long long P = o.pos(xx, yy);
-          if (P > Pcur) heap_push(heap, hn, cap, (int32_t)P, d);
-        }
-        if (xx == 2 && c.mask[(size_t)1 * W + yy]) {
-          long long P = o.pos(1, yy);
-          if (P > Pcur) heap_push(heap, hn, cap, (int32_t)P, d);
-        }
-        if (xx == c.imax - 1 && c.mask[(size_t)c.imax * W + yy]) {
-          long long P = o.pos(c.imax, yy);
-          if (P > Pcur) heap_push(heap, hn, cap, (int32_t)P, d);
-        }
-      }
+  const size_t W = c.W;
+  unsigned own = 0, top = 0, bottom = 0;  // masks of the row itself, row 1, row imax
+#pragma unroll
+  for (int b = 0; b < 25; b++) {
+    const int xx = x + b / 5 - 2, yy = y + b % 5 - 2;
+    if (!((need >> b) & 1u) || xx < 2 || xx > c.imax - 1 || yy < 2 || yy > c.jmax - 1) continue;
+    if (c.mask[(size_t)xx * W + yy]) own |= 1u << b;
+    if (xx == 2 && c.mask[W + yy]) top |= 1u << b;
+    if (xx == c.imax - 1 && c.mask[(size_t)c.imax * W + yy]) bottom |= 1u << b;
+  }
+  bool ok = true;
+#pragma unroll
+  for (int b = 0; b < 25; b++) {
+    const int xx = x + b / 5 - 2, yy = y + b % 5 - 2;
+    int P;
+    if ((own >> b) & 1u) {
+      P = o.pos(xx, yy);
+      if (P > Pcur) ok = ok && q.push(P);
     }
+    if ((top >> b) & 1u) {
+      P = o.pos(1, yy);
+      if (P > Pcur) ok = ok && q.push(P);
+    }
+    if ((bottom >> b) & 1u) {
+      P = o.pos(c.imax, yy);
+      if (P > Pcur) ok = ok && q.push(P);
+    }
+  }
+  return ok;
 }
 
+// The serial sweep in loop order over the flagged positions and the queued
+// re-tests (one thread: each visit depends on the moves before it).
 __global__ void k_slide_replay(const hc_view c, hc_dev* d, const int32_t* list, const int32_t* count,
-                               int32_t* heap, int heap_cap, int global, double factor,
-                               double* total_out, int gated) {
+                               int32_t* gheap, int gheap_cap, double factor, int gated) {
+  __shared__ int32_t sheap[kSharedHeap];
   if (gated && !(d->it_active && d->rest_active && d->do_slide)) return;
   const int n = *count;
-  if (total_out) *total_out = 0;
   if (n == 0) return;
-  Order o{global ? 0 : 1, c.imax, c.jmax};
-  int hn = 0, li = 0;
-  long long last = -1;
-  double total = 0;
-  const int err0 = d->err_code;
+  const Order o{c.imax + 2};
+  Pending q{sheap, 0, kSharedHeap, gheap, gheap_cap};
+  int li = 0, last = -1;
+  int next = list[0];
   while (true) {
-    long long cand = LLONG_MAX;
-    if (li < n) cand = list[li];
-    if (hn > 0 && heap[0] < cand) cand = heap[0];
-    if (cand == LLONG_MAX) break;
-    if (li < n && list[li] == cand) li++;
-    while (hn > 0 && heap[0] <= cand) heap_pop(heap, hn);
+    int cand = INT_MAX;
+    if (li < n) cand = next;
+    if (q.n > 0 && q.h[0] < cand) cand = q.h[0];
+    if (cand == INT_MAX) break;
+    if (li < n && next == cand && ++li < n) next = list[li];
+    while (q.n > 0 && q.h[0] <= cand) heap_pop(q.h, q.n);
     if (cand <= last) continue;
     last = cand;
     int x, y;
     o.cell(cand, x, y);
-    int xc = x;
-    if (!global) {
-      if (xc == c.imax) xc = c.imax - 1;
-      if (xc == 1) xc = 2;
-    }
-    const int moved = slide_visit_held(c, d, xc, y, factor, global != 0, &total);
-    if (moved) push_affected(c, d, o, xc, y, moved, cand, global != 0, heap, hn, heap_cap);
-    if (d->err_code == 301 && err0 != 301) {
-      // heap overflow: finish the sweep visiting every later position
-      d->err_code = err0;
-      for (long long P = cand + 1;; P++) {
+    if (x == c.imax) x = c.imax - 1;
+    if (x == 1) x = 2;
+    const int moved = slide_visit_held(c, d, x, y, factor);
+    if (moved && !push_affected(c, o, x, y, moved, cand, q)) {
+      // the queue is full: finish the sweep visiting every later position
+      for (int P = cand + 1;; P++) {
         int xx, yy;
         o.cell(P, xx, yy);
-        if (global) {
-          if (xx > c.imax - 1) break;
-          if (yy < 2 || yy > c.jmax - 1 || xx < 2) continue;
-          slide_visit_held(c, d, xx, yy, factor, true, &total);
-        } else {
-          if (yy > c.jmax - 1) break;
-          if (xx < 1 || xx > c.imax || yy < 2) continue;
-          if (!c.mask[(size_t)xx * c.W + yy]) continue;
-          int x3 = xx;
-          if (x3 == c.imax) x3 = c.imax - 1;
-          if (x3 == 1) x3 = 2;
-          slide_visit_held(c, d, x3, yy, factor, false, &total);
-        }
+        if (yy > c.jmax - 1) break;
+        if (xx < 1 || xx > c.imax || yy < 2) continue;
+        if (!c.mask[(size_t)xx * c.W + yy]) continue;
+        if (xx == c.imax) xx = c.imax - 1;
+        if (xx == 1) xx = 2;
+        slide_visit_held(c, d, xx, yy, factor);
       }
       break;
     }
   }
   d->s.grain_array_tot = d->grain_tot;
-  if (total_out) *total_out = total;
 }
 
 // ---- creep :5293-5427 ------------------------------------------------------
@@ -495,8 +502,6 @@ static SlideScratch slide_scratch(hc_ctx* c) {
   off += ((nblocks * 4 + 255) / 256) * 256;
   s.count = (int32_t*)(base + off);
   off += 256;
-  s.total = (double*)(base + off);
-  off += 256;
   s.heap = (int32_t*)(base + off);
   s.heap_cap = 1 << 16;
   return s;
@@ -505,16 +510,16 @@ static SlideScratch slide_scratch(hc_ctx* c) {
 size_t slide_scratch_bytes(size_t N2) {
   size_t nblocks = (N2 + 1023) / 1024;
   return ((N2 + 255) / 256) * 256 + ((N2 * 4 + 255) / 256) * 256 + ((nblocks * 4 + 255) / 256) * 256 +
-         512 + (size_t)(1 << 16) * 4 + 256;
+         256 + (size_t)(1 << 16) * 4 + 256;
 }
 
-static void slide_sweep(hc_ctx* c, int global, double factor, int gated) {
+static void slide_sweep(hc_ctx* c, double factor, int gated) {
   SlideScratch s = slide_scratch(c);
   dim3 b(32, 8);
   dim3 g((c->v.jmax + b.x - 1) / b.x, (c->v.imax + b.y - 1) / b.y);
   // positions span the whole padded grid; unflagged positions must read 0
   cudaMemsetAsync(s.flag, 0, c->v.N2, c->cs);
-  k_slide_probe<<<g, b, 0, c->cs>>>(c->v, c->dev, s.flag, global, factor, gated);
+  k_slide_probe<<<g, b, 0, c->cs>>>(c->v, c->dev, s.flag, factor, gated);
   count_launch(c, 1);
   const size_t n = c->v.N2;
   const int nblocks = (int)((n + 1023) / 1024);
@@ -524,8 +529,8 @@ static void slide_sweep(hc_ctx* c, int global, double factor, int gated) {
   count_launch(c, 1);
   k_flag_compact<<<nblocks, 1024, 0, c->cs>>>(s.flag, n, s.block_sums, s.list, c->dev, gated);
   count_launch(c, 1);
-  k_slide_replay<<<1, 1, 0, c->cs>>>(c->v, c->dev, s.list, s.count, s.heap, s.heap_cap, global,
-                                    factor, s.total, gated);
+  k_slide_replay<<<1, 1, 0, c->cs>>>(c->v, c->dev, s.list, s.count, s.heap, s.heap_cap, factor,
+                                    gated);
   count_launch(c, 1);
 }
 
@@ -535,7 +540,7 @@ static double slide_factor(const hc_ctx* c) {
   return std::tan((c->v.p.failureangle * (3.141592654 / 180))) * c->v.p.DX;
 }
 
-void launch_slide3(hc_ctx* c, int gated) { slide_sweep(c, 0, slide_factor(c), gated); }
+void launch_slide3(hc_ctx* c, int gated) { slide_sweep(c, slide_factor(c), gated); }
 
 hc_status run_global_landsliding(hc_ctx* c) {
   // a serial sweep over every cell, up to 200 times: one host core runs it

@@ -3,7 +3,8 @@
 cube_rn (the friction term's h^3) is correctly rounded; glibc's
 pow(h, 3.0), which the reference calls, is not always (about 0.08 % of
 arguments), which is why hydraulic parity is to rounding level rather than
-bitwise.  (The integer-pipe division, cube and square root are checked
+bitwise.  slide_3's tests decided on float estimates never contradict the
+FP64 test.  (The integer-pipe division, cube and square root are checked
 against the GPU's own instructions in test_gpu_arith.py.)"""
 import ctypes as C
 import os
@@ -26,6 +27,10 @@ def numlib():
     lib = C.CDLL(so)
     lib.cube_rn.restype = C.c_double
     lib.cube_rn.argtypes = [C.c_double]
+    lib.slide_est.restype = C.c_int
+    lib.slide_est.argtypes = [C.c_double, C.c_double, C.c_double, C.c_int]
+    lib.slide_est_check.restype = C.c_long
+    lib.slide_est_check.argtypes = [C.c_long, C.c_uint, C.POINTER(C.c_long)]
     return lib
 
 
@@ -46,6 +51,25 @@ def test_glibc_pow_cube_is_not_always_correctly_rounded(numlib):
     libm.pow.argtypes = [C.c_double, C.c_double]
     diff = sum(1 for h in hs if libm.pow(float(h), 3.0) != numlib.cube_rn(float(h)))
     assert diff < 0.01 * len(hs)
+
+
+def test_slide_estimates_never_contradict_the_fp64_test(numlib):
+    decided = C.c_long()
+    n = 4_000_000
+    assert numlib.slide_est_check(n, 7, C.byref(decided)) == 0
+    # the estimates decide the tests away from the threshold
+    assert decided.value > n // 3, decided.value
+    special = [float("nan"), float("inf"), -float("inf"), 1e308, -1e308, 1e-310, 0.0, -0.0,
+               -9999.0, 123.5]
+    for e in special:
+        for e2 in special:
+            for w in special:
+                for diag in (0, 1):
+                    with np.errstate(all="ignore"):
+                        d = np.float64(e) - np.float64(e2)
+                        drop = d / 1.41 if diag else d
+                    r = numlib.slide_est(e, e2, w, diag)
+                    assert r == 2 or r == int(drop > w), (e, e2, w, diag, r)
 
 
 def test_exact_sort_matches_std_sort(tmp_path):
