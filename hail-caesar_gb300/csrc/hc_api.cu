@@ -294,7 +294,7 @@ extern "C" hc_status hc_create(const hc_params* p, size_t max_bytes, hc_ctx** ou
   char* red = nullptr;
   A(red, erode_scratch_bytes(N2, p->imax, p->jmax))
   v.red = (double*)red;
-  A(v.touched, slide_scratch_bytes(N2))
+  A(v.touched, slide_scratch_bytes(N2, p->imax))
   double* lat = nullptr;
   if (sed && p->imax == p->jmax) A(lat, lateral_scratch_bytes(p->imax, p->jmax) / 8 + 1)
   A(c->dev, 1)
@@ -334,7 +334,7 @@ extern "C" hc_status hc_create(const hc_params* p, size_t max_bytes, hc_ctx** ou
     k_fill_u64<<<4096, 256, 0, s>>>(v.alloc_key, N2, ~0ull);
   }
   cudaMemsetAsync(v.red, 0, erode_scratch_bytes(N2, p->imax, p->jmax), s);
-  cudaMemsetAsync(v.touched, 0, slide_scratch_bytes(N2), s);
+  cudaMemsetAsync(v.touched, 0, slide_scratch_bytes(N2, p->imax), s);
   // scalar members at their initialisers (LSDCatchmentModel.hpp)
   hc_dev* hd = c->hdev;
   std::memset(hd, 0, sizeof *hd);

@@ -605,7 +605,7 @@ void launch_slide3(hc_ctx* c, int gated);
 hc_status run_lateral(hc_ctx* c);
 hc_status run_global_landsliding(hc_ctx* c);
 hc_status run_creep(hc_ctx* c, double time);
-size_t slide_scratch_bytes(size_t N2);
+size_t slide_scratch_bytes(size_t N2, int imax);
 
 // host helpers (hc_host.cpp)
 // the drainage sweep order (std::sort's permutation, exact); cached while

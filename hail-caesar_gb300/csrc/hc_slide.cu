@@ -31,13 +31,21 @@ struct SlideScratch {
   int32_t* list;        // positions whose test passed, in loop order
   int32_t* block_sums;
   int32_t* count;
-  int32_t* heap;        // pending re-tests, once the shared-memory heap is full
-  int heap_cap;
+  uint32_t* ring;       // the replay's pending re-tests, when too many for shared memory
 };
 
-// pending re-tests the replay holds in shared memory before it moves its heap
-// to device memory
-constexpr int kSharedHeap = 8192;
+// The replay's pending re-tests: one bit per loop position in a ring of R
+// positions, R the power of two >= 2*(imax+2) + 64.  A move at position P
+// queues positions in (P, P + 2*(imax+2) + 2] only (the 5x5 block around its
+// cell, columns y to y+2), so every pending position lies within R of the
+// last one visited and has a bit of its own.
+constexpr int kSharedRingWords = 8192;  // rings of up to 262,144 positions
+
+__host__ __device__ inline int ring_words(int imax) {
+  long long R = 64;
+  while (R < 2LL * (imax + 2) + 64) R <<= 1;
+  return (int)(R >> 5);
+}
 
 // Loop position of a cell: slide_3 walks columns (y outer, the wet rows of
 // down_scan inner), P = y*(imax+2) + x.  Positions fit 32 bits, as the
@@ -251,64 +259,16 @@ __global__ void k_flag_compact(const uint8_t* flag, size_t n, const int32_t* blo
 }
 
 // ---- the serial replay -----------------------------------------------------
-// A binary min-heap of positions, in shared or device memory.
-__device__ void heap_push(int32_t* h, int& n, int32_t v) {
-  int i = n++;
-  h[i] = v;
-  while (i > 0) {
-    int p = (i - 1) / 2;
-    if (h[p] <= h[i]) break;
-    int t = h[p];
-    h[p] = h[i];
-    h[i] = t;
-    i = p;
-  }
-}
-__device__ void heap_pop(int32_t* h, int& n) {
-  h[0] = h[--n];
-  int i = 0;
-  for (;;) {
-    int l = 2 * i + 1, r = l + 1, m = i;
-    if (l < n && h[l] < h[m]) m = l;
-    if (r < n && h[r] < h[m]) m = r;
-    if (m == i) break;
-    int t = h[m];
-    h[m] = h[i];
-    h[i] = t;
-    i = m;
-  }
-}
-
-// The replay's pending re-tests: a heap in shared memory that moves to
-// device memory (gheap, gcap entries) when it fills.
-struct Pending {
-  int32_t* h;
-  int n, cap;
-  int32_t* gheap;
-  int gcap;
-  // false when the device-memory heap is full too
-  __device__ bool push(int32_t v) {
-    if (n == cap) {
-      if (h == gheap || gcap <= cap) return false;
-      for (int i = 0; i < n; i++) gheap[i] = h[i];
-      h = gheap;
-      cap = gcap;
-    }
-    heap_push(h, n, v);
-    return true;
-  }
-};
-
 // Queue the later loop positions whose visit reads a cell changed by the
 // moves of a visit at (x, y): the visited cell and each moved-to neighbour
 // (bit k of `moved`).  A visit reads the 3x3 block around its cell, so
 // these are the positions whose cell lies within one of a changed cell;
 // every other later position still sees the elevations the probe tested.
 // The down_scan entries that visit row xx of column yy are xx itself and
-// the clamped entries 1 -> 2 and imax -> imax-1.  All masks are loaded
-// before the first push.  Returns false when the queue is full.
-__device__ bool push_affected(const hc_view& c, const Order& o, int x, int y, int moved, int Pcur,
-                              Pending& q) {
+// the clamped entries 1 -> 2 and imax -> imax-1.  Returns the number of
+// positions newly set in the ring.
+__device__ int push_affected(const hc_view& c, const Order& o, int x, int y, int moved, int Pcur,
+                             uint32_t* ring, int RW) {
   constexpr int dxs[8] = {1, 0, -1, -1, -1, 0, 1, 1};
   constexpr int dys[8] = {1, 1, 1, 0, -1, -1, -1, 0};
   // cells of the 5x5 block around (x, y) within one of a changed cell:
@@ -323,79 +283,144 @@ __device__ bool push_affected(const hc_view& c, const Order& o, int x, int y, in
 #pragma unroll
       for (int dy = -1; dy <= 1; dy++) need |= 1u << ((cx + dx + 2) * 5 + (cy + dy + 2));
   }
+  // x and y lie in [2, imax-1] x [2, jmax-1], so every byte below is inside
+  // the padded grid: all 35 are loaded together, before any test
   const size_t W = c.W;
-  unsigned own = 0, top = 0, bottom = 0;  // masks of the row itself, row 1, row imax
+  uint8_t mk[25], mt[5], mb[5];
+#pragma unroll
+  for (int b = 0; b < 25; b++) mk[b] = c.mask[(size_t)(x + b / 5 - 2) * W + (y + b % 5 - 2)];
+#pragma unroll
+  for (int j = 0; j < 5; j++) {
+    mt[j] = c.mask[W + (y + j - 2)];
+    mb[j] = c.mask[(size_t)c.imax * W + (y + j - 2)];
+  }
+  int added = 0;
+  auto push = [&](int P) {
+    if (P <= Pcur) return;
+    uint32_t& w = ring[(P >> 5) & (RW - 1)];
+    const uint32_t bit = 1u << (P & 31);
+    if (!(w & bit)) {
+      w |= bit;
+      added++;
+    }
+  };
 #pragma unroll
   for (int b = 0; b < 25; b++) {
     const int xx = x + b / 5 - 2, yy = y + b % 5 - 2;
     if (!((need >> b) & 1u) || xx < 2 || xx > c.imax - 1 || yy < 2 || yy > c.jmax - 1) continue;
-    if (c.mask[(size_t)xx * W + yy]) own |= 1u << b;
-    if (xx == 2 && c.mask[W + yy]) top |= 1u << b;
-    if (xx == c.imax - 1 && c.mask[(size_t)c.imax * W + yy]) bottom |= 1u << b;
+    if (mk[b]) push(o.pos(xx, yy));
+    if (xx == 2 && mt[b % 5]) push(o.pos(1, yy));
+    if (xx == c.imax - 1 && mb[b % 5]) push(o.pos(c.imax, yy));
   }
-  bool ok = true;
-#pragma unroll
-  for (int b = 0; b < 25; b++) {
-    const int xx = x + b / 5 - 2, yy = y + b % 5 - 2;
-    int P;
-    if ((own >> b) & 1u) {
-      P = o.pos(xx, yy);
-      if (P > Pcur) ok = ok && q.push(P);
-    }
-    if ((top >> b) & 1u) {
-      P = o.pos(1, yy);
-      if (P > Pcur) ok = ok && q.push(P);
-    }
-    if ((bottom >> b) & 1u) {
-      P = o.pos(c.imax, yy);
-      if (P > Pcur) ok = ok && q.push(P);
-    }
-  }
-  return ok;
+  return added;
 }
 
 // The serial sweep in loop order over the flagged positions and the queued
-// re-tests (one thread: each visit depends on the moves before it).
-__global__ void k_slide_replay(const hc_view c, hc_dev* d, const int32_t* list, const int32_t* count,
-                               int32_t* gheap, int gheap_cap, double factor, int gated) {
-  __shared__ int32_t sheap[kSharedHeap];
+// re-tests, by one warp.  A visit that moves nothing changes nothing, so the
+// next kReplayBatch candidates in loop order are probed together, one per
+// lane, against the current elevations; the candidates before the first one
+// that moves are done, that one is visited in full by lane 0 (its moves
+// depend on the moves before it), and the candidates after it stay queued,
+// to be probed again on the changed elevations.  The visits and moves are
+// the serial sweep's, in its order.
+constexpr int kReplayBatch = 8;
+constexpr unsigned kFull = 0xffffffffu;
+
+__device__ __forceinline__ void replay_cell(const hc_view& c, const Order& o, int P, int& x,
+                                            int& y) {
+  o.cell(P, x, y);
+  if (x == c.imax) x = c.imax - 1;  // the clamped first and last rows
+  if (x == 1) x = 2;
+}
+
+__global__ void __launch_bounds__(32) k_slide_replay(const hc_view c, hc_dev* d,
+                                                     const int32_t* list, const int32_t* count,
+                                                     uint32_t* gring, double factor, int gated) {
+  __shared__ uint32_t sring[kSharedRingWords];
+  __shared__ int32_t batch[kReplayBatch];
   if (gated && !(d->it_active && d->rest_active && d->do_slide)) return;
   const int n = *count;
   if (n == 0) return;
+  const int lane = threadIdx.x;
   const Order o{c.imax + 2};
-  Pending q{sheap, 0, kSharedHeap, gheap, gheap_cap};
-  int li = 0, last = -1;
-  int next = list[0];
+  const int RW = ring_words(c.imax);
+  const int R = RW << 5;
+  uint32_t* ring = (RW <= kSharedRingWords) ? sring : gring;
+  for (int i = lane; i < RW; i += 32) ring[i] = 0;
+  __syncwarp();
+  // the same on every lane: next list entry, last position visited, number
+  // of positions pending in the ring
+  int li = 0, last = -1, pend = 0;
   while (true) {
-    int cand = INT_MAX;
-    if (li < n) cand = next;
-    if (q.n > 0 && q.h[0] < cand) cand = q.h[0];
-    if (cand == INT_MAX) break;
-    if (li < n && next == cand && ++li < n) next = list[li];
-    while (q.n > 0 && q.h[0] <= cand) heap_pop(q.h, q.n);
-    if (cand <= last) continue;
-    last = cand;
-    int x, y;
-    o.cell(cand, x, y);
-    if (x == c.imax) x = c.imax - 1;
-    if (x == 1) x = 2;
-    const int moved = slide_visit_held(c, d, x, y, factor);
-    if (moved && !push_affected(c, o, x, y, moved, cand, q)) {
-      // the queue is full: finish the sweep visiting every later position
-      for (int P = cand + 1;; P++) {
-        int xx, yy;
-        o.cell(P, xx, yy);
-        if (yy > c.jmax - 1) break;
-        if (xx < 1 || xx > c.imax || yy < 2) continue;
-        if (!c.mask[(size_t)xx * c.W + yy]) continue;
-        if (xx == c.imax) xx = c.imax - 1;
-        if (xx == 1) xx = 2;
-        slide_visit_held(c, d, xx, yy, factor);
+    const int L = (li < n) ? list[li] : INT_MAX;
+    // the first pending positions of (last, min(L, last + R)), in order
+    int nb = 0;
+    if (pend > 0) {
+      const int s0 = last + 1;
+      const int end = (int)min((long long)L, (long long)last + R);
+      for (int base = s0 & ~31; base < end && nb < kReplayBatch; base += 1024) {
+        const int w0 = base + lane * 32;
+        uint32_t bits = 0;
+        if (w0 < end) {
+          bits = ring[(w0 >> 5) & (RW - 1)];
+          if (w0 < s0) bits &= ~0u << (s0 - w0);
+          if (end - w0 < 32) bits &= (1u << (end - w0)) - 1u;
+        }
+        const int cnt = __popc(bits);
+        int incl = cnt;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+          const int t = __shfl_up_sync(kFull, incl, off);
+          if (lane >= off) incl += t;
+        }
+        int slot = nb + incl - cnt;
+        while (bits && slot < kReplayBatch) {
+          batch[slot++] = w0 + __ffs(bits) - 1;
+          bits &= bits - 1;
+        }
+        nb = min(kReplayBatch, nb + __shfl_sync(kFull, incl, 31));
       }
-      break;
     }
+    const bool tookL = nb < kReplayBatch && L != INT_MAX;
+    if (tookL) {
+      if (lane == 0) batch[nb] = L;
+      nb++;
+    }
+    if (nb == 0) break;
+    __syncwarp();
+    bool mv = false;
+    if (lane < nb) {
+      int x, y;
+      replay_cell(c, o, batch[lane], x, y);
+      mv = slide_probe_cell(c, x, y, factor);
+    }
+    const unsigned ball = __ballot_sync(kFull, mv);
+    // candidates 0..upto are visited now: before the first that moves, that
+    // one, or all of them
+    const int upto = ball ? (__ffs(ball) - 1) : nb - 1;
+    int cleared = 0;
+    if (lane <= upto) {
+      const int P = batch[lane];
+      const uint32_t bit = 1u << (P & 31);
+      cleared = (atomicAnd(&ring[(P >> 5) & (RW - 1)], ~bit) & bit) ? 1 : 0;
+    }
+    pend -= __popc(__ballot_sync(kFull, cleared));
+    if (tookL && upto == nb - 1) li++;
+    last = batch[upto];
+    if (ball) {
+      int added = 0;
+      if (lane == 0) {
+        int x, y;
+        replay_cell(c, o, last, x, y);
+        const int moved = slide_visit_held(c, d, x, y, factor);
+        if (moved) added = push_affected(c, o, x, y, moved, last, ring, RW);
+      }
+      pend += __shfl_sync(kFull, added, 0);
+    }
+    // lane 0's moves and pushes are visible to the warp's next round
+    __syncwarp();
   }
-  d->s.grain_array_tot = d->grain_tot;
+  if (lane == 0) d->s.grain_array_tot = d->grain_tot;
 }
 
 // ---- creep :5293-5427 ------------------------------------------------------
@@ -502,15 +527,14 @@ static SlideScratch slide_scratch(hc_ctx* c) {
   off += ((nblocks * 4 + 255) / 256) * 256;
   s.count = (int32_t*)(base + off);
   off += 256;
-  s.heap = (int32_t*)(base + off);
-  s.heap_cap = 1 << 16;
+  s.ring = (uint32_t*)(base + off);
   return s;
 }
 
-size_t slide_scratch_bytes(size_t N2) {
+size_t slide_scratch_bytes(size_t N2, int imax) {
   size_t nblocks = (N2 + 1023) / 1024;
   return ((N2 + 255) / 256) * 256 + ((N2 * 4 + 255) / 256) * 256 + ((nblocks * 4 + 255) / 256) * 256 +
-         256 + (size_t)(1 << 16) * 4 + 256;
+         256 + (size_t)ring_words(imax) * 4 + 256;
 }
 
 static void slide_sweep(hc_ctx* c, double factor, int gated) {
@@ -529,8 +553,7 @@ static void slide_sweep(hc_ctx* c, double factor, int gated) {
   count_launch(c, 1);
   k_flag_compact<<<nblocks, 1024, 0, c->cs>>>(s.flag, n, s.block_sums, s.list, c->dev, gated);
   count_launch(c, 1);
-  k_slide_replay<<<1, 1, 0, c->cs>>>(c->v, c->dev, s.list, s.count, s.heap, s.heap_cap, factor,
-                                    gated);
+  k_slide_replay<<<1, 32, 0, c->cs>>>(c->v, c->dev, s.list, s.count, s.ring, factor, gated);
   count_launch(c, 1);
 }
 

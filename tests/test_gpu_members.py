@@ -73,12 +73,26 @@ def test_erode_member(gpu_lib, oracle_mod, erosion_case):
     assert_close(m.scalars().time_step, o.scalar("time_step"), 0, "time_step", rtol=1e-12)
 
 
-def test_in_channel_landsliding_member(gpu_lib, oracle_mod):
-    # a steep DEM so that slides happen
-    case = synth.catchment_case(n=30, DX=10.0, hours=72, relief=400.0, lateral=False, fill=False)
-    o, m = mid_run(oracle_mod, case, 300)
+@pytest.mark.parametrize("n", [33, 96])
+def test_in_channel_landsliding_member(gpu_lib, oracle_mod, n):
+    """A mid-run state whose wet cells (the only ones slide_3 tests) are
+    raised by 25 m at one in six, the same in the oracle and on the device:
+    slides follow one another within columns and across them, so re-tests
+    queue behind later flagged positions and batches are cut short by
+    moves."""
+    case = synth.catchment_case(n=n, DX=10.0, hours=72, relief=60.0, lateral=False,
+                                storm_start_h=0.5)
+    o, m = mid_run(oracle_mod, case, 900)
+    e = o.field("elev")
+    wet = np.argwhere(o.field("water_depth") > 0)
+    rng = np.random.default_rng(3)
+    pick = wet[rng.choice(len(wet), size=len(wet) // 6, replace=False)]
+    e[pick[:, 0], pick[:, 1]] += 25.0
+    m.upload("elev", e)
+    before = np.array(e, copy=True)
     m.in_channel_landsliding()
     o.lib.hco_in_channel_landsliding(o.h)
+    assert np.sum(o.field("elev") != before) > 100, "too few moves to test the replay"
     assert_bitwise(m.field("elev"), o.field("elev"), "elev")
     assert_bitwise(m.field("index"), o.field("index"), "index")
     assert_close(m.field("grain"), o.field("grain"), 1e-12, "grain", rtol=1e-12)
