@@ -503,33 +503,46 @@ __global__ void __launch_bounds__(256) k_apply_pre(const hc_view c, hc_dev* d) {
   if (apply_active(c, cell, x)) {
     const hc_params& p = c.p;
     const double ts = d->s.time_step;
-    double erodetot = 0;
+    const bool susp1 = p.isSuspended[1];
+    // every flux is loaded before the first store: the stores would keep the
+    // compiler from issuing a later fraction's loads ahead of them
+    double val1[HC_G], val2[HC_G];
+#pragma unroll
     for (int n = 1; n <= HC_G - 1; n++) {
-      if (n == 1 && p.isSuspended[n]) {
+      if (n == 1 && susp1) continue;
+      val1[n] = (SF(c, 0, n, cell) + SF(c, 1, n, cell) + SF(c, 2, n, cell) + SF(c, 3, n, cell));
+      val2[n] = (SF(c, 0, n, cell + 1) + SF(c, 2, n, cell - 1) + SF(c, 3, n, cell + W) +
+                 SF(c, 1, n, cell - W));
+    }
+    double erodetot = 0, Vpdrop = 0, vs = 0;
+    double dn[HC_G];
+#pragma unroll
+    for (int n = 1; n <= HC_G - 1; n++) {
+      if (n == 1 && susp1) {
         const double ssv = c.ss[cell];
-        double vs = c.vs[cell] + ssv;
+        vs = c.vs[cell] + ssv;
         erodetot -= ssv;
         // inputpointsarray is all false in the reference (zero_values clears
         // it after the reach block), so settling applies everywhere
-        double coeff = (p.fallVelocity[n] * ts) / c.h[cell];
+        double coeff = ddiv_rn(p.fallVelocity[n] * ts, c.h[cell]);
         if (dgt(coeff, 1.0)) coeff = 1;
-        double Vpdrop = coeff * vs;
+        Vpdrop = coeff * vs;
         if (dgt(Vpdrop, 0.001)) Vpdrop = 0.001;
         erodetot += Vpdrop;
         vs -= Vpdrop;
-        c.vs[cell] = vs;
-        PRE(c, 0, cell) = Vpdrop;
       } else {
-        double val1 = (SF(c, 0, n, cell) + SF(c, 1, n, cell) + SF(c, 2, n, cell) +
-                       SF(c, 3, n, cell));
-        double val2 = (SF(c, 0, n, cell + 1) + SF(c, 2, n, cell - 1) + SF(c, 3, n, cell + W) +
-                       SF(c, 1, n, cell - W));
-        const double dn = val2 - val1;
-        PRE(c, n, cell) = dn;
-        erodetot += dn;
-        et3 += val1;
+        dn[n] = val2[n] - val1[n];
+        erodetot += dn[n];
+        et3 += val1[n];
       }
     }
+    if (susp1) {
+      c.vs[cell] = vs;
+      PRE(c, 0, cell) = Vpdrop;
+    }
+#pragma unroll
+    for (int n = 1; n <= HC_G - 1; n++)
+      if (!(n == 1 && susp1)) PRE(c, n, cell) = dn[n];
     PRE(c, 10, cell) = erodetot;
   }
   c.erodetot3[cell] = et3;
