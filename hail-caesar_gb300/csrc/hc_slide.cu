@@ -9,7 +9,7 @@
 // drop steeper than the failure angle over one cell), so the device first
 // tests every cell against the elevations at the start of the sweep, in
 // parallel.  If no test passes, the serial sweep would move nothing either
-// and the sweep is over.  Otherwise one thread replays the sweep in loop
+// and the sweep is over.  Otherwise one warp replays the sweep in loop
 // order, visiting only (a) the cells whose test passed and (b) cells later
 // in the loop whose 3x3 neighbourhood a move has changed - every other cell
 // would evaluate its tests on unchanged elevations, where they failed.  The
