@@ -1,5 +1,5 @@
 """The N>1 path of bench.py on CPU: two gloo ranks, each running its own
-model (the oracle here, the GPU library on a GPU machine), with no data-path
+model (the oracle on CPU, the GPU library on a GPU), with no data-path
 collective; only the timing reduction crosses ranks."""
 import os
 import socket
