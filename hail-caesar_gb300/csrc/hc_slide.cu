@@ -36,9 +36,10 @@ struct SlideScratch {
 
 // The replay's pending re-tests: one bit per loop position in a ring of R
 // positions, R the power of two >= 2*(imax+2) + 64.  A move at position P
-// queues positions in (P, P + 2*(imax+2) + 2] only (the 5x5 block around its
-// cell, columns y to y+2), so every pending position lies within R of the
-// last one visited and has a bit of its own.
+// queues positions in (P, P + 2*(imax+2) + 4] only (the 5x5 block around its
+// cell, columns y to y+2; +4 with the clamped rows 1 -> 2 and imax), so every
+// pending position lies within R of the last one visited and has a bit of
+// its own.
 constexpr int kSharedRingWords = 8192;  // rings of up to 262,144 positions
 
 __host__ __device__ inline int ring_words(int imax) {
