@@ -8,15 +8,16 @@ synthetic input already resident in HBM.
 Workloads (seeded synthetic inputs with the benchmark configurations' shapes):
   catchment2000  (default) catchment mode, 2000 x 2000 cells at 20 m, fractal
                  DEM with 300 m relief pit-filled to one outlet edge,
-                 gamma rain + 60 mm/h storm, per-cell Manning's n, Einstein
-                 transport, lateral3 and slide_3 on; the storm starts at
-                 1 h and the timed steps begin 30 min into it
+                 gamma rain + 60 mm/h storm from 60 min, per-cell Manning's n,
+                 Einstein transport, lateral3 and slide_3 on; 500 iterations
+                 of spin-up (to simulated minute 117.6, inside the storm)
   flow8192       flow-only 8192 x 8192 at 5 m, 30 mm/h rain, erosion off
   reach          reach mode 300 x 100 at 10 m, Wilcock-Crowe
 
---impl gb300 (default) times libhc_gpu; --impl reference times the CPU
-implementation of the path (the oracle port, OpenMP over the reference's own
-column loops) on the host cores, from the same spun-up state definition.
+Both arms spin up by the same number of iterations, so they time the same
+iterations of the same (deterministic) run.  --impl gb300 (default) times
+libhc_gpu; --impl reference times the CPU implementation of the path (the
+oracle port, OpenMP over the reference's own column loops) on the host cores.
 
 Replicas only: under torchrun each rank runs its own model on its own GPU;
 no data moves between ranks; value = all ranks' cell-steps / max rank time.
@@ -42,22 +43,36 @@ from hc_abi import HC_RUN_LATERAL  # noqa: E402
 
 METRIC = "cell-steps/s on 1 GB300 (plain vs batched ensemble); adjoint/forward cost"
 UNIT = "cell-steps/s"
+DATA = "synthetic (seeded generators, hail-caesar_gb300/synth.py)"
+
+
+def workload_config(args, case, desc, spin_its):
+    """The `config` of both arms' lines (identical for the same workload)."""
+    return {"workload": args.workload, "description": desc, "cells": case.cells,
+            "spinup_iterations": spin_its, "timed_iterations": args.steps,
+            "parallelism": "replicas x%d" % args.gpus,
+            "l2": "inputs larger than L2 (model state several GB)"}
 
 
 def make_workload(name, size=0):
-    """(case, spin-up simulated minutes, description)."""
+    """(case, spin-up iterations, description)."""
     if name == "catchment2000":
-        case = synth.catchment_case(n=size or 2000, DX=20.0, hours=72, lateral=True,
-                                    storm_start_h=1.0)
-        return case, 90.0, ("catchment 2000x2000 @20 m, erosion + lateral3 + slide_3, timed 30 min "
-                            "into the 60 mm/h storm (storm from 1 h, spin-up to 1.5 h)")
+        n = size or 2000
+        case = synth.catchment_case(n=n, DX=20.0, hours=72, lateral=True, storm_start_h=1.0)
+        return case, 500, ("catchment %dx%d @20 m, erosion (Einstein, 9 fractions) + lateral3 + "
+                           "slide_3, per-cell n; 60 mm/h storm from 60 min" % (n, n))
     if name == "flow8192":
-        case = synth.flow_case(n=size or 8192, DX=5.0, hours=2)
-        return case, 75.0, "flow-only 8192x8192 @5 m, 30 mm/h, after 75 min"
+        n = size or 8192
+        case = synth.flow_case(n=n, DX=5.0, hours=2)
+        return case, 1500, "flow-only %dx%d @5 m, 30 mm/h" % (n, n)
     if name == "reach":
         case = synth.reach_case(imax=300, jmax=100, DX=10.0, hours=24)
-        return case, 6 * 60.0, "reach 300x100 @10 m, Wilcock, after 6 h (hydrograph peak)"
+        return case, 12000, "reach 300x100 @10 m, Wilcock, triangular hydrograph peaking at 6 h"
     raise SystemExit("unknown workload " + name)
+
+
+def timed_from(desc, iteration, cycle):
+    return "%s; timed from iteration %d (simulated minute %.1f)" % (desc, iteration, cycle)
 
 
 # ---------------------------------------------------------------- helpers
@@ -119,14 +134,27 @@ def measured_peak_hbm():
         return 6800.0, "fallback"
 
 
-def spin_up(model, minutes, flags):
-    """Runs the model until the simulated clock passes `minutes`."""
+def spin_up(model, iterations, flags):
+    """Runs the model for `iterations` iterations (or to the end of its run)."""
     t0 = time.perf_counter()
-    while True:
-        n = model.run(500, flags, records=False)
+    left = iterations
+    while left > 0:
+        n = model.run(min(left, 2000), flags, records=False)
+        left -= n
         s = model.scalars()
         log("spin-up: cycle %.1f min, iteration %d, %.1f s" % (s.cycle, s.counter,
                                                                time.perf_counter() - t0))
+        if n == 0:
+            break
+    return model.scalars()
+
+
+def spin_minutes(model, minutes, flags):
+    """Runs the model in chunks of 500 iterations until the simulated clock
+    passes `minutes` (the adjoint workload's runs)."""
+    while True:
+        n = model.run(500, flags, records=False)
+        s = model.scalars()
         if s.cycle >= minutes or s.cycle / 60 >= model.p.maxcycle or n == 0:
             return s
 
@@ -139,7 +167,18 @@ def log(msg):
 # qx, qy written (48 B); + Manning's n (8 B) when spatially variable;
 # + suspended load (Vsusptot read, qxs, qys written: 24 B) and the two
 # vel_dir entries erosion consumes (16 B) when erosion is on.
-TRAFFIC_SED_FLOW = 121.6  # B per wet cell, profiles/k_flow_route_catchment1400.md
+#
+# Per wet cell of one k_flow_route launch, from one ncu capture of the erosion
+# catchment at 1400 x 1400 (the 2000 x 2000 state is beyond the capture size
+# rule; the counts grow with the wet cells):
+#   python bench.py --size 1400 --steps 20 --warmup 5 --profile-only 2 \
+#       --profile-skip 20  under  ncu --clock-control none -k regex:k_flow_route
+#       -c 1 --metrics dram__bytes_read.sum,dram__bytes_write.sum,
+#       sm__inst_executed_pipe_fp64.sum,sm__pipe_fp64_cycles_active.sum
+FLOW_CAPTURE = {"dram_bytes_per_wet_cell": 121.6, "fp64_warp_inst_per_wet_cell": None,
+                "source": "ncu capture of k_flow_route, catchment 1400x1400 at the "
+                          "same spin-up, scaled by this launch's wet cells"}
+FP64_LANES_PER_CLK_SM = 2  # this GPU's FP64 pipe: a warp instruction takes 16 cycles
 
 
 def flow_bytes_per_cell(p):
@@ -171,13 +210,13 @@ def run_gpu(args, rank, world, dist):
     import hc
     torch.cuda.set_device(rank % max(1, torch.cuda.device_count()))
     t0 = time.perf_counter()
-    case, spin_min, desc = make_workload(args.workload, args.size)
+    case, spin_its, desc = make_workload(args.workload, args.size)
     if args.spinup >= 0:
-        spin_min = args.spinup
+        spin_its = int(args.spinup)
     log("workload generated in %.1f s" % (time.perf_counter() - t0))
     flags = case.flags
     model = hc.Model(case)
-    spin_up(model, spin_min, flags)
+    spin_up(model, spin_its, flags)
     stream = torch.cuda.ExternalStream(model.stream())
     model.run(args.warmup, flags, records=False)
     log("warm-up done")
@@ -205,7 +244,7 @@ def run_gpu(args, rank, world, dist):
     e1 = torch.cuda.Event(enable_timing=True)
     l0 = model.counters()[0]
     st0 = model.run_stats()
-    cyc0 = model.scalars().cycle
+    sc0 = model.scalars()
     torch.cuda.nvtx.range_push("timed")
     e0.record(stream)
     done = model.run(args.steps, flags, records=False)
@@ -214,18 +253,28 @@ def run_gpu(args, rank, world, dist):
     torch.cuda.nvtx.range_pop()
     ms = e0.elapsed_time(e1)
     launches = model.counters()[0] - l0
-    sim_min = model.scalars().cycle - cyc0
+    sim_min = model.scalars().cycle - sc0.cycle
     st1 = model.run_stats()
     host_work = {k: {"count": st1[k][0] - st0[k][0], "host_ms": round(st1[k][1] - st0[k][1], 3)}
-                 for k in st1}
+                 for k in st1 if k != "wet_cell_steps"}
+    wet_steps = st1["wet_cell_steps"][0] - st0["wet_cell_steps"][0]
     clk = clocks.stop() if clocks else None
     ms, total_steps = aggregate_replicas(ms, done, dist, "cuda")
     cells = case.cells
     value = cells * total_steps / (ms / 1e3)
-    out = {"ms": ms, "done": done, "value": value, "clocks": clk, "cells": cells, "desc": desc,
-           "launches": launches, "host_work": host_work, "sim_minutes": sim_min}
+    out = {"ms": ms, "done": done, "value": value, "clocks": clk, "cells": cells,
+           "spin_its": spin_its,
+           "desc": timed_from(desc, int(sc0.counter) + 1, sc0.cycle),
+           "launches": launches, "host_work": host_work, "sim_minutes": sim_min,
+           "wet_cell_steps_per_s": wet_steps / (ms / 1e3) if world == 1 else None}
     if rank != 0 or args.timed_only:
         return out, model, case
+    # the steps' periodic host work (lateral3 every 50 x erode_mult iterations,
+    # a drainage recomputation when the baseflow threshold moves) falls
+    # outside a short timed window: a longer window that holds at least one
+    # of each, amortized per step
+    if not case.params.hydro_only:
+        out["amortized"] = amortized_window(model, case, flags, stream, args.amortize_max)
     # per-phase breakdown of a few iterations (phase by phase, no graph)
     nprof = int(os.environ.get("HC_PROFILE_ITERS", "60"))
     prof = [model.profile_iteration(flags) for _ in range(nprof)]
@@ -237,7 +286,7 @@ def run_gpu(args, rank, world, dist):
     # are deterministic), so that both numbers cover the same iterations
     e2e_steps = max(3, min(args.steps, 200))
     twin = hc.Model(case)
-    spin_up(twin, spin_min, flags)
+    spin_up(twin, spin_its, flags)
     twin.run(args.warmup, flags, records=False)
     torch.cuda.synchronize()
     _, h0, d0 = twin.counters()
@@ -261,17 +310,53 @@ def run_gpu(args, rank, world, dist):
     peak, kind = measured_peak_hbm()
     per_cell = flow_bytes_per_cell(case.params)
     ach = wet * per_cell / (ms_flow / 1e3) / 1e9
-    # DRAM bytes per wet cell of one k_flow_route launch, from the ncu
-    # capture summarised in profiles/ (a smaller case of the same generator),
-    # scaled to this launch by its wet cells
-    traffic_per_cell = None if case.params.hydro_only else TRAFFIC_SED_FLOW
-    out["roofline"] = {"bound": "hbm", "kernel": "k_flow_route", "achieved": ach, "peak": peak,
-                       "unit": "GB/s", "frac": ach / peak,
-                       "traffic": None if traffic_per_cell is None else traffic_per_cell * wet,
-                       "peak_kind": kind, "bytes_per_wet_cell": per_cell, "wet_cells": wet,
-                       "launch_ms": ms_flow,
-                       "limiter": "FP64 pipe (ncu: 67 % of its issue slots, ALU 42 %, DRAM 9 %)"}
+    cap = FLOW_CAPTURE if not case.params.hydro_only else {}
+    roof = {"bound": "hbm", "kernel": "k_flow_route", "achieved": ach, "peak": peak,
+            "unit": "GB/s", "frac": ach / peak,
+            "traffic": (cap["dram_bytes_per_wet_cell"] * wet
+                        if cap.get("dram_bytes_per_wet_cell") else None),
+            "traffic_source": cap.get("source"), "peak_kind": kind,
+            "bytes_per_wet_cell": per_cell, "wet_cells": wet, "launch_ms": ms_flow}
+    # the FP64 pipe, which bounds this kernel: its warp instructions per wet
+    # cell (the capture) x 16 cycles each, against the pipe's cycles in the
+    # launch at the SM clock sampled during the timed region
+    if cap.get("fp64_warp_inst_per_wet_cell") and clk and clk.get("sm_mhz"):
+        sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+        need = cap["fp64_warp_inst_per_wet_cell"] * wet * (32 / FP64_LANES_PER_CLK_SM)
+        have = sms * clk["sm_mhz"] * 1e6 * (ms_flow / 1e3)
+        roof["fp64_pipe"] = {"frac": need / have, "warp_inst_per_wet_cell":
+                             cap["fp64_warp_inst_per_wet_cell"], "sms": sms,
+                             "sm_mhz": clk["sm_mhz"]}
+    out["roofline"] = roof
     return out, model, case
+
+
+def amortized_window(model, case, flags, stream, max_steps):
+    """Runs on from the timed region in chunks of 50 iterations until the
+    window holds a lateral3 call and a drainage recomputation (or max_steps);
+    device time per step over the whole window, with the host work counted."""
+    import torch
+    st0 = model.run_stats()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    n = 0
+    while n < max_steps:
+        n += model.run(50, flags, records=False)
+        st = model.run_stats()
+        if (st["lateral"][0] > st0["lateral"][0] or not (flags & HC_RUN_LATERAL)) and \
+                st["drainage"][0] > st0["drainage"][0]:
+            break
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    st = model.run_stats()
+    return {"steps": n, "ms_per_step": ms / max(1, n),
+            "cell_steps_per_s": case.cells * n / (ms / 1e3),
+            "lateral3_calls": st["lateral"][0] - st0["lateral"][0],
+            "drainage_recomputations": st["drainage"][0] - st0["drainage"][0],
+            "host_ms": round(sum(st[k][1] - st0[k][1] for k in st
+                                 if k not in ("drainage_sweep", "wet_cell_steps")), 3)}
 
 
 def run_ensemble_bench(args, rank):
@@ -325,8 +410,9 @@ def run_ensemble_bench(args, rank):
 
 def run_adjoint_bench(args):
     """C4: gradient of the outlet-Q loss with respect to every cell's n and
-    the rain table over `--steps` iterations (default 4000), checkpoints
-    every 200, against the same iterations run forward only."""
+    elevation and the rain table over --adj-iterations iterations (default
+    4000), at most --adj-states model states kept (binomial checkpointing),
+    against the same iterations run forward only."""
     import torch
     import hc
     torch.cuda.set_device(0)
@@ -337,7 +423,7 @@ def run_adjoint_bench(args):
 
     def spun(c):
         m = hc.Model(c)
-        spin_up(m, spin, 0)
+        spin_minutes(m, spin, 0)
         return m
     _, target = spun(tcase).adj_forward(n_it)
     mf = spun(case)
@@ -347,8 +433,8 @@ def run_adjoint_bench(args):
     torch.cuda.synchronize()
     t_fwd = time.perf_counter() - t0
     ma = spun(case)
-    loss, gn, gr, ms = ma.adj_gradient(n_it, 200, target)
-    ratio = ms[2] / (t_fwd * 1e3)
+    loss, gn, gr, info, ge = ma.adj_gradient(n_it, args.adj_states, target, elev=True)
+    ratio = info["total_ms"] / (t_fwd * 1e3)
     cells = case.cells
     return {"metric": METRIC, "value": ratio, "unit": "adjoint/forward wall-time ratio",
             "n_gpus": 1, "steps": n_it, "warmup": 0, "ms_per_step": ms[2] / n_it,
@@ -357,12 +443,17 @@ def run_adjoint_bench(args):
             "config": {"workload": "adjoint%d" % (args.size or 1024), "cells": cells,
                        "description": "hydro-only %dx%d @10 m, 20 mm/h for 3 h; loss = MSE of "
                                       "outlet Q per simulated minute vs a run with another n "
-                                      "field; gradient w.r.t. per-cell n and the rain table; "
-                                      "checkpoints every 200 iterations" % (case.params.imax,
+                                      "field; gradient w.r.t. per-cell n, elevation and the rain "
+                                      "table; binomial checkpointing" % (case.params.imax,
                                                                            case.params.jmax)},
             "forward_ms": t_fwd * 1e3, "forward_cell_steps_per_s": cells * n_it / t_fwd,
-            "gradient_ms": {"forward_checkpointed": ms[0], "reverse": ms[1], "total": ms[2]},
+            "gradient_ms": {"forward_checkpointed": info["forward_ms"],
+                            "reverse": info["reverse_ms"], "total": info["total_ms"]},
+            "checkpointing": {"max_states": args.adj_states, "segment": info["segment"],
+                              "snapshots": info["snapshots"],
+                              "iterations_advanced_again": info["advanced"]},
             "loss": loss, "grad_n_norm": float(np.sqrt((gn ** 2).sum())),
+            "grad_elev_norm": float(np.sqrt((ge ** 2).sum())),
             "grad_rain_norm": float(np.sqrt((gr ** 2).sum()))}
 
 
@@ -424,14 +515,16 @@ def run_reference(args):
     if args.workload == "adjoint":
         return {"impl": "reference", "unavailable": "the reference has no adjoint of its "
                 "iteration; nothing to time on the CPU for this workload"}
-    case, spin_min, desc = make_workload(args.workload, args.size)
+    case, spin_its, desc = make_workload(args.workload, args.size)
+    if args.spinup >= 0:
+        spin_its = int(args.spinup)
     flags = case.flags
     o = oracle.Oracle(case, omp=True)
-    while True:
-        o.iterate(2000, flags)
-        if o.scalar("cycle") >= spin_min:
-            break
+    # the same iterations as the GPU arm: spin-up, warm-up, then the timed
+    # steps of the same deterministic run
+    o.iterate(spin_its, flags)
     o.iterate(args.warmup, flags)
+    it0, cyc0 = int(o.scalar("counter")), o.scalar("cycle")
     t0 = time.perf_counter()
     o.iterate(args.steps, flags)
     dt = time.perf_counter() - t0
@@ -440,10 +533,12 @@ def run_reference(args):
     return {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": {"workload": args.workload, "description": desc,
-                                            "cells": case.cells},
+            "data": DATA, "config": workload_config(args, case, timed_from(desc, it0 + 1, cyc0),
+                                                    spin_its),
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": "%d steps after spin-up, OpenMP port" % args.steps},
+                             "sample": "%d steps after %d spin-up + %d warm-up iterations, OpenMP "
+                                       "port (-O3) on %d threads" % (args.steps, spin_its,
+                                                                     args.warmup, cores)},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
@@ -458,13 +553,18 @@ def main():
     ap.add_argument("--members", type=int, default=96, help="ensemble members")
     ap.add_argument("--adj-iterations", type=int, default=4000,
                     help="adjoint: iterations of the differentiated run")
+    ap.add_argument("--adj-states", type=int, default=220,
+                    help="adjoint: model states kept at once (binomial checkpointing)")
     ap.add_argument("--spinup-iters", type=int, default=300,
                     help="ensemble: iterations each member runs before timing")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--size", type=int, default=0,
                     help="override the grid side (smaller runs for profiling)")
     ap.add_argument("--spinup", type=float, default=-1,
-                    help="override the spin-up, simulated minutes")
+                    help="override the spin-up: iterations (simulated minutes for the "
+                         "adjoint workload)")
+    ap.add_argument("--amortize-max", type=int, default=1000,
+                    help="longest window of the amortized per-step figure")
     ap.add_argument("--timed-only", action="store_true",
                     help="only the timed steps (no e2e, profile, kernel timing or CPU leg); "
                          "for runs under a profiler")
@@ -507,12 +607,11 @@ def main():
             "metric": METRIC, "value": out["value"], "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": out["ms"] / out["done"],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded generators, hail-caesar_gb300/synth.py)",
-            "config": {"workload": args.workload, "description": out["desc"],
-                       "cells": out["cells"], "parallelism": "replicas x%d" % world,
-                       "l2": "inputs larger than L2 (model state several GB)"},
+            "data": DATA, "config": workload_config(args, case, out["desc"], out["spin_its"]),
             "clocks": out["clocks"], "e2e": out["e2e"], "roofline": out["roofline"],
             "gpu_launches": out["launches"], "phases_ms": out["phases_ms"],
+            "wet_cell_steps_per_s": out["wet_cell_steps_per_s"],
+            "amortized": out.get("amortized"),
             "host_work": out["host_work"], "simulated_minutes_timed": out["sim_minutes"],
         }
         if world == 1:

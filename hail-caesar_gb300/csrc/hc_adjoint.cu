@@ -23,6 +23,7 @@
 #include "hc_internal.cuh"
 
 #include <chrono>
+#include <functional>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -39,9 +40,9 @@ namespace {
 constexpr double kG = 9.81;
 
 // value and partial derivatives of a face discharge with respect to the
-// previous discharge q, the two depths and n^2
+// previous discharge q, the two depths, n^2 and the two elevations
 struct DQ {
-  double v, dq, dh0, dh1, dnn;
+  double v, dq, dh0, dh1, dnn, de0, de1;
 };
 
 // Three-way test of A > B from float estimates (as the forward kernel's):
@@ -62,12 +63,16 @@ __device__ __forceinline__ int decide(float a, float b) {
 __device__ DQ face_dq(double q, double e0, double h0, double e1, double h1, double nn, double dt,
                       int es, const hc_params& p, double rDX, const hc_divisor& dxd) {
   const double DX = p.DX;
-  DQ r = {0, 0, 0, 0, 0};
+  DQ r = {0, 0, 0, 0, 0, 0, 0};
   const double a0 = e0 + h0, a1 = e1 + h1;
   const bool a1max = a0 < a1;
   const double hflow = smax(a0, a1) - smax(e1, e0);
   if (!(hflow > p.hflow_threshold)) return r;  // q = 0
+  // hflow = max(surfaces) - max(beds): its derivatives by the depths, and
+  // by the elevations (through both maxima)
   const double dhf0 = a1max ? 0.0 : 1.0, dhf1 = a1max ? 1.0 : 0.0;
+  const bool e0max = e1 < e0;
+  const double dhfe0 = dhf0 - (e0max ? 1.0 : 0.0), dhfe1 = dhf1 - (e0max ? 0.0 : 1.0);
   double slope = ddiv_by(a1 - a0, dxd), ds0 = -rDX, ds1 = rDX;
   if (es == 1) slope = p.edgeslope, ds0 = ds1 = 0;
   if (es == -1) slope = 0 - p.edgeslope, ds0 = ds1 = 0;
@@ -96,6 +101,8 @@ __device__ DQ face_dq(double q, double e0, double h0, double e1, double h1, doub
     d_nn = -qn * dF_nn * rD;
   }
   double dh0 = d_hf * dhf0 + d_s * ds0, dh1 = d_hf * dhf1 + d_s * ds1;
+  // the slope reads the surfaces e + h, so an elevation moves it like a depth
+  double de0 = d_hf * dhfe0 + d_s * ds0, de1 = d_hf * dhfe1 + d_s * ds1;
   // Froude limit (:3124-3134): |q/hflow| / sqrt(g*hflow) > froude_limit
   const double fl = p.froude_limit;
   if (qn != 0) {
@@ -107,10 +114,10 @@ __device__ DQ face_dq(double q, double e0, double h0, double e1, double h1, doub
       const double g = 1.5 * sg * fl;
       if (qn > 0) {
         qn = hflow * (sg * fl);
-        d_q = 0, d_nn = 0, dh0 = g * dhf0, dh1 = g * dhf1;
+        d_q = 0, d_nn = 0, dh0 = g * dhf0, dh1 = g * dhf1, de0 = g * dhfe0, de1 = g * dhfe1;
       } else {
         qn = 0 - (hflow * (sg * fl));
-        d_q = 0, d_nn = 0, dh0 = -g * dhf0, dh1 = -g * dhf1;
+        d_q = 0, d_nn = 0, dh0 = -g * dhf0, dh1 = -g * dhf1, de0 = -g * dhfe0, de1 = -g * dhfe1;
       }
     }
   }
@@ -121,7 +128,7 @@ __device__ DQ face_dq(double q, double e0, double h0, double e1, double h1, doub
     if (t == 0) t = ((qn * dt / DX) > (h0 / 4)) ? 1 : -1;
     if (t > 0) {
       qn = ddiv_rn(ddiv_rn(h0 * DX, 5.0), dt);
-      d_q = 0, d_nn = 0, dh0 = ddiv_rn(ddiv_rn(DX, 5.0), dt), dh1 = 0;
+      d_q = 0, d_nn = 0, dh0 = ddiv_rn(ddiv_rn(DX, 5.0), dt), dh1 = 0, de0 = de1 = 0;
     }
   }
   if (qn < 0) {
@@ -129,7 +136,7 @@ __device__ DQ face_dq(double q, double e0, double h0, double e1, double h1, doub
     if (t == 0) t = (fabs(qn * dt / DX) > (h1 / 4)) ? 1 : -1;
     if (t > 0) {
       qn = 0 - ddiv_rn(ddiv_rn(h1 * DX, 5.0), dt);
-      d_q = 0, d_nn = 0, dh0 = 0, dh1 = -ddiv_rn(ddiv_rn(DX, 5.0), dt);
+      d_q = 0, d_nn = 0, dh0 = 0, dh1 = -ddiv_rn(ddiv_rn(DX, 5.0), dt), de0 = de1 = 0;
     }
   }
   r.v = qn;
@@ -137,6 +144,8 @@ __device__ DQ face_dq(double q, double e0, double h0, double e1, double h1, doub
   r.dh0 = dh0;
   r.dh1 = dh1;
   r.dnn = d_nn;
+  r.de0 = de0;
+  r.de1 = de1;
   return r;
 }
 
@@ -155,7 +164,9 @@ struct AdjBufs {
   const uint8_t* point;  // input-point cells of this iteration
   double *lam, *mux, *muy;  // adjoints of h, qx, qy (in: after, out: before)
   double *lamd, *p0x, *p0y, *p1x, *p1y;
+  double *pe0, *pe1x, *pe1y;  // elevation terms: own faces, to the cell above, to the left
   double *gn;   // accumulated dL/dn per cell
+  double *ge;   // accumulated dL/d(elevation) per cell
   double *gj;   // dL/dj per zone for this iteration
 };
 
@@ -202,6 +213,7 @@ __global__ void k_adj_flow(const hc_view c, AdjBufs b, AdjStep st) {
   const double mux = b.mux[cell] + k * (ml(cell - W) - ml(cell));
   const double muy = b.muy[cell] + k * (ml(cell - 1) - ml(cell));
   double ox = mux, oy = muy, p0x = 0, p1x = 0, p0y = 0, p1y = 0, gn = 0;
+  double pe0 = 0, pe1x = 0, pe1y = 0;
   const double e0 = c.elev[cell];
   if (b.mask[cell] && e0 > -9999) {
     const hc_params& p = c.p;
@@ -224,6 +236,8 @@ __global__ void k_adj_flow(const hc_view c, AdjBufs b, AdjStep st) {
         p0x = r.dh0 * mux;
         p1x = r.dh1 * mux;
         gn += r.dnn * mux;
+        pe0 += r.de0 * mux;
+        pe1x = r.de1 * mux;
       }
     }
     {
@@ -236,6 +250,8 @@ __global__ void k_adj_flow(const hc_view c, AdjBufs b, AdjStep st) {
         p0y = r.dh0 * muy;
         p1y = r.dh1 * muy;
         gn += r.dnn * muy;
+        pe0 += r.de0 * muy;
+        pe1y = r.de1 * muy;
       }
     }
     b.gn[cell] += gn * 2 * n;
@@ -246,6 +262,9 @@ __global__ void k_adj_flow(const hc_view c, AdjBufs b, AdjStep st) {
   b.p1x[cell] = p1x;
   b.p0y[cell] = p0y;
   b.p1y[cell] = p1y;
+  b.pe0[cell] = pe0;
+  b.pe1x[cell] = pe1x;
+  b.pe1y[cell] = pe1y;
 }
 
 // the depth adjoint before the iteration (inputs add a constant), and the
@@ -262,6 +281,7 @@ __global__ void __launch_bounds__(256) k_adj_gather(const hc_view c, AdjBufs b, 
     const size_t W = c.W, cell = (size_t)i * W + j;
     const double la = b.lamd[cell] + b.p0x[cell] + b.p0y[cell] + b.p1x[cell + W] + b.p1y[cell + 1];
     b.lam[cell] = la;
+    b.ge[cell] += b.pe0[cell] + b.pe1x[cell + W] + b.pe1y[cell + 1];
     const int rf = c.rfarea[cell];
     if (b.point[cell] && rf >= 0 && rf <= HC_MAX_RF) {
       mine = la * st.damt[rf];
@@ -457,10 +477,119 @@ extern "C" hc_status hc_adj_forward(hc_ctx* c, int64_t n, const double* fixed, d
   return HC_OK;
 }
 
-extern "C" hc_status hc_adj_gradient(hc_ctx* c, int64_t n, int32_t every, const double* q_target,
-                                     int64_t n_target, double* loss, double* grad_n,
-                                     double* grad_rain, double* ms) {
-  if (!c || n <= 0 || every <= 0 || !q_target || n_target < 0) return HC_ERR_ARG;
+// ---- binomial checkpointing (Griewank's revolve, by recursion) -----------
+// The run is cut into m segments of K iterations.  Reversing segments
+// [a, b) with the state at a in a snapshot and s more snapshots free: one
+// segment is a leaf (replay it from the state at a, keeping each
+// iteration's state, then run its adjoint iterations last first); with no
+// snapshot free, every segment from the last down is reached again from a;
+// otherwise the state at a split point mid is made (advancing from a) and
+// kept, [mid, b) is reversed with s-1 snapshots and [a, mid) with s.  With
+// r the smallest repetition number with C(s+r, s) >= b-a, any mid with
+// b-mid <= C(s-1+r, s-1) and mid-a <= C(s+r-1, s) gives the least
+// recomputation (r advances per segment at most); this takes the first.
+namespace {
+
+double binom(int s, int r) {  // C(s + r, s), saturating
+  double v = 1;
+  for (int k = 1; k <= s; k++) {
+    v = v * (r + k) / k;
+    if (v > 1e18) return 1e18;
+  }
+  return v;
+}
+
+int repetitions(int64_t l, int s) {
+  int r = 0;
+  while (binom(s, r) < (double)l) r++;
+  return r;
+}
+
+int64_t split_point(int64_t a, int64_t b, int s) {
+  const int64_t l = b - a;
+  const int r = repetitions(l, s);
+  const double right = binom(s - 1, r);  // segments [mid, b) may hold
+  int64_t m = (right >= (double)l) ? 1 : l - (int64_t)right;
+  if (m < 1) m = 1;
+  if (m > l - 1) m = l - 1;
+  return a + m;
+}
+
+// segments advanced again to reverse [a, b) with s free snapshots (the
+// leaves' replays not counted); on the right spine of the recursion the
+// split points were kept by the forward run and cost nothing
+double schedule_cost(int64_t a, int64_t b, int s, bool spine) {
+  const int64_t l = b - a;
+  if (l <= 1) return 0;
+  if (s == 0) return (double)l * (l - 1) / 2;
+  const int64_t mid = split_point(a, b, s);
+  return (spine ? 0.0 : (double)(mid - a)) + schedule_cost(mid, b, s - 1, spine) +
+         schedule_cost(a, mid, s, false);
+}
+
+struct Revolve {
+  hc_ctx* c;
+  int64_t n, K, m;            // iterations, segment length, segments
+  std::vector<Checkpoint>* slots;
+  std::vector<int64_t> slot_of;  // segment -> snapshot slot holding its start (-1 none)
+  std::vector<int> free_slots;
+  std::function<hc_status(int64_t)> leaf;          // reverse segment g from the state now
+  std::function<hc_status(int64_t, int64_t)> advance;  // iterations [t0, t1) forward
+  int64_t advances = 0;      // iterations advanced beyond the first sweep
+
+  hc_status restore(int64_t g) { return load_state(c, (*slots)[(size_t)slot_of[(size_t)g]]); }
+  hc_status keep(int64_t g) {
+    if (free_slots.empty()) return hc_fail(c, HC_ERR_STATE, "adjoint: no snapshot slot left");
+    const int k = free_slots.back();
+    free_slots.pop_back();
+    slot_of[(size_t)g] = k;
+    return save_state(c, (*slots)[(size_t)k], false);
+  }
+  void drop(int64_t g) {
+    if (slot_of[(size_t)g] >= 0 && g != 0) {
+      free_slots.push_back((int)slot_of[(size_t)g]);
+      slot_of[(size_t)g] = -1;
+    }
+  }
+  hc_status reach(int64_t from, int64_t to) {  // segment boundaries
+    HC_TRY(restore(from));
+    if (to > from) {
+      advances += std::min(n, to * K) - from * K;
+      HC_TRY(advance(from * K, std::min(n, to * K)));
+    }
+    return HC_OK;
+  }
+  hc_status reverse(int64_t a, int64_t b, int s) {
+    if (b - a == 1) {
+      HC_TRY(restore(a));
+      return leaf(a);
+    }
+    if (s == 0) {
+      for (int64_t g = b - 1; g >= a; g--) {
+        HC_TRY(reach(a, g));
+        HC_TRY(leaf(g));
+      }
+      return HC_OK;
+    }
+    const int64_t mid = split_point(a, b, s);
+    const bool had = slot_of[(size_t)mid] >= 0;  // kept by the first sweep
+    if (!had) {
+      HC_TRY(reach(a, mid));
+      HC_TRY(keep(mid));
+    }
+    HC_TRY(reverse(mid, b, s - 1));
+    drop(mid);
+    return reverse(a, mid, s);
+  }
+};
+
+}  // namespace
+
+extern "C" hc_status hc_adj_gradient(hc_ctx* c, int64_t n, int32_t max_states,
+                                     const double* q_target, int64_t n_target, double* loss,
+                                     double* grad_n, double* grad_rain, double* grad_elev,
+                                     double* ms) {
+  if (!c || n <= 0 || max_states < 2 || !q_target || n_target < 0) return HC_ERR_ARG;
   hc_view& v = c->v;
   if (!v.p.hydro_only) return hc_fail(c, HC_ERR_UNSUPPORTED, "adjoint runs are hydro-only");
   if (v.p.spatially_complex_rainfall)
@@ -468,14 +597,35 @@ extern "C" hc_status hc_adj_gradient(hc_ctx* c, int64_t n, int32_t every, const 
   if (!c->prepared) return hc_fail(c, HC_ERR_STATE, "hc_prepare must come before the run");
   const auto t_all = std::chrono::steady_clock::now();
   const size_t N2 = v.N2;
-  const int64_t nseg = (n + every - 1) / every;
   cudaStream_t s = c->s;
+  // The states kept: snapshots (run state at a segment start) and the K
+  // iteration states of the segment being reversed, max_states in all.
+  // Segment length: the one with the least recomputation; of those the
+  // longest (fewer, longer replays: less launch and host overhead).
+  int64_t K = 1;
+  int snaps = 0;
+  {
+    double best = 1e300;
+    for (int64_t k = 1; k < max_states && k <= n; k = (k < 8) ? k + 1 : k + k / 8) {
+      const int sn = (int)(max_states - k);  // snapshots, the initial state's included
+      const int64_t m = (n + k - 1) / k;
+      const double cost = schedule_cost(0, m, std::min<int64_t>(sn, m) - 1, true) * (double)k;
+      if (cost <= best) {
+        best = cost;
+        K = k;
+        snaps = sn;
+      }
+    }
+  }
+  const int64_t nseg = (n + K - 1) / K;
+  if (snaps > nseg) snaps = (int)nseg;
   // replay slots, set in the view for the whole call (k_adj_save is part of
   // the graphs while they are set)
   Dev sh, sqx, sqy, smask;
-  if (dmalloc(sh, (size_t)every * N2 * 8) || dmalloc(sqx, (size_t)(every + 1) * N2 * 8) ||
-      dmalloc(sqy, (size_t)(every + 1) * N2 * 8) || dmalloc(smask, (size_t)every * N2))
-    return hc_fail(c, HC_ERR_NOMEM, "adjoint: out of device memory (segment of %d)", every);
+  if (dmalloc(sh, (size_t)K * N2 * 8) || dmalloc(sqx, (size_t)(K + 1) * N2 * 8) ||
+      dmalloc(sqy, (size_t)(K + 1) * N2 * 8) || dmalloc(smask, (size_t)K * N2))
+    return hc_fail(c, HC_ERR_NOMEM, "adjoint: out of device memory (segment of %lld)",
+                   (long long)K);
   struct SlotGuard {
     hc_ctx* c;
     ~SlotGuard() {
@@ -491,21 +641,44 @@ extern "C" hc_status hc_adj_gradient(hc_ctx* c, int64_t n, int32_t every, const 
   v.adj_sqy = sqy.as<double>();
   v.adj_smask = smask.as<uint8_t>();
   c->graph_iters = 0;
-  // ---------------- forward, checkpointed, recording time steps and Q
+  std::vector<Checkpoint> cps((size_t)snaps + 1);  // + the state at the end
+  for (auto& cp : cps) HC_TRY(save_state(c, cp, true));
+  Revolve rv;
+  rv.c = c;
+  rv.n = n;
+  rv.K = K;
+  rv.m = nseg;
+  rv.slots = &cps;
+  rv.slot_of.assign((size_t)nseg + 1, -1);
+  for (int k = snaps - 1; k >= 1; k--) rv.free_slots.push_back(k);
+  rv.slot_of[0] = 0;
+  // the snapshots of the first sweep: the split points down the right spine
+  std::vector<char> first((size_t)nseg + 1, 0);
+  {
+    int64_t a = 0;
+    int sl = snaps - 1;
+    while (nseg - a > 1 && sl > 0) {
+      a = split_point(a, nseg, sl);
+      first[(size_t)a] = 1;
+      sl--;
+    }
+  }
+  // ---------------- forward, recording time steps and Q, keeping the
+  // first sweep's snapshots
   Dev dt;
   HC_CU(dmalloc(dt, (size_t)n * HC_ADJ_REC * 8), "adjoint record");
-  std::vector<Checkpoint> cps((size_t)nseg + 1);
   HC_TRY(ctx_pull(c));
   const double cycle0 = c->hdev->s.cycle, time1_0 = c->hdev->s.time_1;
   HC_TRY(adj_mode(c, dt.as<double>(), n, 1, 0));  // no saves in the forward run
   std::vector<hc_step_record> rec((size_t)n);
   const auto t_fwd = std::chrono::steady_clock::now();
+  HC_TRY(save_state(c, cps[0], false));
   int64_t done_all = 0;
   for (int64_t g = 0; g < nseg; g++) {
-    HC_TRY(save_state(c, cps[(size_t)g], true));
-    const int64_t len = std::min<int64_t>(every, n - g * every);
+    if (g > 0 && first[(size_t)g]) HC_TRY(rv.keep(g));
+    const int64_t len = std::min<int64_t>(K, n - g * K);
     int64_t done = 0;
-    HC_TRY(hc_run(c, len, 0, rec.data() + g * every, &done));
+    HC_TRY(hc_run(c, len, 0, rec.data() + g * K, &done));
     done_all += done;
     if (done != len) {
       adj_mode(c, nullptr, 0, 0, 0);
@@ -513,7 +686,7 @@ extern "C" hc_status hc_adj_gradient(hc_ctx* c, int64_t n, int32_t every, const 
                      (long long)done_all, (long long)n);
     }
   }
-  HC_TRY(save_state(c, cps[(size_t)nseg], true));
+  HC_TRY(save_state(c, cps[(size_t)snaps], false));  // the end, where the model is left
   HC_CU(cudaStreamSynchronize(s), "adjoint forward");
   const double ms_fwd = ms_since(t_fwd);
   std::vector<double> arec((size_t)n * HC_ADJ_REC);
@@ -530,24 +703,28 @@ extern "C" hc_status hc_adj_gradient(hc_ctx* c, int64_t n, int32_t every, const 
     gQ[(size_t)at[(size_t)k]] = 2 * d / (double)S;
   }
   if (loss) *loss = L;
-  // ---------------- reverse, one segment at a time
+  // ---------------- reverse
   const auto t_rev = std::chrono::steady_clock::now();
-  const int64_t K = every;
-  Dev lam, mux, muy, lamd, p0x, p0y, p1x, p1y, gn, gj;
+  Dev lam, mux, muy, lamd, p0x, p0y, p1x, p1y, pe0, pe1x, pe1y, gn, ge, gj;
   if (dmalloc(lam, N2 * 8) || dmalloc(mux, N2 * 8) || dmalloc(muy, N2 * 8) ||
       dmalloc(lamd, N2 * 8) || dmalloc(p0x, N2 * 8) || dmalloc(p0y, N2 * 8) ||
-      dmalloc(p1x, N2 * 8) || dmalloc(p1y, N2 * 8) || dmalloc(gn, N2 * 8) ||
-      dmalloc(gj, (size_t)n * (HC_MAX_RF + 1) * 8)) {
+      dmalloc(p1x, N2 * 8) || dmalloc(p1y, N2 * 8) || dmalloc(pe0, N2 * 8) ||
+      dmalloc(pe1x, N2 * 8) || dmalloc(pe1y, N2 * 8) || dmalloc(gn, N2 * 8) ||
+      dmalloc(ge, N2 * 8) || dmalloc(gj, (size_t)n * (HC_MAX_RF + 1) * 8)) {
     adj_mode(c, nullptr, 0, 0, 0);
     return hc_fail(c, HC_ERR_NOMEM, "adjoint: out of device memory");
   }
-  for (Dev* d : {&lam, &mux, &muy, &lamd, &p0x, &p0y, &p1x, &p1y, &gn})
+  for (Dev* d : {&lam, &mux, &muy, &lamd, &p0x, &p0y, &p1x, &p1y, &pe0, &pe1x, &pe1y, &gn, &ge})
     cudaMemsetAsync(d->p, 0, N2 * 8, s);
   cudaMemsetAsync(gj.p, 0, (size_t)n * (HC_MAX_RF + 1) * 8, s);
   dim3 b(32, 8), gr((v.jmax + 31) / 32, (v.imax + 7) / 8);
-  for (int64_t g = nseg - 1; g >= 0; g--) {
+  rv.advance = [&](int64_t t0, int64_t t1) -> hc_status {
+    HC_TRY(adj_mode(c, dt.as<double>(), n, 2, t0));  // imposed steps, no saves
+    int64_t done = 0;
+    return hc_run(c, t1 - t0, 0, nullptr, &done);
+  };
+  rv.leaf = [&](int64_t g) -> hc_status {
     const int64_t t0 = g * K, len = std::min<int64_t>(K, n - t0);
-    HC_TRY(load_state(c, cps[(size_t)g]));
     // replay as one graph run; k_adj_save keeps every iteration's state
     HC_TRY(adj_mode(c, dt.as<double>(), n, 2, t0, t0, len));
     PointsLog pts;
@@ -588,7 +765,11 @@ extern "C" hc_status hc_adj_gradient(hc_ctx* c, int64_t n, int32_t every, const 
       bb.p0y = p0y.as<double>();
       bb.p1x = p1x.as<double>();
       bb.p1y = p1y.as<double>();
+      bb.pe0 = pe0.as<double>();
+      bb.pe1x = pe1x.as<double>();
+      bb.pe1y = pe1y.as<double>();
       bb.gn = gn.as<double>();
+      bb.ge = ge.as<double>();
       bb.gj = gj.as<double>() + (size_t)t * (HC_MAX_RF + 1);
       const double* na = pts.nact_at(t);
       const double* ct = pts.cnt_at(t);
@@ -605,11 +786,14 @@ extern "C" hc_status hc_adj_gradient(hc_ctx* c, int64_t n, int32_t every, const 
     }
     HC_CU(cudaGetLastError(), "adjoint kernels");
     HC_CU(cudaStreamSynchronize(s), "adjoint");  // pts' buffers are freed next
-  }
+    return HC_OK;
+  };
+  HC_TRY(rv.reverse(0, nseg, snaps - 1));
   HC_CU(cudaStreamSynchronize(s), "adjoint");
   const double ms_rev = ms_since(t_rev);
   // ---------------- results
   if (grad_n) HC_CU(cudaMemcpy(grad_n, gn.p, N2 * 8, cudaMemcpyDeviceToHost), "adjoint gradient");
+  if (grad_elev) HC_CU(cudaMemcpy(grad_elev, ge.p, N2 * 8, cudaMemcpyDeviceToHost), "adjoint gradient");
   if (grad_rain) {
     int rows = 0, cols = 0;
     const float* rain = ctx_rain(c, &rows, &cols);
@@ -639,12 +823,15 @@ extern "C" hc_status hc_adj_gradient(hc_ctx* c, int64_t n, int32_t every, const 
     }
   }
   // leave the model where the forward run ended
-  HC_TRY(load_state(c, cps[(size_t)nseg]));
+  HC_TRY(load_state(c, cps[(size_t)snaps]));
   HC_TRY(adj_mode(c, nullptr, 0, 0, 0));
   if (ms) {
     ms[0] = ms_fwd;
     ms[1] = ms_rev;
     ms[2] = ms_since(t_all);
+    ms[3] = (double)K;
+    ms[4] = (double)snaps;
+    ms[5] = (double)rv.advances;
   }
   return HC_OK;
 }

@@ -281,11 +281,15 @@ extern "C" hc_status hc_create(const hc_params* p, size_t max_bytes, hc_ctx** ou
   A(v.edge, E2) A(v.edge2, E2) A(v.veg, 4 * E2)
   A(v.cin_x, (size_t)p->imax * p->jmax + 2) A(v.cin_y, (size_t)p->imax * p->jmax + 2)
   A(v.wet, N2) A(v.wet_sums, (N2 + 1023) / 1024 + 1)
+  // partial sums: one per block of scan_area (32 x 8 cells) or of a grid_sum
+  v.vpart_cap = (int)std::max<size_t>(
+      (size_t)((p->jmax + 31) / 32) * (size_t)((p->imax + 7) / 8), 152 * 8);
+  A(v.vpart, (size_t)v.vpart_cap)
   A(v.drain_pos, N2) A(v.drain_f0, N2) A(v.drain_f1, N2) A(v.drain_pend, N2) A(v.drain_dt, N2)
   A(v.drain_frac, 9 * N2) A(v.drain_multi, N2)
   A(v.drain_aux, 1)
   if (sed) {
-    A(v.sflux, 40 * N2) A(v.grain, 11 * N2) A(v.strata, 90 * N2) A(v.alloc_key, N2)
+    A(v.sflux, 40 * N2) A(v.sdirty, N2) A(v.grain, 11 * N2) A(v.strata, 90 * N2) A(v.alloc_key, N2)
     A(v.erodetot, N2) A(v.erodetot3, N2) A(v.pre, 11 * N2) A(v.chains, 4 * N2)
     A(v.drain_snap, N2) A(v.ent_list, N2) A(v.ent_qs, 2 * N2)
   } else {
@@ -294,7 +298,7 @@ extern "C" hc_status hc_create(const hc_params* p, size_t max_bytes, hc_ctx** ou
   char* red = nullptr;
   A(red, erode_scratch_bytes(N2, p->imax, p->jmax))
   v.red = (double*)red;
-  A(v.touched, slide_scratch_bytes(N2, p->imax))
+  A(v.touched, slide_scratch_bytes(N2, std::max(p->imax, p->jmax)))
   double* lat = nullptr;
   if (sed && p->imax == p->jmax) A(lat, lateral_scratch_bytes(p->imax, p->jmax) / 8 + 1)
   A(c->dev, 1)
@@ -328,13 +332,14 @@ extern "C" hc_status hc_create(const hc_params* p, size_t max_bytes, hc_ctx** ou
   cudaMemsetAsync(v.erodetot, 0, N2 * 8, s);
   if (sed) {
     cudaMemsetAsync(v.sflux, 0, 40 * N2 * 8, s);
+    cudaMemsetAsync(v.sdirty, 0, N2, s);
     cudaMemsetAsync(v.grain, 0, 11 * N2 * 8, s);
     cudaMemsetAsync(v.strata, 0, 90 * N2 * 8, s);
     cudaMemsetAsync(v.erodetot3, 0, N2 * 8, s);
     k_fill_u64<<<4096, 256, 0, s>>>(v.alloc_key, N2, ~0ull);
   }
   cudaMemsetAsync(v.red, 0, erode_scratch_bytes(N2, p->imax, p->jmax), s);
-  cudaMemsetAsync(v.touched, 0, slide_scratch_bytes(N2, p->imax), s);
+  cudaMemsetAsync(v.touched, 0, slide_scratch_bytes(N2, std::max(p->imax, p->jmax)), s);
   // scalar members at their initialisers (LSDCatchmentModel.hpp)
   hc_dev* hd = c->hdev;
   std::memset(hd, 0, sizeof *hd);
@@ -369,7 +374,7 @@ static hc_status free_all(hc_ctx* c) {
                   v.edge, v.edge2, v.veg, v.cin_x, v.cin_y, v.erodetot, v.erodetot3, v.pre,
                   v.chains, v.ent_list, v.ent_qs, v.drain_pos, v.drain_f0, v.drain_f1, v.drain_pend, v.drain_dt, v.drain_frac, v.drain_multi,
                   v.drain_snap, v.drain_aux, v.alloc_key, v.red, v.touched, v.topm, v.rain, v.rec, c->dev, v.wet,
-                  v.wet_sums,
+                  v.wet_sums, v.vpart, v.sdirty,
                   v.reach[0], v.reach[1], v.reach[2], extra(c).lateral};
   for (void* q : ptrs)
     if (q) cudaFree(q);
@@ -485,6 +490,7 @@ extern "C" hc_status hc_upload(hc_ctx* c, hc_field f, const void* host, size_t n
         for (int n = 0; n < 10; n++) planes[(size_t)n * N2 + cell] = h[cell * 10 + n];
       HC_CU(cudaMemcpy(v.sflux + (size_t)dir * 10 * N2, planes.data(), 10 * N2 * 8,
                        cudaMemcpyHostToDevice), "upload");
+      HC_CU(cudaMemset(v.sdirty, 1, N2), "upload");  // any entry may be nonzero now
       break;
     }
     case HC_F_GRAIN: case HC_F_STRATA: {
@@ -712,6 +718,7 @@ extern "C" hc_status hc_set_reach(hc_ctx* c, int32_t point, const float* data, i
 static hc_status device_error(hc_ctx* c) {
   const int e = c->hdev->err_code;
   if (e == 301) return hc_fail(c, HC_ERR_NONFINITE, "non-finite water depth (device error 301)");
+  if (e == 401) return hc_fail(c, HC_ERR_TIMEOUT, "drainage sweep: a device wait gave up (401)");
   return hc_fail(c, HC_ERR_STATE, "device error %d", e);
 }
 
@@ -805,7 +812,19 @@ static hc_status recompute_points(hc_ctx* c, bool snapshot) {
   HC_CU(cudaStreamSynchronize(c->s), "drainage");
   c->area_valid = true;
   HC_TRY(pull(c));
+  if ((c->hdev->pause & HC_PAUSE_ERROR) && c->hdev->err_code == 401) {
+    // a bounded wait of the sweep ran out: the context stays usable, and
+    // the next hc_run makes this recomputation again before its iterations
+    const hc_status st = device_error(c);
+    c->hdev->err_code = 0;
+    c->hdev->pause &= ~HC_PAUSE_ERROR;
+    c->area_valid = false;
+    c->drain_retry = true;
+    HC_TRY(push(c));
+    return st;
+  }
   if (c->hdev->pause & HC_PAUSE_ERROR) return device_error(c);
+  c->drain_retry = false;
   if (!keep_area) c->stat_n[HC_STAT_DRAINAGE_LEVELS] += c->hdev->drain_levels;
   if (c->points_hook) c->points_hook(c, c->points_hook_arg);
   return HC_OK;
@@ -872,7 +891,32 @@ extern "C" hc_status hc_prepare(hc_ctx* c) {
   }
   c->prepared = true;
   c->graph_iters = 0;  // parameters of the view changed: rebuild the graph
+  launch_mass_reset(c);  // the water ledger starts from the state as prepared
+  HC_TRY(pull(c));
   return HC_OK;
+}
+
+// ------------------------------------------------------------------ water ledger
+extern "C" hc_status hc_mass_balance(hc_ctx* c, hc_mass* m) {
+  if (!c || !m) return HC_ERR_ARG;
+  launch_volume(c);
+  HC_TRY(pull(c));
+  const hc_dev* d = c->hdev;
+  const double a2 = c->v.p.DX * c->v.p.DX;
+  m->volume0 = d->vol0 * a2;
+  m->volume = d->vol_now * a2;
+  // terms of an iteration whose water_flux_out has not run yet count too
+  m->inflow = (d->vin_tot + d->vin_step) * a2;
+  m->outflow = d->vout_tot * a2;
+  m->lost = (d->vlost_tot + d->vlost_step) * a2;
+  m->mask_edge = (d->vmask_tot + d->vmask_step) * a2;
+  return HC_OK;
+}
+
+extern "C" hc_status hc_mass_reset(hc_ctx* c) {
+  if (!c) return HC_ERR_ARG;
+  launch_mass_reset(c);
+  return pull(c);
 }
 
 // ------------------------------------------------------------------ members
@@ -948,6 +992,25 @@ extern "C" hc_status hc_in_channel_landsliding(hc_ctx* c) {
   HC_TRY(pull(c));
   if (c->hdev->pause & HC_PAUSE_ERROR)
     return device_error(c);
+  return HC_OK;
+}
+
+extern "C" hc_status hc_global_landsliding(hc_ctx* c, int32_t* sweeps) {
+  if (!c) return HC_ERR_ARG;
+  if (c->v.p.hydro_only) return hc_fail(c, HC_ERR_STATE, "erosion arrays absent (hydro_only)");
+  int n = 0;
+  HC_TRY(run_global_landsliding(c, &n));
+  if (sweeps) *sweeps = n;
+  HC_CU(cudaStreamSynchronize(c->s), "global_landsliding");
+  return HC_OK;
+}
+
+extern "C" hc_status hc_creep(hc_ctx* c, double time) {
+  if (!c) return HC_ERR_ARG;
+  if (c->v.p.hydro_only) return hc_fail(c, HC_ERR_STATE, "erosion arrays absent (hydro_only)");
+  HC_TRY(run_creep(c, time));
+  HC_TRY(pull(c));
+  if (c->hdev->pause & HC_PAUSE_ERROR) return device_error(c);
   return HC_OK;
 }
 
@@ -1156,7 +1219,7 @@ static hc_status host_steps(hc_ctx* c, int flags) {
         StatTimer st(c, HC_STAT_GLOBAL_SLIDE);
         hd->s.creep_time2 += p.global_landsliding_interval;
         HC_TRY(push(c));
-        HC_TRY(run_global_landsliding(c));
+        HC_TRY(run_global_landsliding(c, nullptr));
         HC_TRY(pull(c));
       }
     }
@@ -1201,6 +1264,13 @@ static hc_status run_begin(hc_ctx* c, int64_t n, int32_t flags, bool want_rec, b
   hd->rec_index = 0;
   hd->flags = flags;
   HC_TRY(push(c));
+  if (c->drain_retry) {
+    // the recomputation a timed-out wait left undone, from the elevations at
+    // the start of the iteration that asked for it (erosion runs)
+    StatTimer st(c, HC_STAT_DRAINAGE);
+    HC_TRY(recompute_points(c, true));
+    HC_TRY(pull(c));
+  }
   if (!c->graph_iters || c->graph_flags != flags) HC_TRY(build_graph(c, flags));
   if (!c->chunk_done) HC_CU(cudaEventCreateWithFlags(&c->chunk_done, cudaEventDisableTiming),
                             "event");
@@ -1313,8 +1383,19 @@ extern "C" hc_status hc_run_ensemble(hc_ctx** ctxs, int32_t m, int64_t n, int32_
   return HC_OK;
 }
 
+extern "C" hc_status hc_test_bounded_waits(hc_ctx* c, int32_t spins, int32_t extra_arrivals) {
+  if (!c || spins < 0 || extra_arrivals < 0) return HC_ERR_ARG;
+  c->v.wait_spins = spins;
+  c->v.barrier_extra = spins > 0 ? extra_arrivals : 0;
+  return HC_OK;
+}
+
 extern "C" hc_status hc_get_run_stats(hc_ctx* c, int64_t* counts, double* host_ms, int32_t n) {
   if (!c || n < 0) return HC_ERR_ARG;
+  if (n > HC_STAT_WET_CELL_STEPS) {
+    HC_TRY(pull(c));
+    c->stat_n[HC_STAT_WET_CELL_STEPS] = (int64_t)c->hdev->wet_steps;
+  }
   for (int k = 0; k < n && k < HC_STAT_COUNT; k++) {
     if (counts) counts[k] = c->stat_n[k];
     if (host_ms) host_ms[k] = c->stat_ms[k];

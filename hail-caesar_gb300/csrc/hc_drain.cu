@@ -256,21 +256,23 @@ struct DrainSync {
 // level costs more than the work.
 constexpr unsigned kSoloMax = 2048;
 
-__device__ __forceinline__ bool grid_barrier(DrainSync* g, unsigned nblocks) {
+// `limit`: spins before giving up; `expect`: arrivals that open it (the
+// number of blocks, unless a test asks for more)
+__device__ __forceinline__ bool grid_barrier(DrainSync* g, unsigned expect, long limit) {
   __shared__ bool ok;
   __syncthreads();
   if (threadIdx.x == 0) {
     ok = true;
     const unsigned my = *(volatile unsigned*)&g->gen;
     __threadfence();
-    if (atomicAdd(&g->arrive, 1u) == nblocks - 1) {
+    if (atomicAdd(&g->arrive, 1u) == expect - 1) {
       g->arrive = 0;
       __threadfence();
       atomicAdd(&g->gen, 1u);
     } else {
       long spins = 0;
       while (*(volatile unsigned*)&g->gen == my) {
-        if (++spins > (1L << 22) || *(volatile unsigned*)&g->err) {
+        if (++spins > limit || *(volatile unsigned*)&g->err) {
           atomicExch(&g->err, 1u);
           ok = false;
           break;
@@ -430,6 +432,13 @@ __global__ void __launch_bounds__(512, 1) k_drain_sweep(const hc_view c, hc_dev*
   const unsigned gtid = blockIdx.x * blockDim.x + threadIdx.x;
   const unsigned gsize = nblocks * blockDim.x;
   const unsigned long long M = (unsigned long long)c.imax * c.jmax;
+  // the waits' limits (a test may shorten them and make the barrier
+  // expect more arrivals than there are blocks)
+  const bool test = c.wait_spins > 0;
+  const long bar_limit = test ? (long)c.wait_spins : (1L << 22);
+  const long solo_limit = test ? (long)c.wait_spins : (1L << 24);
+  const unsigned expect = nblocks + (test ? (unsigned)c.barrier_extra : 0u);
+  const unsigned solo_max = (test && c.barrier_extra > 0) ? 0u : kSoloMax;
   unsigned long long done = 0;
   unsigned level = 0;
   uint32_t* fr[2] = {c.drain_f0, c.drain_f1};
@@ -437,7 +446,7 @@ __global__ void __launch_bounds__(512, 1) k_drain_sweep(const hc_view c, hc_dev*
     const unsigned cur = level % 3, nxt = (level + 1) % 3;
     const unsigned n_in = *(volatile unsigned*)&g->count[cur];
     if (n_in == 0 || *(volatile unsigned*)&g->err) break;
-    if (n_in <= kSoloMax) {
+    if (n_in <= solo_max) {
       if (blockIdx.x == 0) {
         unsigned n = n_in;
         for (;;) {
@@ -455,7 +464,7 @@ __global__ void __launch_bounds__(512, 1) k_drain_sweep(const hc_view c, hc_dev*
             if (threadIdx.x == 0) atomicExch(&g->err, 2u);
             break;
           }
-          if (n == 0 || n > kSoloMax) break;
+          if (n == 0 || n > solo_max) break;
         }
         if (threadIdx.x == 0) {
           g->count[level % 3] = n;
@@ -470,7 +479,7 @@ __global__ void __launch_bounds__(512, 1) k_drain_sweep(const hc_view c, hc_dev*
           s_ok = true;
           long spins = 0;
           while (*(volatile unsigned*)&g->solo_level <= level) {
-            if (++spins > (1L << 24) || *(volatile unsigned*)&g->err) {
+            if (++spins > solo_limit || *(volatile unsigned*)&g->err) {
               atomicExch(&g->err, 1u);
               s_ok = false;
               break;
@@ -494,7 +503,7 @@ __global__ void __launch_bounds__(512, 1) k_drain_sweep(const hc_view c, hc_dev*
       if (gtid == 0) atomicExch(&g->err, 2u);
       break;
     }
-    if (!grid_barrier(g, nblocks)) break;
+    if (!grid_barrier(g, expect, bar_limit)) break;
   }
   if (gtid == 0) {
     d->drain_done = (unsigned)done;

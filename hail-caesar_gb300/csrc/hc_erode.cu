@@ -63,7 +63,9 @@ __global__ void k_erode_begin(const hc_view c, hc_dev* d, int gated, double mult
 // entrainment pass
 // ---------------------------------------------------------------------------
 // Two kernels.  k_entrain_tau, one thread per cell, clears the pass's
-// outputs, makes the records of cells that ask for one, sums the squared
+// outputs (the 40 outgoing-flux entries only where the last transport wrote
+// some, sdirty: clearing zeros was 320 B of writes per masked cell and
+// pass), makes the records of cells that ask for one, sums the squared
 // velocities and slopes, and lists the cells with flow (qtot > 0; one
 // atomic per warp).  k_entrain computes the shear stress and the transport
 // of the listed cells only, so its warps are full: in a storm, a third or
@@ -84,11 +86,14 @@ __global__ void __launch_bounds__(128) k_entrain_tau(const hc_view c, hc_dev* d)
     if (c.mask[cell]) {
       c.vel[cell] = 0;
       c.tau[cell] = 0;
-      for (int n = 0; n < HC_G; n++) {
-        SF(c, 0, n, cell) = 0;
-        SF(c, 1, n, cell) = 0;
-        SF(c, 2, n, cell) = 0;
-        SF(c, 3, n, cell) = 0;
+      if (c.sdirty[cell]) {
+        for (int n = 0; n < HC_G; n++) {
+          SF(c, 0, n, cell) = 0;
+          SF(c, 1, n, cell) = 0;
+          SF(c, 2, n, cell) = 0;
+          SF(c, 3, n, cell) = 0;
+        }
+        c.sdirty[cell] = 0;
       }
       c.ss[cell] = 0;
       const double h = c.h[cell];
@@ -248,6 +253,7 @@ __device__ double entrain_cell(const hc_view& c, hc_dev* d, size_t cell, double 
   // vegetation terms (:4459-4488) vanish: vegetation is not supported
   // (hc_create rejects vegetation_on) and veg stays zero.
   if (dgt0(temptot1)) {
+    c.sdirty[cell] = 1;  // the next pass clears this cell's flux entries
     for (int k = 0; k < 4; k++) {
       const int pp = 1 + 2 * k;
       const int x2 = ix + kDXc[pp], y2 = jy + kDYc[pp];

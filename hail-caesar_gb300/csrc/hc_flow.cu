@@ -138,7 +138,9 @@ __global__ void k_control(const hc_view c, hc_dev* d, hc_iter_handles hh) {
       double prop = (((row + 1) * rdt) - s.cycle) / rdt;
       double input = i1 + ((i2 - i1) * (1 - prop));
       s.waterinput += (input / div);
-      c.h[cell] += (input / div) / (DX * DX) * fdt;
+      const double add = (input / div) / (DX * DX) * fdt;
+      c.h[cell] += add;
+      if (x >= 1 && x <= c.imax && y >= 1 && y <= c.jmax) d->vin_step += add;
     }
   }
 
@@ -168,6 +170,9 @@ __global__ void k_control(const hc_view c, hc_dev* d, hc_iter_handles hh) {
     for (int z = 0; z <= rf; z++) s.waterinput += c.runoff_count[z] * (s.j_mean[z] * DX * DX);
     for (int z = 0; z <= rf; z++)
       s.waterinput += c.runoff_count[z] * ((d->input_amt[z] / fdt2) * DX * DX);
+    // ledger: k_runoff_inputs adds input_amt[z] to each computed cell of state z
+    for (int z = 0; z <= rf; z++)
+      if (c.runoff_count[z] > 0) d->vin_step += c.runoff_count[z] * d->input_amt[z];
     d->input_dt = fdt2;
     // new_jmeanmax (:3575-3586), over the states that hold a computed cell
     double jmm = 0;
@@ -266,16 +271,24 @@ __global__ void k_control(const hc_view c, hc_dev* d, hc_iter_handles hh) {
 }
 
 // catchment input points (:3463-3477): one thread per point
+// The ledger counts what lands on the grid (rows 1..imax, columns 1..jmax):
+// with no point found the reference still visits one (totalinputpoints
+// forced to 1, :3765), whose coordinates may be stale or the padding corner.
 __global__ void k_inputs(const hc_view c, hc_dev* d) {
   if (!d->it_active) return;
   const hc_scalars& s = d->s;
   const int total = (int)s.totalinputpoints;
+  double added = 0;
   for (int z = 1 + blockIdx.x * blockDim.x + threadIdx.x; z <= total;
        z += gridDim.x * blockDim.x) {
     const int i = c.cin_x[z], j = c.cin_y[z];
     const size_t cell = (size_t)i * c.W + j;
-    c.h[cell] += d->input_amt[c.rfarea[cell]];
+    const double a = d->input_amt[c.rfarea[cell]];
+    c.h[cell] += a;
+    if (i >= 1 && i <= c.imax && j >= 1 && j <= c.jmax) added += a;
   }
+  double tot;
+  if (grid_sum(added, c.vpart, &d->sum_done, &tot)) d->vin_step += tot;
 }
 
 // Distributed runoff (:3560-3573): every computed cell (rows 1 .. imax-1,
@@ -533,8 +546,23 @@ __global__ void __launch_bounds__(256) k_depth_update(const hc_view c, hc_dev* d
   // order like the values; tests run on the integer pipe (dgt0 etc.)
   long long m = 0;
   bool nonfinite = false;
+  double lost = 0;  // water zeroed at no-data cells (the ledger's `lost`)
+  // The ledger's mask-edge term: a face between a listed cell and one
+  // outside the wet list changes only the listed cell's depth (the other is
+  // not updated), so the water crossing it appears or vanishes.  The same
+  // expression as the update, over those faces only.
+  double edge = 0;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nw; k += gridDim.x * blockDim.x) {
     const size_t cell = (size_t)c.wet[k];
+    {
+      const uint8_t mu = c.mask[cell - W], md = c.mask[cell + W], ml = c.mask[cell - 1],
+                    mr = c.mask[cell + 1];
+      if (!(mu & md & ml & mr)) {
+        const double ux1 = md ? 0.0 : c.qx[cell + W], ux0 = mu ? 0.0 : c.qx[cell];
+        const double uy1 = mr ? 0.0 : c.qy[cell + 1], uy0 = ml ? 0.0 : c.qy[cell];
+        edge += ddiv_by(dt * (ux1 - ux0 + uy1 - uy0), c.dxd);
+      }
+    }
     double h = c.h[cell];
     h += ddiv_by(dt * (c.qx[cell + W] - c.qx[cell] + c.qy[cell + 1] - c.qy[cell]), c.dxd);
     // hydro-only runs keep Vsusptot at zero (no sediment source exists)
@@ -543,15 +571,23 @@ __global__ void __launch_bounds__(256) k_depth_update(const hc_view c, hc_dev* d
                             c.dxd);
     nonfinite |= disnan(h);
     if (dgt0(h)) {
-      if (dbits(c.elev[cell]) == kNoDataBits) h = 0;
-      else m = max(m, dbits(h));
+      if (dbits(c.elev[cell]) == kNoDataBits) {
+        lost += h;
+        h = 0;
+      } else {
+        m = max(m, dbits(h));
+      }
     }
     c.h[cell] = h;
   }
+  // no flux enters a no-data cell, so this is empty in practice (its order
+  // of addition is not fixed)
+  if (!deq0(lost)) atomicAdd(&d->vlost_step, lost);
   if (nonfinite) {
     d->err_code = 301;  // a NaN water depth: the run cannot continue
     atomicOr((unsigned int*)&d->pause, HC_PAUSE_ERROR);
   }
+  const double esum = block_sum(edge);
   for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
   const int t = threadIdx.x;
   if ((t & 31) == 0) warp_max[t >> 5] = m;
@@ -560,35 +596,50 @@ __global__ void __launch_bounds__(256) k_depth_update(const hc_view c, hc_dev* d
     long long b = 0;
     for (int w = 0; w < (int)blockDim.x / 32; w++) b = max(b, warp_max[w]);
     if (b > 0) atomicMax(&d->maxdepth_bits, (unsigned long long)b);
+    c.vpart[blockIdx.x] = esum;
     __threadfence();
     last = (atomicAdd(&d->depth_done, 1u) == gridDim.x - 1);
   }
   __syncthreads();
-  if (last && t == 0) {
+  if (last) {
     __threadfence();
-    unsigned long long bits = atomicExch(&d->maxdepth_bits, 0ull);
-    d->s.maxdepth = __longlong_as_double((long long)bits);
-    d->maxdepth_step = d->s.maxdepth;
-    d->depth_done = 0;
+    // the blocks' mask-edge sums, added in block order
+    double a = 0;
+    for (int k = t; k < (int)gridDim.x; k += blockDim.x) a += ((volatile double*)c.vpart)[k];
+    const double etot = block_sum(a);
+    if (t == 0) {
+      unsigned long long bits = atomicExch(&d->maxdepth_bits, 0ull);
+      d->s.maxdepth = __longlong_as_double((long long)bits);
+      d->maxdepth_step = d->s.maxdepth;
+      d->vmask_step += etot;
+      d->depth_done = 0;
+    }
   }
 }
 
 // ---------------------------------------------------------------------------
 // scan_area :3821-3849 (every scan_area_interval_iter iterations)
 // ---------------------------------------------------------------------------
+// Also the ledger's volume: the depth sum of its block (rows 1..imax,
+// columns 1..jmax) into vpart, added up in order by k_wet_scan.
 __global__ void __launch_bounds__(256) k_scan_area(const hc_view c, const hc_dev* __restrict__ d,
                                                     int gated) {
   if (gated && !(d->it_active && d->do_scan)) return;
   const int j = 1 + blockIdx.x * blockDim.x + threadIdx.x;
   const int i = 1 + blockIdx.y * blockDim.y + threadIdx.y;
-  if (i > c.imax || j > c.jmax) return;
-  const size_t W = c.W;
-  const size_t cell = (size_t)i * W + j;
-  const double* h = c.h;
-  bool wet = h[cell] > 0 || h[cell - 1] > 0 || h[cell + 1] > 0 || h[cell - W] > 0 ||
-             h[cell - W - 1] > 0 || h[cell - W + 1] > 0 || h[cell + W - 1] > 0 ||
-             h[cell + W + 1] > 0 || h[cell + W] > 0;
-  c.mask[cell] = wet ? 1 : 0;
+  double v = 0;
+  if (i <= c.imax && j <= c.jmax) {
+    const size_t W = c.W;
+    const size_t cell = (size_t)i * W + j;
+    const double* h = c.h;
+    v = h[cell];
+    bool wet = v > 0 || h[cell - 1] > 0 || h[cell + 1] > 0 || h[cell - W] > 0 ||
+               h[cell - W - 1] > 0 || h[cell - W + 1] > 0 || h[cell + W - 1] > 0 ||
+               h[cell + W + 1] > 0 || h[cell + W] > 0;
+    c.mask[cell] = wet ? 1 : 0;
+  }
+  const double bsum = block_sum(v);
+  if (threadIdx.x == 0 && threadIdx.y == 0) c.vpart[blockIdx.x + blockIdx.y * gridDim.x] = bsum;
 }
 
 // The wet list: mask bytes counted per block of 1024 cells, the counts
@@ -608,11 +659,22 @@ __global__ void __launch_bounds__(1024) k_wet_count(const hc_view c, const hc_de
   }
 }
 
+// nvol: blocks of the k_scan_area launch before it, whose volume partials it
+// adds up (0: none, the list is rebuilt from a mask kept as it was)
 __global__ void __launch_bounds__(1024) k_wet_scan(const hc_view c, hc_dev* d, int nblocks,
-                                                   int gated) {
+                                                   int gated, int nvol) {
   __shared__ int buf[1024];
   __shared__ int carry;
   if (gated && !(d->it_active && d->do_scan)) return;
+  if (nvol > 0) {
+    double a = 0;
+    for (int k = threadIdx.x; k < nvol; k += blockDim.x) a += c.vpart[k];
+    const double tot = block_sum(a);
+    if (threadIdx.x == 0) {
+      d->vol_scan = tot;
+      d->vol_scan_counter = d->s.counter;
+    }
+  }
   if (threadIdx.x == 0) carry = 0;
   __syncthreads();
   for (int base = 0; base < nblocks; base += 1024) {
@@ -667,13 +729,14 @@ __global__ void __launch_bounds__(1024) k_wet_write(const hc_view c, const hc_de
 __global__ void __launch_bounds__(1024) k_flux_out(const hc_view c, hc_dev* d, int gated, int record,
                                                     hc_step_record* rec, int64_t rec_cap) {
   __shared__ double part[1024];
+  __shared__ double vpart[1024];
   if (gated && !(d->it_active && d->rest_active)) return;
   const hc_params& p = c.p;
   const int imax = c.imax, jmax = c.jmax;
   const double thr = p.water_depth_erosion_threshold, DX = p.DX;
   const double fdt = d->s.time_step;
   const int n1 = 2 * imax, n2 = n1 + 2 * jmax;
-  double acc = 0;
+  double acc = 0, vacc = 0;  // the outflow rate, and the depth taken off
   for (int k = threadIdx.x; k < n2; k += blockDim.x) {
     int i, j;
     if (k < n1) {
@@ -698,13 +761,18 @@ __global__ void __launch_bounds__(1024) k_flux_out(const hc_view c, hc_dev* d, i
     double& h = c.h[(size_t)i * c.W + j];
     if (h > thr) {
       acc += (h - thr) * DX * DX / fdt;
+      vacc += h - thr;
       h = thr;
     }
   }
   part[threadIdx.x] = acc;
+  vpart[threadIdx.x] = vacc;
   __syncthreads();
   for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-    if ((int)threadIdx.x < w) part[threadIdx.x] += part[threadIdx.x + w];
+    if ((int)threadIdx.x < w) {
+      part[threadIdx.x] += part[threadIdx.x + w];
+      vpart[threadIdx.x] += vpart[threadIdx.x + w];
+    }
     __syncthreads();
   }
   if (threadIdx.x == 0) {
@@ -723,8 +791,22 @@ __global__ void __launch_bounds__(1024) k_flux_out(const hc_view c, hc_dev* d, i
       r.sediQ = s.sediQ;
       r.globalsediq = s.globalsediq;
       r.baseflow = s.baseflow;
+      const double a2 = DX * DX;
+      r.vol_in = d->vin_step * a2;
+      r.vol_out = (vpart[0] + d->vlost_step) * a2;
+      r.vol_mask = d->vmask_step * a2;
+      r.volume = (d->vol_scan_counter == s.counter) ? d->vol_scan * a2 : __longlong_as_double(0x7ff8000000000000LL);
     }
     if (record) d->rec_index++;
+    if (gated) d->wet_steps += (unsigned long long)d->wet_count;
+    // the ledger: this iteration's terms join the totals
+    d->vin_tot += d->vin_step;
+    d->vout_tot += vpart[0];
+    d->vlost_tot += d->vlost_step;
+    d->vmask_tot += d->vmask_step;
+    d->vin_step = 0;
+    d->vlost_step = 0;
+    d->vmask_step = 0;
     if (gated) {
       if (!p.hydro_only && !(d->flags & HC_RUN_NOHILL) &&
           (s.cycle > s.creep_time || s.cycle > s.creep_time2))
@@ -732,6 +814,26 @@ __global__ void __launch_bounds__(1024) k_flux_out(const hc_view c, hc_dev* d, i
       if (!(s.cycle / 60 < p.maxcycle)) d->pause |= HC_PAUSE_FINISHED;
     }
   }
+}
+
+// The depth sum of the grid (rows 1..imax, columns 1..jmax) now, in a fixed
+// order (hc_mass_balance; the ledger's start).
+__global__ void __launch_bounds__(256) k_volume(const hc_view c, hc_dev* d) {
+  const size_t n = (size_t)c.imax * c.jmax;
+  double a = 0;
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+       k += (size_t)gridDim.x * blockDim.x) {
+    const size_t i = 1 + k / c.jmax, j = 1 + k % c.jmax;
+    a += c.h[i * c.W + j];
+  }
+  double tot;
+  if (grid_sum(a, c.vpart, &d->sum_done, &tot)) d->vol_now = tot;
+}
+
+__global__ void k_mass_reset(hc_dev* d) {
+  d->vol0 = d->vol_now;
+  d->vin_tot = d->vout_tot = d->vlost_tot = d->vmask_tot = 0;
+  d->vin_step = d->vlost_step = d->vmask_step = 0;
 }
 
 }  // namespace
@@ -755,7 +857,7 @@ void launch_inputs(hc_ctx* c) {
   }
   // grid-stride over the current list (its length lives on the device)
   int n = c->v.cin_cap;
-  int blocks = std::min((n + 255) / 256, 152 * 4);
+  int blocks = std::min((n + 255) / 256, std::min(152 * 4, c->v.vpart_cap));
   if (blocks < 1) blocks = 1;
   k_inputs<<<blocks, 256, 0, c->cs>>>(c->v, c->dev);
   count_launch(c, 1);
@@ -786,22 +888,45 @@ void launch_depth_update(hc_ctx* c, int gated) {
   count_launch(c, 1);
 }
 
+static void wet_list(hc_ctx* c, int gated, int nvol);
+
 void launch_scan_area(hc_ctx* c, int gated) {
   dim3 b(32, 8);
-  k_scan_area<<<grid2d(c, b), b, 0, c->cs>>>(c->v, c->dev, gated);
+  const dim3 g = grid2d(c, b);
+  k_scan_area<<<g, b, 0, c->cs>>>(c->v, c->dev, gated);
   count_launch(c, 1);
-  launch_wet_list(c, gated);
+  wet_list(c, gated, (int)(g.x * g.y));
 }
 
-void launch_wet_list(hc_ctx* c, int gated) {
+void launch_wet_list(hc_ctx* c, int gated) { wet_list(c, gated, 0); }
+
+static void wet_list(hc_ctx* c, int gated, int nvol) {
   const int nb = (int)((c->v.N2 + 1023) / 1024);
   k_wet_count<<<nb, 1024, 0, c->cs>>>(c->v, c->dev, gated);
-  k_wet_scan<<<1, 1024, 0, c->cs>>>(c->v, c->dev, nb, gated);
+  k_wet_scan<<<1, 1024, 0, c->cs>>>(c->v, c->dev, nb, gated, nvol);
   k_wet_write<<<nb, 1024, 0, c->cs>>>(c->v, c->dev, gated);
   count_launch(c, 3);
 }
 
 void launch_flux_out(hc_ctx* c, int gated, int record) {
   k_flux_out<<<1, 1024, 0, c->cs>>>(c->v, c->dev, gated, record, c->v.rec, c->v.rec_cap);
+  count_launch(c, 1);
+}
+
+// grid of the grid_sum kernels: at most the SMs x 4 blocks of 256 (the
+// partials array holds vpart_cap entries)
+static int sum_blocks(const hc_ctx* c, size_t n) {
+  const size_t need = (n + 255) / 256;
+  return (int)std::max<size_t>(1, std::min<size_t>(need, (size_t)std::min(152 * 4, c->v.vpart_cap)));
+}
+
+void launch_volume(hc_ctx* c) {
+  k_volume<<<sum_blocks(c, (size_t)c->v.imax * c->v.jmax), 256, 0, c->cs>>>(c->v, c->dev);
+  count_launch(c, 1);
+}
+
+void launch_mass_reset(hc_ctx* c) {
+  launch_volume(c);
+  k_mass_reset<<<1, 1, 0, c->cs>>>(c->dev);
   count_launch(c, 1);
 }

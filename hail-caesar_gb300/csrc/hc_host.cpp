@@ -226,46 +226,6 @@ void host_topmodel_table(const hc_params* p, const float* rain, int rows, int co
   }
 }
 
-// global_landsliding :5529-5654.  A serial relaxation over the whole grid
-// (x outer, y inner; every test sees the moves before it; up to 200 sweeps
-// until nothing moves).  It changes elevations only and runs once a
-// simulated day, so it runs here on the host, in the reference's order,
-// on a downloaded copy of elev.  Returns the number of sweeps.
-int host_global_landsliding(const hc_params* p, const double* bedrock, double* elev) {
-  const unsigned imax = p->imax, jmax = p->jmax;
-  const size_t W = jmax + 2;
-  const double factor = std::tan((p->failureangle * (3.141592654 / 180))) * p->DX;
-  const double active = p->active, EF = p->ERODEFACTOR;
-  static const int ox[8] = {1, 0, -1, -1, -1, 0, 1, 1};
-  static const int oy[8] = {1, 1, 1, 0, -1, -1, -1, 0};
-  unsigned inc = 0;
-  double total = 0;
-  do {
-    total = 0;
-    inc++;
-    for (unsigned x = 2; x < imax; x++)
-      for (unsigned y = 2; y < jmax; y++) {
-        const size_t c = (size_t)x * W + y;
-        double wet_factor = factor;
-        if (elev[c] <= (bedrock[c] + active)) wet_factor = 10 * p->DX;
-        for (int k = 0; k < 8; k++) {
-          const size_t nb = (size_t)(x + ox[k]) * W + (y + oy[k]);
-          const bool diag = (ox[k] != 0 && oy[k] != 0);
-          const double drop = diag ? ((elev[c] - elev[nb]) / 1.41) : (elev[c] - elev[nb]);
-          if (drop > wet_factor && elev[nb] > -9999) {
-            double diff = (diag ? ((elev[c] - elev[nb]) / 1.41) : (elev[c] - elev[nb])) - wet_factor;
-            if ((elev[c] - diff) < (bedrock[c] + active)) diff = (elev[c] - (bedrock[c] + active));
-            if (diff > EF) diff = EF;
-            elev[c] -= diff;
-            elev[nb] += diff;
-            total += diff;
-          }
-        }
-      }
-  } while (total > 0 && inc < 200);
-  return (int)inc;
-}
-
 // Derivatives of the TOPMODEL table (host_topmodel_table) with respect to the
 // rain table, by forward-mode differentiation of the same recurrence: for
 // table rows t < nsteps, zone n (1..rfnum) and rain row k < rows,

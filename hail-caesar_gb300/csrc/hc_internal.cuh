@@ -91,6 +91,17 @@ struct hc_dev {
   unsigned int xresume, yresume;  // long chains handed from the thread to the warp walkers
   unsigned int xtake, ytake;      // chains taken so far by the thread walkers
   unsigned int ent_n;     // cells listed for the transport of an entrainment pass
+  // water ledger, as sums of water depth (m; times DX^2 gives m^3)
+  double vin_step;        // added by the inputs since the last water_flux_out
+  double vlost_step;      // zeroed by depth_update at no-data cells, likewise
+  double vmask_step;      // crossed faces between a listed and an unlisted cell, likewise
+  double vin_tot, vout_tot, vlost_tot, vmask_tot;  // since the ledger started
+  double vol0;            // depth sum of the grid when the ledger started
+  double vol_scan;        // depth sum of the grid at the last scan_area
+  double vol_scan_counter;  // the iteration (counter) of that scan_area
+  double vol_now;         // depth sum of the grid, written by k_volume
+  unsigned int sum_done;  // blocks finished in a grid_sum (left at zero)
+  unsigned long long wet_steps;  // wet-list length summed over the iterations run
 };
 
 // Working state of a drainage recomputation (hc_drain.cu): the radix
@@ -127,6 +138,7 @@ struct hc_view {
   double *elev, *h, *qx, *qy, *qxs, *qys, *vs, *vel, *tau, *bed, *man, *area, *ss;
   double *vd;        // 4 * N2
   double *sflux;     // 4 dirs * 10 fractions * N2 ; dir order su, sr, sd, sl
+  uint8_t *sdirty;   // N2: 1 where the cell's sflux entries may be nonzero
   double *grain;     // 11 * N2
   double *strata;    // 10 * 9 * N2
   int32_t *index;
@@ -180,7 +192,13 @@ struct hc_view {
   uint8_t *touched;              // N2 bytes
   double *red;                   // reduction scratch
   int32_t *scan_tmp;             // scan scratch
+  double *vpart; int vpart_cap;  // per-block partial sums (grid_sum, scan_area's volume)
   hc_step_record *rec; int64_t rec_cap;
+  // test hook of the bounded device waits (hc_test_bounded_waits): when
+  // wait_spins > 0 the drainage sweep's waits give up after that many spins,
+  // and its grid barrier expects barrier_extra arrivals more than there are
+  // blocks (with no single-block frontiers), so that every wait runs out
+  int wait_spins, barrier_extra;
 };
 
 // Conditional-node handles of one captured iteration (CUDA graph IF nodes):
@@ -212,6 +230,7 @@ struct hc_ctx {
   void* drainage_cache;    // sweep order of the drainage area, reused while elev is unchanged
   struct hc_sort_work* sort_work;  // device sort of the elevations (hc_sort.cu)
   bool area_valid;         // device area matches the cached sweep order
+  bool drain_retry;        // a drainage recomputation gave up: redo it first
   // called after every recomputation of the input points (adjoint replays)
   void (*points_hook)(hc_ctx*, void*);
   void* points_hook_arg;
@@ -240,6 +259,54 @@ inline void count_launch(hc_ctx* c, int n) {
 
 // ---------------------------------------------------------------- helpers
 #define HC_DEV __device__ __forceinline__
+
+// Sum of one double per thread over the block, in a fixed order (warp
+// shuffles, then the warps in order); the result is valid in thread 0.
+// Every thread of the block calls it; blockDim a multiple of 32, <= 1024.
+__device__ __forceinline__ double block_sum(double v) {
+  __shared__ double ws[32];
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int t = threadIdx.x + threadIdx.y * blockDim.x;
+  const int nw = (blockDim.x * blockDim.y) >> 5;
+  __syncthreads();  // ws may still be read by a previous call
+  if ((t & 31) == 0) ws[t >> 5] = v;
+  __syncthreads();
+  double s = 0;
+  if (t == 0)
+    for (int w = 0; w < nw; w++) s += ws[w];
+  return s;
+}
+
+// Deterministic grid-wide sum: each block stores its block_sum in part[b];
+// the last block to finish adds part[0..blocks) in a fixed order (thread t
+// takes t, t+bs, ...; then block_sum) and returns true in its thread 0 with
+// the total in *out.  *done is left at zero.  Every thread of every block
+// calls it.
+__device__ __forceinline__ bool grid_sum(double v, double* part, unsigned int* done,
+                                         double* out) {
+  __shared__ bool last;
+  const int t = threadIdx.x + threadIdx.y * blockDim.x;
+  const int bs = blockDim.x * blockDim.y;
+  const unsigned nb = gridDim.x * gridDim.y;
+  const unsigned b = blockIdx.x + blockIdx.y * gridDim.x;
+  const double s = block_sum(v);
+  if (t == 0) {
+    part[b] = s;
+    __threadfence();
+    last = (atomicAdd(done, 1u) == nb - 1);
+  }
+  __syncthreads();
+  if (!last) return false;
+  __threadfence();
+  double a = 0;
+  for (unsigned k = t; k < nb; k += bs) a += ((volatile double*)part)[k];
+  const double tot = block_sum(a);
+  if (t == 0) {
+    *out = tot;
+    *done = 0;
+  }
+  return t == 0;
+}
 
 // std::max(a, b) as libstdc++ defines it: (a < b) ? b : a
 HC_DEV double smax(double a, double b) { return (a < b) ? b : a; }
@@ -593,6 +660,8 @@ void launch_depth_update(hc_ctx* c, int gated);
 void launch_scan_area(hc_ctx* c, int gated);
 void launch_wet_list(hc_ctx* c, int gated);  // rebuild the wet-cell list from the mask
 void launch_flux_out(hc_ctx* c, int gated, int record);
+void launch_volume(hc_ctx* c);           // hc_dev::vol_now = depth sum of the grid
+void launch_mass_reset(hc_ctx* c);       // the ledger starts again from vol_now
 void launch_erode_begin(hc_ctx* c, int gated, double mult);
 // next: the conditional handle of the following pass (set when retrying);
 // has_next 0 outside graph capture
@@ -603,9 +672,9 @@ void launch_lateral_check(hc_ctx* c);
 size_t erode_scratch_bytes(size_t N2, int imax, int jmax);
 void launch_slide3(hc_ctx* c, int gated);
 hc_status run_lateral(hc_ctx* c);
-hc_status run_global_landsliding(hc_ctx* c);
+hc_status run_global_landsliding(hc_ctx* c, int* sweeps);
 hc_status run_creep(hc_ctx* c, double time);
-size_t slide_scratch_bytes(size_t N2, int imax);
+size_t slide_scratch_bytes(size_t N2, int n);  // n = max(imax, jmax)
 
 // host helpers (hc_host.cpp)
 // the drainage sweep order (std::sort's permutation, exact); cached while
@@ -634,7 +703,6 @@ hc_status hc_fail(hc_ctx* c, hc_status st, const char* fmt, ...);
 hc_status hc_cuda(hc_ctx* c, cudaError_t e, const char* what);
 void* host_drainage_cache_new();
 void host_drainage_cache_free(void* p);
-int host_global_landsliding(const hc_params* p, const double* bedrock, double* elev);
 void host_topmodel_tangent(const hc_params* p, const float* rain, int rows, int cols, int nsteps,
                            double* d_old, double* d_new);
 void host_topmodel_table(const hc_params* p, const float* rain, int rows, int cols,

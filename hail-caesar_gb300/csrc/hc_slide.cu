@@ -1,7 +1,7 @@
 // Slope failure and creep:
 //   in_channel_landsliding :5429-5527 ("slide_3", every 10 iterations)
-//   global_landsliding     :5529-5654 (daily; its serial sweep runs on a host
-//                          core, hc_host.cpp)
+//   global_landsliding     :5529-5654 (daily: the same probe and warp replay
+//                          over every cell, sweep after sweep)
 //   creep                  :5293-5427 (host-driven, every 10 days)
 //
 // slide_3 is a sequential relaxation: every test sees the elevations left by
@@ -424,6 +424,218 @@ __global__ void __launch_bounds__(32) k_slide_replay(const hc_view c, hc_dev* d,
   if (lane == 0) d->s.grain_array_tot = d->grain_tot;
 }
 
+// ---- global_landsliding :5529-5654 ----------------------------------------
+// The daily sweep visits every cell of rows 2..imax-1, columns 2..jmax-1,
+// rows outer (cell order, so a loop position is the cell index), with the
+// same eight tests in the same order as slide_3 but on elevations only
+// (no grain records), the wet factor 10*DX below bedrock + active, and every
+// move capped at ERODEFACTOR.  Sweeps repeat while the last one moved a
+// positive total (at most 200).  As for slide_3: a parallel probe of every
+// cell against the elevations at the start of the sweep, then one warp
+// replays the sweep over the flagged cells and the later cells whose 3x3
+// block a move changed.
+
+struct GOrder {
+  int W;  // jmax + 2
+  __device__ __forceinline__ int pos(int x, int y) const { return x * W + y; }
+  __device__ __forceinline__ void cell(int P, int& x, int& y) const {
+    x = P / W;
+    y = P - x * W;
+  }
+};
+
+__device__ bool gslide_probe_cell(const hc_view& c, int x, int y, double factor) {
+  constexpr int dxs[8] = {1, 0, -1, -1, -1, 0, 1, 1};
+  constexpr int dys[8] = {1, 1, 1, 0, -1, -1, -1, 0};
+  const size_t W = c.W;
+  const size_t cell = (size_t)x * W + y;
+  double en[8];
+#pragma unroll
+  for (int k = 0; k < 8; k++) en[k] = c.elev[(size_t)(x + dxs[k]) * W + (y + dys[k])];
+  const double e = c.elev[cell];
+  const double wet_factor = (e <= (c.bed[cell] + c.p.active)) ? 10 * c.p.DX : factor;
+  const float fe = approx_f(e), fw = approx_f(wet_factor);
+  int undecided = 0;
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    const int r = drop_above_est(fe, approx_f(en[k]), fw, dxs[k] != 0 && dys[k] != 0);
+    if (r == 1 && dkey(en[k]) > kNoDataKey) return true;
+    if (r == 2) undecided |= 1 << k;
+  }
+  if (!undecided) return false;
+#pragma unroll
+  for (int k = 0; k < 8; k++)
+    if (((undecided >> k) & 1) && drop_above_exact(e, en[k], wet_factor, dxs[k] != 0 && dys[k] != 0))
+      return true;
+  return false;
+}
+
+// The visit (:5553-5630): the eight tests in order on the elevations held
+// in registers, each move as the reference makes it; returns the moved
+// directions and adds the moves to *total in order.
+__device__ int gslide_visit(const hc_view& c, int x, int y, double factor, double* total) {
+  constexpr int dxs[8] = {1, 0, -1, -1, -1, 0, 1, 1};
+  constexpr int dys[8] = {1, 1, 1, 0, -1, -1, -1, 0};
+  const size_t W = c.W;
+  const size_t cell = (size_t)x * W + y;
+  double en[8];
+#pragma unroll
+  for (int k = 0; k < 8; k++) en[k] = c.elev[(size_t)(x + dxs[k]) * W + (y + dys[k])];
+  double e = c.elev[cell];
+  const double bed = c.bed[cell], active = c.p.active, EF = c.p.ERODEFACTOR;
+  double wet_factor = factor;
+  if (e <= (bed + active)) wet_factor = 10 * c.p.DX;
+  const float fw = approx_f(wet_factor);
+  int moved = 0;
+  for (int k = 0; k < 8; k++) {
+    const bool diag = dxs[k] != 0 && dys[k] != 0;
+    const double e2 = en[k];
+    if (drop_above_est(approx_f(e), approx_f(e2), fw, diag) == 0) continue;
+    const double drop = diag ? ((e - e2) / 1.41) : (e - e2);
+    if (!(drop > wet_factor && e2 > -9999)) continue;
+    double diff = drop - wet_factor;
+    if ((e - diff) < (bed + active)) diff = (e - (bed + active));
+    if (diff > EF) diff = EF;
+    e -= diff;
+    en[k] = e2 + diff;
+    c.elev[cell] = e;
+    c.elev[(size_t)(x + dxs[k]) * W + (y + dys[k])] = en[k];
+    *total += diff;
+    moved |= 1 << k;
+  }
+  return moved;
+}
+
+__global__ void k_gslide_probe(const hc_view c, uint8_t* flag, double factor) {
+  const int y = 1 + blockIdx.x * blockDim.x + threadIdx.x;
+  const int x = 1 + blockIdx.y * blockDim.y + threadIdx.y;
+  if (x > c.imax || y > c.jmax) return;
+  uint8_t f = 0;
+  if (x >= 2 && x <= c.imax - 1 && y >= 2 && y <= c.jmax - 1)
+    f = gslide_probe_cell(c, x, y, factor) ? 1 : 0;
+  flag[(size_t)x * c.W + y] = f;
+}
+
+// The later positions whose visit reads a cell the visit at (x, y) changed
+// (the cell and each moved-to neighbour): every cell of the loop within one
+// of a changed cell.  All lie within 2*W + 2 positions of (x, y).
+__device__ int gpush_affected(const hc_view& c, const GOrder& o, int x, int y, int moved, int Pcur,
+                              uint32_t* ring, int RW) {
+  constexpr int dxs[8] = {1, 0, -1, -1, -1, 0, 1, 1};
+  constexpr int dys[8] = {1, 1, 1, 0, -1, -1, -1, 0};
+  unsigned need = 0;
+#pragma unroll
+  for (int k = -1; k < 8; k++) {
+    if (k >= 0 && !((moved >> k) & 1)) continue;
+    const int cx = (k < 0) ? 0 : dxs[k], cy = (k < 0) ? 0 : dys[k];
+#pragma unroll
+    for (int dx = -1; dx <= 1; dx++)
+#pragma unroll
+      for (int dy = -1; dy <= 1; dy++) need |= 1u << ((cx + dx + 2) * 5 + (cy + dy + 2));
+  }
+  int added = 0;
+  for (int b = 0; b < 25; b++) {
+    const int xx = x + b / 5 - 2, yy = y + b % 5 - 2;
+    if (!((need >> b) & 1u) || xx < 2 || xx > c.imax - 1 || yy < 2 || yy > c.jmax - 1) continue;
+    const int P = o.pos(xx, yy);
+    if (P <= Pcur) continue;
+    uint32_t& w = ring[(P >> 5) & (RW - 1)];
+    const uint32_t bit = 1u << (P & 31);
+    if (!(w & bit)) {
+      w |= bit;
+      added++;
+    }
+  }
+  return added;
+}
+
+// One sweep's replay by one warp, as k_slide_replay does it for slide_3;
+// *total receives the sweep's total (the moves' sum in the serial order).
+__global__ void __launch_bounds__(32) k_gslide_replay(const hc_view c, const int32_t* list,
+                                                      const int32_t* count, uint32_t* gring,
+                                                      double factor, double* total) {
+  __shared__ uint32_t sring[kSharedRingWords];
+  __shared__ int32_t batch[kReplayBatch];
+  const int n = *count;
+  const int lane = threadIdx.x;
+  double tot = 0;
+  if (n > 0) {
+    const GOrder o{(int)c.W};
+    const int RW = ring_words(c.jmax);
+    const int R = RW << 5;
+    uint32_t* ring = (RW <= kSharedRingWords) ? sring : gring;
+    for (int i = lane; i < RW; i += 32) ring[i] = 0;
+    __syncwarp();
+    int li = 0, last = -1, pend = 0;
+    while (true) {
+      const int L = (li < n) ? list[li] : INT_MAX;
+      int nb = 0;
+      if (pend > 0) {
+        const int s0 = last + 1;
+        const int end = (int)min((long long)L, (long long)last + R);
+        for (int base = s0 & ~31; base < end && nb < kReplayBatch; base += 1024) {
+          const int w0 = base + lane * 32;
+          uint32_t bits = 0;
+          if (w0 < end) {
+            bits = ring[(w0 >> 5) & (RW - 1)];
+            if (w0 < s0) bits &= ~0u << (s0 - w0);
+            if (end - w0 < 32) bits &= (1u << (end - w0)) - 1u;
+          }
+          const int cnt = __popc(bits);
+          int incl = cnt;
+#pragma unroll
+          for (int off = 1; off < 32; off <<= 1) {
+            const int t = __shfl_up_sync(kFull, incl, off);
+            if (lane >= off) incl += t;
+          }
+          int slot = nb + incl - cnt;
+          while (bits && slot < kReplayBatch) {
+            batch[slot++] = w0 + __ffs(bits) - 1;
+            bits &= bits - 1;
+          }
+          nb = min(kReplayBatch, nb + __shfl_sync(kFull, incl, 31));
+        }
+      }
+      const bool tookL = nb < kReplayBatch && L != INT_MAX;
+      if (tookL) {
+        if (lane == 0) batch[nb] = L;
+        nb++;
+      }
+      if (nb == 0) break;
+      __syncwarp();
+      bool mv = false;
+      if (lane < nb) {
+        int x, y;
+        o.cell(batch[lane], x, y);
+        mv = gslide_probe_cell(c, x, y, factor);
+      }
+      const unsigned ball = __ballot_sync(kFull, mv);
+      const int upto = ball ? (__ffs(ball) - 1) : nb - 1;
+      int cleared = 0;
+      if (lane <= upto) {
+        const int P = batch[lane];
+        const uint32_t bit = 1u << (P & 31);
+        cleared = (atomicAnd(&ring[(P >> 5) & (RW - 1)], ~bit) & bit) ? 1 : 0;
+      }
+      pend -= __popc(__ballot_sync(kFull, cleared));
+      if (tookL && upto == nb - 1) li++;
+      last = batch[upto];
+      if (ball) {
+        int added = 0;
+        if (lane == 0) {
+          int x, y;
+          o.cell(last, x, y);
+          const int moved = gslide_visit(c, x, y, factor, &tot);
+          if (moved) added = gpush_affected(c, o, x, y, moved, last, ring, RW);
+        }
+        pend += __shfl_sync(kFull, added, 0);
+      }
+      __syncwarp();
+    }
+  }
+  if (lane == 0) *total = tot;
+}
+
 // ---- creep :5293-5427 ------------------------------------------------------
 // temp of the move from (x,y) to neighbour k, 0 when there is none
 __device__ __forceinline__ double creep_temp(const hc_view& c, int x, int y, int k, double time) {
@@ -532,10 +744,12 @@ static SlideScratch slide_scratch(hc_ctx* c) {
   return s;
 }
 
-size_t slide_scratch_bytes(size_t N2, int imax) {
+// n: the longer side of the grid (slide_3's ring spans columns of imax+2
+// positions, global landsliding's rows of jmax+2)
+size_t slide_scratch_bytes(size_t N2, int n) {
   size_t nblocks = (N2 + 1023) / 1024;
   return ((N2 + 255) / 256) * 256 + ((N2 * 4 + 255) / 256) * 256 + ((nblocks * 4 + 255) / 256) * 256 +
-         256 + (size_t)ring_words(imax) * 4 + 256;
+         256 + (size_t)ring_words(n) * 4 + 256;
 }
 
 static void slide_sweep(hc_ctx* c, double factor, int gated) {
@@ -566,20 +780,34 @@ static double slide_factor(const hc_ctx* c) {
 
 void launch_slide3(hc_ctx* c, int gated) { slide_sweep(c, slide_factor(c), gated); }
 
-hc_status run_global_landsliding(hc_ctx* c) {
-  // a serial sweep over every cell, up to 200 times: one host core runs it
-  // far faster than one GPU thread, and it touches elevations only
-  const size_t N2 = c->v.N2;
-  std::vector<double> elev(N2), bed(N2);
-  cudaError_t e = cudaStreamSynchronize(c->s);
-  if (e == cudaSuccess) e = cudaMemcpy(elev.data(), c->v.elev, N2 * 8, cudaMemcpyDeviceToHost);
-  if (e == cudaSuccess) e = cudaMemcpy(bed.data(), c->v.bed, N2 * 8, cudaMemcpyDeviceToHost);
-  if (e != cudaSuccess) return hc_cuda(c, e, "global_landsliding");
-  c->d2h_bytes += 2 * N2 * 8;
-  host_global_landsliding(&c->v.p, bed.data(), elev.data());
-  e = cudaMemcpy(c->v.elev, elev.data(), N2 * 8, cudaMemcpyHostToDevice);
-  if (e != cudaSuccess) return hc_cuda(c, e, "global_landsliding");
-  c->h2d_bytes += N2 * 8;
+// global_landsliding :5529-5654: sweeps while the last one moved a positive
+// total, at most 200; each sweep a probe, the flagged cells' list and the
+// replay, then one 16-byte read of the sweep's count and total.
+hc_status run_global_landsliding(hc_ctx* c, int* sweeps) {
+  SlideScratch s = slide_scratch(c);
+  dim3 b(32, 8);
+  dim3 g((c->v.jmax + b.x - 1) / b.x, (c->v.imax + b.y - 1) / b.y);
+  const size_t n = c->v.N2;
+  const int nblocks = (int)((n + 1023) / 1024);
+  double* total = (double*)c->v.red;  // bytes 0-7 of the reduction scratch
+  struct { double total; int32_t count; int32_t pad; } h = {0, 0, 0};
+  int inc = 0;
+  do {
+    inc++;
+    cudaMemsetAsync(s.flag, 0, n, c->s);
+    k_gslide_probe<<<g, b, 0, c->s>>>(c->v, s.flag, slide_factor(c));
+    k_flag_count<<<nblocks, 1024, 0, c->s>>>(s.flag, n, s.block_sums, c->dev, 0);
+    k_flag_scan<<<1, 1024, 0, c->s>>>(s.block_sums, nblocks, s.count, c->dev, 0);
+    k_flag_compact<<<nblocks, 1024, 0, c->s>>>(s.flag, n, s.block_sums, s.list, c->dev, 0);
+    k_gslide_replay<<<1, 32, 0, c->s>>>(c->v, s.list, s.count, s.ring, slide_factor(c), total);
+    count_launch(c, 5);
+    cudaError_t e = cudaMemcpyAsync(&h.total, total, 8, cudaMemcpyDeviceToHost, c->s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&h.count, s.count, 4, cudaMemcpyDeviceToHost, c->s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->s);
+    if (e != cudaSuccess) return hc_cuda(c, e, "global_landsliding");
+    c->d2h_bytes += 12;
+  } while (h.total > 0 && inc < 200);
+  if (sweeps) *sweeps = inc;
   return HC_OK;
 }
 

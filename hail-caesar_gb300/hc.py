@@ -13,8 +13,8 @@ import os
 
 import numpy as np
 
-from hc_abi import (hc_params, hc_scalars, hc_step_record, FIELD_ID, STATUS, STEP_FIELDS,
-                    field_shape, field_dtype)
+from hc_abi import (hc_params, hc_scalars, hc_step_record, hc_mass, FIELD_ID, STATUS,
+                    STEP_FIELDS, field_shape, field_dtype)
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libhc_gpu.so")
@@ -57,6 +57,8 @@ def load_library(path=LIB_PATH):
         "hc_erode": (C.c_int, [vp, C.c_double, P(C.c_double)]),
         "hc_lateral_channel_erode": (C.c_int, [vp]),
         "hc_in_channel_landsliding": (C.c_int, [vp]),
+        "hc_global_landsliding": (C.c_int, [vp, P(C.c_int32)]),
+        "hc_creep": (C.c_int, [vp, C.c_double]),
         "hc_run": (C.c_int, [vp, C.c_int64, C.c_int32, vp, P(C.c_int64)]),
         "hc_stream": (vp, [vp]),
         "hc_run_ensemble": (C.c_int, [P(vp), C.c_int32, C.c_int64, C.c_int32, P(C.c_int64)]),
@@ -67,9 +69,12 @@ def load_library(path=LIB_PATH):
         "hc_snapshot_end": (C.c_int, [vp]),
         "hc_adj_forward": (C.c_int, [vp, C.c_int64, vp, vp, vp, C.c_int64, P(C.c_int64)]),
         "hc_adj_gradient": (C.c_int, [vp, C.c_int64, C.c_int32, vp, C.c_int64, P(C.c_double),
-                                      vp, vp, vp]),
+                                      vp, vp, vp, vp]),
         "hc_profile_iteration": (C.c_int, [vp, C.c_int32, P(C.c_double)]),
         "hc_drainage_sort": (C.c_int, [vp, C.c_uint64, vp, P(C.c_int32)]),
+        "hc_mass_balance": (C.c_int, [vp, P(hc_mass)]),
+        "hc_mass_reset": (C.c_int, [vp]),
+        "hc_test_bounded_waits": (C.c_int, [vp, C.c_int32, C.c_int32]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -191,10 +196,19 @@ class Model:
     def in_channel_landsliding(self):
         self._check(self.lib.hc_in_channel_landsliding(self.h), "in_channel_landsliding")
 
+    def global_landsliding(self):
+        """Returns the number of sweeps made."""
+        n = C.c_int32()
+        self._check(self.lib.hc_global_landsliding(self.h, C.byref(n)), "global_landsliding")
+        return n.value
+
+    def creep(self, time):
+        self._check(self.lib.hc_creep(self.h, float(time)), "creep")
+
     # ---- whole iterations
     def run(self, n, flags=None, records=True):
         """Runs up to n iterations of the main loop; returns the per-iteration
-        records as an (iterations, 10) float64 array (fields STEP_FIELDS)."""
+        records as an (iterations, 14) float64 array (fields STEP_FIELDS)."""
         flags = self.case.flags if flags is None else flags
         rec = np.zeros((max(n, 1), len(STEP_FIELDS)), dtype=np.float64) if records else None
         done = C.c_int64()
@@ -204,6 +218,23 @@ class Model:
 
     def stream(self):
         return self.lib.hc_stream(self.h)
+
+    # ---- water ledger
+    def mass_balance(self):
+        """{volume0, volume, inflow, outflow, lost, mask_edge} in m^3 since
+        hc_prepare (or mass_reset); volume is measured now."""
+        m = hc_mass()
+        self._check(self.lib.hc_mass_balance(self.h, C.byref(m)), "mass_balance")
+        return {k: getattr(m, k) for k, _ in hc_mass._fields_}
+
+    def test_bounded_waits(self, spins, extra_arrivals=1):
+        """Shortens the drainage sweep's device waits and makes them run out
+        (spins 0: back to normal); see hc_test_bounded_waits."""
+        self._check(self.lib.hc_test_bounded_waits(self.h, spins, extra_arrivals),
+                    "test_bounded_waits")
+
+    def mass_reset(self):
+        self._check(self.lib.hc_mass_reset(self.h), "mass_reset")
 
     def bench_kernel(self, kernel, reps):
         """(mean ms per launch, wet cells) of one kernel, timed with CUDA
@@ -253,24 +284,32 @@ class Model:
                                             C.byref(ns)), "adj_forward")
         return rec, q[:min(ns.value, max_samples)].copy()
 
-    def adj_gradient(self, n, every, target):
+    def adj_gradient(self, n, max_states, target, elev=False):
         """(loss, dL/dn per cell (imax+2, jmax+2), dL/drain (rain rows, cols),
-        [forward, reverse, total] ms) over n iterations from the current
-        state; checkpoints every `every` iterations."""
+        info) over n iterations from the current state, keeping at most
+        max_states model states (binomial checkpointing); with elev=True also
+        dL/d(elevation) per cell, as a fifth element.  info: forward_ms,
+        reverse_ms, total_ms, segment, snapshots, advanced (iterations run
+        again beyond the forward run and the segment replays)."""
         p = self.p
         t = np.ascontiguousarray(target, dtype=np.float64)
         gn = np.zeros((p.imax + 2, p.jmax + 2), dtype=np.float64)
+        ge = np.zeros((p.imax + 2, p.jmax + 2), dtype=np.float64)
         gr = np.zeros(self.case.rain.shape, dtype=np.float64)
         loss = C.c_double()
-        ms = (C.c_double * 3)()
-        self._check(self.lib.hc_adj_gradient(self.h, n, every, t.ctypes.data, len(t),
-                                             C.byref(loss), gn.ctypes.data, gr.ctypes.data, ms),
-                    "adj_gradient")
-        return loss.value, gn, gr, list(ms)
+        ms = (C.c_double * 6)()
+        self._check(self.lib.hc_adj_gradient(self.h, n, max_states, t.ctypes.data, len(t),
+                                             C.byref(loss), gn.ctypes.data, gr.ctypes.data,
+                                             ge.ctypes.data, ms), "adj_gradient")
+        info = dict(zip(("forward_ms", "reverse_ms", "total_ms", "segment", "snapshots",
+                         "advanced"), list(ms)))
+        if elev:
+            return loss.value, gn, gr, info, ge
+        return loss.value, gn, gr, info
 
     RUN_STATS = ["chunks", "erode_retry", "lateral", "creep", "global_slide", "drainage",
                  "drainage_sort", "drainage_sweep", "drainage_levels", "idle_iters",
-                 "drainage_host_sort"]
+                 "drainage_host_sort", "wet_cell_steps"]
 
     def run_stats(self):
         """{kind: (count, host ms)} of hc_run's host-side work so far."""

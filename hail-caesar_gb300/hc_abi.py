@@ -76,10 +76,17 @@ class hc_scalars(C.Structure):
 class hc_step_record(C.Structure):
     _fields_ = [(n, C.c_double) for n in (
         "counter", "cycle", "time_step", "maxdepth", "waterOut", "waterinput",
-        "erode_mult", "sediQ", "globalsediq", "baseflow")]
+        "erode_mult", "sediQ", "globalsediq", "baseflow", "vol_in", "vol_out", "vol_mask", "volume")]
 
 
 STEP_FIELDS = [f[0] for f in hc_step_record._fields_]
+# the fields the reference harness (oracle/ref_harness.cpp) records
+REF_STEP_FIELDS = STEP_FIELDS[:10]
+
+
+class hc_mass(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("volume0", "volume", "inflow", "outflow", "lost",
+                                             "mask_edge")]
 
 # hc_field enum, in declaration order
 FIELDS = ["elev", "water_depth", "qx", "qy", "qxs", "qys", "Vsusptot", "Vel", "Tau",

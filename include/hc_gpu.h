@@ -127,10 +127,27 @@ typedef struct hc_scalars {
   double stop_flag;       /* nonzero: host-side work needed before resuming */
 } hc_scalars;
 
-/* Per-iteration record of hc_run (same fields as oracle/ref_harness). */
+/* Per-iteration record of hc_run.  The first ten fields are those of
+ * oracle/ref_harness (the reference's own members after the iteration).  The
+ * last four are the water ledger of the iteration, which the reference does
+ * not keep (its waterinput / waterOut are rates for the time-step control):
+ *   vol_in   water the inputs added to the grid (reach points, catchment
+ *            input points, distributed runoff), m^3;
+ *   vol_out  water water_flux_out took off the edges plus water depth_update
+ *            zeroed at no-data cells, m^3;
+ *   vol_mask water that crossed a face between a cell of the wet list and
+ *            one outside it, m^3 (signed: + appeared, - vanished).  The
+ *            reference updates only listed cells (down_scan, rebuilt every
+ *            scan_area_interval_iter iterations), so such a face changes one
+ *            side's depth only; this is the one place its scheme does not
+ *            conserve water;
+ *   volume   sum of water depth x DX^2 over the grid (rows 1..imax, columns
+ *            1..jmax) right after depth_update, m^3, on iterations that run
+ *            scan_area (the full-grid pass that measures it); NaN on others. */
 typedef struct hc_step_record {
   double counter, cycle, time_step, maxdepth, waterOut, waterinput,
       erode_mult, sediQ, globalsediq, baseflow;
+  double vol_in, vol_out, vol_mask, volume;
 } hc_step_record;
 
 /* Fields that hc_upload / hc_download move, in the reference's layouts. */
@@ -246,6 +263,12 @@ hc_status hc_erode(hc_ctx* ctx, double mult, double* tempbmax);
 hc_status hc_lateral_channel_erode(hc_ctx* ctx);
 /* in_channel_landsliding :5429-5527 */
 hc_status hc_in_channel_landsliding(hc_ctx* ctx);
+/* global_landsliding :5529-5654 (daily in main.cpp's loop, call_global_landsliding
+ * :1986-1996); *sweeps (optional) receives the number of sweeps made */
+hc_status hc_global_landsliding(hc_ctx* ctx, int32_t* sweeps);
+/* creep(time) :5293-5427 (every creep_time_interval minutes, slope_creep
+ * :1976-1984, with time = creep_coeff) */
+hc_status hc_creep(hc_ctx* ctx, double time);
 
 /* ---- whole iterations ----
  * Runs up to n iterations of main.cpp:139-204 on the device (the same
@@ -257,6 +280,28 @@ hc_status hc_in_channel_landsliding(hc_ctx* ctx);
  * iteration.  *done = iterations run. */
 hc_status hc_run(hc_ctx* ctx, int64_t n, int32_t flags, hc_step_record* rec,
                  int64_t* done);
+
+/* Water-mass ledger (no counterpart in the reference; its only ledger is the
+ * pair of rates waterinput :3435/:3460 and waterOut :3046 that
+ * set_maximum_timestep :1905 compares).  Volumes in m^3, accumulated by every
+ * iteration (and member call) since hc_prepare or hc_mass_reset:
+ *   volume - (volume0 + inflow - outflow - lost + mask_edge)
+ * is what is left unexplained: rounding only, since every other face flux
+ * leaves one cell and enters its neighbour.  hc_mass_balance measures
+ * `volume` now, with a deterministic device reduction over rows 1..imax,
+ * columns 1..jmax. */
+typedef struct hc_mass {
+  double volume0;    /* water on the grid when the ledger started */
+  double volume;     /* water on the grid now */
+  double inflow;     /* added by the inputs (reach, catchment points, runoff) */
+  double outflow;    /* taken off the edges by water_flux_out */
+  double lost;       /* zeroed by depth_update at no-data cells */
+  double mask_edge;  /* net water that crossed faces at the wet list's border
+                        (see hc_step_record::vol_mask) */
+} hc_mass;
+hc_status hc_mass_balance(hc_ctx* ctx, hc_mass* m);
+/* Starts the ledger again from the water on the grid now. */
+hc_status hc_mass_reset(hc_ctx* ctx);
 
 /* Raster output while the run goes on (no counterpart in the reference,
  * which writes between iterations): hc_snapshot_begin copies a field with a
@@ -286,19 +331,26 @@ hc_status hc_run_ensemble(hc_ctx** ctxs, int32_t m, int64_t n, int32_t flags, in
  * time steps; passing such a record as `fixed` imposes those time steps
  * instead of the adaptive ones (finite-difference runs of a perturbed model).
  *
- * hc_adj_gradient runs n iterations from the current state (checkpoints
- * every `every` iterations), evaluates loss = mean over the samples of
- * (Q - q_target)^2 and its gradient with respect to every cell's Manning's n
- * (grad_n: (imax+2)(jmax+2) doubles) and every entry of the rain table
- * (grad_rain: rows x cols as given to hc_set_rain).  Time steps, wet mask and
- * input points are held at the run's values.  The model is left at the end
- * of the n iterations.  ms (optional, 3 doubles): forward, reverse, total. */
+ * hc_adj_gradient runs n iterations from the current state, evaluates
+ * loss = mean over the samples of (Q - q_target)^2 and its gradient with
+ * respect to every cell's Manning's n (grad_n), every cell's elevation
+ * (grad_elev; both (imax+2)(jmax+2) doubles) and every entry of the rain
+ * table (grad_rain: rows x cols as given to hc_set_rain).  Time steps, wet
+ * mask and input points are held at the run's values (they are piecewise
+ * constant in the parameters).  Memory: at most max_states model states
+ * (h, qx, qy, wet mask: 25 bytes a cell each) are kept at once, as
+ * binomial checkpoints (Griewank's revolve) of segments of K iterations plus
+ * the K iteration states of the segment being reversed; K is the one with
+ * the least recomputation.  The model is left at the end of the n
+ * iterations.  ms (optional, 6 doubles): forward ms, reverse ms, total ms,
+ * K, snapshots, iterations run again beyond the forward run and the
+ * segments' replays. */
 #define HC_ADJ_RECORD 22
 hc_status hc_adj_forward(hc_ctx* ctx, int64_t n, const double* fixed, double* rec_out,
                          double* q_samples, int64_t q_cap, int64_t* n_samples);
-hc_status hc_adj_gradient(hc_ctx* ctx, int64_t n, int32_t every, const double* q_target,
+hc_status hc_adj_gradient(hc_ctx* ctx, int64_t n, int32_t max_states, const double* q_target,
                           int64_t n_target, double* loss, double* grad_n, double* grad_rain,
-                          double* ms);
+                          double* grad_elev, double* ms);
 
 /* What hc_run spent on the host (no counterpart in the reference): for
  * each kind below, how many times it ran and its host wall time in ms,
@@ -316,9 +368,22 @@ enum {
   HC_STAT_DRAINAGE_LEVELS, /* frontiers the accumulations went through (count) */
   HC_STAT_IDLE_ITERS,      /* captured iterations skipped after a pause */
   HC_STAT_DRAINAGE_HOST_SORT, /* of the sorts, those the host finished (see hc_drainage_sort) */
+  HC_STAT_WET_CELL_STEPS,  /* count: wet-list cells summed over the iterations run (the
+                              cells the reference's down_scan loops visit) */
   HC_STAT_COUNT
 };
 hc_status hc_get_run_stats(hc_ctx* ctx, int64_t* counts, double* host_ms, int32_t n);
+
+/* Test hook of the bounded device waits (no counterpart in the reference).
+ * The drainage recomputation (drainage_area_D8 :2091-2271) runs as one
+ * cooperative kernel whose blocks wait for one another at grid barriers;
+ * every such wait gives up after a bounded number of spins, and the call
+ * that launched it returns HC_ERR_TIMEOUT with the context still usable (hc_run
+ * then redoes the recomputation first thing in its next call).  spins > 0
+ * sets that bound (0 restores the built-in ones) and makes each barrier
+ * expect extra_arrivals more blocks than were launched, so that every wait
+ * runs out: the way the tests check this path without a fault. */
+hc_status hc_test_bounded_waits(hc_ctx* ctx, int32_t spins, int32_t extra_arrivals);
 
 /* Stream the context issues its work on (a cudaStream_t). */
 void* hc_stream(hc_ctx* ctx);

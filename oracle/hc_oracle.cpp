@@ -64,6 +64,7 @@ struct hco_model {
   std::vector<double> grain;           // nrec * 11
   std::vector<double> strata;          // nrec * 10 * 11
   std::vector<int32_t> index, down_scan, rfarea;
+  std::vector<uint8_t> listed;  // membership of down_scan (the ledger's mask-edge term)
   std::vector<uint8_t> inputpointsarray;
   std::vector<double> edge, edge2, veg;  // (imax+1)(jmax+1) [*4]
   std::vector<int32_t> cin_x, cin_y;
@@ -73,6 +74,13 @@ struct hco_model {
   double mannings;
   double cycle = 0, previous = 0, time_step = 1, maxdepth = 10;
   double waterinput = 0, waterOut = 0, iod = 0, temptot = 0;
+  // water ledger of the current iteration (sums of depth, m): added by the
+  // inputs to rows 1..imax / columns 1..jmax, taken off the edges by
+  // water_flux_out, zeroed at no-data cells by depth_update; and the depth
+  // sum of the grid at the last scan_area with its iteration
+  double vin_it = 0, vout_it = 0, vlost_it = 0, vmask_it = 0, vol_scan = 0;
+  long vol_scan_counter = -1;
+  bool on_grid(long i, long j) const { return i >= 1 && i <= imax && j >= 1 && j <= jmax; }
   int counter = 0;
   double erode_call = 0, erode_mult = 1, lateralcounter = 1;
   double time_1 = 1, baseflow = 0, sediQ = 0, globalsediq = 0, tempbmax = 0;
@@ -429,6 +437,7 @@ static void catchment_water_input_grid(hco_model* m, double fdt) {
       if (amt > m->p.ERODEFACTOR) amt = m->p.ERODEFACTOR;
       m->waterinput += (amt / fdt) * DX * DX;
       m->H(i, j) += amt;
+      m->vin_it += amt;
     }
   double new_jmeanmax = 0;
   for (unsigned a = 1; a <= m->imax; a++)
@@ -458,6 +467,7 @@ static void catchment_water_input_and_hydrology(hco_model* m, double fdt) {  // 
     double amt = (m->j_mean[rf] * m->nActualGridCells[rf]) / (m->cin_counter[rf]) * fdt;
     if (amt > m->p.ERODEFACTOR) amt = m->p.ERODEFACTOR;
     m->H(i, j) += amt;
+    if (m->on_grid(i, j)) m->vin_it += amt;
   }
   if (m->cycle >= m->time_1) {
     do {
@@ -675,7 +685,9 @@ static void reach_water_and_sediment_input(hco_model* m) {  // :3301-3452
     double prop = (((r + 1) * rdt) - m->cycle) / rdt;
     double input = i1 + ((i2 - i1) * (1 - prop));
     m->waterinput += (input / div);
-    m->H(x, y) += (input / div) / (DX * DX) * fdt;
+    const double add = (input / div) / (DX * DX) * fdt;
+    m->H(x, y) += add;
+    if (m->on_grid(x, y)) m->vin_it += add;
   }
 }
 
@@ -779,7 +791,16 @@ extern "C" void hco_depth_update(hco_model* m) {
   double* Hd = m->water_depth.data();
   m->maxdepth = 0;
   double l_max = m->maxdepth;
-  HCO_PRAGMA(omp parallel for reduction(max : l_max) schedule(static))
+  // The ledger (not part of the reference): a face between a listed cell
+  // and one outside down_scan changes only the listed cell's depth, so the
+  // water crossing it appears or vanishes; `edge` sums it, in the same
+  // expression form as the update.
+  std::vector<uint8_t>& L = m->listed;
+  L.assign(m->N2, 0);
+  for (unsigned y = 1; y <= jmax; y++)
+    for (int inc = 1; m->DS(y, inc) > 0; inc++) L[m->DS(y, inc) * W + y] = 1;
+  double lost = 0, edge = 0;
+  HCO_PRAGMA(omp parallel for reduction(max : l_max) reduction(+ : lost, edge) schedule(static))
   for (unsigned y = 1; y <= jmax; y++) {
     int inc = 1;
     double tmax = 0;
@@ -787,17 +808,27 @@ extern "C" void hco_depth_update(hco_model* m) {
       unsigned x = m->DS(y, inc);
       inc++;
       const size_t c = x * W + y;
+      if (!L[c - W] || !L[c + W] || !L[c - 1] || !L[c + 1]) {
+        const double ux1 = L[c + W] ? 0.0 : m->qx[c + W], ux0 = L[c - W] ? 0.0 : m->qx[c];
+        const double uy1 = L[c + 1] ? 0.0 : m->qy[c + 1], uy0 = L[c - 1] ? 0.0 : m->qy[c];
+        edge += dt * (ux1 - ux0 + uy1 - uy0) / DX;
+      }
       Hd[c] += dt * (m->qx[c + W] - m->qx[c] + m->qy[c + 1] - m->qy[c]) / DX;
       if (susp)
         m->Vsusptot[c] += dt * (m->qxs[c + W] - m->qxs[c] + m->qys[c + 1] - m->qys[c]) / DX;
       if (Hd[c] > 0) {
-        if (m->elev[c] == -9999) Hd[c] = 0;
+        if (m->elev[c] == -9999) {
+          lost += Hd[c];
+          Hd[c] = 0;
+        }
         if (Hd[c] > tmax) tmax = Hd[c];
       }
     }
     if (tmax > l_max) l_max = tmax;
   }
   m->maxdepth = l_max;
+  m->vlost_it += lost;
+  m->vmask_it += edge;
 }
 
 // ---------------------------------------------------------------------------
@@ -818,6 +849,13 @@ extern "C" void hco_scan_area(hco_model* m) {
       }
     }
   }
+  // the ledger's volume after depth_update (not part of the reference)
+  double vol = 0;
+  HCO_PRAGMA(omp parallel for reduction(+ : vol) schedule(static))
+  for (unsigned i = 1; i <= imax; i++)
+    for (unsigned j = 1; j <= jmax; j++) vol += m->H(i, j);
+  m->vol_scan = vol;
+  m->vol_scan_counter = m->counter;
 }
 
 // ---------------------------------------------------------------------------
@@ -831,6 +869,7 @@ extern "C" void hco_water_flux_out(hco_model* m) {
     double& h = m->H(i, j);
     if (h > thr) {
       m->temptot += (h - thr) * DX * DX / fdt;
+      m->vout_it += h - thr;
       h = thr;
     }
   };
@@ -1597,7 +1636,13 @@ extern "C" long hco_iterate(hco_model* m, long n, int flags, hco_step_record* re
       r.sediQ = m->sediQ;
       r.globalsediq = m->globalsediq;
       r.baseflow = m->baseflow;
+      const double a2 = m->DX * m->DX;
+      r.vol_in = m->vin_it * a2;
+      r.vol_out = (m->vout_it + m->vlost_it) * a2;
+      r.vol_mask = m->vmask_it * a2;
+      r.volume = (m->vol_scan_counter == m->counter) ? m->vol_scan * a2 : std::nan("");
     }
+    m->vin_it = m->vout_it = m->vlost_it = m->vmask_it = 0;
     it++;
     if (n >= 0 && it >= n) break;
   } while (m->cycle / 60 < p.maxcycle);

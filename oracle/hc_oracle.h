@@ -35,6 +35,7 @@ typedef struct hco_model hco_model;
 typedef struct hco_step_record {
   double counter, cycle, time_step, maxdepth, waterOut, waterinput,
       erode_mult, sediQ, globalsediq, baseflow;
+  double vol_in, vol_out, vol_mask, volume;  /* the water ledger, as in hc_step_record */
 } hco_step_record;
 
 hco_model* hco_create(const hc_params* p);

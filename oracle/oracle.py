@@ -36,13 +36,14 @@ class _Rec(C.Structure):
 
 def build(quiet=True):
     """Builds liboracle(.so, _omp.so); also the reference harness when the
-    reference checkout is present."""
+    environment's HC_REFERENCE names the reference checkout."""
     targets = ["oracle"]
-    if os.path.isdir(os.environ.get("HC_REFERENCE", "/root/reference")):
+    ref = os.environ.get("HC_REFERENCE", "")
+    if ref and os.path.isdir(os.path.join(ref, "src", "catchmentmodel")):
         targets.append("ref")
     cmd = ["make", "-s", "-C", HERE, "-j8"] + targets
-    if "HC_REFERENCE" in os.environ:
-        cmd.append("REF=" + os.environ["HC_REFERENCE"])
+    if "ref" in targets:
+        cmd.append("REF=" + ref)
     subprocess.run(cmd, check=True, stdout=subprocess.DEVNULL if quiet else None)
 
 

@@ -10,7 +10,8 @@ the reference checkout exists; the fixtures travel, the reference does not).
 2. ref_<case>.npz - final state and per-iteration records of the unmodified
    reference sources (oracle/_ref/ref_harness) on small seeded synthetic cases.
 
-Usage:  python tests/golden/make_golden.py [--reference /root/reference]
+Usage:  python tests/golden/make_golden.py --reference <reference checkout>
+        (or HC_REFERENCE set in the environment)
 """
 import argparse
 import json
@@ -183,8 +184,10 @@ def make_synthetic():
 
 if __name__ == "__main__":
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=os.environ.get("HC_REFERENCE"))
     a = ap.parse_args()
+    if not a.reference:
+        ap.error("name the reference checkout: --reference or HC_REFERENCE")
     os.environ["HC_REFERENCE"] = a.reference
     make_boscastle(a.reference)
     make_synthetic()

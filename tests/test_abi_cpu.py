@@ -44,7 +44,8 @@ def test_params_default_matches_python(gpu_lib):
 def test_struct_sizes_match_header_layout():
     # hc_params is all int32/double members; its size must be a multiple of 8
     assert C.sizeof(hc_abi.hc_params) % 8 == 0
-    assert C.sizeof(hc_abi.hc_step_record) == 80
+    assert C.sizeof(hc_abi.hc_step_record) == 14 * 8
+    assert C.sizeof(hc_abi.hc_mass) == 6 * 8
 
 
 @pytest.mark.parametrize("name", hc_abi.FIELDS)

@@ -1,0 +1,194 @@
+"""GPU parity on the benchmark configurations themselves, and the water
+ledger.
+
+* C1, the reach case at its full size (300 rows along the flow x 100
+  columns, 10 m, Wilcock-Crowe, 9 fractions): water depth and elevation
+  within 1e-9 m after 1,000 iterations with masks and grain-record indices
+  identical; then the whole 24 h run, with the outlet discharge and the
+  sediment yield within 1e-6 relative and the water ledger closed to 1e-10.
+* C2's feature set (per-cell Manning's n, Einstein transport, lateral3,
+  slide_3) on a 200 x 200 catchment for 1,500 iterations through a storm.
+* The reference's own known-good answers (test/basic_kga_tests.py:81-90):
+  the Boscastle 50 m water depths at 3360 min and the 72 h hydrograph, run
+  through hc_run, at the reference test's rtol 1e-3.
+
+The oracle (oracle/hc_oracle.cpp) is the checker; tests/test_oracle_pin.py
+pins it to the reference's sources and to the same known-good answers.
+"""
+import numpy as np
+import pytest
+
+import synth
+from hc_abi import STEP_FIELDS
+from helpers import assert_bitwise, assert_close
+from test_oracle_pin import boscastle_case, hydrograph
+
+pytestmark = pytest.mark.gpu
+
+COL = {k: i for i, k in enumerate(STEP_FIELDS)}
+H_ATOL = 1e-9  # m: water depth and elevation after 1,000 steps
+CLOSURE = 1e-10  # relative: the water ledger
+
+
+def closure_error(mass):
+    """Unexplained water of an hc_mass_balance result, relative to the
+    larger of the water on the grid and the water put in."""
+    want = (mass["volume0"] + mass["inflow"] - mass["outflow"] - mass["lost"]
+            + mass["mask_edge"])
+    scale = max(abs(mass["volume"]), abs(mass["inflow"]), 1e-300)
+    return abs(mass["volume"] - want) / scale
+
+
+def record_closure(rec):
+    """The same from the per-iteration records: the volume measured after
+    depth_update on scan iterations against the sum of the ledger's terms up
+    to there (that iteration's outflow comes after the measurement)."""
+    vin = np.cumsum(rec[:, COL["vol_in"]])
+    vout = np.cumsum(rec[:, COL["vol_out"]]) - rec[:, COL["vol_out"]]
+    vmask = np.cumsum(rec[:, COL["vol_mask"]])
+    vol = rec[:, COL["volume"]]
+    k = ~np.isnan(vol)
+    err = np.abs(vol[k] - (vin[k] + vmask[k] - vout[k]))
+    return float(np.max(err / np.maximum(np.abs(vol[k]), np.abs(vin[k])).clip(1e-300)))
+
+
+def test_reach_c1_first_1000_steps(gpu_lib, oracle_mod):
+    import hc
+    case = synth.reach_case()  # 300 x 100 at 10 m, the C1 configuration
+    m = hc.Model(case)
+    g = m.run(1000)
+    o = oracle_mod.Oracle(case)
+    r = o.iterate(1000)
+    assert g.shape == r.shape
+    for c in ("counter", "erode_mult"):
+        assert_bitwise(g[:, COL[c]], r[:, COL[c]], c)
+    assert_bitwise(m.field("down_scan"), o.field("down_scan"), "down_scan")
+    assert_bitwise(m.field("index"), o.field("index"), "index")
+    for k in ("water_depth", "elev"):
+        assert_close(m.field(k), o.field(k), H_ATOL, k)
+    for k in ("grain", "strata", "Vsusptot"):
+        assert_close(m.field(k), o.field(k), H_ATOL, k)
+    assert np.any(m.field("index") != -9999), "no grain record was made"
+
+
+def test_reach_c1_whole_run(gpu_lib, oracle_mod):
+    """The whole 24 h: outlet discharge per iteration and the sediment yield
+    within 1e-6 relative of the oracle, the same iterations, and the water
+    ledger closed to 1e-10 (on the device and in the oracle alike)."""
+    import hc
+    case = synth.reach_case()
+    m = hc.Model(case)
+    g = m.run(200000)
+    o = oracle_mod.Oracle(case)
+    r = o.iterate(-1)
+    assert g.shape == r.shape, (g.shape, r.shape)
+    assert g[-1, COL["cycle"]] / 60 >= case.params.maxcycle
+    assert_bitwise(g[:, COL["counter"]], r[:, COL["counter"]], "counter")
+    assert_close(g[:, COL["cycle"]], r[:, COL["cycle"]], 0, "cycle", rtol=1e-9)
+    # outlet discharge (water_flux_out's sum) and sediment yield
+    assert_close(g[:, COL["waterOut"]], r[:, COL["waterOut"]], 1e-9, "waterOut", rtol=1e-6)
+    assert_close(g[:, COL["sediQ"]], r[:, COL["sediQ"]], 1e-12, "sediQ", rtol=1e-6)
+    assert_close(g[:, COL["globalsediq"]], r[:, COL["globalsediq"]], 1e-12, "globalsediq",
+                 rtol=1e-6)
+    assert g[-1, COL["globalsediq"]] > 0, "no sediment left the reach"
+    # the hourly hydrograph the reference writes
+    qg = hydrograph(g, 60.0)
+    qr = hydrograph(r, 60.0)
+    assert len(qg) == len(qr) >= 23
+    assert_close(qg, qr, 1e-9, "hourly discharge", rtol=1e-6)
+    # water ledger: device terms against the oracle's, then closure
+    for c in ("vol_in", "vol_out", "vol_mask"):
+        assert_close(np.cumsum(g[:, COL[c]]), np.cumsum(r[:, COL[c]]), 1e-6, c, rtol=1e-9)
+    assert_close(g[:, COL["volume"]], r[:, COL["volume"]], 1e-6, "volume", rtol=1e-9)
+    assert record_closure(g) <= CLOSURE
+    assert record_closure(r) <= CLOSURE
+    mass = m.mass_balance()
+    assert mass["inflow"] > 0 and mass["outflow"] > 0
+    assert closure_error(mass) <= CLOSURE, mass
+    # the totals are the records' sums
+    assert_close(mass["inflow"], np.sum(g[:, COL["vol_in"]]), 0, "inflow", rtol=1e-12)
+    assert_close(mass["outflow"], np.sum(g[:, COL["vol_out"]]), 0, "outflow", rtol=1e-12)
+
+
+def test_catchment_c2_features_200(gpu_lib, oracle_mod):
+    """C2's feature set at 200 x 200: per-cell n, Einstein, lateral3 and
+    slide_3, 1,500 iterations into a 60 mm/h storm."""
+    import hc
+    case = synth.catchment_case(n=200, DX=20.0, hours=72, lateral=True, storm_start_h=0.5)
+    m = hc.Model(case)
+    g = m.run(1500)
+    o = oracle_mod.Oracle(case)
+    r = o.iterate(1500)
+    assert g.shape == r.shape
+    for c in ("counter", "erode_mult"):
+        assert_bitwise(g[:, COL[c]], r[:, COL[c]], c)
+    for c in ("cycle", "time_step", "maxdepth", "waterinput", "baseflow"):
+        assert_close(g[:, COL[c]], r[:, COL[c]], 0, c, rtol=1e-9)
+    assert_close(g[:, COL["waterOut"]], r[:, COL["waterOut"]], 1e-12, "waterOut", rtol=1e-6)
+    assert_close(g[:, COL["globalsediq"]], r[:, COL["globalsediq"]], 1e-12, "globalsediq",
+                 rtol=1e-6)
+    assert_bitwise(m.field("index"), o.field("index"), "index")
+    assert_bitwise(m.field("down_scan"), o.field("down_scan"), "down_scan")
+    for k in ("elev", "water_depth", "grain", "strata", "Vsusptot"):
+        assert_close(m.field(k), o.field(k), H_ATOL, k)
+    assert_close(m.field("edge"), o.field("edge"), 1e-9, "edge")
+    e0 = np.full_like(m.field("elev"), -9999.0)
+    e0[1:-1, 1:-1] = case.elev
+    assert np.sum(m.field("elev") != e0) > 1000, "erosion hardly moved the bed"
+    assert np.sum(m.field("edge") != 0) > 1000, "lateral3 left no edge field"
+    assert record_closure(g) <= CLOSURE
+    assert closure_error(m.mass_balance()) <= CLOSURE
+
+
+@pytest.mark.parametrize("tag", ["normal", "flipped"])
+def test_boscastle_kga_through_hc_run(gpu_lib, tag):
+    """The reference's own regression test on the device: hc_run to the
+    3360 min raster save (main.cpp's save_raster_output), water depths at
+    the raster's 6 significant digits within rtol 1e-3 of the known-good
+    raster, and the 72 h hydrograph within rtol 1e-3."""
+    import hc
+    case, z = boscastle_case(tag)
+    interval = float(z[tag + "_raster_interval"])
+    a = hc.Model(case)
+    g = a.run(400000)
+    assert g[-1, COL["cycle"]] / 60 >= case.params.maxcycle
+    # the iteration at which the raster named 3360 is written
+    save, k_save = 0.0, None
+    for k, cyc in enumerate(g[:, COL["cycle"]]):
+        if cyc >= save:
+            if int(cyc) == 3360:
+                k_save = k
+                break
+            save += interval
+    assert k_save is not None
+    b = hc.Model(case)
+    b.run(k_save + 1, records=False)
+    wd = b.field("water_depth")[1:-1, 1:-1]
+    got = np.array([float("%.6g" % v) for v in wd.ravel()]).reshape(wd.shape)
+    np.testing.assert_allclose(got, z[tag + "_wd3360"], rtol=1e-3)
+    q = hydrograph(g, float(z[tag + "_interval"]))
+    want = z[tag + "_hydrograph"]
+    assert len(q) == len(want)
+    np.testing.assert_allclose(np.round(q, 6), want, rtol=1e-3)
+    assert closure_error(a.mass_balance()) <= CLOSURE
+
+
+def test_mass_balance_runoff_and_reset(gpu_lib):
+    """Distributed runoff (every cell an input) keeps the ledger closed, and
+    hc_mass_reset starts it from the water on the grid."""
+    import hc
+    case = synth.catchment_case(n=40, DX=20.0, hours=72, relief=60.0, hydro_only=True,
+                                lateral=False, storm_start_h=0.5)
+    case.params.spatially_complex_rainfall = 1
+    m = hc.Model(case)
+    g = m.run(3000)
+    mass = m.mass_balance()
+    assert mass["inflow"] > 0
+    assert closure_error(mass) <= CLOSURE, mass
+    assert record_closure(g) <= CLOSURE
+    m.mass_reset()
+    again = m.mass_balance()
+    assert again["volume0"] == again["volume"] == mass["volume"]
+    assert again["inflow"] == again["outflow"] == again["mask_edge"] == 0
+    m.run(500, records=False)
+    assert closure_error(m.mass_balance()) <= CLOSURE

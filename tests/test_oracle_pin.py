@@ -97,7 +97,7 @@ def test_oracle_matches_reference_fixture(oracle_mod, name):
     z = np.load(os.path.join(GOLD, "ref_%s.npz" % name))
     o = oracle_mod.Oracle(case)
     rec = o.iterate(n)
-    assert_bitwise(rec, z["records"], "records")
+    assert_bitwise(rec[:, :10], z["records"], "records")
     for k in z.files:
         if k in ("records", "iterations") or k.startswith("s_"):
             continue
@@ -133,7 +133,7 @@ def test_oracle_matches_live_reference(oracle_mod, kind):
     st, rec = oracle_mod.run_reference(case, n)
     o = oracle_mod.Oracle(case)
     r = o.iterate(n)
-    assert_bitwise(r, rec, "records")
+    assert_bitwise(r[:, :10], rec, "records")
     for k in ("elev", "water_depth", "qx", "qy", "index", "grain", "strata", "edge", "Vsusptot"):
         if k in st:
             assert_bitwise(o.field(k), st[k], k)

@@ -59,9 +59,10 @@ def test_noalloc_matches_depth_update_twice(gpu_lib):
         torch.cuda.synchronize()
         h_ref = m.field("water_depth")
         assert s.maxdepth > 0
+        # both compute the same IEEE quotients in the same order: bit for bit
         for k in ("water_depth", "Vsusptot"):
             got = dev[k].cpu().numpy()
             ref = m.field(k)
-            assert np.allclose(got, ref, rtol=0, atol=1e-12), (call, k, np.abs(got - ref).max())
-        assert abs(maxd.item() - s.maxdepth) <= 1e-12, (call, maxd.item(), s.maxdepth)
+            assert np.array_equal(got, ref, equal_nan=True), (call, k, np.nanmax(np.abs(got - ref)))
+        assert maxd.item() == s.maxdepth, (call, maxd.item(), s.maxdepth)
         assert np.abs(h_ref).max() > 0
