@@ -30,6 +30,12 @@ import sys
 import threading
 import time
 
+# hc_run_ensemble keeps one stream per member in flight: let the device give
+# them as many hardware queues as it has (the default 8 would make
+# unrelated members' kernels wait on one another).  Read when the CUDA
+# context is created, so before torch initialises it.
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+
 import numpy as np
 
 ROOT = os.path.dirname(os.path.abspath(__file__))

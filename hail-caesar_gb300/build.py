@@ -20,7 +20,7 @@ NVFLAGS = ["-O3", "-std=c++17", "--fmad=false", "-lineinfo", "-Xcompiler", "-fPI
            "-Xcompiler", "-ffp-contract=off", "-Xptxas", "-warn-spills"]
 SOURCES = ["hc_api.cu", "hc_flow.cu", "hc_erode.cu", "hc_slide.cu", "hc_lateral.cu",
            "hc_host.cpp", "hc_drain.cu", "hc_adjoint.cu", "hc_noalloc.cu",
-           "hc_sort.cu"]
+           "hc_sort.cu", "hc_tune.cu"]
 
 
 def nvcc():

@@ -167,11 +167,23 @@ struct AdjBufs {
   double *pe0, *pe1x, *pe1y;  // elevation terms: own faces, to the cell above, to the left
   double *gn;   // accumulated dL/dn per cell
   double *ge;   // accumulated dL/d(elevation) per cell
+  uint8_t *pflag;  // the cell's face terms (p*, pe*) may be nonzero
   double *gj;   // dL/dj per zone for this iteration
 };
 
 __device__ __forceinline__ bool edge_cell(const hc_view& c, int i, int j) {
   return i == 1 || i == c.imax || j == 1 || j == c.jmax;
+}
+
+// A cell outside the wet list that is no input point and no edge cell
+// keeps its depth through an iteration: its depth adjoint passes through
+// unchanged (k_adj_depth leaves lamd unwritten there; readers take lam),
+// and a cell whose faces and whose up and left neighbours are all outside
+// the list has no face terms (its p* entries are zero; pflag says which
+// entries may not be).  Dry parts of the grid so cost a few bytes a cell.
+__device__ __forceinline__ bool depth_active(const hc_view& c, const AdjBufs& b, size_t cell,
+                                             int i, int j) {
+  return b.mask[cell] || b.point[cell] || i == 1 || i == c.imax || j == 1 || j == c.jmax;
 }
 
 // water_flux_out and depth_update, reversed: lamd = adjoint of the depth
@@ -181,6 +193,7 @@ __global__ void k_adj_depth(const hc_view c, AdjBufs b, AdjStep st) {
   const int i = 1 + blockIdx.y * blockDim.y + threadIdx.y;
   if (i > c.imax || j > c.jmax) return;
   const size_t W = c.W, cell = (size_t)i * W + j;
+  if (!depth_active(c, b, cell, i, j)) return;
   const int rf = c.rfarea[cell];
   double ha = b.h0[cell];
   if (b.point[cell] && rf >= 0 && rf <= HC_MAX_RF) ha += st.amt[rf];
@@ -207,6 +220,15 @@ __global__ void k_adj_flow(const hc_view c, AdjBufs b, AdjStep st) {
   const int i = 1 + blockIdx.y * blockDim.y + threadIdx.y;
   if (i > c.imax || j > c.jmax) return;
   const size_t W = c.W, cell = (size_t)i * W + j;
+  if (!(b.mask[cell] || b.mask[cell - W] || b.mask[cell - 1])) {
+    // no face of this cell moves, and no listed depth reads its discharges
+    if (b.pflag[cell]) {
+      b.p0x[cell] = b.p1x[cell] = b.p0y[cell] = b.p1y[cell] = 0;
+      b.pe0[cell] = b.pe1x[cell] = b.pe1y[cell] = 0;
+      b.pflag[cell] = 0;
+    }
+    return;
+  }
   const double k = st.fdt / c.p.DX;
   auto ml = [&](size_t q) { return b.mask[q] ? b.lamd[q] : 0.0; };
   // depth_update reads qx[cell] (-) and, for the cell above, qx[cell] (+)
@@ -265,6 +287,7 @@ __global__ void k_adj_flow(const hc_view c, AdjBufs b, AdjStep st) {
   b.pe0[cell] = pe0;
   b.pe1x[cell] = pe1x;
   b.pe1y[cell] = pe1y;
+  b.pflag[cell] = 1;
 }
 
 // the depth adjoint before the iteration (inputs add a constant), and the
@@ -277,9 +300,12 @@ __global__ void __launch_bounds__(256) k_adj_gather(const hc_view c, AdjBufs b, 
   const int warp = t >> 5, lane = t & 31;
   double mine = 0;
   int myrf = -1;
-  if (i <= c.imax && j <= c.jmax) {
-    const size_t W = c.W, cell = (size_t)i * W + j;
-    const double la = b.lamd[cell] + b.p0x[cell] + b.p0y[cell] + b.p1x[cell + W] + b.p1y[cell + 1];
+  const size_t W = c.W, cell = (size_t)i * W + j;
+  const bool in = i <= c.imax && j <= c.jmax;
+  const bool dact = in && depth_active(c, b, cell, i, j);
+  if (in && (dact || b.pflag[cell] || b.pflag[cell + W] || b.pflag[cell + 1])) {
+    const double la = (dact ? b.lamd[cell] : b.lam[cell]) + b.p0x[cell] + b.p0y[cell] +
+                      b.p1x[cell + W] + b.p1y[cell + 1];
     b.lam[cell] = la;
     b.ge[cell] += b.pe0[cell] + b.pe1x[cell + W] + b.pe1y[cell + 1];
     const int rf = c.rfarea[cell];
@@ -705,8 +731,8 @@ extern "C" hc_status hc_adj_gradient(hc_ctx* c, int64_t n, int32_t max_states,
   if (loss) *loss = L;
   // ---------------- reverse
   const auto t_rev = std::chrono::steady_clock::now();
-  Dev lam, mux, muy, lamd, p0x, p0y, p1x, p1y, pe0, pe1x, pe1y, gn, ge, gj;
-  if (dmalloc(lam, N2 * 8) || dmalloc(mux, N2 * 8) || dmalloc(muy, N2 * 8) ||
+  Dev lam, mux, muy, lamd, p0x, p0y, p1x, p1y, pe0, pe1x, pe1y, gn, ge, gj, pflag;
+  if (dmalloc(pflag, N2) || dmalloc(lam, N2 * 8) || dmalloc(mux, N2 * 8) || dmalloc(muy, N2 * 8) ||
       dmalloc(lamd, N2 * 8) || dmalloc(p0x, N2 * 8) || dmalloc(p0y, N2 * 8) ||
       dmalloc(p1x, N2 * 8) || dmalloc(p1y, N2 * 8) || dmalloc(pe0, N2 * 8) ||
       dmalloc(pe1x, N2 * 8) || dmalloc(pe1y, N2 * 8) || dmalloc(gn, N2 * 8) ||
@@ -717,6 +743,7 @@ extern "C" hc_status hc_adj_gradient(hc_ctx* c, int64_t n, int32_t max_states,
   for (Dev* d : {&lam, &mux, &muy, &lamd, &p0x, &p0y, &p1x, &p1y, &pe0, &pe1x, &pe1y, &gn, &ge})
     cudaMemsetAsync(d->p, 0, N2 * 8, s);
   cudaMemsetAsync(gj.p, 0, (size_t)n * (HC_MAX_RF + 1) * 8, s);
+  cudaMemsetAsync(pflag.p, 0, N2, s);
   dim3 b(32, 8), gr((v.jmax + 31) / 32, (v.imax + 7) / 8);
   rv.advance = [&](int64_t t0, int64_t t1) -> hc_status {
     HC_TRY(adj_mode(c, dt.as<double>(), n, 2, t0));  // imposed steps, no saves
@@ -770,6 +797,7 @@ extern "C" hc_status hc_adj_gradient(hc_ctx* c, int64_t n, int32_t max_states,
       bb.pe1y = pe1y.as<double>();
       bb.gn = gn.as<double>();
       bb.ge = ge.as<double>();
+      bb.pflag = pflag.as<uint8_t>();
       bb.gj = gj.as<double>() + (size_t)t * (HC_MAX_RF + 1);
       const double* na = pts.nact_at(t);
       const double* ct = pts.cnt_at(t);

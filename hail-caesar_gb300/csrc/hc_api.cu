@@ -265,6 +265,10 @@ extern "C" hc_status hc_create(const hc_params* p, size_t max_bytes, hc_ctx** ou
   const size_t N2 = v.N2, E2 = v.E2;
   const bool sed = !p->hydro_only;
   cudaGetDevice(&c->device);
+  cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, c->device);
+  if (c->sms < 1) c->sms = 1;
+  c->flow_shape = 0;
+  c->tuned_key = -1;
   if (cudaStreamCreateWithFlags(&c->s, cudaStreamNonBlocking) != cudaSuccess ||
       cudaStreamCreateWithFlags(&c->s2, cudaStreamNonBlocking) != cudaSuccess) {
     cudaGetLastError();
@@ -1271,6 +1275,7 @@ static hc_status run_begin(hc_ctx* c, int64_t n, int32_t flags, bool want_rec, b
     HC_TRY(recompute_points(c, true));
     HC_TRY(pull(c));
   }
+  HC_TRY(autotune(c, false));  // launch shapes for this shape class (hc_tune.cu)
   if (!c->graph_iters || c->graph_flags != flags) HC_TRY(build_graph(c, flags));
   if (!c->chunk_done) HC_CU(cudaEventCreateWithFlags(&c->chunk_done, cudaEventDisableTiming),
                             "event");

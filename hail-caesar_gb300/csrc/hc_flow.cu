@@ -320,6 +320,22 @@ struct FaceOut {
   int dir;  // 1: positive, -1: negative, 0: none
 };
 
+// The limiters' FP64 tests, for the faces whose float estimates cannot
+// decide them: out of line, so that their FP64 instructions (a hardware
+// division among them) issue only where they run.
+static __device__ __noinline__ bool depth_exceeds(double qn, double dt, double DX, double h) {
+  return (qn * dt / DX) > (h / 4);  // :3138, :3218
+}
+static __device__ __noinline__ bool depth_exceeds_neg(double qn, double dt, double DX, double h) {
+  return fabs(qn * dt / DX) > (h / 4);  // :3144, :3219
+}
+static __device__ __noinline__ bool sed_exceeds(double qs, double dt, double v, double DX) {
+  return qs * dt > (v * DX) / 4;  // :3163
+}
+static __device__ __noinline__ bool sed_exceeds_neg(double qs, double dt, double v, double DX) {
+  return fabs(qs * dt) > (v * DX) / 4;  // :3169
+}
+
 // Three-way test of A > B from float estimates a, b, each within a relative
 // 2^-18 of A, B (or flushed to 0 below 2^-126, inf above the float range):
 // +1 surely greater, -1 surely not, 0 too close to call (the caller then
@@ -403,7 +419,7 @@ __device__ __forceinline__ void inertial_face(double& q, double& qs, double& vel
   // run one after the other, as in the reference
   if (dgt0(qn)) {
     int t = decide_gt(approx_abs_f(qn) * dtf / c.DXf, approx_f(h0) * 0.25f);
-    if (t == 0) t = ((qn * dt / DX) > (h0 / 4)) ? 1 : -1;
+    if (t == 0) t = depth_exceeds(qn, dt, DX, h0) ? 1 : -1;
     if (t > 0) {
       qn = ddiv_rn(ddiv_rn(h0 * DX, 5.0), dt);
       qoh_valid = false;
@@ -411,7 +427,7 @@ __device__ __forceinline__ void inertial_face(double& q, double& qs, double& vel
   }
   if (dlt0(qn)) {
     int t = decide_gt(approx_abs_f(qn) * dtf / c.DXf, approx_f(h1) * 0.25f);
-    if (t == 0) t = (fabs(qn * dt / DX) > (h1 / 4)) ? 1 : -1;
+    if (t == 0) t = depth_exceeds_neg(qn, dt, DX, h1) ? 1 : -1;
     if (t > 0) {
       qn = zero_minus(ddiv_rn(ddiv_rn(h1 * DX, 5.0), dt));
       qoh_valid = false;
@@ -425,12 +441,12 @@ __device__ __forceinline__ void inertial_face(double& q, double& qs, double& vel
     // qs*dt > V*DX/4 (giving cell) caps the sediment flux
     if (dgt0(qs)) {
       int t = decide_gt(approx_abs_f(qs) * dtf, approx_f(v0) * c.DXf * 0.25f);
-      if (t == 0) t = (qs * dt > (v0 * DX) / 4) ? 1 : -1;
+      if (t == 0) t = sed_exceeds(qs, dt, v0, DX) ? 1 : -1;
       if (t > 0) qs = ddiv_rn(ddiv_rn(v0 * DX, 5.0), dt);
     }
     if (dlt0(qs)) {
       int t = decide_gt(approx_abs_f(qs) * dtf, approx_f(v1) * c.DXf * 0.25f);
-      if (t == 0) t = (fabs(qs * dt) > (v1 * DX) / 4) ? 1 : -1;
+      if (t == 0) t = sed_exceeds_neg(qs, dt, v1, DX) ? 1 : -1;
       if (t > 0) qs = zero_minus(ddiv_rn(ddiv_rn(v1 * DX, 5.0), dt));
     }
   }
@@ -520,10 +536,12 @@ __device__ __forceinline__ void flow_cell(const hc_view& c, const hc_dev* __rest
 }
 
 // One thread per wet cell, grid-stride over the wet list: cells outside the
-// mask are never touched, as in the reference's down_scan loops.
-template <bool kSed>
-__global__ void __launch_bounds__(256) k_flow_route(const hc_view c, const hc_dev* __restrict__ d,
-                                                     int gated) {
+// mask are never touched, as in the reference's down_scan loops.  MINB,
+// the blocks of 256 a multiprocessor must hold, sets the register budget
+// (3: 80 registers, 4: 64, 5: 48, 6: 40; the autotuner picks one).
+template <bool kSed, int MINB>
+__global__ void __launch_bounds__(256, MINB) k_flow_route(const hc_view c,
+                                                          const hc_dev* __restrict__ d, int gated) {
   if (gated && !d->it_active) return;
   const int n = d->wet_count;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
@@ -875,13 +893,33 @@ static int list_blocks(const hc_ctx* c) {
   return (int)std::min<size_t>(need, 152 * 8);
 }
 
-void launch_flow_route(hc_ctx* c, int gated) {
-  if (c->v.p.hydro_only)
-    k_flow_route<false><<<list_blocks(c), 256, 0, c->cs>>>(c->v, c->dev, gated);
-  else
-    k_flow_route<true><<<list_blocks(c), 256, 0, c->cs>>>(c->v, c->dev, gated);
+// The launch shapes of k_flow_route the autotuner chooses from: blocks per
+// multiprocessor (the register budget) and waves of the grid (grid = SMs x
+// blocks per SM x waves; one wave: every block resident at once).
+const FlowShape kFlowShapes[kFlowShapeCount] = {
+    {4, 0}, {3, 1}, {4, 1}, {5, 1}, {6, 1}, {3, 4}, {4, 4}, {5, 4}, {6, 4}};
+
+template <bool kSed>
+static void flow_launch(hc_ctx* c, int gated, int shape) {
+  const FlowShape f = kFlowShapes[shape];
+  int blocks = f.waves ? c->sms * f.minb * f.waves : list_blocks(c);
+  blocks = std::max(1, std::min(blocks, (int)((c->v.N2 + 255) / 256)));
+  switch (f.minb) {
+    case 3: k_flow_route<kSed, 3><<<blocks, 256, 0, c->cs>>>(c->v, c->dev, gated); break;
+    case 5: k_flow_route<kSed, 5><<<blocks, 256, 0, c->cs>>>(c->v, c->dev, gated); break;
+    case 6: k_flow_route<kSed, 6><<<blocks, 256, 0, c->cs>>>(c->v, c->dev, gated); break;
+    default: k_flow_route<kSed, 4><<<blocks, 256, 0, c->cs>>>(c->v, c->dev, gated); break;
+  }
+}
+
+void launch_flow_route_shape(hc_ctx* c, int gated, int shape) {
+  if (shape < 0 || shape >= kFlowShapeCount) shape = 0;
+  if (c->v.p.hydro_only) flow_launch<false>(c, gated, shape);
+  else flow_launch<true>(c, gated, shape);
   count_launch(c, 1);
 }
+
+void launch_flow_route(hc_ctx* c, int gated) { launch_flow_route_shape(c, gated, c->flow_shape); }
 
 void launch_depth_update(hc_ctx* c, int gated) {
   k_depth_update<<<list_blocks(c), 256, 0, c->cs>>>(c->v, c->dev, gated);

@@ -231,6 +231,10 @@ struct hc_ctx {
   struct hc_sort_work* sort_work;  // device sort of the elevations (hc_sort.cu)
   bool area_valid;         // device area matches the cached sweep order
   bool drain_retry;        // a drainage recomputation gave up: redo it first
+  int sms;                 // multiprocessors of the device
+  int flow_shape;          // launch shape of k_flow_route (kFlowShapes), autotuned
+  int64_t tuned_key;       // the shape class flow_shape was chosen for (-1: none)
+  double tune_ms[16];      // the autotuner's times per shape (ms per launch)
   // called after every recomputation of the input points (adjoint replays)
   void (*points_hook)(hc_ctx*, void*);
   void* points_hook_arg;
@@ -510,6 +514,11 @@ HC_DEV hc_divisor ddiv_prep(double b) {
   return d;
 }
 
+// The hardware division, out of line: inlined, the compiler predicates its
+// FP64 instructions into every call site, where they take FP64 issue slots
+// whether the fallback runs or not.
+static __device__ __noinline__ double ddiv_hw(double a, double b) { return __ddiv_rn(a, b); }
+
 HC_DEV double ddiv_by(double a, const hc_divisor& d) {
   const unsigned long long A = (unsigned long long)__double_as_longlong(a);
   const unsigned long long M52 = (1ull << 52) - 1, H52 = 1ull << 52;
@@ -527,7 +536,7 @@ HC_DEV double ddiv_by(double a, const hc_divisor& d) {
     if (d.ok && (A << 1) == 0)
       return __longlong_as_double(
           (long long)((A ^ (unsigned long long)__double_as_longlong(d.b)) & 0x8000000000000000ull));
-    return __ddiv_rn(a, d.b);
+    return ddiv_hw(a, d.b);
   }
   unsigned long long q, r;
   if (mb == H52) {  // b a power of two: exact
@@ -660,6 +669,15 @@ void launch_depth_update(hc_ctx* c, int gated);
 void launch_scan_area(hc_ctx* c, int gated);
 void launch_wet_list(hc_ctx* c, int gated);  // rebuild the wet-cell list from the mask
 void launch_flux_out(hc_ctx* c, int gated, int record);
+// k_flow_route's launch shapes (hc_flow.cu) and the autotuner (hc_tune.cu)
+struct FlowShape {
+  int minb;   // blocks of 256 per multiprocessor (register budget)
+  int waves;  // grid = SMs x minb x waves; 0: the wet-list default grid
+};
+constexpr int kFlowShapeCount = 9;
+extern const FlowShape kFlowShapes[kFlowShapeCount];
+void launch_flow_route_shape(hc_ctx* c, int gated, int shape);
+hc_status autotune(hc_ctx* c, bool force);
 void launch_volume(hc_ctx* c);           // hc_dev::vol_now = depth sum of the grid
 void launch_mass_reset(hc_ctx* c);       // the ledger starts again from vol_now
 void launch_erode_begin(hc_ctx* c, int gated, double mult);

@@ -75,6 +75,7 @@ def load_library(path=LIB_PATH):
         "hc_mass_balance": (C.c_int, [vp, P(hc_mass)]),
         "hc_mass_reset": (C.c_int, [vp]),
         "hc_test_bounded_waits": (C.c_int, [vp, C.c_int32, C.c_int32]),
+        "hc_autotune": (C.c_int, [vp, C.c_int32, P(C.c_int32), P(C.c_double), C.c_int32]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -232,6 +233,15 @@ class Model:
         (spins 0: back to normal); see hc_test_bounded_waits."""
         self._check(self.lib.hc_test_bounded_waits(self.h, spins, extra_arrivals),
                     "test_bounded_waits")
+
+    def autotune(self, force=False):
+        """(launch shape in use, [ms per launch of each shape of the last
+        tuning]) of k_flow_route; force=True times the shapes now."""
+        shape = C.c_int32()
+        ms = (C.c_double * 9)()
+        self._check(self.lib.hc_autotune(self.h, 1 if force else 0, C.byref(shape), ms, 9),
+                    "autotune")
+        return shape.value, list(ms)
 
     def mass_reset(self):
         self._check(self.lib.hc_mass_reset(self.h), "mass_reset")

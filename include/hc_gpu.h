@@ -385,6 +385,16 @@ hc_status hc_get_run_stats(hc_ctx* ctx, int64_t* counts, double* host_ms, int32_
  * runs out: the way the tests check this path without a fault. */
 hc_status hc_test_bounded_waits(hc_ctx* ctx, int32_t spins, int32_t extra_arrivals);
 
+/* Launch-shape autotuner (no counterpart in the reference).  hc_run times
+ * k_flow_route's launch shapes (register budget and grid) on the live state
+ * the first time a context reaches a shape class (erosion terms, Manning's n
+ * field, wet-list length to a power of two; below 65,536 wet cells the
+ * default shape is kept) and caches the fastest per class for the process.
+ * The timing launches leave the model state as it was.  force != 0 times
+ * them now; *shape (optional) receives the shape in use, ms (optional, n
+ * doubles) the last timings per shape in ms per launch. */
+hc_status hc_autotune(hc_ctx* ctx, int32_t force, int32_t* shape, double* ms, int32_t n);
+
 /* Stream the context issues its work on (a cudaStream_t). */
 void* hc_stream(hc_ctx* ctx);
 
