@@ -364,7 +364,7 @@ double ms_since(std::chrono::steady_clock::time_point t0) {
 
 // the run state a hydro-only iteration reads and writes
 struct Checkpoint {
-  Dev h, qx, qy, mask, wet, cinx, ciny, dev;
+  Dev h, qx, qy, mask, border, wet, cinx, ciny, dev;
 };
 
 hc_status save_state(hc_ctx* c, Checkpoint& k, bool alloc) {
@@ -372,7 +372,8 @@ hc_status save_state(hc_ctx* c, Checkpoint& k, bool alloc) {
   const size_t N2 = v.N2, nc = (size_t)v.cin_cap + 2;
   if (alloc) {
     if (dmalloc(k.h, N2 * 8) || dmalloc(k.qx, N2 * 8) || dmalloc(k.qy, N2 * 8) ||
-        dmalloc(k.mask, N2) || dmalloc(k.wet, N2 * 4) || dmalloc(k.cinx, nc * 4) ||
+        dmalloc(k.mask, N2) || dmalloc(k.border, N2) || dmalloc(k.wet, N2 * 4) ||
+        dmalloc(k.cinx, nc * 4) ||
         dmalloc(k.ciny, nc * 4) || dmalloc(k.dev, sizeof(hc_dev)))
       return hc_fail(c, HC_ERR_NOMEM, "adjoint checkpoint: out of device memory");
   }
@@ -381,6 +382,7 @@ hc_status save_state(hc_ctx* c, Checkpoint& k, bool alloc) {
   cudaMemcpyAsync(k.qx.p, v.qx, N2 * 8, cudaMemcpyDeviceToDevice, s);
   cudaMemcpyAsync(k.qy.p, v.qy, N2 * 8, cudaMemcpyDeviceToDevice, s);
   cudaMemcpyAsync(k.mask.p, v.mask, N2, cudaMemcpyDeviceToDevice, s);
+  cudaMemcpyAsync(k.border.p, v.border, N2, cudaMemcpyDeviceToDevice, s);
   cudaMemcpyAsync(k.wet.p, v.wet, N2 * 4, cudaMemcpyDeviceToDevice, s);
   cudaMemcpyAsync(k.cinx.p, v.cin_x, nc * 4, cudaMemcpyDeviceToDevice, s);
   cudaMemcpyAsync(k.ciny.p, v.cin_y, nc * 4, cudaMemcpyDeviceToDevice, s);
@@ -396,6 +398,7 @@ hc_status load_state(hc_ctx* c, Checkpoint& k) {
   cudaMemcpyAsync(v.qx, k.qx.p, N2 * 8, cudaMemcpyDeviceToDevice, s);
   cudaMemcpyAsync(v.qy, k.qy.p, N2 * 8, cudaMemcpyDeviceToDevice, s);
   cudaMemcpyAsync(v.mask, k.mask.p, N2, cudaMemcpyDeviceToDevice, s);
+  cudaMemcpyAsync(v.border, k.border.p, N2, cudaMemcpyDeviceToDevice, s);
   cudaMemcpyAsync(v.wet, k.wet.p, N2 * 4, cudaMemcpyDeviceToDevice, s);
   cudaMemcpyAsync(v.cin_x, k.cinx.p, nc * 4, cudaMemcpyDeviceToDevice, s);
   cudaMemcpyAsync(v.cin_y, k.ciny.p, nc * 4, cudaMemcpyDeviceToDevice, s);

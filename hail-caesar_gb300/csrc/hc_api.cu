@@ -281,7 +281,7 @@ extern "C" hc_status hc_create(const hc_params* p, size_t max_bytes, hc_ctx** ou
   if (st == HC_OK) st = dalloc(c, &(ptr), (n));
   A(v.elev, N2) A(v.h, N2) A(v.qx, N2) A(v.qy, N2) A(v.qxs, N2) A(v.qys, N2) A(v.vs, N2)
   A(v.vel, N2) A(v.tau, N2) A(v.bed, N2) A(v.man, N2) A(v.area, N2) A(v.ss, N2)
-  A(v.vd, 4 * N2) A(v.index, N2) A(v.mask, N2) A(v.rfarea, N2)
+  A(v.vd, 4 * N2) A(v.index, N2) A(v.mask, N2) A(v.border, N2) A(v.rfarea, N2)
   A(v.edge, E2) A(v.edge2, E2) A(v.veg, 4 * E2)
   A(v.cin_x, (size_t)p->imax * p->jmax + 2) A(v.cin_y, (size_t)p->imax * p->jmax + 2)
   A(v.wet, N2) A(v.wet_sums, (N2 + 1023) / 1024 + 1)
@@ -327,6 +327,7 @@ extern "C" hc_status hc_create(const hc_params* p, size_t max_bytes, hc_ctx** ou
   cudaMemsetAsync(v.vd, 0, 4 * N2 * 8, s);
   fill_i(c, v.index, N2, -9999);
   cudaMemsetAsync(v.mask, 0, N2, s);
+  cudaMemsetAsync(v.border, 0, N2, s);
   fill_i(c, v.rfarea, N2, 1);
   cudaMemsetAsync(v.edge, 0, E2 * 8, s);
   cudaMemsetAsync(v.edge2, 0, E2 * 8, s);
@@ -378,7 +379,7 @@ static hc_status free_all(hc_ctx* c) {
                   v.edge, v.edge2, v.veg, v.cin_x, v.cin_y, v.erodetot, v.erodetot3, v.pre,
                   v.chains, v.ent_list, v.ent_qs, v.drain_pos, v.drain_f0, v.drain_f1, v.drain_pend, v.drain_dt, v.drain_frac, v.drain_multi,
                   v.drain_snap, v.drain_aux, v.alloc_key, v.red, v.touched, v.topm, v.rain, v.rec, c->dev, v.wet,
-                  v.wet_sums, v.vpart, v.sdirty,
+                  v.wet_sums, v.vpart, v.sdirty, v.border,
                   v.reach[0], v.reach[1], v.reach[2], extra(c).lateral};
   for (void* q : ptrs)
     if (q) cudaFree(q);

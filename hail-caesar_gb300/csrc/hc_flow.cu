@@ -572,14 +572,12 @@ __global__ void __launch_bounds__(256) k_depth_update(const hc_view c, hc_dev* d
   double edge = 0;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nw; k += gridDim.x * blockDim.x) {
     const size_t cell = (size_t)c.wet[k];
-    {
+    if (c.border[cell]) {  // k_wet_write marks the listed cells on the border
       const uint8_t mu = c.mask[cell - W], md = c.mask[cell + W], ml = c.mask[cell - 1],
                     mr = c.mask[cell + 1];
-      if (!(mu & md & ml & mr)) {
-        const double ux1 = md ? 0.0 : c.qx[cell + W], ux0 = mu ? 0.0 : c.qx[cell];
-        const double uy1 = mr ? 0.0 : c.qy[cell + 1], uy0 = ml ? 0.0 : c.qy[cell];
-        edge += ddiv_by(dt * (ux1 - ux0 + uy1 - uy0), c.dxd);
-      }
+      const double ux1 = md ? 0.0 : c.qx[cell + W], ux0 = mu ? 0.0 : c.qx[cell];
+      const double uy1 = mr ? 0.0 : c.qy[cell + 1], uy0 = ml ? 0.0 : c.qy[cell];
+      edge += ddiv_by(dt * (ux1 - ux0 + uy1 - uy0), c.dxd);
     }
     double h = c.h[cell];
     h += ddiv_by(dt * (c.qx[cell + W] - c.qx[cell] + c.qy[cell + 1] - c.qy[cell]), c.dxd);
@@ -736,6 +734,10 @@ __global__ void __launch_bounds__(1024) k_wet_write(const hc_view c, const hc_de
   }
   __syncthreads();
   if (v) c.wet[c.wet_sums[blockIdx.x] + wb[warp] + incl - 1] = (int32_t)i;
+  // the wet list's border (listed cells are in rows 1..imax, columns
+  // 1..jmax, so their four neighbours lie inside the padded grid)
+  if (i < c.N2)
+    c.border[i] = v && !(c.mask[i - 1] && c.mask[i + 1] && c.mask[i - c.W] && c.mask[i + c.W]);
 }
 
 // ---------------------------------------------------------------------------

@@ -143,6 +143,7 @@ struct hc_view {
   double *strata;    // 10 * 9 * N2
   int32_t *index;
   uint8_t *mask;
+  uint8_t *border;   // N2: 1 where a listed cell has an unlisted 4-neighbour (wet-list border)
   int32_t *rfarea;
   double *edge, *edge2, *veg;  // E2, E2, 4*E2 (reference layout)
   int32_t *cin_x, *cin_y;      // catchment input points (1-based lists)
