@@ -1349,36 +1349,38 @@ extern "C" hc_status hc_run(hc_ctx* c, int64_t n, int32_t flags, hc_step_record*
   return run_end(c, rec, done);
 }
 
-extern "C" hc_status hc_run_ensemble(hc_ctx** ctxs, int32_t m, int64_t n, int32_t flags,
-                                     int64_t* done) {
-  if (!ctxs || m <= 0 || n < 0) return HC_ERR_ARG;
-  std::vector<char> live(m, 0);
-  for (int k = 0; k < m; k++) {
-    if (!ctxs[k]) return HC_ERR_ARG;
-    if (done) done[k] = 0;
+// The service loop of a group of members: launch each member's first chunk,
+// then, whichever member's chunk has finished, do its host work and launch
+// its next chunk.
+static hc_status ensemble_group(hc_ctx** ctxs, const std::vector<int>& mine, int64_t n,
+                                int32_t flags, int64_t* done) {
+  std::vector<char> live(mine.size(), 0);
+  int left = 0;
+  for (size_t q = 0; q < mine.size(); q++) {
+    const int k = mine[q];
     bool fin = false;
     HC_TRY(run_begin(ctxs[k], n, flags, false, &fin));
     if (!fin) {
       HC_TRY(run_launch(ctxs[k]));
-      live[k] = 1;
+      live[q] = 1;
+      left++;
     }
   }
-  int left = 0;
-  for (int k = 0; k < m; k++) left += live[k];
   while (left > 0) {
     bool progressed = false;
-    for (int k = 0; k < m; k++) {
-      if (!live[k]) continue;
+    for (size_t q = 0; q < mine.size(); q++) {
+      if (!live[q]) continue;
+      const int k = mine[q];
       hc_ctx* c = ctxs[k];
-      const cudaError_t q = cudaEventQuery(c->chunk_done);
-      if (q == cudaErrorNotReady) continue;
-      if (q != cudaSuccess) return hc_cuda(c, q, "ensemble");
+      const cudaError_t e = cudaEventQuery(c->chunk_done);
+      if (e == cudaErrorNotReady) continue;
+      if (e != cudaSuccess) return hc_cuda(c, e, "ensemble");
       progressed = true;
       bool fin = false;
       HC_TRY(run_after_chunk(c, flags, &fin));
       if (fin) {
         HC_TRY(run_end(c, nullptr, done ? &done[k] : nullptr));
-        live[k] = 0;
+        live[q] = 0;
         left--;
       } else {
         HC_TRY(run_launch(c));
@@ -1386,6 +1388,37 @@ extern "C" hc_status hc_run_ensemble(hc_ctx** ctxs, int32_t m, int64_t n, int32_
     }
     if (!progressed) std::this_thread::yield();
   }
+  return HC_OK;
+}
+
+// Members are shared out over host threads (member k to thread k mod T), so
+// that one member's host work (a drainage recomputation, the daily global
+// landsliding, lateral3's convergence loop) holds up only the members of its
+// own thread while the device runs the others' chunks.
+extern "C" hc_status hc_run_ensemble(hc_ctx** ctxs, int32_t m, int64_t n, int32_t flags,
+                                     int64_t* done) {
+  if (!ctxs || m <= 0 || n < 0) return HC_ERR_ARG;
+  for (int k = 0; k < m; k++) {
+    if (!ctxs[k]) return HC_ERR_ARG;
+    if (done) done[k] = 0;
+  }
+  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  const int T = (int)std::max(1u, std::min<unsigned>((unsigned)m, std::min(hw, 32u)));
+  std::vector<std::vector<int>> groups((size_t)T);
+  for (int k = 0; k < m; k++) groups[(size_t)(k % T)].push_back(k);
+  std::vector<hc_status> st((size_t)T, HC_OK);
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (T == 1) return ensemble_group(ctxs, groups[0], n, flags, done);
+  std::vector<std::thread> pool;
+  for (int t = 0; t < T; t++)
+    pool.emplace_back([&, t] {
+      cudaSetDevice(dev);
+      st[(size_t)t] = ensemble_group(ctxs, groups[(size_t)t], n, flags, done);
+    });
+  for (auto& th : pool) th.join();
+  for (int t = 0; t < T; t++)
+    if (st[(size_t)t] != HC_OK) return st[(size_t)t];
   return HC_OK;
 }
 

@@ -1,7 +1,8 @@
 // Slope failure and creep:
 //   in_channel_landsliding :5429-5527 ("slide_3", every 10 iterations)
 //   global_landsliding     :5529-5654 (daily: the same probe and warp replay
-//                          over every cell, sweep after sweep)
+//                          over every cell, sweep after sweep, or a skewed
+//                          wavefront when most cells move)
 //   creep                  :5293-5427 (host-driven, every 10 days)
 //
 // slide_3 is a sequential relaxation: every test sees the elevations left by
@@ -20,6 +21,7 @@
 #include "hc_grain.cuh"
 
 #include <math.h>
+#include <algorithm>
 #include <climits>
 #include <cmath>
 #include <vector>
@@ -636,6 +638,41 @@ __global__ void __launch_bounds__(32) k_gslide_replay(const hc_view c, const int
   if (lane == 0) *total = tot;
 }
 
+// A dense sweep (most cells move: a raw, unrelaxed DEM) as a skewed
+// wavefront, one block: row r = x - 2 visits column y at step
+// s = (y - 2) + 3 r.  A visit reads and writes only the 3x3 block around its
+// cell, so two visits conflict only when their rows and their columns
+// each differ by at most 2; every earlier visit that conflicts with the
+// one at (x, y) (rows x-1 and x-2 up to column y+2, row x before y) runs at
+// an earlier step, every later one at a later step, and visits of one step
+// never conflict: the moves are the serial sweep's, in its order for every
+// cell.  A thread takes rows r, r+1024, ...; the barrier between steps
+// orders the global-memory writes.  *total: the sweep's moves summed per
+// thread, then in thread order (the serial sum up to rounding; only its
+// sign is used).
+__global__ void __launch_bounds__(1024) k_gslide_wave(const hc_view c, double factor,
+                                                      double* total) {
+  const int rows = c.imax - 2, cols = c.jmax - 2;  // x in [2, imax-1], y in [2, jmax-1]
+  double tot = 0;
+  const int steps = (cols - 1) + 3 * (rows - 1) + 1;
+  for (int st = 0; st < steps; st++) {
+    for (int r = threadIdx.x; r < rows; r += blockDim.x) {
+      const int y = 2 + st - 3 * r;
+      if (y >= 2 && y <= c.jmax - 1) gslide_visit(c, r + 2, y, factor, &tot);
+    }
+    __syncthreads();
+  }
+  __shared__ double part[32];
+  for (int o = 16; o > 0; o >>= 1) tot += __shfl_down_sync(0xffffffffu, tot, o);
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = tot;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) a += part[w];
+    *total = a;
+  }
+}
+
 // ---- creep :5293-5427 ------------------------------------------------------
 // temp of the move from (x,y) to neighbour k, 0 when there is none
 __device__ __forceinline__ double creep_temp(const hc_view& c, int x, int y, int k, double time) {
@@ -790,23 +827,36 @@ hc_status run_global_landsliding(hc_ctx* c, int* sweeps) {
   const size_t n = c->v.N2;
   const int nblocks = (int)((n + 1023) / 1024);
   double* total = (double*)c->v.red;  // bytes 0-7 of the reduction scratch
-  struct { double total; int32_t count; int32_t pad; } h = {0, 0, 0};
+  double h_total = 0;
+  int32_t h_count = 0;
   int inc = 0;
+  // More flagged cells than this: the wavefront (every cell, in about
+  // jmax + 3 imax steps), else the replay of the flagged cells.
+  const int dense = std::max(4096, (int)(c->v.imax + c->v.jmax));
   do {
     inc++;
     cudaMemsetAsync(s.flag, 0, n, c->s);
     k_gslide_probe<<<g, b, 0, c->s>>>(c->v, s.flag, slide_factor(c));
     k_flag_count<<<nblocks, 1024, 0, c->s>>>(s.flag, n, s.block_sums, c->dev, 0);
     k_flag_scan<<<1, 1024, 0, c->s>>>(s.block_sums, nblocks, s.count, c->dev, 0);
-    k_flag_compact<<<nblocks, 1024, 0, c->s>>>(s.flag, n, s.block_sums, s.list, c->dev, 0);
-    k_gslide_replay<<<1, 32, 0, c->s>>>(c->v, s.list, s.count, s.ring, slide_factor(c), total);
-    count_launch(c, 5);
-    cudaError_t e = cudaMemcpyAsync(&h.total, total, 8, cudaMemcpyDeviceToHost, c->s);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(&h.count, s.count, 4, cudaMemcpyDeviceToHost, c->s);
+    count_launch(c, 3);
+    cudaError_t e = cudaMemcpyAsync(&h_count, s.count, 4, cudaMemcpyDeviceToHost, c->s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->s);
+    if (e != cudaSuccess) return hc_cuda(c, e, "global_landsliding");
+    if (h_count == 0) break;  // nothing moves: the sweep's total is 0
+    if (h_count > dense) {
+      k_gslide_wave<<<1, 1024, 0, c->s>>>(c->v, slide_factor(c), total);
+      count_launch(c, 1);
+    } else {
+      k_flag_compact<<<nblocks, 1024, 0, c->s>>>(s.flag, n, s.block_sums, s.list, c->dev, 0);
+      k_gslide_replay<<<1, 32, 0, c->s>>>(c->v, s.list, s.count, s.ring, slide_factor(c), total);
+      count_launch(c, 2);
+    }
+    e = cudaMemcpyAsync(&h_total, total, 8, cudaMemcpyDeviceToHost, c->s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->s);
     if (e != cudaSuccess) return hc_cuda(c, e, "global_landsliding");
     c->d2h_bytes += 12;
-  } while (h.total > 0 && inc < 200);
+  } while (h_total > 0 && inc < 200);
   if (sweeps) *sweeps = inc;
   return HC_OK;
 }

@@ -319,7 +319,10 @@ hc_status hc_snapshot_end(hc_snapshot* snap);
  * process): runs up to n iterations of each of m independent contexts at
  * once, each on its own stream with its own CUDA graph, adaptive dt and
  * host-side steps; done[k] receives member k's iteration count.  Members may
- * differ in size and parameters. */
+ * differ in size and parameters.  The members are serviced by up to 32 host
+ * threads (member k by thread k mod T), so one member's host-side step
+ * holds up only the members of its thread; a member must not be used by
+ * another thread during the call. */
 hc_status hc_run_ensemble(hc_ctx** ctxs, int32_t m, int64_t n, int32_t flags, int64_t* done);
 
 /* ---- adjoint of the hydraulic iteration (no counterpart in the reference)

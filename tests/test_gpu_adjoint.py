@@ -13,7 +13,7 @@ import synth
 pytestmark = pytest.mark.gpu
 
 WARM, N, EVERY = 250, 160, 48
-REL = 1e-5     # central differences: the wider relative step
+REL = 1e-4     # central differences: the wider relative step
 TOL = 1e-6     # adjoint against finite differences, relative
 
 
@@ -117,9 +117,9 @@ def test_manning_gradient_32_directions(setup):
 
 
 def test_elevation_gradient_directions(setup_elev):
-    """Directions in the DEM against central finite differences.  The steps
-    stay far below the pit filling's 1e-4 m increments, which order the
-    cells of flats: 1e-3 m per unit of the direction, times REL."""
+    """Directions in the DEM against central finite differences: 1e-3 m per
+    unit of the direction, times REL (far below the jitter between
+    neighbours, so that no pair of beds changes order)."""
     case, target, rec, loss, ge = setup_elev
     z = case.elev
 
@@ -147,10 +147,16 @@ def elev_loss(case, elev_window, rec, target):
 
 @pytest.fixture(scope="module")
 def setup_elev(gpu_lib, setup):
-    case, target, rec, q, loss, gn, gr = setup
-    m = warm_model(case)
-    loss2, gn2, gr2, info, ge = m.adj_gradient(N, EVERY, target, elev=True)
-    assert loss2 == loss
+    """The DEM with a seeded jitter below 1 mm: the pit filling leaves flats
+    of exactly equal elevations, where max(e0, e1) has a kink that any
+    perturbation of one of the two cells crosses (a central difference
+    there averages the two one-sided derivatives)."""
+    case0, target, rec0, q, loss0, gn, gr = setup
+    case = base_case()
+    rng = np.random.default_rng(23)
+    case.elev = np.ascontiguousarray(case.elev + rng.uniform(0.0, 1e-3, case.elev.shape))
+    rec, _ = warm_model(case).adj_forward(N)
+    loss, gn2, gr2, info, ge = warm_model(case).adj_gradient(N, EVERY, target, elev=True)
     assert np.abs(ge).max() > 0
     return case, target, rec, loss, ge
 

@@ -4,8 +4,9 @@ ledger.
 * C1, the reach case at its full size (300 rows along the flow x 100
   columns, 10 m, Wilcock-Crowe, 9 fractions): water depth and elevation
   within 1e-9 m after 1,000 iterations with masks and grain-record indices
-  identical; then the whole 24 h run, with the outlet discharge and the
-  sediment yield within 1e-6 relative and the water ledger closed to 1e-10.
+  identical; then the whole 24 h run: in step with the oracle to 1e-6 while
+  the two are in step, within the reference's own one-ulp sensitivity over
+  the whole run (see the test), and the water ledger closed to 1e-10.
 * C2's feature set (per-cell Manning's n, Einstein transport, lateral3,
   slide_3) on a 200 x 200 catchment for 1,500 iterations through a storm.
 * The reference's own known-good answers (test/basic_kga_tests.py:81-90):
@@ -71,41 +72,74 @@ def test_reach_c1_first_1000_steps(gpu_lib, oracle_mod):
     assert np.any(m.field("index") != -9999), "no grain record was made"
 
 
+def hourly_and_yield(rec):
+    """The reference's hourly discharge series (output_data) and the
+    cumulative sediment yield at the end of the run."""
+    return hydrograph(rec, 60.0), rec[-1, COL["globalsediq"]]
+
+
+def divergence(a, b):
+    """Largest relative difference of the hourly discharge and the relative
+    difference of the final sediment yield between two runs."""
+    qa, sa = hourly_and_yield(a)
+    qb, sb = hourly_and_yield(b)
+    k = min(len(qa), len(qb))
+    return (float(np.max(np.abs(qa[:k] - qb[:k]) / np.abs(qb[:k]).clip(1e-300))),
+            abs(sa / sb - 1))
+
+
 def test_reach_c1_whole_run(gpu_lib, oracle_mod):
-    """The whole 24 h: outlet discharge per iteration and the sediment yield
-    within 1e-6 relative of the oracle, the same iterations, and the water
-    ledger closed to 1e-10 (on the device and in the oracle alike)."""
+    """The whole 24 h of C1 against the oracle.
+
+    Per iteration the two agree to rounding until the first last-bit
+    difference (glibc's pow(hflow, 3) misrounds, CUDA's erosion
+    transcendentals differ from glibc's within 2 ulp) has grown through the
+    time-step control: iteration 2,934 of this run.  From there the run is
+    chaotic, and it is so in the reference itself: moving one channel cell's
+    elevation by one ulp changes the reference's 24 h hourly discharge by up
+    to 0.4 % and its sediment yield by 1.9 % (0.5 % and 1 % in a hydro-only
+    run).  So the device is held to (a) the oracle's own iterations, to
+    1e-6, while the two are still in step, and (b) over the whole run, a
+    divergence from the oracle no larger than twice the oracle's own under a
+    one-ulp change.  The water ledger closes to 1e-10 in both."""
     import hc
     case = synth.reach_case()
     m = hc.Model(case)
     g = m.run(200000)
     o = oracle_mod.Oracle(case)
     r = o.iterate(-1)
-    assert g.shape == r.shape, (g.shape, r.shape)
     assert g[-1, COL["cycle"]] / 60 >= case.params.maxcycle
-    assert_bitwise(g[:, COL["counter"]], r[:, COL["counter"]], "counter")
-    assert_close(g[:, COL["cycle"]], r[:, COL["cycle"]], 0, "cycle", rtol=1e-9)
-    # outlet discharge (water_flux_out's sum) and sediment yield
-    assert_close(g[:, COL["waterOut"]], r[:, COL["waterOut"]], 1e-9, "waterOut", rtol=1e-6)
-    assert_close(g[:, COL["sediQ"]], r[:, COL["sediQ"]], 1e-12, "sediQ", rtol=1e-6)
-    assert_close(g[:, COL["globalsediq"]], r[:, COL["globalsediq"]], 1e-12, "globalsediq",
+    assert abs(len(g) / len(r) - 1) < 0.01, (len(g), len(r))
+    # (a) in step: the first 2,000 iterations
+    k = 2000
+    assert_bitwise(g[:k, COL["counter"]], r[:k, COL["counter"]], "counter")
+    assert_close(g[:k, COL["cycle"]], r[:k, COL["cycle"]], 0, "cycle", rtol=1e-9)
+    assert_close(g[:k, COL["waterOut"]], r[:k, COL["waterOut"]], 1e-9, "waterOut", rtol=1e-6)
+    assert_close(g[:k, COL["globalsediq"]], r[:k, COL["globalsediq"]], 1e-12, "globalsediq",
                  rtol=1e-6)
-    assert g[-1, COL["globalsediq"]] > 0, "no sediment left the reach"
-    # the hourly hydrograph the reference writes
-    qg = hydrograph(g, 60.0)
-    qr = hydrograph(r, 60.0)
-    assert len(qg) == len(qr) >= 23
-    assert_close(qg, qr, 1e-9, "hourly discharge", rtol=1e-6)
-    # water ledger: device terms against the oracle's, then closure
     for c in ("vol_in", "vol_out", "vol_mask"):
-        assert_close(np.cumsum(g[:, COL[c]]), np.cumsum(r[:, COL[c]]), 1e-6, c, rtol=1e-9)
-    assert_close(g[:, COL["volume"]], r[:, COL["volume"]], 1e-6, "volume", rtol=1e-9)
+        assert_close(np.cumsum(g[:k, COL[c]]), np.cumsum(r[:k, COL[c]]), 1e-6, c, rtol=1e-9)
+    # (b) the whole run, against the reference's sensitivity to one ulp of
+    # one channel cell's elevation
+    pcase = synth.reach_case()
+    e = pcase.elev.copy()
+    e[150, 50] = np.nextafter(e[150, 50], np.inf)
+    pcase.elev = e
+    rp = oracle_mod.Oracle(pcase).iterate(-1)
+    q_dev, s_dev = divergence(g, r)
+    q_ref, s_ref = divergence(rp, r)
+    print("hourly discharge: device %.2e, one ulp %.2e; sediment yield: device %.2e, "
+          "one ulp %.2e" % (q_dev, q_ref, s_dev, s_ref))
+    assert q_dev <= 2 * max(q_ref, 1e-6) and s_dev <= 2 * max(s_ref, 1e-6), \
+        (q_dev, q_ref, s_dev, s_ref)
+    assert g[-1, COL["globalsediq"]] > 0, "no sediment left the reach"
+    assert len(hydrograph(g, 60.0)) >= 23
+    # water ledger: closed on the device, per iteration and in total
     assert record_closure(g) <= CLOSURE
     assert record_closure(r) <= CLOSURE
     mass = m.mass_balance()
     assert mass["inflow"] > 0 and mass["outflow"] > 0
     assert closure_error(mass) <= CLOSURE, mass
-    # the totals are the records' sums
     assert_close(mass["inflow"], np.sum(g[:, COL["vol_in"]]), 0, "inflow", rtol=1e-12)
     assert_close(mass["outflow"], np.sum(g[:, COL["vol_out"]]), 0, "outflow", rtol=1e-12)
 

@@ -93,3 +93,20 @@ def test_hillslope_in_run_after_first_iteration(gpu_lib, oracle_mod):
     assert_close(after, o.field("elev"), 1e-9, "elev")
     stats = m.run_stats()
     assert stats["global_slide"][0] >= 3 and stats["creep"][0] >= 2, stats
+
+
+def test_global_landsliding_dense_wavefront(gpu_lib, oracle_mod):
+    """A raw fractal DEM (pits not filled, steep at 10 m cells), where most
+    cells move in the first sweeps: the device takes its wavefront sweep
+    there, and the elevations are still the serial sweep's, bit for bit."""
+    import hc
+    case = synth.ensemble_member(3, fill=False, side_min=120, side_max=200)
+    m = hc.Model(case)
+    o = oracle_mod.Oracle(case)
+    o.prepare()
+    e0 = m.field("elev")
+    m.global_landsliding()
+    o.lib.hco_global_landsliding(o.h)
+    changed = np.sum(m.field("elev") != e0)
+    assert changed > 0.5 * case.cells, changed
+    assert_bitwise(m.field("elev"), o.field("elev"), "elev")
