@@ -362,22 +362,18 @@ __device__ __forceinline__ int decide_gt(float a, float b) {
 // reference's FP64 expression is evaluated only when the estimate is within
 // 1e-4 of the threshold.  The branch taken - and so the result - is always
 // the reference's.
+// The face past the hflow gate: hflow (> hflow_threshold) and dA = a1 - a0
+// (the surface difference) as the gate formed them.
 template <bool kSusp, bool kVel>
-__device__ __forceinline__ void inertial_face(double& q, double& qs, double& vel_out, int& vdir,
-                                              double e0, double h0, double a0, double e1,
-                                              double h1, double a1, double v0, double v1,
-                                              double c0, double nn, double dt, int edge_slope,
-                                              const hc_view& c) {
+__device__ __forceinline__ void inertial_face_core(double& q, double& qs, double& vel_out,
+                                                   int& vdir, double hflow, double dA, double h0,
+                                                   double h1, double v0, double v1, double c0,
+                                                   double nn, double dt, int edge_slope,
+                                                   const hc_view& c) {
   const hc_params& p = c.p;
   const double DX = p.DX;
   vdir = 0;
-  double hflow = imax_d(a0, a1) - imax_d(e1, e0);
-  if (!(dkey(hflow) > c.thr_key)) {  // hflow > hflow_threshold
-    q = 0;
-    qs = 0;
-    return;
-  }
-  double slope = ddiv_by(a1 - a0, c.dxd);
+  double slope = ddiv_by(dA, c.dxd);
   if (edge_slope == 1) slope = p.edgeslope;
   if (edge_slope == -1) slope = zero_minus(p.edgeslope);
   const double ghd = kG * hflow * dt;
@@ -465,6 +461,23 @@ __device__ __forceinline__ void inertial_face(double& q, double& qs, double& vel
   q = qn;
 }
 
+template <bool kSusp, bool kVel>
+__device__ __forceinline__ void inertial_face(double& q, double& qs, double& vel_out, int& vdir,
+                                              double e0, double h0, double a0, double e1,
+                                              double h1, double a1, double v0, double v1,
+                                              double c0, double nn, double dt, int edge_slope,
+                                              const hc_view& c) {
+  vdir = 0;
+  double hflow = imax_d(a0, a1) - imax_d(e1, e0);
+  if (!(dkey(hflow) > c.thr_key)) {  // hflow > hflow_threshold
+    q = 0;
+    qs = 0;
+    return;
+  }
+  inertial_face_core<kSusp, kVel>(q, qs, vel_out, vdir, hflow, a1 - a0, h0, h1, v0, v1, c0, nn,
+                                  dt, edge_slope, c);
+}
+
 template <bool kSed>
 __device__ __forceinline__ void flow_cell(const hc_view& c, const hc_dev* __restrict__ d,
                                           size_t cell) {
@@ -546,6 +559,142 @@ __global__ void __launch_bounds__(256, MINB) k_flow_route(const hc_view c,
   const int n = d->wet_count;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
     flow_cell<kSed>(c, d, (size_t)c.wet[k]);
+}
+
+// Face-compacted flow_route.  In a storm about half the listed cells are dry
+// and two faces in three fail the gate (both cells dry) or the hflow
+// threshold, so a warp evaluating its 32 cells' faces in turn issues the
+// FP64 instructions of a face with a third of its lanes.  Here each lane
+// first classifies its cell's two faces (the gate and hflow: two additions
+// and compares) and writes q = qs = 0 for gated faces below the threshold;
+// the faces that go on are queued in the warp's shared-memory queue (cell,
+// face, hflow, a1 - a0), and whenever 32 are queued the warp evaluates them
+// together, one per lane, the rest carried over to the next cells.  Every
+// face is evaluated from the same inputs by the same expressions as in
+// k_flow_route, so the results are the same bit for bit.
+constexpr int kFaceQ = 96;  // queue entries per warp: < 32 carried + 64 new
+
+template <bool kSed>
+__device__ __forceinline__ void face_work(const hc_view& c, const hc_dev* __restrict__ d,
+                                          uint32_t f, double hflow, double dA, double dt) {
+  const size_t W = c.W, N2 = c.N2;
+  const size_t cell = f >> 1;
+  const bool yface = f & 1u;
+  const size_t nb = yface ? cell - 1 : cell - W;
+  const int i = (int)(cell / W), j = (int)(cell - (size_t)i * W);
+  const hc_params& p = c.p;
+  const double n = p.spatially_var_mannings ? c.man[cell] : p.mannings;
+  const double nn = n * n;
+  const bool susp = kSed && p.isSuspended[1] != 0;
+  const double h0 = c.h[cell], h1 = c.h[nb];
+  const double v0 = susp ? c.vs[cell] : 0.0;
+  const double c0 = (susp && !deq0(v0)) ? ddiv_rn(v0, h0) : v0;
+  double* qa = yface ? c.qy : c.qx;
+  double* qsa = yface ? c.qys : c.qxs;
+  double q = qa[cell], qs = kSed ? qsa[cell] : 0.0, vel = 0;
+  int vdir;
+  const int es = yface ? ((j == c.jmax) ? 1 : ((j <= 2) ? -1 : 0))
+                       : ((i == c.imax) ? 1 : ((i <= 2) ? -1 : 0));
+  if (susp)
+    inertial_face_core<true, kSed>(q, qs, vel, vdir, hflow, dA, h0, h1, v0, c.vs[nb], c0, nn,
+                                   dt, es, c);
+  else
+    inertial_face_core<false, kSed>(q, qs, vel, vdir, hflow, dA, h0, h1, v0, 0.0, c0, nn, dt,
+                                    es, c);
+  qa[cell] = q;
+  if (kSed) {
+    qsa[cell] = qs;
+    // x face: vel_dir[x][y][7] / vel_dir[x-1][y][3]; y face: [x][y][1] / [x][y-1][5]
+    if (vdir == 1) c.vd[(yface ? 0 : 3) * N2 + cell] = vel;
+    if (vdir == -1) c.vd[(yface ? 2 : 1) * N2 + nb] = vel;
+  }
+}
+
+template <bool kSed, int MINB>
+__global__ void __launch_bounds__(256, MINB) k_flow_route_q(const hc_view c,
+                                                            const hc_dev* __restrict__ d,
+                                                            int gated) {
+  __shared__ uint32_t qf[8][kFaceQ];
+  __shared__ double qh[8][kFaceQ], qa[8][kFaceQ];
+  if (gated && !d->it_active) return;
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t* Q = qf[warp];
+  double* HF = qh[warp];
+  double* DA = qa[warp];
+  const int n = d->wet_count;
+  const double dt = d->s.flow_timestep;
+  const size_t W = c.W;
+  const int warps = gridDim.x * (blockDim.x >> 5);
+  int qn = 0;  // the same on every lane
+  for (int base = (blockIdx.x * (blockDim.x >> 5) + warp) * 32; base < n; base += warps * 32) {
+    const int k = base + lane;
+    bool fx = false, fy = false;
+    double hx = 0, hy = 0, ax = 0, ay = 0;
+    uint32_t cell = 0;
+    if (k < n) {
+      cell = (uint32_t)c.wet[k];
+      const double e0 = c.elev[cell];
+      if (dkey(e0) > kNoDataKey) {  // e > -9999
+        const double h0 = c.h[cell];
+        const double a0 = e0 + h0;
+        const bool wet0 = dgt0(h0);
+        {
+          const size_t up = cell - W;
+          const double h1 = c.h[up], e1 = c.elev[up];
+          if ((wet0 || dgt0(h1)) && dkey(e1) > kNoDataKey) {
+            const double a1 = e1 + h1;
+            hx = imax_d(a0, a1) - imax_d(e1, e0);
+            ax = a1 - a0;
+            fx = dkey(hx) > c.thr_key;
+            if (!fx) {
+              c.qx[cell] = 0;
+              if (kSed) c.qxs[cell] = 0;
+            }
+          }
+        }
+        {
+          const size_t lf = cell - 1;
+          const double h1 = c.h[lf], e1 = c.elev[lf];
+          if ((wet0 || dgt0(h1)) && dkey(e1) > kNoDataKey) {
+            const double a1 = e1 + h1;
+            hy = imax_d(a0, a1) - imax_d(e1, e0);
+            ay = a1 - a0;
+            fy = dkey(hy) > c.thr_key;
+            if (!fy) {
+              c.qy[cell] = 0;
+              if (kSed) c.qys[cell] = 0;
+            }
+          }
+        }
+      }
+    }
+    const unsigned bx = __ballot_sync(FULL, fx), by = __ballot_sync(FULL, fy);
+    const unsigned below = (1u << lane) - 1u;
+    const int nx = __popc(bx);
+    if (fx) {
+      const int s = qn + __popc(bx & below);
+      Q[s] = cell << 1;
+      HF[s] = hx;
+      DA[s] = ax;
+    }
+    if (fy) {
+      const int s = qn + nx + __popc(by & below);
+      Q[s] = (cell << 1) | 1u;
+      HF[s] = hy;
+      DA[s] = ay;
+    }
+    qn += nx + __popc(by);
+    __syncwarp();
+    while (qn >= 32) {
+      qn -= 32;
+      const uint32_t f = Q[qn + lane];
+      const double hf = HF[qn + lane], da = DA[qn + lane];
+      __syncwarp();  // the entries are read before the next cells' are written
+      face_work<kSed>(c, d, f, hf, da, dt);
+    }
+  }
+  if (lane < qn) face_work<kSed>(c, d, Q[lane], HF[lane], DA[lane], dt);
 }
 
 // ---------------------------------------------------------------------------
@@ -899,13 +1048,22 @@ static int list_blocks(const hc_ctx* c) {
 // multiprocessor (the register budget) and waves of the grid (grid = SMs x
 // blocks per SM x waves; one wave: every block resident at once).
 const FlowShape kFlowShapes[kFlowShapeCount] = {
-    {4, 0}, {3, 1}, {4, 1}, {5, 1}, {6, 1}, {3, 4}, {4, 4}, {5, 4}, {6, 4}};
+    {4, 0, 0}, {3, 1, 0}, {4, 1, 0}, {5, 1, 0}, {6, 1, 0}, {3, 4, 0}, {4, 4, 0}, {5, 4, 0},
+    {6, 4, 0}, {3, 1, 1}, {4, 1, 1}, {5, 1, 1}, {3, 4, 1}, {4, 4, 1}, {5, 4, 1}};
 
 template <bool kSed>
 static void flow_launch(hc_ctx* c, int gated, int shape) {
   const FlowShape f = kFlowShapes[shape];
   int blocks = f.waves ? c->sms * f.minb * f.waves : list_blocks(c);
   blocks = std::max(1, std::min(blocks, (int)((c->v.N2 + 255) / 256)));
+  if (f.compact) {
+    switch (f.minb) {
+      case 3: k_flow_route_q<kSed, 3><<<blocks, 256, 0, c->cs>>>(c->v, c->dev, gated); break;
+      case 5: k_flow_route_q<kSed, 5><<<blocks, 256, 0, c->cs>>>(c->v, c->dev, gated); break;
+      default: k_flow_route_q<kSed, 4><<<blocks, 256, 0, c->cs>>>(c->v, c->dev, gated); break;
+    }
+    return;
+  }
   switch (f.minb) {
     case 3: k_flow_route<kSed, 3><<<blocks, 256, 0, c->cs>>>(c->v, c->dev, gated); break;
     case 5: k_flow_route<kSed, 5><<<blocks, 256, 0, c->cs>>>(c->v, c->dev, gated); break;

@@ -234,6 +234,7 @@ struct hc_ctx {
   bool drain_retry;        // a drainage recomputation gave up: redo it first
   int sms;                 // multiprocessors of the device
   int flow_shape;          // launch shape of k_flow_route (kFlowShapes), autotuned
+  bool flow_pinned;        // the caller fixed flow_shape (hc_set_launch_shape)
   int64_t tuned_key;       // the shape class flow_shape was chosen for (-1: none)
   double tune_ms[16];      // the autotuner's times per shape (ms per launch)
   // called after every recomputation of the input points (adjoint replays)
@@ -672,10 +673,11 @@ void launch_wet_list(hc_ctx* c, int gated);  // rebuild the wet-cell list from t
 void launch_flux_out(hc_ctx* c, int gated, int record);
 // k_flow_route's launch shapes (hc_flow.cu) and the autotuner (hc_tune.cu)
 struct FlowShape {
-  int minb;   // blocks of 256 per multiprocessor (register budget)
-  int waves;  // grid = SMs x minb x waves; 0: the wet-list default grid
+  int minb;     // blocks of 256 per multiprocessor (register budget)
+  int waves;    // grid = SMs x minb x waves; 0: the wet-list default grid
+  int compact;  // 1: the face-compacted kernel (k_flow_route_q)
 };
-constexpr int kFlowShapeCount = 9;
+constexpr int kFlowShapeCount = 15;
 extern const FlowShape kFlowShapes[kFlowShapeCount];
 void launch_flow_route_shape(hc_ctx* c, int gated, int shape);
 hc_status autotune(hc_ctx* c, bool force);

@@ -48,6 +48,7 @@ struct Saved {
 }  // namespace
 
 hc_status autotune(hc_ctx* c, bool force) {
+  if (c->flow_pinned && !force) return HC_OK;
   const int wet = c->hdev->wet_count;
   if (!force && wet < (1 << 16)) return HC_OK;  // too little work to time; the default shape
   const int64_t key = shape_class(c, wet);
@@ -141,5 +142,18 @@ extern "C" hc_status hc_autotune(hc_ctx* c, int32_t force, int32_t* shape, doubl
   if (force) HC_TRY(autotune(c, true));
   if (shape) *shape = c->flow_shape;
   for (int k = 0; k < n && k < kFlowShapeCount; k++) ms[k] = c->tune_ms[k];
+  return HC_OK;
+}
+
+extern "C" hc_status hc_set_launch_shape(hc_ctx* c, int32_t shape) {
+  if (!c || shape < -1 || shape >= kFlowShapeCount) return HC_ERR_ARG;
+  if (shape < 0) {
+    c->flow_pinned = false;
+    c->tuned_key = -1;  // tune again at the next hc_run
+    return HC_OK;
+  }
+  if (shape != c->flow_shape) c->graph_iters = 0;
+  c->flow_shape = shape;
+  c->flow_pinned = true;
   return HC_OK;
 }

@@ -76,6 +76,7 @@ def load_library(path=LIB_PATH):
         "hc_mass_reset": (C.c_int, [vp]),
         "hc_test_bounded_waits": (C.c_int, [vp, C.c_int32, C.c_int32]),
         "hc_autotune": (C.c_int, [vp, C.c_int32, P(C.c_int32), P(C.c_double), C.c_int32]),
+        "hc_set_launch_shape": (C.c_int, [vp, C.c_int32]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -238,10 +239,14 @@ class Model:
         """(launch shape in use, [ms per launch of each shape of the last
         tuning]) of k_flow_route; force=True times the shapes now."""
         shape = C.c_int32()
-        ms = (C.c_double * 9)()
-        self._check(self.lib.hc_autotune(self.h, 1 if force else 0, C.byref(shape), ms, 9),
+        ms = (C.c_double * 15)()
+        self._check(self.lib.hc_autotune(self.h, 1 if force else 0, C.byref(shape), ms, 15),
                     "autotune")
         return shape.value, list(ms)
+
+    def set_launch_shape(self, shape):
+        """Fixes k_flow_route's launch shape (-1: the autotuner chooses)."""
+        self._check(self.lib.hc_set_launch_shape(self.h, shape), "set_launch_shape")
 
     def mass_reset(self):
         self._check(self.lib.hc_mass_reset(self.h), "mass_reset")

@@ -389,7 +389,8 @@ hc_status hc_get_run_stats(hc_ctx* ctx, int64_t* counts, double* host_ms, int32_
 hc_status hc_test_bounded_waits(hc_ctx* ctx, int32_t spins, int32_t extra_arrivals);
 
 /* Launch-shape autotuner (no counterpart in the reference).  hc_run times
- * k_flow_route's launch shapes (register budget and grid) on the live state
+ * k_flow_route's launch shapes (register budget, grid, and the face-compacted
+ * variant of the kernel) on the live state
  * the first time a context reaches a shape class (erosion terms, Manning's n
  * field, wet-list length to a power of two; below 65,536 wet cells the
  * default shape is kept) and caches the fastest per class for the process.
@@ -397,6 +398,9 @@ hc_status hc_test_bounded_waits(hc_ctx* ctx, int32_t spins, int32_t extra_arriva
  * them now; *shape (optional) receives the shape in use, ms (optional, n
  * doubles) the last timings per shape in ms per launch. */
 hc_status hc_autotune(hc_ctx* ctx, int32_t force, int32_t* shape, double* ms, int32_t n);
+/* Fixes k_flow_route's launch shape (0 .. 14; every shape computes the same
+ * results), or -1: back to the autotuner. */
+hc_status hc_set_launch_shape(hc_ctx* ctx, int32_t shape);
 
 /* Stream the context issues its work on (a cudaStream_t). */
 void* hc_stream(hc_ctx* ctx);
