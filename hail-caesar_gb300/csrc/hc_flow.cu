@@ -701,7 +701,7 @@ __global__ void __launch_bounds__(256, MINB) k_flow_route_q(const hc_view c,
 // depth_update :3259-3299 with the maxdepth reduction (warp shuffle, block,
 // then the last block publishes the grid result).
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_depth_update(const hc_view c, hc_dev* d, int gated) {
+__global__ void __launch_bounds__(256, 6) k_depth_update(const hc_view c, hc_dev* d, int gated) {
   __shared__ long long warp_max[8];
   __shared__ bool last;
   if (gated && !d->it_active) return;

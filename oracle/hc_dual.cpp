@@ -13,8 +13,10 @@
 // (the adjoint holds them fixed too); the input points are listed from the
 // drainage area as get_catchment_input_points (:3741-3767) does, again
 // whenever the baseflow threshold moves (:3524-3539).  The derivative seeds
-// are a direction in Manning's n.  Returns the number of outlet-Q samples,
-// the loss over them and its directional derivative.
+// are a direction in Manning's n (dman) and one in the elevations (delev;
+// either may be null); the branch tests use the values, as the adjoint's
+// recorded run does.  Returns the number of outlet-Q samples, the loss over
+// them and its directional derivative.
 
 #include <cmath>
 #include <cstdint>
@@ -42,7 +44,7 @@ inline D dmax(D a, D b) { return (a.v < b.v) ? b : a; }  // std::max
 
 extern "C" int hco_dual_run(
     int imax, int jmax, double DX, const double* elev, const double* man, const double* dman,
-    const int32_t* rfarea, double* h_io, double* qx_io, double* qy_io, uint8_t* mask_io,
+    const double* delev, const int32_t* rfarea, double* h_io, double* qx_io, double* qy_io, uint8_t* mask_io,
     const double* area, double baseflow, double min_q, double min_q_max, int rfnum,
     const double* nact,                            // per zone (0..16)
     int64_t n, const double* rec, int rec_stride,  // per iteration: [1] input dt, [2] flow dt, [3+z] j
@@ -52,8 +54,9 @@ extern "C" int hco_dual_run(
     double* loss, double* dloss) {
   const size_t W = (size_t)jmax + 2, N2 = (size_t)(imax + 2) * W;
   const double g = 9.81;
-  std::vector<D> h(N2), qx(N2), qy(N2), nn(N2);
+  std::vector<D> h(N2), qx(N2), qy(N2), nn(N2), E(N2);
   for (size_t k = 0; k < N2; k++) {
+    E[k] = D{elev[k], delev ? delev[k] : 0.0};
     h[k] = mk(h_io[k]);
     qx[k] = mk(qx_io[k]);
     qy[k] = mk(qy_io[k]);
@@ -83,9 +86,9 @@ extern "C" int hco_dual_run(
   };
   points();
   double prev = cycle0, counter = counter0;
-  auto face = [&](D q, double e0, D h0, double e1, D h1, D n2, double dt, int es) -> D {
-    const D a0 = mk(e0) + h0, a1 = mk(e1) + h1;
-    const D hflow = dmax(a0, a1) - dmax(mk(e1), mk(e0));
+  auto face = [&](D q, D e0, D h0, D e1, D h1, D n2, double dt, int es) -> D {
+    const D a0 = e0 + h0, a1 = e1 + h1;
+    const D hflow = dmax(a0, a1) - dmax(e1, e0);
     if (!(hflow.v > hflow_threshold)) return mk(0.0);
     D slope = (a1 - a0) / mk(DX);
     if (es == 1) slope = mk(edgeslope);
@@ -122,10 +125,10 @@ extern "C" int hco_dual_run(
         if (!mask[cell] || !(elev[cell] > -9999)) continue;
         const D n2 = nn[cell];
         if ((h[cell].v > 0 || h[cell - W].v > 0) && elev[cell - W] > -9999)
-          nqx[cell] = face(qx[cell], elev[cell], h[cell], elev[cell - W], h[cell - W], n2, fdt,
+          nqx[cell] = face(qx[cell], E[cell], h[cell], E[cell - W], h[cell - W], n2, fdt,
                            (i == imax) ? 1 : ((i <= 2) ? -1 : 0));
         if ((h[cell].v > 0 || h[cell - 1].v > 0) && elev[cell - 1] > -9999)
-          nqy[cell] = face(qy[cell], elev[cell], h[cell], elev[cell - 1], h[cell - 1], n2, fdt,
+          nqy[cell] = face(qy[cell], E[cell], h[cell], E[cell - 1], h[cell - 1], n2, fdt,
                            (j == jmax) ? 1 : ((j <= 2) ? -1 : 0));
       }
     qx.swap(nqx);
