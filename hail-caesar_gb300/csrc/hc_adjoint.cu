@@ -214,70 +214,63 @@ __global__ void k_adj_depth(const hc_view c, AdjBufs b, AdjStep st) {
 
 // flow_route reversed, per cell for its two faces: discharge adjoints
 // before the iteration, the depth terms each face passes to its two cells,
-// and the n gradient
-__global__ void k_adj_flow(const hc_view c, AdjBufs b, AdjStep st) {
-  const int j = 1 + blockIdx.x * blockDim.x + threadIdx.x;
-  const int i = 1 + blockIdx.y * blockDim.y + threadIdx.y;
-  if (i > c.imax || j > c.jmax) return;
-  const size_t W = c.W, cell = (size_t)i * W + j;
-  if (!(b.mask[cell] || b.mask[cell - W] || b.mask[cell - 1])) {
-    // no face of this cell moves, and no listed depth reads its discharges
-    if (b.pflag[cell]) {
-      b.p0x[cell] = b.p1x[cell] = b.p0y[cell] = b.p1y[cell] = 0;
-      b.pe0[cell] = b.pe1x[cell] = b.pe1y[cell] = 0;
-      b.pflag[cell] = 0;
-    }
-    return;
-  }
-  const double k = st.fdt / c.p.DX;
-  auto ml = [&](size_t q) { return b.mask[q] ? b.lamd[q] : 0.0; };
-  // depth_update reads qx[cell] (-) and, for the cell above, qx[cell] (+)
-  const double mux = b.mux[cell] + k * (ml(cell - W) - ml(cell));
-  const double muy = b.muy[cell] + k * (ml(cell - 1) - ml(cell));
+// the n and elevation gradients.  The cells whose faces need face_dq are
+// compacted: in a storm about half the listed cells are dry, so a warp
+// running its 32 cells' faces in place issues the FP64 work with a fraction
+// of its lanes.  Each lane first forms its cell's discharge adjoints (and
+// writes the cell out when it is no listed cell above no-data); the cells
+// that go on are queued per warp with their adjoints, and whenever 32 are
+// queued the warp runs their faces together, the rest carried over to the
+// warp's next 32 cells.  A cell's outputs are written once, by one lane.
+constexpr int kAdjQ = 64;  // < 32 carried + 32 new
+
+__device__ __forceinline__ void adj_cell_faces(const hc_view& c, const AdjBufs& b,
+                                               const AdjStep& st, size_t cell, double mux,
+                                               double muy) {
+  const size_t W = c.W;
+  const int i = (int)(cell / W), j = (int)(cell - (size_t)i * W);
+  const hc_params& p = c.p;
+  const double e0 = c.elev[cell];
+  const double n = p.spatially_var_mannings ? c.man[cell] : p.mannings;
+  const double nn = n * n;
+  auto hin = [&](size_t q) {
+    const int rf = c.rfarea[q];
+    double h = b.h0[q];
+    if (b.point[q] && rf >= 0 && rf <= HC_MAX_RF) h += st.amt[rf];
+    return h;
+  };
   double ox = mux, oy = muy, p0x = 0, p1x = 0, p0y = 0, p1y = 0, gn = 0;
   double pe0 = 0, pe1x = 0, pe1y = 0;
-  const double e0 = c.elev[cell];
-  if (b.mask[cell] && e0 > -9999) {
-    const hc_params& p = c.p;
-    const double n = p.spatially_var_mannings ? c.man[cell] : p.mannings;
-    const double nn = n * n;
-    auto hin = [&](size_t q) {
-      const int rf = c.rfarea[q];
-      double h = b.h0[q];
-      if (b.point[q] && rf >= 0 && rf <= HC_MAX_RF) h += st.amt[rf];
-      return h;
-    };
-    const double h0 = hin(cell);
-    {
-      const size_t up = cell - W;
-      const double h1 = hin(up), e1 = c.elev[up];
-      if ((h0 > 0 || h1 > 0) && e1 > -9999) {
-        const int es = (i == c.imax) ? 1 : ((i <= 2) ? -1 : 0);
-        const DQ r = face_dq(b.qx0[cell], e0, h0, e1, h1, nn, st.fdt, es, p, c.rDX, c.dxd);
-        ox = r.dq * mux;
-        p0x = r.dh0 * mux;
-        p1x = r.dh1 * mux;
-        gn += r.dnn * mux;
-        pe0 += r.de0 * mux;
-        pe1x = r.de1 * mux;
-      }
+  const double h0 = hin(cell);
+  {
+    const size_t up = cell - W;
+    const double h1 = hin(up), e1 = c.elev[up];
+    if ((h0 > 0 || h1 > 0) && e1 > -9999) {
+      const int es = (i == c.imax) ? 1 : ((i <= 2) ? -1 : 0);
+      const DQ r = face_dq(b.qx0[cell], e0, h0, e1, h1, nn, st.fdt, es, p, c.rDX, c.dxd);
+      ox = r.dq * mux;
+      p0x = r.dh0 * mux;
+      p1x = r.dh1 * mux;
+      gn += r.dnn * mux;
+      pe0 += r.de0 * mux;
+      pe1x = r.de1 * mux;
     }
-    {
-      const size_t lf = cell - 1;
-      const double h1 = hin(lf), e1 = c.elev[lf];
-      if ((h0 > 0 || h1 > 0) && e1 > -9999) {
-        const int es = (j == c.jmax) ? 1 : ((j <= 2) ? -1 : 0);
-        const DQ r = face_dq(b.qy0[cell], e0, h0, e1, h1, nn, st.fdt, es, p, c.rDX, c.dxd);
-        oy = r.dq * muy;
-        p0y = r.dh0 * muy;
-        p1y = r.dh1 * muy;
-        gn += r.dnn * muy;
-        pe0 += r.de0 * muy;
-        pe1y = r.de1 * muy;
-      }
-    }
-    b.gn[cell] += gn * 2 * n;
   }
+  {
+    const size_t lf = cell - 1;
+    const double h1 = hin(lf), e1 = c.elev[lf];
+    if ((h0 > 0 || h1 > 0) && e1 > -9999) {
+      const int es = (j == c.jmax) ? 1 : ((j <= 2) ? -1 : 0);
+      const DQ r = face_dq(b.qy0[cell], e0, h0, e1, h1, nn, st.fdt, es, p, c.rDX, c.dxd);
+      oy = r.dq * muy;
+      p0y = r.dh0 * muy;
+      p1y = r.dh1 * muy;
+      gn += r.dnn * muy;
+      pe0 += r.de0 * muy;
+      pe1y = r.de1 * muy;
+    }
+  }
+  b.gn[cell] += gn * 2 * n;
   b.mux[cell] = ox;
   b.muy[cell] = oy;
   b.p0x[cell] = p0x;
@@ -288,6 +281,68 @@ __global__ void k_adj_flow(const hc_view c, AdjBufs b, AdjStep st) {
   b.pe1x[cell] = pe1x;
   b.pe1y[cell] = pe1y;
   b.pflag[cell] = 1;
+}
+
+__global__ void __launch_bounds__(256, 3) k_adj_flow_c(const hc_view c, AdjBufs b, AdjStep st) {
+  __shared__ uint32_t qc[8][kAdjQ];
+  __shared__ double qx_[8][kAdjQ], qy_[8][kAdjQ];
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t* Q = qc[warp];
+  double* MX = qx_[warp];
+  double* MY = qy_[warp];
+  const size_t W = c.W;
+  const int cpr = (c.jmax + 31) / 32;  // chunks of 32 columns per row
+  const long long chunks = (long long)c.imax * cpr;
+  const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
+  const double k = st.fdt / c.p.DX;
+  int qn = 0;  // the same on every lane
+  for (long long ch = (long long)blockIdx.x * (blockDim.x >> 5) + warp; ch < chunks; ch += warps) {
+    const int i = 1 + (int)(ch / cpr);
+    const int j = 1 + (int)(ch % cpr) * 32 + lane;
+    bool go = false;
+    size_t cell = 0;
+    double mux = 0, muy = 0;
+    if (j <= c.jmax) {
+      cell = (size_t)i * W + j;
+      if (!(b.mask[cell] || b.mask[cell - W] || b.mask[cell - 1])) {
+        if (b.pflag[cell]) {
+          b.p0x[cell] = b.p1x[cell] = b.p0y[cell] = b.p1y[cell] = 0;
+          b.pe0[cell] = b.pe1x[cell] = b.pe1y[cell] = 0;
+          b.pflag[cell] = 0;
+        }
+      } else {
+        auto ml = [&](size_t q) { return b.mask[q] ? b.lamd[q] : 0.0; };
+        mux = b.mux[cell] + k * (ml(cell - W) - ml(cell));
+        muy = b.muy[cell] + k * (ml(cell - 1) - ml(cell));
+        go = b.mask[cell] && c.elev[cell] > -9999;
+        if (!go) {
+          b.mux[cell] = mux;
+          b.muy[cell] = muy;
+          b.p0x[cell] = b.p1x[cell] = b.p0y[cell] = b.p1y[cell] = 0;
+          b.pe0[cell] = b.pe1x[cell] = b.pe1y[cell] = 0;
+          b.pflag[cell] = 1;
+        }
+      }
+    }
+    const unsigned bg = __ballot_sync(FULL, go);
+    if (go) {
+      const int s = qn + __popc(bg & ((1u << lane) - 1u));
+      Q[s] = (uint32_t)cell;
+      MX[s] = mux;
+      MY[s] = muy;
+    }
+    qn += __popc(bg);
+    __syncwarp();
+    if (qn >= 32) {
+      qn -= 32;
+      const uint32_t q = Q[qn + lane];
+      const double mx = MX[qn + lane], my = MY[qn + lane];
+      __syncwarp();
+      adj_cell_faces(c, b, st, q, mx, my);
+    }
+  }
+  if (lane < qn) adj_cell_faces(c, b, st, Q[lane], MX[lane], MY[lane]);
 }
 
 // the depth adjoint before the iteration (inputs add a constant), and the
@@ -812,7 +867,7 @@ extern "C" hc_status hc_adj_gradient(hc_ctx* c, int64_t n, int32_t max_states,
         st.damt[z] = da;
       }
       k_adj_depth<<<gr, b, 0, s>>>(v, bb, st);
-      k_adj_flow<<<gr, b, 0, s>>>(v, bb, st);
+      k_adj_flow_c<<<c->sms * 3, 256, 0, s>>>(v, bb, st);
       k_adj_gather<<<gr, b, 0, s>>>(v, bb, st);
     }
     HC_CU(cudaGetLastError(), "adjoint kernels");
