@@ -389,7 +389,8 @@ static hc_status free_all(hc_ctx* c) {
   sort_work_free(c->sort_work);
   free(extra(c).h_rain);
   if (c->graph) cudaGraphExecDestroy(c->graph);
-  if (c->graph1) cudaGraphExecDestroy(c->graph1);
+  for (auto& t : c->tail)
+    if (t) cudaGraphExecDestroy(t);
   if (c->chunk_done) cudaEventDestroy(c->chunk_done);
   if (c->s) cudaStreamDestroy(c->s);
   if (c->s2) cudaStreamDestroy(c->s2);
@@ -1116,9 +1117,11 @@ static hc_status capture_iteration(hc_ctx* c, int flags) {
   return HC_OK;
 }
 
-static int graph_chunk() {
+// iterations per chunk graph: HC_GRAPH_ITERS if set, else what the caller
+// asked for (hc_run_ensemble: 128), else 32
+static int graph_chunk(const hc_ctx* c) {
   const char* e = getenv("HC_GRAPH_ITERS");
-  int k = e ? atoi(e) : 32;
+  int k = e ? atoi(e) : (c->chunk_pref > 0 ? c->chunk_pref : 32);
   return std::max(1, std::min(k, 4096));
 }
 
@@ -1159,13 +1162,17 @@ static hc_status build_one(hc_ctx* c, int flags, int K, cudaGraphExec_t* exec,
   return HC_OK;
 }
 
-// The chunk graph (K iterations) and a one-iteration graph for the tail of
-// a run shorter than K (a paused chunk skips the rest of its iterations, so
-// short runs would pay for K).
+// The chunk graph (K iterations).  Runs shorter than K take the graphs of
+// 2^k iterations (made when first needed; a paused chunk skips the rest of
+// its iterations, so short runs would pay for K).
 static hc_status build_graph(hc_ctx* c, int flags) {
-  const int K = graph_chunk();
+  const int K = graph_chunk(c);
+  for (auto& t : c->tail)
+    if (t) {
+      cudaGraphExecDestroy(t);
+      t = nullptr;
+    }
   HC_TRY(build_one(c, flags, K, &c->graph, &c->graph_kernels));
-  HC_TRY(build_one(c, flags, 1, &c->graph1, &c->graph1_kernels));
   c->graph_iters = K;
   c->graph_flags = flags;
   return HC_OK;
@@ -1277,7 +1284,8 @@ static hc_status run_begin(hc_ctx* c, int64_t n, int32_t flags, bool want_rec, b
     HC_TRY(pull(c));
   }
   HC_TRY(autotune(c, false));  // launch shapes for this shape class (hc_tune.cu)
-  if (!c->graph_iters || c->graph_flags != flags) HC_TRY(build_graph(c, flags));
+  if (!c->graph_iters || c->graph_flags != flags || c->graph_iters != graph_chunk(c))
+    HC_TRY(build_graph(c, flags));
   if (!c->chunk_done) HC_CU(cudaEventCreateWithFlags(&c->chunk_done, cudaEventDisableTiming),
                             "event");
   return HC_OK;
@@ -1288,10 +1296,18 @@ static hc_status run_launch(hc_ctx* c) {
   c->body_k0 = c->hdev->body_kernels;
   c->budget0 = c->hdev->budget;
   c->stat_n[HC_STAT_CHUNKS]++;
-  const bool small = c->budget0 < c->graph_iters;
-  c->chunk_iters = small ? 1 : c->graph_iters;
-  HC_CU(cudaGraphLaunch(small ? c->graph1 : c->graph, c->s), "graph launch");
-  c->launches += small ? c->graph1_kernels : c->graph_kernels;
+  if (c->budget0 >= c->graph_iters) {
+    c->chunk_iters = c->graph_iters;
+    HC_CU(cudaGraphLaunch(c->graph, c->s), "graph launch");
+    c->launches += c->graph_kernels;
+  } else {
+    int k = 0;
+    while (k + 1 < 12 && (2LL << k) <= c->budget0) k++;
+    if (!c->tail[k]) HC_TRY(build_one(c, c->graph_flags, 1 << k, &c->tail[k], &c->tail_kernels[k]));
+    c->chunk_iters = 1 << k;
+    HC_CU(cudaGraphLaunch(c->tail[k], c->s), "graph launch");
+    c->launches += c->tail_kernels[k];
+  }
   c->d2h_bytes += sizeof(hc_dev);
   HC_CU(cudaMemcpyAsync(c->hdev, c->dev, sizeof(hc_dev), cudaMemcpyDeviceToHost, c->s), "pull");
   HC_CU(cudaEventRecord(c->chunk_done, c->s), "event");
@@ -1402,6 +1418,8 @@ extern "C" hc_status hc_run_ensemble(hc_ctx** ctxs, int32_t m, int64_t n, int32_
     if (!ctxs[k]) return HC_ERR_ARG;
     if (done) done[k] = 0;
   }
+  // longer chunks: fewer host turns per member while the others run
+  for (int k = 0; k < m; k++) ctxs[k]->chunk_pref = 128;
   const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
   const int T = (int)std::max(1u, std::min<unsigned>((unsigned)m, std::min(hw, 32u)));
   std::vector<std::vector<int>> groups((size_t)T);

@@ -243,8 +243,11 @@ struct hc_ctx {
   // CUDA graph of K iterations
   cudaGraphExec_t graph; int graph_iters; int graph_flags;
   int64_t graph_kernels;   // kernel nodes in the graph
-  cudaGraphExec_t graph1;  // the same for one iteration
-  int64_t graph1_kernels;
+  // graphs of 2^k iterations (k < 12) for runs shorter than a chunk, made
+  // when first needed: a short run takes the fewest launches (20 = 16 + 4)
+  cudaGraphExec_t tail[12];
+  int64_t tail_kernels[12];
+  int chunk_pref;          // iterations per chunk graph asked for (0: the default)
   int chunk_iters;         // iterations in the chunk last launched
   cudaEvent_t chunk_done;  // a launched chunk and its control-block copy are done
   int64_t run_n;           // iterations asked of the current run

@@ -133,11 +133,13 @@ def test_elevation_gradient_directions(setup_elev):
 
     def f_of(seed):
         v = direction(seed)
-        return lambda h: elev_loss(case, z + h * v, rec, target)
+        # a quarter of the n directions' step: at REL the input points
+        # already change (an area crosses MIN_Q) in most directions
+        return lambda h: elev_loss(case, z + (h / 4) * v, rec, target)
 
     def ad_of(seed):
-        return float(np.sum(ge[1:-1, 1:-1] * direction(seed)))
-    check_directions(ad_of, f_of, range(12), need=0)
+        return float(np.sum(ge[1:-1, 1:-1] * direction(seed))) / 4
+    check_directions(ad_of, f_of, range(12), need=4)
 
 
 def elev_loss(case, elev_window, rec, target):
