@@ -181,9 +181,11 @@ def log(msg):
 #       --profile-skip 20  under  ncu --clock-control none -k regex:k_flow_route
 #       -c 1 --metrics dram__bytes_read.sum,dram__bytes_write.sum,
 #       sm__inst_executed_pipe_fp64.sum,sm__pipe_fp64_cycles_active.sum
-FLOW_CAPTURE = {"dram_bytes_per_wet_cell": 121.6, "fp64_warp_inst_per_wet_cell": None,
-                "source": "ncu capture of k_flow_route, catchment 1400x1400 at the "
-                          "same spin-up, scaled by this launch's wet cells"}
+FLOW_CAPTURE = {"dram_bytes_per_wet_cell": 115.0, "fp64_warp_inst_per_wet_cell": 1.048,
+                "source": "ncu capture of k_flow_route_q (face-compacted), catchment "
+                          "1400x1400, 500-iteration spin-up + 25 iterations, 1,663,494 wet "
+                          "cells: 191.3 MB DRAM, 1.743 M FP64 warp instructions; scaled by "
+                          "this launch's wet cells"}
 FP64_LANES_PER_CLK_SM = 2  # this GPU's FP64 pipe: a warp instruction takes 16 cycles
 
 
@@ -293,7 +295,9 @@ def run_gpu(args, rank, world, dist):
     e2e_steps = max(3, min(args.steps, 200))
     twin = hc.Model(case)
     spin_up(twin, spin_its, flags)
-    twin.run(args.warmup, flags, records=False)
+    # warm-up with records: the record buffer and the graphs that use it
+    # exist before the timed calls
+    twin.run(args.warmup, flags, records=True)
     torch.cuda.synchronize()
     _, h0, d0 = twin.counters()
     t0 = time.perf_counter()
@@ -399,6 +403,17 @@ def run_ensemble_bench(args, rank):
     torch.cuda.synchronize()
     t_ens = time.perf_counter() - t0
     clk = clocks.stop()
+    # then per member, after the timed runs (each call returns after its
+    # member's last iteration): the fixed cost per iteration against the
+    # per-cell cost, least squares
+    per = []
+    for c_, m in zip(cases, models):
+        t1 = time.perf_counter()
+        m.run(k, 0, records=False)
+        per.append((c_.cells, (time.perf_counter() - t1) * 1e3 / k))
+    A = np.array([[1.0, c_] for c_, _ in per])
+    fixed_ms, per_cell_ms = np.linalg.lstsq(A, np.array([t for _, t in per]), rcond=None)[0]
+    log("plain per member: ms/iteration = %.4f + %.3e x cells" % (fixed_ms, per_cell_ms))
     steps_plain = sum(c.cells * d for c, d in zip(cases, done_plain))
     steps_ens = sum(c.cells * d for c, d in zip(cases, done))
     value = steps_ens / t_ens
@@ -413,6 +428,7 @@ def run_ensemble_bench(args, rank):
                        "parallelism": "one stream + graph per member",
                        "timing": "host clock between device synchronisations"},
             "clocks": clk, "plain_value": steps_plain / t_plain,
+            "plain_ms_per_iteration_fit": {"fixed": fixed_ms, "per_mcell": per_cell_ms * 1e6},
             "batched_over_plain": (steps_ens / t_ens) / (steps_plain / t_plain)}
 
 
@@ -456,7 +472,9 @@ def run_adjoint_bench(args):
                                                                            case.params.jmax)},
             "forward_ms": t_fwd * 1e3, "forward_cell_steps_per_s": cells * n_it / t_fwd,
             "gradient_ms": {"forward_checkpointed": info["forward_ms"],
-                            "reverse": info["reverse_ms"], "total": info["total_ms"]},
+                            "reverse": info["reverse_ms"], "total": info["total_ms"],
+                            "reverse_replays": info["replay_ms"],
+                            "reverse_adjoint_iterations": info["adjoint_iterations_ms"]},
             "checkpointing": {"max_states": args.adj_states, "segment": info["segment"],
                               "snapshots": info["snapshots"],
                               "iterations_advanced_again": info["advanced"]},

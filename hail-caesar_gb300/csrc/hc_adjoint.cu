@@ -15,15 +15,19 @@
 // recorded values (they are piecewise constant in the parameters).  The
 // rain enters through TOPMODEL's j (host_topmodel_tangent).
 //
-// Memory: the state (h, qx, qy and the small run state) is checkpointed
-// every K iterations during the forward run; the reverse pass replays one
-// segment at a time from its checkpoint, keeping every iteration's state
-// of the segment, and runs the adjoint iterations backwards through it.
+// Memory: the state (h, qx, qy and the small run state) is checkpointed at
+// segment starts (every K iterations, binomial schedule) during the forward
+// run; the reverse pass replays one segment at a time from its checkpoint,
+// keeping every iteration's state of the segment, and runs the adjoint
+// iterations backwards through it.  With two slot sets, the replay of a
+// segment (the model's stream) overlaps the adjoint iterations of the
+// segment after it (a second stream).
 
 #include "hc_internal.cuh"
 
 #include <chrono>
 #include <functional>
+#include <memory>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -56,45 +60,59 @@ __device__ __forceinline__ int decide(float a, float b) {
   return 0;
 }
 
+// The depth limits' exact tests (:3138, :3144), out of line: the float
+// estimate decides almost every face, and inlined, these FP64 instructions
+// would take FP64 issue slots at every call site whether they run or not.
+static __device__ __noinline__ bool adj_depth_exceeds(double qn, double dt, double DX, double h) {
+  return (qn * dt / DX) > (h / 4);
+}
+static __device__ __noinline__ bool adj_depth_exceeds_neg(double qn, double dt, double DX,
+                                                          double h) {
+  return fabs(qn * dt / DX) > (h / 4);
+}
+
 // One face (:3096-3191), as the device evaluates it, with derivatives.
 // The value and the branch decisions are the forward kernel's (exact FP64
 // where a branch is decided, float estimates first, as there); the
-// derivatives, which need no exact rounding, use reciprocals.
-__device__ DQ face_dq(double q, double e0, double h0, double e1, double h1, double nn, double dt,
-                      int es, const hc_params& p, double rDX, const hc_divisor& dxd) {
+// derivatives, which need no exact rounding, use reciprocals.  hflow =
+// max(surfaces) - max(beds) and dA = a1 - a0 come from the caller (which
+// decided hflow > hflow_threshold), with e0max = (e1 < e0); a1 > a0 exactly
+// when dA > 0.  h0 and h1 are read only by the depth limits.  Comparisons
+// run on the integer pipe (dkey etc.), as in the forward kernel.
+template <class H0, class H1>
+__device__ DQ face_dq(double q, double hflow, double dA, bool e0max, H0 h0f, H1 h1f, double nn,
+                      double dt, int es, const hc_params& p, double rDX, const hc_divisor& dxd,
+                      float DXf, float flf) {
   const double DX = p.DX;
   DQ r = {0, 0, 0, 0, 0, 0, 0};
-  const double a0 = e0 + h0, a1 = e1 + h1;
-  const bool a1max = a0 < a1;
-  const double hflow = smax(a0, a1) - smax(e1, e0);
-  if (!(hflow > p.hflow_threshold)) return r;  // q = 0
+  const bool a1max = dgt0(dA);
   // hflow = max(surfaces) - max(beds): its derivatives by the depths, and
   // by the elevations (through both maxima)
   const double dhf0 = a1max ? 0.0 : 1.0, dhf1 = a1max ? 1.0 : 0.0;
-  const bool e0max = e1 < e0;
   const double dhfe0 = dhf0 - (e0max ? 1.0 : 0.0), dhfe1 = dhf1 - (e0max ? 0.0 : 1.0);
-  double slope = ddiv_by(a1 - a0, dxd), ds0 = -rDX, ds1 = rDX;
+  double slope = ddiv_by(dA, dxd), ds0 = -rDX, ds1 = rDX;
   if (es == 1) slope = p.edgeslope, ds0 = ds1 = 0;
-  if (es == -1) slope = 0 - p.edgeslope, ds0 = ds1 = 0;
+  if (es == -1) slope = zero_minus(p.edgeslope), ds0 = ds1 = 0;
   const double ghd = kG * hflow * dt;
   const double rhf = ddiv_rn(1.0, hflow);
   // qn and its derivatives with respect to q, hflow, slope, nn
   double qn, d_q, d_hf, d_s, d_nn;
-  if (q == 0) {
+  if (deq0(q)) {
     qn = q - (ghd * slope);
     d_q = 1;
     d_hf = -kG * dt * slope;
     d_s = -ghd;
     d_nn = 0;
   } else {
+    const double aq = __longlong_as_double(dbits(q) & 0x7fffffffffffffffLL);  // fabs
     const double c3 = icube_rn(hflow);
-    const double F = ddiv_rn(ghd * nn * fabs(q), c3);
+    const double F = ddiv_rn(ghd * nn * aq, c3);
     const double D = 1 + F, N = q - (ghd * slope);
     qn = ddiv_rn(N, D);
     const double rD = ddiv_rn(1.0, D), rc3 = ddiv_rn(1.0, c3);
-    const double dF_q = ghd * nn * (q > 0 ? 1.0 : -1.0) * rc3;
+    const double dF_q = ghd * nn * (dgt0(q) ? 1.0 : -1.0) * rc3;
     const double dF_hf = -2 * F * rhf;
-    const double dF_nn = ghd * fabs(q) * rc3;
+    const double dF_nn = ghd * aq * rc3;
     d_q = rD - qn * dF_q * rD;
     d_hf = (-kG * dt * slope) * rD - qn * dF_hf * rD;
     d_s = -ghd * rD;
@@ -105,37 +123,39 @@ __device__ DQ face_dq(double q, double e0, double h0, double e1, double h1, doub
   double de0 = d_hf * dhfe0 + d_s * ds0, de1 = d_hf * dhfe1 + d_s * ds1;
   // Froude limit (:3124-3134): |q/hflow| / sqrt(g*hflow) > froude_limit
   const double fl = p.froude_limit;
-  if (qn != 0) {
+  if (!deq0(qn)) {
     const float hf = approx_abs_f(hflow);
-    int t = decide(approx_abs_f(qn) / (hf * sqrtf(9.81f * hf)), (float)fl);
+    int t = decide(approx_abs_f(qn) / (hf * sqrtf(9.81f * hf)), flf);
     if (t == 0) t = dgt(ddiv_rn(fabs(ddiv_rn(qn, hflow)), isqrt_rn(kG * hflow)), fl) ? 1 : -1;
     if (t > 0) {
       const double sg = isqrt_rn(kG * hflow);
       const double g = 1.5 * sg * fl;
-      if (qn > 0) {
+      if (dgt0(qn)) {
         qn = hflow * (sg * fl);
         d_q = 0, d_nn = 0, dh0 = g * dhf0, dh1 = g * dhf1, de0 = g * dhfe0, de1 = g * dhfe1;
       } else {
-        qn = 0 - (hflow * (sg * fl));
+        qn = zero_minus(hflow * (sg * fl));
         d_q = 0, d_nn = 0, dh0 = -g * dhf0, dh1 = -g * dhf1, de0 = -g * dhfe0, de1 = -g * dhfe1;
       }
     }
   }
   // depth limits (:3138-3148), one after the other
-  const float dtf = approx_abs_f(dt), dxf = (float)DX;
-  if (qn > 0) {
-    int t = decide(approx_abs_f(qn) * dtf / dxf, approx_f(h0) * 0.25f);
-    if (t == 0) t = ((qn * dt / DX) > (h0 / 4)) ? 1 : -1;
+  const float dtf = approx_abs_f(dt);
+  if (dgt0(qn)) {
+    const double h0 = h0f();
+    int t = decide(approx_abs_f(qn) * dtf / DXf, approx_f(h0) * 0.25f);
+    if (t == 0) t = adj_depth_exceeds(qn, dt, DX, h0) ? 1 : -1;
     if (t > 0) {
       qn = ddiv_rn(ddiv_rn(h0 * DX, 5.0), dt);
       d_q = 0, d_nn = 0, dh0 = ddiv_rn(ddiv_rn(DX, 5.0), dt), dh1 = 0, de0 = de1 = 0;
     }
   }
-  if (qn < 0) {
-    int t = decide(approx_abs_f(qn) * dtf / dxf, approx_f(h1) * 0.25f);
-    if (t == 0) t = (fabs(qn * dt / DX) > (h1 / 4)) ? 1 : -1;
+  if (dlt0(qn)) {
+    const double h1 = h1f();
+    int t = decide(approx_abs_f(qn) * dtf / DXf, approx_f(h1) * 0.25f);
+    if (t == 0) t = adj_depth_exceeds_neg(qn, dt, DX, h1) ? 1 : -1;
     if (t > 0) {
-      qn = 0 - ddiv_rn(ddiv_rn(h1 * DX, 5.0), dt);
+      qn = zero_minus(ddiv_rn(ddiv_rn(h1 * DX, 5.0), dt));
       d_q = 0, d_nn = 0, dh0 = 0, dh1 = -ddiv_rn(ddiv_rn(DX, 5.0), dt), de0 = de1 = 0;
     }
   }
@@ -164,7 +184,9 @@ struct AdjBufs {
   const uint8_t* point;  // input-point cells of this iteration
   double *lam, *mux, *muy;  // adjoints of h, qx, qy (in: after, out: before)
   double *lamd, *p0x, *p0y, *p1x, *p1y;
-  double *pe0, *pe1x, *pe1y;  // elevation terms: own faces, to the cell above, to the left
+  // elevation terms: the x and y faces' own-cell terms, to the cell above,
+  // to the left; the faces' n terms (dL/d(n^2) by face)
+  double *pe0x, *pe0y, *pe1x, *pe1y, *gx, *gy;
   double *gn;   // accumulated dL/dn per cell
   double *ge;   // accumulated dL/d(elevation) per cell
   uint8_t *pflag;  // the cell's face terms (p*, pe*) may be nonzero
@@ -202,95 +224,90 @@ __global__ void k_adj_depth(const hc_view c, AdjBufs b, AdjStep st) {
   if (b.mask[cell]) {
     hd += ddiv_by(st.fdt * (b.qx1[cell + W] - b.qx1[cell] + b.qy1[cell + 1] - b.qy1[cell]),
                   c.dxd);
-    if (hd > 0 && c.elev[cell] == -9999) zeroed = true;
+    if (dgt0(hd) && dbits(c.elev[cell]) == kNoDataBits) zeroed = true;
   }
   double lam = b.lam[cell];
   // water_flux_out clamps an edge cell above the threshold: its depth after
   // the iteration is a constant, and the excess went into Q
-  if (edge_cell(c, i, j) && !zeroed && hd > c.p.water_depth_erosion_threshold)
+  if (edge_cell(c, i, j) && !zeroed && dgt(hd, c.p.water_depth_erosion_threshold))
     lam = st.gQ * c.p.DX * c.p.DX / st.ts;
   b.lamd[cell] = zeroed ? 0.0 : lam;
 }
 
-// flow_route reversed, per cell for its two faces: discharge adjoints
-// before the iteration, the depth terms each face passes to its two cells,
-// the n and elevation gradients.  The cells whose faces need face_dq are
-// compacted: in a storm about half the listed cells are dry, so a warp
-// running its 32 cells' faces in place issues the FP64 work with a fraction
-// of its lanes.  Each lane first forms its cell's discharge adjoints (and
-// writes the cell out when it is no listed cell above no-data); the cells
-// that go on are queued per warp with their adjoints, and whenever 32 are
-// queued the warp runs their faces together, the rest carried over to the
-// warp's next 32 cells.  A cell's outputs are written once, by one lane.
-constexpr int kAdjQ = 64;  // < 32 carried + 32 new
+// flow_route reversed, face by face: discharge adjoints before the
+// iteration, the depth terms each face passes to its two cells, the n and
+// elevation terms.  Only the faces that flowed (hflow above the threshold)
+// need face_dq, and in a storm about half the listed cells' faces do not:
+// a warp running its 32 cells' faces in place would issue the FP64 work with
+// a fraction of its lanes.  So each lane first forms its cell's discharge
+// adjoints and writes out every face that needs no face_dq (a face of a cell
+// that is not updated keeps its adjoint; one set to zero passes none); the
+// faces that flowed are queued per warp with hflow, the surface difference
+// and their discharge adjoint, and whenever 32 are queued the warp runs them
+// together, the rest carried over to the warp's next 32 cells.  Each output
+// entry is written once, by one lane.
+constexpr int kAdjQ = 96;  // queue entries per warp: < 32 carried + 64 new
 
-__device__ __forceinline__ void adj_cell_faces(const hc_view& c, const AdjBufs& b,
-                                               const AdjStep& st, size_t cell, double mux,
-                                               double muy) {
-  const size_t W = c.W;
-  const int i = (int)(cell / W), j = (int)(cell - (size_t)i * W);
-  const hc_params& p = c.p;
-  const double e0 = c.elev[cell];
-  const double n = p.spatially_var_mannings ? c.man[cell] : p.mannings;
-  const double nn = n * n;
-  auto hin = [&](size_t q) {
+struct AdjQueue {
+  uint32_t f[kAdjQ];  // cell << 2 | (e1 < e0) << 1 | y face
+  double hf[kAdjQ], da[kAdjQ], mu[kAdjQ];
+};
+
+__device__ __forceinline__ double adj_hin(const hc_view& c, const AdjBufs& b, const AdjStep& st,
+                                          size_t q) {
+  double h = b.h0[q];
+  if (b.point[q]) {
     const int rf = c.rfarea[q];
-    double h = b.h0[q];
-    if (b.point[q] && rf >= 0 && rf <= HC_MAX_RF) h += st.amt[rf];
-    return h;
-  };
-  double ox = mux, oy = muy, p0x = 0, p1x = 0, p0y = 0, p1y = 0, gn = 0;
-  double pe0 = 0, pe1x = 0, pe1y = 0;
-  const double h0 = hin(cell);
-  {
-    const size_t up = cell - W;
-    const double h1 = hin(up), e1 = c.elev[up];
-    if ((h0 > 0 || h1 > 0) && e1 > -9999) {
-      const int es = (i == c.imax) ? 1 : ((i <= 2) ? -1 : 0);
-      const DQ r = face_dq(b.qx0[cell], e0, h0, e1, h1, nn, st.fdt, es, p, c.rDX, c.dxd);
-      ox = r.dq * mux;
-      p0x = r.dh0 * mux;
-      p1x = r.dh1 * mux;
-      gn += r.dnn * mux;
-      pe0 += r.de0 * mux;
-      pe1x = r.de1 * mux;
-    }
+    if (rf >= 0 && rf <= HC_MAX_RF) h += st.amt[rf];
   }
-  {
-    const size_t lf = cell - 1;
-    const double h1 = hin(lf), e1 = c.elev[lf];
-    if ((h0 > 0 || h1 > 0) && e1 > -9999) {
-      const int es = (j == c.jmax) ? 1 : ((j <= 2) ? -1 : 0);
-      const DQ r = face_dq(b.qy0[cell], e0, h0, e1, h1, nn, st.fdt, es, p, c.rDX, c.dxd);
-      oy = r.dq * muy;
-      p0y = r.dh0 * muy;
-      p1y = r.dh1 * muy;
-      gn += r.dnn * muy;
-      pe0 += r.de0 * muy;
-      pe1y = r.de1 * muy;
-    }
-  }
-  b.gn[cell] += gn * 2 * n;
-  b.mux[cell] = ox;
-  b.muy[cell] = oy;
-  b.p0x[cell] = p0x;
-  b.p1x[cell] = p1x;
-  b.p0y[cell] = p0y;
-  b.p1y[cell] = p1y;
-  b.pe0[cell] = pe0;
-  b.pe1x[cell] = pe1x;
-  b.pe1y[cell] = pe1y;
-  b.pflag[cell] = 1;
+  return h;
 }
 
-__global__ void __launch_bounds__(256, 3) k_adj_flow_c(const hc_view c, AdjBufs b, AdjStep st) {
-  __shared__ uint32_t qc[8][kAdjQ];
-  __shared__ double qx_[8][kAdjQ], qy_[8][kAdjQ];
+__device__ __forceinline__ void adj_face(const hc_view& c, const AdjBufs& b, const AdjStep& st,
+                                         uint32_t f, double hflow, double dA, double mu) {
+  const size_t W = c.W;
+  const size_t cell = f >> 2;
+  const bool yface = f & 1u, e0max = (f >> 1) & 1u;
+  const size_t nb = yface ? cell - 1 : cell - W;
+  const int i = (int)(cell / W), j = (int)(cell - (size_t)i * W);
+  const hc_params& p = c.p;
+  const double n = p.spatially_var_mannings ? c.man[cell] : p.mannings;
+  const double nn = n * n;
+  const int es = yface ? ((j == c.jmax) ? 1 : ((j <= 2) ? -1 : 0))
+                       : ((i == c.imax) ? 1 : ((i <= 2) ? -1 : 0));
+  const double q = yface ? b.qy0[cell] : b.qx0[cell];
+  const DQ r = face_dq(
+      q, hflow, dA, e0max, [&] { return adj_hin(c, b, st, cell); },
+      [&] { return adj_hin(c, b, st, nb); }, nn, st.fdt, es, p, c.rDX, c.dxd, c.DXf, c.flf);
+  if (yface) {
+    b.muy[cell] = r.dq * mu;
+    b.p0y[cell] = r.dh0 * mu;
+    b.p1y[cell] = r.dh1 * mu;
+    b.pe0y[cell] = r.de0 * mu;
+    b.pe1y[cell] = r.de1 * mu;
+    b.gy[cell] = r.dnn * mu;
+  } else {
+    b.mux[cell] = r.dq * mu;
+    b.p0x[cell] = r.dh0 * mu;
+    b.p1x[cell] = r.dh1 * mu;
+    b.pe0x[cell] = r.de0 * mu;
+    b.pe1x[cell] = r.de1 * mu;
+    b.gx[cell] = r.dnn * mu;
+  }
+}
+
+__device__ __forceinline__ void adj_zero_x(const AdjBufs& b, size_t cell) {
+  b.p0x[cell] = b.p1x[cell] = b.pe0x[cell] = b.pe1x[cell] = b.gx[cell] = 0;
+}
+__device__ __forceinline__ void adj_zero_y(const AdjBufs& b, size_t cell) {
+  b.p0y[cell] = b.p1y[cell] = b.pe0y[cell] = b.pe1y[cell] = b.gy[cell] = 0;
+}
+
+__global__ void __launch_bounds__(256, 4) k_adj_flow_c(const hc_view c, AdjBufs b, AdjStep st) {
+  __shared__ AdjQueue qs[8];
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  uint32_t* Q = qc[warp];
-  double* MX = qx_[warp];
-  double* MY = qy_[warp];
+  AdjQueue& Q = qs[warp];
   const size_t W = c.W;
   const int cpr = (c.jmax + 31) / 32;  // chunks of 32 columns per row
   const long long chunks = (long long)c.imax * cpr;
@@ -300,49 +317,97 @@ __global__ void __launch_bounds__(256, 3) k_adj_flow_c(const hc_view c, AdjBufs 
   for (long long ch = (long long)blockIdx.x * (blockDim.x >> 5) + warp; ch < chunks; ch += warps) {
     const int i = 1 + (int)(ch / cpr);
     const int j = 1 + (int)(ch % cpr) * 32 + lane;
-    bool go = false;
+    bool fx = false, fy = false, ex = false, ey = false;
     size_t cell = 0;
-    double mux = 0, muy = 0;
+    double mux = 0, muy = 0, hx = 0, ax = 0, hy = 0, ay = 0;
     if (j <= c.jmax) {
       cell = (size_t)i * W + j;
       if (!(b.mask[cell] || b.mask[cell - W] || b.mask[cell - 1])) {
         if (b.pflag[cell]) {
-          b.p0x[cell] = b.p1x[cell] = b.p0y[cell] = b.p1y[cell] = 0;
-          b.pe0[cell] = b.pe1x[cell] = b.pe1y[cell] = 0;
+          adj_zero_x(b, cell);
+          adj_zero_y(b, cell);
           b.pflag[cell] = 0;
         }
       } else {
         auto ml = [&](size_t q) { return b.mask[q] ? b.lamd[q] : 0.0; };
         mux = b.mux[cell] + k * (ml(cell - W) - ml(cell));
         muy = b.muy[cell] + k * (ml(cell - 1) - ml(cell));
-        go = b.mask[cell] && c.elev[cell] > -9999;
-        if (!go) {
+        const double e0 = c.elev[cell];
+        b.pflag[cell] = 1;
+        if (!(b.mask[cell] && dkey(e0) > kNoDataKey)) {
+          // flow_route leaves both faces alone
           b.mux[cell] = mux;
           b.muy[cell] = muy;
-          b.p0x[cell] = b.p1x[cell] = b.p0y[cell] = b.p1y[cell] = 0;
-          b.pe0[cell] = b.pe1x[cell] = b.pe1y[cell] = 0;
-          b.pflag[cell] = 1;
+          adj_zero_x(b, cell);
+          adj_zero_y(b, cell);
+        } else {
+          const double h0 = adj_hin(c, b, st, cell);
+          const double a0 = e0 + h0;
+          const bool wet0 = dgt0(h0);
+          double ox = mux, oy = muy;
+          {
+            const size_t up = cell - W;
+            const double h1 = adj_hin(c, b, st, up), e1 = c.elev[up];
+            if ((wet0 || dgt0(h1)) && dkey(e1) > kNoDataKey) {
+              const double a1 = e1 + h1;
+              hx = imax_d(a0, a1) - imax_d(e1, e0);
+              ax = a1 - a0;
+              ex = dlt(e1, e0);
+              fx = dkey(hx) > c.thr_key;
+              if (!fx) ox = 0;  // q set to zero: no adjoint passes back
+            }
+          }
+          {
+            const size_t lf = cell - 1;
+            const double h1 = adj_hin(c, b, st, lf), e1 = c.elev[lf];
+            if ((wet0 || dgt0(h1)) && dkey(e1) > kNoDataKey) {
+              const double a1 = e1 + h1;
+              hy = imax_d(a0, a1) - imax_d(e1, e0);
+              ay = a1 - a0;
+              ey = dlt(e1, e0);
+              fy = dkey(hy) > c.thr_key;
+              if (!fy) oy = 0;
+            }
+          }
+          if (!fx) {
+            b.mux[cell] = ox;
+            adj_zero_x(b, cell);
+          }
+          if (!fy) {
+            b.muy[cell] = oy;
+            adj_zero_y(b, cell);
+          }
         }
       }
     }
-    const unsigned bg = __ballot_sync(FULL, go);
-    if (go) {
-      const int s = qn + __popc(bg & ((1u << lane) - 1u));
-      Q[s] = (uint32_t)cell;
-      MX[s] = mux;
-      MY[s] = muy;
+    const unsigned bx = __ballot_sync(FULL, fx), by = __ballot_sync(FULL, fy);
+    const unsigned below = (1u << lane) - 1u;
+    const int nx = __popc(bx);
+    if (fx) {
+      const int s = qn + __popc(bx & below);
+      Q.f[s] = ((uint32_t)cell << 2) | (ex ? 2u : 0u);
+      Q.hf[s] = hx;
+      Q.da[s] = ax;
+      Q.mu[s] = mux;
     }
-    qn += __popc(bg);
+    if (fy) {
+      const int s = qn + nx + __popc(by & below);
+      Q.f[s] = ((uint32_t)cell << 2) | (ey ? 2u : 0u) | 1u;
+      Q.hf[s] = hy;
+      Q.da[s] = ay;
+      Q.mu[s] = muy;
+    }
+    qn += nx + __popc(by);
     __syncwarp();
-    if (qn >= 32) {
+    while (qn >= 32) {
       qn -= 32;
-      const uint32_t q = Q[qn + lane];
-      const double mx = MX[qn + lane], my = MY[qn + lane];
-      __syncwarp();
-      adj_cell_faces(c, b, st, q, mx, my);
+      const uint32_t f = Q.f[qn + lane];
+      const double hf = Q.hf[qn + lane], da = Q.da[qn + lane], mu = Q.mu[qn + lane];
+      __syncwarp();  // the entries are read before the next cells' are written
+      adj_face(c, b, st, f, hf, da, mu);
     }
   }
-  if (lane < qn) adj_cell_faces(c, b, st, Q[lane], MX[lane], MY[lane]);
+  if (lane < qn) adj_face(c, b, st, Q.f[lane], Q.hf[lane], Q.da[lane], Q.mu[lane]);
 }
 
 // the depth adjoint before the iteration (inputs add a constant), and the
@@ -362,7 +427,15 @@ __global__ void __launch_bounds__(256) k_adj_gather(const hc_view c, AdjBufs b, 
     const double la = (dact ? b.lamd[cell] : b.lam[cell]) + b.p0x[cell] + b.p0y[cell] +
                       b.p1x[cell + W] + b.p1y[cell + 1];
     b.lam[cell] = la;
-    b.ge[cell] += b.pe0[cell] + b.pe1x[cell + W] + b.pe1y[cell + 1];
+    b.ge[cell] += (b.pe0x[cell] + b.pe0y[cell]) + b.pe1x[cell + W] + b.pe1y[cell + 1];
+    if (b.pflag[cell]) {
+      // the faces' n^2 terms, as dL/dn (n^2 = n*n)
+      const double g2 = b.gx[cell] + b.gy[cell];
+      if (!deq0(g2)) {
+        const double n = c.p.spatially_var_mannings ? c.man[cell] : c.p.mannings;
+        b.gn[cell] += g2 * 2 * n;
+      }
+    }
     const int rf = c.rfarea[cell];
     if (b.point[cell] && rf >= 0 && rf <= HC_MAX_RF) {
       mine = la * st.damt[rf];
@@ -389,12 +462,16 @@ __global__ void __launch_bounds__(256) k_adj_save(const hc_view c, const hc_dev*
   const int64_t k = d->adj_i - 1 - d->adj_slot_t0;  // k_control has counted this iteration
   if (k < 0 || k >= d->adj_slot_n) return;
   const size_t N2 = c.N2, off = (size_t)k * N2;
+  double* __restrict__ sh = d->adj_slot_h + off;
+  double* __restrict__ sqx = d->adj_slot_qx + off;
+  double* __restrict__ sqy = d->adj_slot_qy + off;
+  uint8_t* __restrict__ sm = d->adj_slot_mask + off;
   for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < N2;
        q += (size_t)gridDim.x * blockDim.x) {
-    c.adj_sh[off + q] = c.h[q];
-    c.adj_sqx[off + q] = c.qx[q];
-    c.adj_sqy[off + q] = c.qy[q];
-    c.adj_smask[off + q] = c.mask[q];
+    sh[q] = c.h[q];
+    sqx[q] = c.qx[q];
+    sqy[q] = c.qy[q];
+    sm[q] = c.mask[q];
   }
 }
 
@@ -462,11 +539,23 @@ hc_status load_state(hc_ctx* c, Checkpoint& k) {
   return ctx_pull(c);
 }
 
+// A segment's iteration states: h, qx, qy and the wet mask of K
+// iterations (qx, qy one more: the discharges after the last), and the
+// event that marks the last adjoint iteration that read them.
+struct SlotSet {
+  Dev h, qx, qy, mask;
+  cudaEvent_t free_ev = nullptr;
+  ~SlotSet() {
+    if (free_ev) cudaEventDestroy(free_ev);
+  }
+};
+
 // switches the time-step recording on (mode 1) or imposes recorded steps
 // (mode 2) for the next iterations, from record index i0
-// (k_adj_save keeps the states of iterations slot_t0 .. slot_t0+slot_n-1)
+// (k_adj_save keeps the states of iterations slot_t0 .. slot_t0+slot_n-1
+// in the slot set `set`)
 hc_status adj_mode(hc_ctx* c, double* buf, int64_t n, int mode, int64_t i0,
-                   int64_t slot_t0 = 0, int64_t slot_n = 0) {
+                   int64_t slot_t0 = 0, int64_t slot_n = 0, SlotSet* set = nullptr) {
   if (c->v.adj_dt != buf) {
     c->v.adj_dt = buf;
     c->graph_iters = 0;  // the graphs hold the view by value
@@ -476,7 +565,13 @@ hc_status adj_mode(hc_ctx* c, double* buf, int64_t n, int mode, int64_t i0,
   c->hdev->adj_i = i0;
   c->hdev->adj_n = buf ? n : 0;
   c->hdev->adj_slot_t0 = slot_t0;
-  c->hdev->adj_slot_n = slot_n;
+  c->hdev->adj_slot_n = set ? slot_n : 0;
+  if (set) {
+    c->hdev->adj_slot_h = set->h.as<double>();
+    c->hdev->adj_slot_qx = set->qx.as<double>();
+    c->hdev->adj_slot_qy = set->qy.as<double>();
+    c->hdev->adj_slot_mask = set->mask.as<uint8_t>();
+  }
   return ctx_push(c);
 }
 
@@ -496,7 +591,10 @@ struct PointsLog {
     const hc_scalars& sc = c->hdev->s;
     nact.emplace_back(sc.nActualGridCells, sc.nActualGridCells + HC_MAX_RF + 1);
     cnt.emplace_back(sc.catchment_input_counter, sc.catchment_input_counter + HC_MAX_RF + 1);
-    if (dmalloc(*f, c->v.N2) != cudaSuccess) return hc_fail(c, HC_ERR_NOMEM, "adjoint points");
+    // stream-ordered: no device-wide synchronisation while adjoint
+    // iterations run on the other stream
+    if (cudaMallocAsync(&f->p, c->v.N2, c->s) != cudaSuccess)
+      return hc_fail(c, HC_ERR_NOMEM, "adjoint points");
     cudaMemsetAsync(f->p, 0, c->v.N2, c->s);
     k_point_flags<<<152 * 4, 256, 0, c->s>>>(c->v, f->as<uint8_t>(),
                                              (int)c->hdev->s.totalinputpoints);
@@ -679,37 +777,63 @@ extern "C" hc_status hc_adj_gradient(hc_ctx* c, int64_t n, int32_t max_states,
   if (v.p.spatially_complex_rainfall)
     return hc_fail(c, HC_ERR_UNSUPPORTED, "adjoint runs use the zoned rainfall inputs");
   if (!c->prepared) return hc_fail(c, HC_ERR_STATE, "hc_prepare must come before the run");
+  if (v.N2 >= (size_t)1 << 30)  // k_adj_flow_c queues a face as cell << 2 | 2 bits
+    return hc_fail(c, HC_ERR_UNSUPPORTED, "adjoint runs take grids of fewer than 2^30 cells");
   const auto t_all = std::chrono::steady_clock::now();
   const size_t N2 = v.N2;
   cudaStream_t s = c->s;
   // The states kept: snapshots (run state at a segment start) and the K
-  // iteration states of the segment being reversed, max_states in all.
-  // Segment length: the one with the least recomputation; of those the
-  // longest (fewer, longer replays: less launch and host overhead).
+  // iteration states of a segment, max_states in all.  With two slot sets
+  // the replay of one segment runs while the adjoint iterations of the one
+  // after it read the other set (two streams); a second set costs K states.
+  // Segment length and sets: the least recomputation; of those two sets,
+  // then the longest segment (fewer, longer replays: less launch and host
+  // overhead).
   int64_t K = 1;
-  int snaps = 0;
+  int snaps = 0, nsets = 1;
   {
     double best = 1e300;
-    for (int64_t k = 1; k < max_states && k <= n; k = (k < 8) ? k + 1 : k + k / 8) {
-      const int sn = (int)(max_states - k);  // snapshots, the initial state's included
-      const int64_t m = (n + k - 1) / k;
-      const double cost = schedule_cost(0, m, std::min<int64_t>(sn, m) - 1, true) * (double)k;
-      if (cost <= best) {
-        best = cost;
-        K = k;
-        snaps = sn;
+    for (int sets = 1; sets <= 2; sets++)
+      for (int64_t k = 1; sets * k < max_states && k <= n; k = (k < 8) ? k + 1 : k + k / 8) {
+        const int sn = (int)(max_states - sets * k);  // snapshots, the initial state's included
+        const int64_t m = (n + k - 1) / k;
+        const double cost = schedule_cost(0, m, std::min<int64_t>(sn, m) - 1, true) * (double)k;
+        if (cost < best || (cost == best && (sets > nsets || k > K))) {
+          best = cost;
+          K = k;
+          snaps = sn;
+          nsets = sets;
+        }
       }
-    }
   }
   const int64_t nseg = (n + K - 1) / K;
   if (snaps > nseg) snaps = (int)nseg;
-  // replay slots, set in the view for the whole call (k_adj_save is part of
-  // the graphs while they are set)
-  Dev sh, sqx, sqy, smask;
-  if (dmalloc(sh, (size_t)K * N2 * 8) || dmalloc(sqx, (size_t)(K + 1) * N2 * 8) ||
-      dmalloc(sqy, (size_t)(K + 1) * N2 * 8) || dmalloc(smask, (size_t)K * N2))
-    return hc_fail(c, HC_ERR_NOMEM, "adjoint: out of device memory (segment of %lld)",
-                   (long long)K);
+  if (nseg < 2) nsets = 1;
+  SlotSet sets[2];
+  for (int x = 0; x < nsets; x++) {
+    SlotSet& S = sets[x];
+    if (dmalloc(S.h, (size_t)K * N2 * 8) || dmalloc(S.qx, (size_t)(K + 1) * N2 * 8) ||
+        dmalloc(S.qy, (size_t)(K + 1) * N2 * 8) || dmalloc(S.mask, (size_t)K * N2))
+      return hc_fail(c, HC_ERR_NOMEM, "adjoint: out of device memory (segment of %lld)",
+                     (long long)K);
+    HC_CU(cudaEventCreateWithFlags(&S.free_ev, cudaEventDisableTiming), "adjoint event");
+  }
+  // the adjoint iterations' stream
+  struct Stream {
+    cudaStream_t s = nullptr;
+    cudaEvent_t rep = nullptr;
+    ~Stream() {
+      if (s) {
+        cudaStreamSynchronize(s);
+        cudaStreamDestroy(s);
+      }
+      if (rep) cudaEventDestroy(rep);
+    }
+  } rs;
+  HC_CU(cudaStreamCreateWithFlags(&rs.s, cudaStreamNonBlocking), "adjoint stream");
+  HC_CU(cudaEventCreateWithFlags(&rs.rep, cudaEventDisableTiming), "adjoint event");
+  const cudaStream_t sr = rs.s;
+  // k_adj_save is part of the graphs while the view's slot pointers are set
   struct SlotGuard {
     hc_ctx* c;
     ~SlotGuard() {
@@ -720,10 +844,10 @@ extern "C" hc_status hc_adj_gradient(hc_ctx* c, int64_t n, int32_t max_states,
       c->points_hook_arg = nullptr;
     }
   } guard{c};
-  v.adj_sh = sh.as<double>();
-  v.adj_sqx = sqx.as<double>();
-  v.adj_sqy = sqy.as<double>();
-  v.adj_smask = smask.as<uint8_t>();
+  v.adj_sh = sets[0].h.as<double>();
+  v.adj_sqx = sets[0].qx.as<double>();
+  v.adj_sqy = sets[0].qy.as<double>();
+  v.adj_smask = sets[0].mask.as<uint8_t>();
   c->graph_iters = 0;
   std::vector<Checkpoint> cps((size_t)snaps + 1);  // + the state at the end
   for (auto& cp : cps) HC_TRY(save_state(c, cp, true));
@@ -789,20 +913,37 @@ extern "C" hc_status hc_adj_gradient(hc_ctx* c, int64_t n, int32_t max_states,
   if (loss) *loss = L;
   // ---------------- reverse
   const auto t_rev = std::chrono::steady_clock::now();
-  Dev lam, mux, muy, lamd, p0x, p0y, p1x, p1y, pe0, pe1x, pe1y, gn, ge, gj, pflag;
+  Dev lam, mux, muy, lamd, p0x, p0y, p1x, p1y, pe0x, pe0y, pe1x, pe1y, gx, gy, gn, ge, gj, pflag;
   if (dmalloc(pflag, N2) || dmalloc(lam, N2 * 8) || dmalloc(mux, N2 * 8) || dmalloc(muy, N2 * 8) ||
       dmalloc(lamd, N2 * 8) || dmalloc(p0x, N2 * 8) || dmalloc(p0y, N2 * 8) ||
-      dmalloc(p1x, N2 * 8) || dmalloc(p1y, N2 * 8) || dmalloc(pe0, N2 * 8) ||
-      dmalloc(pe1x, N2 * 8) || dmalloc(pe1y, N2 * 8) || dmalloc(gn, N2 * 8) ||
+      dmalloc(p1x, N2 * 8) || dmalloc(p1y, N2 * 8) || dmalloc(pe0x, N2 * 8) ||
+      dmalloc(pe0y, N2 * 8) || dmalloc(pe1x, N2 * 8) || dmalloc(pe1y, N2 * 8) ||
+      dmalloc(gx, N2 * 8) || dmalloc(gy, N2 * 8) || dmalloc(gn, N2 * 8) ||
       dmalloc(ge, N2 * 8) || dmalloc(gj, (size_t)n * (HC_MAX_RF + 1) * 8)) {
     adj_mode(c, nullptr, 0, 0, 0);
     return hc_fail(c, HC_ERR_NOMEM, "adjoint: out of device memory");
   }
-  for (Dev* d : {&lam, &mux, &muy, &lamd, &p0x, &p0y, &p1x, &p1y, &pe0, &pe1x, &pe1y, &gn, &ge})
-    cudaMemsetAsync(d->p, 0, N2 * 8, s);
-  cudaMemsetAsync(gj.p, 0, (size_t)n * (HC_MAX_RF + 1) * 8, s);
-  cudaMemsetAsync(pflag.p, 0, N2, s);
+  for (Dev* d : {&lam, &mux, &muy, &lamd, &p0x, &p0y, &p1x, &p1y, &pe0x, &pe0y, &pe1x, &pe1y,
+                 &gx, &gy, &gn, &ge})
+    cudaMemsetAsync(d->p, 0, N2 * 8, sr);
+  cudaMemsetAsync(gj.p, 0, (size_t)n * (HC_MAX_RF + 1) * 8, sr);
+  cudaMemsetAsync(pflag.p, 0, N2, sr);
   dim3 b(32, 8), gr((v.jmax + 31) / 32, (v.imax + 7) / 8);
+  double ms_replay = 0;  // host time in the segments' replays
+  // device time of each segment's adjoint iterations (event pairs on sr)
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> kev;
+  struct EvGuard {
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>>* v;
+    ~EvGuard() {
+      for (auto& e : *v) {
+        cudaEventDestroy(e.first);
+        cudaEventDestroy(e.second);
+      }
+    }
+  } evg{&kev};
+  // the points logs live until the adjoint iterations that read them ran
+  std::vector<std::unique_ptr<PointsLog>> logs;
+  int64_t leaves = 0;
   rv.advance = [&](int64_t t0, int64_t t1) -> hc_status {
     HC_TRY(adj_mode(c, dt.as<double>(), n, 2, t0));  // imposed steps, no saves
     int64_t done = 0;
@@ -810,21 +951,41 @@ extern "C" hc_status hc_adj_gradient(hc_ctx* c, int64_t n, int32_t max_states,
   };
   rv.leaf = [&](int64_t g) -> hc_status {
     const int64_t t0 = g * K, len = std::min<int64_t>(K, n - t0);
-    // replay as one graph run; k_adj_save keeps every iteration's state
-    HC_TRY(adj_mode(c, dt.as<double>(), n, 2, t0, t0, len));
-    PointsLog pts;
+    SlotSet& S = sets[nsets == 2 ? (leaves & 1) : 0];
+    leaves++;
+    // the replay overwrites the set once the adjoint iterations that read
+    // it last are done
+    HC_CU(cudaStreamWaitEvent(s, S.free_ev, 0), "adjoint");
+    // replay as graph runs; k_adj_save keeps every iteration's state
+    HC_TRY(adj_mode(c, dt.as<double>(), n, 2, t0, t0, len, &S));
+    logs.emplace_back(new PointsLog());
+    PointsLog& pts = *logs.back();
     HC_TRY(pts.add(c, t0));
     c->points_hook = points_hook;
     c->points_hook_arg = &pts;
     int64_t done = 0;
-    const hc_status rs = hc_run(c, len, 0, nullptr, &done);
+    const auto t_rp = std::chrono::steady_clock::now();
+    const hc_status rs_ = hc_run(c, len, 0, nullptr, &done);
     c->points_hook = nullptr;
     c->points_hook_arg = nullptr;
-    HC_TRY(rs);
+    HC_TRY(rs_);
+    ms_replay += ms_since(t_rp);
     HC_TRY(adj_mode(c, dt.as<double>(), n, 2, t0 + len));  // saves off
-    cudaMemcpyAsync(v.adj_sqx + (size_t)len * N2, v.qx, N2 * 8, cudaMemcpyDeviceToDevice, s);
-    cudaMemcpyAsync(v.adj_sqy + (size_t)len * N2, v.qy, N2 * 8, cudaMemcpyDeviceToDevice, s);
-    // adjoint iterations, last first
+    double* const sqx = S.qx.as<double>();
+    double* const sqy = S.qy.as<double>();
+    cudaMemcpyAsync(sqx + (size_t)len * N2, v.qx, N2 * 8, cudaMemcpyDeviceToDevice, s);
+    cudaMemcpyAsync(sqy + (size_t)len * N2, v.qy, N2 * 8, cudaMemcpyDeviceToDevice, s);
+    HC_CU(cudaEventRecord(rs.rep, s), "adjoint");
+    HC_CU(cudaStreamWaitEvent(sr, rs.rep, 0), "adjoint");
+    cudaEvent_t e0, e1;
+    HC_CU(cudaEventCreate(&e0), "adjoint event");
+    if (cudaEventCreate(&e1) != cudaSuccess) {
+      cudaEventDestroy(e0);
+      return hc_fail(c, HC_ERR_CUDA, "adjoint event");
+    }
+    kev.emplace_back(e0, e1);
+    HC_CU(cudaEventRecord(e0, sr), "adjoint");
+    // adjoint iterations, last first, on sr
     for (int64_t k = len - 1; k >= 0; k--) {
       const int64_t t = t0 + k;
       const double* r = arec.data() + (size_t)t * HC_ADJ_REC;
@@ -835,12 +996,12 @@ extern "C" hc_status hc_adj_gradient(hc_ctx* c, int64_t n, int32_t max_states,
       st.ts = rec[(size_t)t].time_step;
       st.gQ = gQ[(size_t)t];
       AdjBufs bb;
-      bb.h0 = v.adj_sh + (size_t)k * N2;
-      bb.qx0 = v.adj_sqx + (size_t)k * N2;
-      bb.qy0 = v.adj_sqy + (size_t)k * N2;
-      bb.mask = v.adj_smask + (size_t)k * N2;
-      bb.qx1 = v.adj_sqx + (size_t)(k + 1) * N2;
-      bb.qy1 = v.adj_sqy + (size_t)(k + 1) * N2;
+      bb.h0 = S.h.as<double>() + (size_t)k * N2;
+      bb.qx0 = sqx + (size_t)k * N2;
+      bb.qy0 = sqy + (size_t)k * N2;
+      bb.mask = S.mask.as<uint8_t>() + (size_t)k * N2;
+      bb.qx1 = sqx + (size_t)(k + 1) * N2;
+      bb.qy1 = sqy + (size_t)(k + 1) * N2;
       bb.point = pts.at(t);
       bb.lam = lam.as<double>();
       bb.mux = mux.as<double>();
@@ -850,7 +1011,10 @@ extern "C" hc_status hc_adj_gradient(hc_ctx* c, int64_t n, int32_t max_states,
       bb.p0y = p0y.as<double>();
       bb.p1x = p1x.as<double>();
       bb.p1y = p1y.as<double>();
-      bb.pe0 = pe0.as<double>();
+      bb.pe0x = pe0x.as<double>();
+      bb.pe0y = pe0y.as<double>();
+      bb.gx = gx.as<double>();
+      bb.gy = gy.as<double>();
       bb.pe1x = pe1x.as<double>();
       bb.pe1y = pe1y.as<double>();
       bb.gn = gn.as<double>();
@@ -866,17 +1030,25 @@ extern "C" hc_status hc_adj_gradient(hc_ctx* c, int64_t n, int32_t max_states,
         st.amt[z] = a;
         st.damt[z] = da;
       }
-      k_adj_depth<<<gr, b, 0, s>>>(v, bb, st);
-      k_adj_flow_c<<<c->sms * 3, 256, 0, s>>>(v, bb, st);
-      k_adj_gather<<<gr, b, 0, s>>>(v, bb, st);
+      k_adj_depth<<<gr, b, 0, sr>>>(v, bb, st);
+      k_adj_flow_c<<<c->sms * 4, 256, 0, sr>>>(v, bb, st);
+      k_adj_gather<<<gr, b, 0, sr>>>(v, bb, st);
     }
     HC_CU(cudaGetLastError(), "adjoint kernels");
-    HC_CU(cudaStreamSynchronize(s), "adjoint");  // pts' buffers are freed next
+    HC_CU(cudaEventRecord(e1, sr), "adjoint");
+    HC_CU(cudaEventRecord(S.free_ev, sr), "adjoint");
     return HC_OK;
   };
   HC_TRY(rv.reverse(0, nseg, snaps - 1));
+  HC_CU(cudaStreamSynchronize(sr), "adjoint");
   HC_CU(cudaStreamSynchronize(s), "adjoint");
   const double ms_rev = ms_since(t_rev);
+  double ms_kernels = 0;
+  for (auto& e : kev) {
+    float f = 0;
+    HC_CU(cudaEventElapsedTime(&f, e.first, e.second), "adjoint event");
+    ms_kernels += f;
+  }
   // ---------------- results
   if (grad_n) HC_CU(cudaMemcpy(grad_n, gn.p, N2 * 8, cudaMemcpyDeviceToHost), "adjoint gradient");
   if (grad_elev) HC_CU(cudaMemcpy(grad_elev, ge.p, N2 * 8, cudaMemcpyDeviceToHost), "adjoint gradient");
@@ -918,6 +1090,8 @@ extern "C" hc_status hc_adj_gradient(hc_ctx* c, int64_t n, int32_t max_states,
     ms[3] = (double)K;
     ms[4] = (double)snaps;
     ms[5] = (double)rv.advances;
+    ms[6] = ms_replay;
+    ms[7] = ms_kernels;
   }
   return HC_OK;
 }

@@ -1162,9 +1162,10 @@ static hc_status build_one(hc_ctx* c, int flags, int K, cudaGraphExec_t* exec,
   return HC_OK;
 }
 
-// The chunk graph (K iterations).  Runs shorter than K take the graphs of
-// 2^k iterations (made when first needed; a paused chunk skips the rest of
-// its iterations, so short runs would pay for K).
+// The chunk graph (K iterations) and, for runs shorter than K, the graphs of
+// 2^k < K iterations (a paused chunk skips the rest of its iterations, so a
+// short run would otherwise pay for K).  All are made and uploaded here, so
+// that no later hc_run instantiates a graph between its launches.
 static hc_status build_graph(hc_ctx* c, int flags) {
   const int K = graph_chunk(c);
   for (auto& t : c->tail)
@@ -1173,6 +1174,11 @@ static hc_status build_graph(hc_ctx* c, int flags) {
       t = nullptr;
     }
   HC_TRY(build_one(c, flags, K, &c->graph, &c->graph_kernels));
+  HC_CU(cudaGraphUpload(c->graph, c->s), "graph upload");
+  for (int k = 0; k < 12 && (1 << k) < K; k++) {
+    HC_TRY(build_one(c, flags, 1 << k, &c->tail[k], &c->tail_kernels[k]));
+    HC_CU(cudaGraphUpload(c->tail[k], c->s), "graph upload");
+  }
   c->graph_iters = K;
   c->graph_flags = flags;
   return HC_OK;
@@ -1256,11 +1262,14 @@ static hc_status run_begin(hc_ctx* c, int64_t n, int32_t flags, bool want_rec, b
     return hc_fail(c, HC_ERR_UNSUPPORTED, "lateral3 needs a square grid");
   hc_view& v = c->v;
   if (want_rec && v.rec_cap < n) {
+    // at least 4096 records, so that short runs with records (one
+    // iteration per call) do not rebuild the graphs as n grows
+    const int64_t cap = std::max<int64_t>(n, 4096);
     if (v.rec) cudaFree(v.rec);
     v.rec = nullptr;
     v.rec_cap = 0;
-    HC_TRY(dalloc(c, &v.rec, (size_t)n));
-    v.rec_cap = n;
+    HC_TRY(dalloc(c, &v.rec, (size_t)cap));
+    v.rec_cap = cap;
     c->graph_iters = 0;  // the view changed
   }
   HC_TRY(pull(c));

@@ -86,6 +86,8 @@ struct hc_dev {
   int adj_mode;           // 0 off, 1 record the time steps, 2 impose them
   int64_t adj_i, adj_n;   // next iteration, capacity of hc_view::adj_dt
   int64_t adj_slot_t0, adj_slot_n;  // iterations whose state k_adj_save keeps
+  double *adj_slot_h, *adj_slot_qx, *adj_slot_qy;  // ... and where (slot k at k * N2)
+  uint8_t *adj_slot_mask;
   unsigned int xchains;   // chain starts of the +/-x apply pass (hc_view::chains)
   unsigned int ychains;   // chain starts of the +/-y apply pass
   unsigned int xresume, yresume;  // long chains handed from the thread to the warp walkers
@@ -183,8 +185,9 @@ struct hc_view {
   // adjoint runs (hc_adjoint.cu): per-iteration time steps, recorded or
   // imposed (HC_ADJ_REC stride per iteration; see hc_dev::adj_mode)
   double *adj_dt;
-  // adjoint replay: each iteration's state before it (slot = iteration -
-  // hc_dev::adj_slot_t0), saved by k_adj_save when these are set
+  // adjoint replay: set while the graphs carry k_adj_save, which keeps each
+  // iteration's state before it in the slot set that hc_dev::adj_slot_*
+  // names (slot = iteration - hc_dev::adj_slot_t0)
   double *adj_sh, *adj_sqx, *adj_sqy;
   uint8_t *adj_smask;
   unsigned long long *alloc_key; // N2: serial-order key of the first grain-record request

@@ -312,12 +312,12 @@ class Model:
         ge = np.zeros((p.imax + 2, p.jmax + 2), dtype=np.float64)
         gr = np.zeros(self.case.rain.shape, dtype=np.float64)
         loss = C.c_double()
-        ms = (C.c_double * 6)()
+        ms = (C.c_double * 8)()
         self._check(self.lib.hc_adj_gradient(self.h, n, max_states, t.ctypes.data, len(t),
                                              C.byref(loss), gn.ctypes.data, gr.ctypes.data,
                                              ge.ctypes.data, ms), "adj_gradient")
         info = dict(zip(("forward_ms", "reverse_ms", "total_ms", "segment", "snapshots",
-                         "advanced"), list(ms)))
+                         "advanced", "replay_ms", "adjoint_iterations_ms"), list(ms)))
         if elev:
             return loss.value, gn, gr, info, ge
         return loss.value, gn, gr, info

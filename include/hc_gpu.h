@@ -343,11 +343,15 @@ hc_status hc_run_ensemble(hc_ctx** ctxs, int32_t m, int64_t n, int32_t flags, in
  * constant in the parameters).  Memory: at most max_states model states
  * (h, qx, qy, wet mask: 25 bytes a cell each) are kept at once, as
  * binomial checkpoints (Griewank's revolve) of segments of K iterations plus
- * the K iteration states of the segment being reversed; K is the one with
- * the least recomputation.  The model is left at the end of the n
- * iterations.  ms (optional, 6 doubles): forward ms, reverse ms, total ms,
- * K, snapshots, iterations run again beyond the forward run and the
- * segments' replays. */
+ * the K iteration states of the segment being reversed, or of two segments
+ * when the cap allows it without more recomputation: then one segment is
+ * replayed while the adjoint iterations of the next run on a second stream.
+ * K is the one with the least recomputation.  The model is left at the end
+ * of the n iterations.  ms (optional, 8 doubles): forward ms, reverse ms,
+ * total ms, K, snapshots, iterations run again beyond the forward run and
+ * the segments' replays, then the reverse's parts, which overlap: host ms
+ * replaying the segments (keeping their states), device ms of the adjoint
+ * iterations. */
 #define HC_ADJ_RECORD 22
 hc_status hc_adj_forward(hc_ctx* ctx, int64_t n, const double* fixed, double* rec_out,
                          double* q_samples, int64_t q_cap, int64_t* n_samples);
