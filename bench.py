@@ -69,8 +69,9 @@ def make_workload(name, size=0):
                            "slide_3, per-cell n; 60 mm/h storm from 60 min" % (n, n))
     if name == "flow8192":
         n = size or 8192
-        case = synth.flow_case(n=n, DX=5.0, hours=2)
-        return case, 1500, "flow-only %dx%d @5 m, 30 mm/h" % (n, n)
+        case = synth.flow_case(n=n, DX=5.0, hours=2, grid_rain=True)
+        return case, 1500, ("flow-only %dx%d @5 m, 30 mm/h on every cell (distributed "
+                            "TOPMODEL runoff grid)" % (n, n))
     if name == "reach":
         case = synth.reach_case(imax=300, jmax=100, DX=10.0, hours=24)
         return case, 12000, "reach 300x100 @10 m, Wilcock, triangular hydrograph peaking at 6 h"
@@ -494,7 +495,8 @@ def cpu_sample(model, case, flags, budget_s=15.0):
     n = 0
     t0 = time.perf_counter()
     while time.perf_counter() - t0 < budget_s:
-        o.iterate(1, flags)
+        if len(o.iterate(1, flags)) == 0:  # the run ended (maxcycle)
+            break
         n += 1
     dt = time.perf_counter() - t0
     return {"value": case.cells * n / dt, "unit": UNIT, "cores": cores, "kind": "port",

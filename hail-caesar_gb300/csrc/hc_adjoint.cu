@@ -70,6 +70,16 @@ static __device__ __noinline__ bool adj_depth_exceeds_neg(double qn, double dt, 
                                                           double h) {
   return fabs(qn * dt / DX) > (h / 4);
 }
+// The other rare paths, out of line too (smaller code: fewer instruction
+// fetch stalls): the limits' value (x * DX / 5) / dt, the Froude test's exact
+// form and sqrt(g hflow).
+static __device__ __noinline__ double adj_limit_value(double x, double DX, double dt) {
+  return ddiv_rn(ddiv_rn(x * DX, 5.0), dt);
+}
+static __device__ __noinline__ bool adj_froude_exceeds(double qn, double hflow, double fl) {
+  return dgt(ddiv_rn(fabs(ddiv_rn(qn, hflow)), isqrt_rn(kG * hflow)), fl);
+}
+static __device__ __noinline__ double adj_sqrt_ghf(double hflow) { return isqrt_rn(kG * hflow); }
 
 // One face (:3096-3191), as the device evaluates it, with derivatives.
 // The value and the branch decisions are the forward kernel's (exact FP64
@@ -126,9 +136,9 @@ __device__ DQ face_dq(double q, double hflow, double dA, bool e0max, H0 h0f, H1 
   if (!deq0(qn)) {
     const float hf = approx_abs_f(hflow);
     int t = decide(approx_abs_f(qn) / (hf * sqrtf(9.81f * hf)), flf);
-    if (t == 0) t = dgt(ddiv_rn(fabs(ddiv_rn(qn, hflow)), isqrt_rn(kG * hflow)), fl) ? 1 : -1;
+    if (t == 0) t = adj_froude_exceeds(qn, hflow, fl) ? 1 : -1;
     if (t > 0) {
-      const double sg = isqrt_rn(kG * hflow);
+      const double sg = adj_sqrt_ghf(hflow);
       const double g = 1.5 * sg * fl;
       if (dgt0(qn)) {
         qn = hflow * (sg * fl);
@@ -146,8 +156,8 @@ __device__ DQ face_dq(double q, double hflow, double dA, bool e0max, H0 h0f, H1 
     int t = decide(approx_abs_f(qn) * dtf / DXf, approx_f(h0) * 0.25f);
     if (t == 0) t = adj_depth_exceeds(qn, dt, DX, h0) ? 1 : -1;
     if (t > 0) {
-      qn = ddiv_rn(ddiv_rn(h0 * DX, 5.0), dt);
-      d_q = 0, d_nn = 0, dh0 = ddiv_rn(ddiv_rn(DX, 5.0), dt), dh1 = 0, de0 = de1 = 0;
+      qn = adj_limit_value(h0, DX, dt);
+      d_q = 0, d_nn = 0, dh0 = adj_limit_value(1.0, DX, dt), dh1 = 0, de0 = de1 = 0;
     }
   }
   if (dlt0(qn)) {
@@ -155,8 +165,8 @@ __device__ DQ face_dq(double q, double hflow, double dA, bool e0max, H0 h0f, H1 
     int t = decide(approx_abs_f(qn) * dtf / DXf, approx_f(h1) * 0.25f);
     if (t == 0) t = adj_depth_exceeds_neg(qn, dt, DX, h1) ? 1 : -1;
     if (t > 0) {
-      qn = zero_minus(ddiv_rn(ddiv_rn(h1 * DX, 5.0), dt));
-      d_q = 0, d_nn = 0, dh0 = 0, dh1 = -ddiv_rn(ddiv_rn(DX, 5.0), dt), de0 = de1 = 0;
+      qn = zero_minus(adj_limit_value(h1, DX, dt));
+      d_q = 0, d_nn = 0, dh0 = 0, dh1 = -adj_limit_value(1.0, DX, dt), de0 = de1 = 0;
     }
   }
   r.v = qn;

@@ -10,8 +10,8 @@
 //   k_apply_*        the gather-apply pass with the in-line +/-x lateral
 //                    erosion (:4570-4682) and the +/-y lateral pass
 //                    (:4684-4747), walked in order along independent chains
-//   k_edge_out       sediment leaving the four edges (:4750-4841)
-//   k_erode_post     erode_mult / erode_call of call_erosion
+//   k_edge_out       sediment leaving the four edges (:4750-4841), then
+//                    erode_mult / erode_call of call_erosion
 //
 // Allocation order.  The reference numbers grain records (addGS) in the order
 // its serial loop asks for them: during the entrainment pass a cell asks for
@@ -327,7 +327,7 @@ __global__ void __launch_bounds__(128) k_entrain(const hc_view c, hc_dev* d, int
     }
     if (has_next) {
       cudaGraphSetConditional(next, d->erode_retry ? 1u : 0u);
-      if (d->erode_retry) d->body_kernels += 7;  // the next pass's kernels
+      if (d->erode_retry) d->body_kernels += 5;  // the next pass's kernels
     }
     d->s.tempbmax = tempbmax;  // tempbmax of the last pass
   }
@@ -354,9 +354,12 @@ __global__ void k_alloc_mark(const hc_view c, hc_dev* d, uint32_t* bits) {
   atomicOr(&bits[P >> 2], (1u << sub) << ((P & 3) * 8));
 }
 
-// Per-block counts of requested records (1024 threads x 4 positions).
-__global__ void k_alloc_count(const hc_view c, const hc_dev* d, const uint32_t* bits,
-                              int32_t* block_sums, size_t nwords) {
+// Per-block counts of requested records (1024 threads x 4 positions); the
+// block that finishes last scans them (exclusive, in place) and stores the
+// total.
+__global__ void __launch_bounds__(1024) k_alloc_count(const hc_view c, hc_dev* d,
+                                                      const uint32_t* bits, int32_t* block_sums,
+                                                      size_t nwords, int32_t* total_out) {
   __shared__ int ws[32];
   if (!d->alloc_count) return;
   const size_t w = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -369,38 +372,16 @@ __global__ void k_alloc_count(const hc_view c, const hc_dev* d, const uint32_t* 
     for (int k = 0; k < (int)blockDim.x / 32; k++) s += ws[k];
     block_sums[blockIdx.x] = s;
   }
+  if (!last_to_arrive(&d->alloc_arrive)) return;
+  const int total = scan_block_counts(block_sums, (int)gridDim.x);
+  if (threadIdx.x == 0) *total_out = total;
 }
 
-// Exclusive scan of the block counts (one block, loops over chunks).
-__global__ void k_alloc_scan_blocks(const hc_dev* d, int32_t* block_sums, int nblocks,
-                                    int32_t* total_out) {
-  __shared__ int buf[1024];
-  __shared__ int carry;
-  if (!d->alloc_count) return;
-  if (threadIdx.x == 0) carry = 0;
-  __syncthreads();
-  for (int base = 0; base < nblocks; base += 1024) {
-    int k = base + threadIdx.x;
-    int v = (k < nblocks) ? block_sums[k] : 0;
-    buf[threadIdx.x] = v;
-    __syncthreads();
-    for (int off = 1; off < 1024; off <<= 1) {
-      int t = (threadIdx.x >= (unsigned)off) ? buf[threadIdx.x - off] : 0;
-      __syncthreads();
-      buf[threadIdx.x] += t;
-      __syncthreads();
-    }
-    if (k < nblocks) block_sums[k] = carry + buf[threadIdx.x] - v;
-    __syncthreads();
-    if (threadIdx.x == 1023) carry += buf[1023];
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) *total_out = carry;
-}
-
-// Assign row numbers in key order and clear the bits.
-__global__ void k_alloc_assign(const hc_view c, hc_dev* d, uint32_t* bits,
-                               const int32_t* block_sums, size_t nwords) {
+// Assign row numbers in key order and clear the bits; the block that
+// finishes last adds the new records to the count.
+__global__ void __launch_bounds__(1024) k_alloc_assign(const hc_view c, hc_dev* d,
+                                                       uint32_t* bits, const int32_t* block_sums,
+                                                       size_t nwords, const int32_t* total) {
   __shared__ int ws[32];
   __shared__ int wbase[32];
   if (!d->alloc_count) return;
@@ -447,13 +428,13 @@ __global__ void k_alloc_assign(const hc_view c, hc_dev* d, uint32_t* bits,
     }
     bits[w] = 0u;
   }
-}
-
-__global__ void k_alloc_finish(hc_dev* d, const int32_t* total) {
-  if (!d->alloc_count) return;
-  d->grain_tot += *total;
-  d->s.grain_array_tot = d->grain_tot;
-  d->alloc_count = 0;
+  // every block has read grain_tot and alloc_count when the last arrives
+  if (!last_to_arrive(&d->assign_arrive)) return;
+  if (threadIdx.x == 0) {
+    d->grain_tot += *total;
+    d->s.grain_array_tot = d->grain_tot;
+    d->alloc_count = 0;
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -1302,7 +1283,7 @@ __global__ void __launch_bounds__(128) k_apply_ychains_w(const hc_view c, hc_dev
 // order by its own warp.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(1024) k_edge_out(const hc_view c, hc_dev* d, double* contrib,
-                                                    int32_t* list) {
+                                                    int32_t* list, int post) {
   __shared__ int cnt_s[1024];
   __shared__ float gsum[HC_G + 1];
   if (!(d->it_active && d->rest_active && d->do_erode) || d->erode_retry) return;
@@ -1425,19 +1406,14 @@ __global__ void __launch_bounds__(1024) k_edge_out(const hc_view c, hc_dev* d, d
       s.globalsediq += gsum[n] * DX * DX;
       s.sum_grain[n] += gsum[n] * DX * DX;
     }
-  }
-}
-
-// call_erosion :2277-2294 after erode() returned
-__global__ void k_erode_post(const hc_view c, hc_dev* d, int gated) {
-  if (gated && !(d->it_active && d->rest_active && d->do_erode)) return;
-  if (d->erode_retry) return;
-  hc_scalars& s = d->s;
-  if (gated) {
-    s.erode_mult = x86_trunc_to_int(c.p.ERODEFACTOR / s.tempbmax);
-    if (s.erode_mult < 1) s.erode_mult = 1;
-    if (s.erode_mult > 5) s.erode_mult = 5;
-    s.erode_call = s.counter + s.erode_mult;
+    // call_erosion :2277-2294 after erode() returned (post: the iteration's
+    // own erosion call, not a measurement launch)
+    if (post) {
+      s.erode_mult = x86_trunc_to_int(p.ERODEFACTOR / s.tempbmax);
+      if (s.erode_mult < 1) s.erode_mult = 1;
+      if (s.erode_mult > 5) s.erode_mult = 5;
+      s.erode_call = s.counter + s.erode_mult;
+    }
   }
 }
 
@@ -1502,13 +1478,11 @@ void launch_erode_pass(hc_ctx* c, int max_passes, cudaGraphConditionalHandle nex
   k_alloc_mark<<<nb, 256, 0, c->cs>>>(c->v, c->dev, s.bits);
   count_launch(c, 1);
   int nblocks = (int)((nwords + 1023) / 1024);
-  k_alloc_count<<<nblocks, 1024, 0, c->cs>>>(c->v, c->dev, s.bits, s.block_sums, nwords);
+  k_alloc_count<<<nblocks, 1024, 0, c->cs>>>(c->v, c->dev, s.bits, s.block_sums, nwords,
+                                             s.total);
   count_launch(c, 1);
-  k_alloc_scan_blocks<<<1, 1024, 0, c->cs>>>(c->dev, s.block_sums, nblocks, s.total);
-  count_launch(c, 1);
-  k_alloc_assign<<<nblocks, 1024, 0, c->cs>>>(c->v, c->dev, s.bits, s.block_sums, nwords);
-  count_launch(c, 1);
-  k_alloc_finish<<<1, 1, 0, c->cs>>>(c->dev, s.total);
+  k_alloc_assign<<<nblocks, 1024, 0, c->cs>>>(c->v, c->dev, s.bits, s.block_sums, nwords,
+                                              s.total);
   count_launch(c, 1);
 }
 
@@ -1523,9 +1497,7 @@ void launch_erode_finish(hc_ctx* c, int gated) {
   k_apply_ychains_t<<<kWalkBlocks, 128, 0, c->cs>>>(c->v, c->dev);
   k_apply_ychains_w<<<kWalkBlocks, 128, 0, c->cs>>>(c->v, c->dev);
   count_launch(c, 6);
-  k_edge_out<<<1, 1024, 0, c->cs>>>(c->v, c->dev, s.contrib, nullptr);
-  count_launch(c, 1);
-  k_erode_post<<<1, 1, 0, c->cs>>>(c->v, c->dev, gated);
+  k_edge_out<<<1, 1024, 0, c->cs>>>(c->v, c->dev, s.contrib, nullptr, gated);
   count_launch(c, 1);
 }
 

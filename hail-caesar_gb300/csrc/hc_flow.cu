@@ -258,9 +258,9 @@ __global__ void k_control(const hc_view c, hc_dev* d, hc_iter_handles hh) {
   d->erode_retry = d->do_erode;
   d->do_slide = !p.hydro_only && ((long long)s.counter % p.in_channel_landslide_iter_interval) == 0;
   if (hh.has) {
-    // kernels inside the bodies enabled here: scan 4, erosion 8 + 8, slide_3 5
-    d->body_kernels += (d->do_scan ? 4 : 0) + (d->do_erode && !p.hydro_only ? 16 : 0) +
-                       (d->do_slide ? 5 : 0);
+    // kernels inside the bodies enabled here: scan 3, erosion 6 + 7, slide_3 4
+    d->body_kernels += (d->do_scan ? 3 : 0) + (d->do_erode && !p.hydro_only ? 13 : 0) +
+                       (d->do_slide ? 4 : 0);
     cudaGraphSetConditional(hh.scan, d->do_scan ? 1u : 0u);
     if (!p.hydro_only) {
       cudaGraphSetConditional(hh.erode, d->do_erode ? 1u : 0u);
@@ -336,6 +336,23 @@ static __device__ __noinline__ bool sed_exceeds_neg(double qs, double dt, double
   return fabs(qs * dt) > (v * DX) / 4;  // :3169
 }
 
+// The limiters' replacement values and the Froude test's exact form, out of
+// line as well: they run for few faces, and inlined, their integer-pipe
+// divisions and square roots would double the kernel's code, whose
+// instruction fetches stall the warps more than anything else.
+// (x * DX / 5) / dt, the depth and sediment limits' value (:3140, :3165)
+static __device__ __noinline__ double limit_value(double x, double DX, double dt) {
+  return ddiv_rn(ddiv_rn(x * DX, 5.0), dt);
+}
+// |q/hflow| / sqrt(g hflow) > froude_limit, exactly (:3124)
+static __device__ __noinline__ bool froude_exceeds(double qoh, double hflow, double fl) {
+  return dgt(ddiv_rn(fabs(qoh), isqrt_rn(kG * hflow)), fl);
+}
+// hflow * (sqrt(g hflow) * froude_limit), the Froude limit's value (:3127)
+static __device__ __noinline__ double froude_value(double hflow, double fl) {
+  return hflow * (isqrt_rn(kG * hflow) * fl);
+}
+
 // Three-way test of A > B from float estimates a, b, each within a relative
 // 2^-18 of A, B (or flushed to 0 below 2^-126, inf above the float range):
 // +1 surely greater, -1 surely not, 0 too close to call (the caller then
@@ -377,12 +394,13 @@ __device__ __forceinline__ void inertial_face_core(double& q, double& qs, double
   if (edge_slope == 1) slope = p.edgeslope;
   if (edge_slope == -1) slope = zero_minus(p.edgeslope);
   const double ghd = kG * hflow * dt;
-  double qn;
-  if (deq0(q)) {
-    // (0 - ghd*slope) / (1 + (ghd*nn*0)/h^3) = (0 - ghd*slope) / 1
-    qn = q - (ghd * slope);
-  } else {
-    qn = ddiv_rn(q - (ghd * slope), 1 + ddiv_rn(ghd * nn * fabs(q), icube_rn(hflow)));
+  // the numerator once for both branches (a branch apiece would issue its
+  // FP64 instructions twice in a warp that holds both)
+  double qn = q - (ghd * slope);
+  // q = 0: (0 - ghd*slope) / (1 + (ghd*nn*0)/h^3) = (0 - ghd*slope) / 1
+  if (!deq0(q)) {
+    const double aq = __longlong_as_double(dbits(q) & 0x7fffffffffffffffLL);  // fabs
+    qn = ddiv_rn(qn, 1 + ddiv_rn(ghd * nn * aq, icube_rn(hflow)));
   }
   const float hf = approx_abs_f(hflow);
   const float dtf = approx_abs_f(dt);
@@ -403,10 +421,10 @@ __device__ __forceinline__ void inertial_face_core(double& q, double& qs, double
     int t = decide_gt(fr, c.flf);
     if (t == 0) {
       if (!qoh_valid) qoh = ddiv_rn(qn, hflow);
-      t = dgt(ddiv_rn(fabs(qoh), isqrt_rn(kG * hflow)), p.froude_limit) ? 1 : -1;
+      t = froude_exceeds(qoh, hflow, p.froude_limit) ? 1 : -1;
     }
     if (t > 0) {
-      const double lim = hflow * (isqrt_rn(kG * hflow) * p.froude_limit);
+      const double lim = froude_value(hflow, p.froude_limit);
       qn = dgt0(qn) ? lim : zero_minus(lim);
       qoh_valid = false;
     }
@@ -417,7 +435,7 @@ __device__ __forceinline__ void inertial_face_core(double& q, double& qs, double
     int t = decide_gt(approx_abs_f(qn) * dtf / c.DXf, approx_f(h0) * 0.25f);
     if (t == 0) t = depth_exceeds(qn, dt, DX, h0) ? 1 : -1;
     if (t > 0) {
-      qn = ddiv_rn(ddiv_rn(h0 * DX, 5.0), dt);
+      qn = limit_value(h0, DX, dt);
       qoh_valid = false;
     }
   }
@@ -425,25 +443,25 @@ __device__ __forceinline__ void inertial_face_core(double& q, double& qs, double
     int t = decide_gt(approx_abs_f(qn) * dtf / c.DXf, approx_f(h1) * 0.25f);
     if (t == 0) t = depth_exceeds_neg(qn, dt, DX, h1) ? 1 : -1;
     if (t > 0) {
-      qn = zero_minus(ddiv_rn(ddiv_rn(h1 * DX, 5.0), dt));
+      qn = zero_minus(limit_value(h1, DX, dt));
       qoh_valid = false;
     }
   }
   const bool qpos = dgt0(qn), qneg = dlt0(qn);
   if (kSusp) {
     // qs = q * (V/h) of the giving cell; V = 0 gives 0 * q (a signed zero)
-    if (qpos) qs = qn * c0;
-    if (qneg) qs = qn * (deq0(v1) ? v1 : ddiv_rn(v1, h1));  // h1 > 0 here, as h0 above
+    // (one product for both signs: h1 > 0 here, as h0 above)
+    if (qpos || qneg) qs = qn * (qpos ? c0 : (deq0(v1) ? v1 : ddiv_rn(v1, h1)));
     // qs*dt > V*DX/4 (giving cell) caps the sediment flux
     if (dgt0(qs)) {
       int t = decide_gt(approx_abs_f(qs) * dtf, approx_f(v0) * c.DXf * 0.25f);
       if (t == 0) t = sed_exceeds(qs, dt, v0, DX) ? 1 : -1;
-      if (t > 0) qs = ddiv_rn(ddiv_rn(v0 * DX, 5.0), dt);
+      if (t > 0) qs = limit_value(v0, DX, dt);
     }
     if (dlt0(qs)) {
       int t = decide_gt(approx_abs_f(qs) * dtf, approx_f(v1) * c.DXf * 0.25f);
       if (t == 0) t = sed_exceeds_neg(qs, dt, v1, DX) ? 1 : -1;
-      if (t > 0) qs = zero_minus(ddiv_rn(ddiv_rn(v1 * DX, 5.0), dt));
+      if (t > 0) qs = zero_minus(limit_value(v1, DX, dt));
     }
   }
   if (kVel) {
@@ -728,12 +746,23 @@ __global__ void __launch_bounds__(256, 6) k_depth_update(const hc_view c, hc_dev
       const double uy1 = mr ? 0.0 : c.qy[cell + 1], uy0 = ml ? 0.0 : c.qy[cell];
       edge += ddiv_by(dt * (ux1 - ux0 + uy1 - uy0), c.dxd);
     }
+    // Where the four fluxes are zero (either sign) the update adds a signed
+    // zero, which leaves any value but -0 as it is: the FP64 work is skipped
+    // then (dry pockets of the list; cells without suspended load).
+    constexpr long long kNegZero = (long long)0x8000000000000000ULL;
     double h = c.h[cell];
-    h += ddiv_by(dt * (c.qx[cell + W] - c.qx[cell] + c.qy[cell + 1] - c.qy[cell]), c.dxd);
+    {
+      const double a = c.qx[cell + W], b = c.qx[cell], e = c.qy[cell + 1], f = c.qy[cell];
+      if (((dbits(a) | dbits(b) | dbits(e) | dbits(f)) << 1) != 0 || dbits(h) == kNegZero)
+        h += ddiv_by(dt * (a - b + e - f), c.dxd);
+    }
     // hydro-only runs keep Vsusptot at zero (no sediment source exists)
-    if (susp)
-      c.vs[cell] += ddiv_by(dt * (c.qxs[cell + W] - c.qxs[cell] + c.qys[cell + 1] - c.qys[cell]),
-                            c.dxd);
+    if (susp) {
+      const double a = c.qxs[cell + W], b = c.qxs[cell], e = c.qys[cell + 1], f = c.qys[cell];
+      const double v = c.vs[cell];
+      if (((dbits(a) | dbits(b) | dbits(e) | dbits(f)) << 1) != 0 || dbits(v) == kNegZero)
+        c.vs[cell] = v + ddiv_by(dt * (a - b + e - f), c.dxd);
+    }
     nonfinite |= disnan(h);
     if (dgt0(h)) {
       if (dbits(c.elev[cell]) == kNoDataBits) {
@@ -786,7 +815,7 @@ __global__ void __launch_bounds__(256, 6) k_depth_update(const hc_view c, hc_dev
 // scan_area :3821-3849 (every scan_area_interval_iter iterations)
 // ---------------------------------------------------------------------------
 // Also the ledger's volume: the depth sum of its block (rows 1..imax,
-// columns 1..jmax) into vpart, added up in order by k_wet_scan.
+// columns 1..jmax) into vpart, added up in order by k_wet_count's last block.
 __global__ void __launch_bounds__(256) k_scan_area(const hc_view c, const hc_dev* __restrict__ d,
                                                     int gated) {
   if (gated && !(d->it_active && d->do_scan)) return;
@@ -809,7 +838,12 @@ __global__ void __launch_bounds__(256) k_scan_area(const hc_view c, const hc_dev
 
 // The wet list: mask bytes counted per block of 1024 cells, the counts
 // scanned, the cell numbers written in ascending order.
-__global__ void __launch_bounds__(1024) k_wet_count(const hc_view c, const hc_dev* d, int gated) {
+// The block counts, then, in the block that finishes last, their exclusive
+// scan (the wet list's offsets per block) and the list's length.  nvol:
+// blocks of the k_scan_area launch before it, whose volume partials the same
+// block adds up (0: none, the list is rebuilt from a mask kept as it was).
+__global__ void __launch_bounds__(1024) k_wet_count(const hc_view c, hc_dev* d, int gated,
+                                                    int nvol) {
   __shared__ int ws[32];
   if (gated && !(d->it_active && d->do_scan)) return;
   const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -822,15 +856,7 @@ __global__ void __launch_bounds__(1024) k_wet_count(const hc_view c, const hc_de
     for (int k = 0; k < 32; k++) s += ws[k];
     c.wet_sums[blockIdx.x] = s;
   }
-}
-
-// nvol: blocks of the k_scan_area launch before it, whose volume partials it
-// adds up (0: none, the list is rebuilt from a mask kept as it was)
-__global__ void __launch_bounds__(1024) k_wet_scan(const hc_view c, hc_dev* d, int nblocks,
-                                                   int gated, int nvol) {
-  __shared__ int buf[1024];
-  __shared__ int carry;
-  if (gated && !(d->it_active && d->do_scan)) return;
+  if (!last_to_arrive(&d->wet_arrive)) return;
   if (nvol > 0) {
     double a = 0;
     for (int k = threadIdx.x; k < nvol; k += blockDim.x) a += c.vpart[k];
@@ -840,25 +866,8 @@ __global__ void __launch_bounds__(1024) k_wet_scan(const hc_view c, hc_dev* d, i
       d->vol_scan_counter = d->s.counter;
     }
   }
-  if (threadIdx.x == 0) carry = 0;
-  __syncthreads();
-  for (int base = 0; base < nblocks; base += 1024) {
-    const int k = base + threadIdx.x;
-    const int v = (k < nblocks) ? c.wet_sums[k] : 0;
-    buf[threadIdx.x] = v;
-    __syncthreads();
-    for (int off = 1; off < 1024; off <<= 1) {
-      const int t = (threadIdx.x >= (unsigned)off) ? buf[threadIdx.x - off] : 0;
-      __syncthreads();
-      buf[threadIdx.x] += t;
-      __syncthreads();
-    }
-    if (k < nblocks) c.wet_sums[k] = carry + buf[threadIdx.x] - v;
-    __syncthreads();
-    if (threadIdx.x == 1023) carry += buf[1023];
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) d->wet_count = carry;
+  const int total = scan_block_counts(c.wet_sums, (int)gridDim.x);
+  if (threadIdx.x == 0) d->wet_count = total;
 }
 
 __global__ void __launch_bounds__(1024) k_wet_write(const hc_view c, const hc_dev* d, int gated) {
@@ -1100,10 +1109,9 @@ void launch_wet_list(hc_ctx* c, int gated) { wet_list(c, gated, 0); }
 
 static void wet_list(hc_ctx* c, int gated, int nvol) {
   const int nb = (int)((c->v.N2 + 1023) / 1024);
-  k_wet_count<<<nb, 1024, 0, c->cs>>>(c->v, c->dev, gated);
-  k_wet_scan<<<1, 1024, 0, c->cs>>>(c->v, c->dev, nb, gated, nvol);
+  k_wet_count<<<nb, 1024, 0, c->cs>>>(c->v, c->dev, gated, nvol);
   k_wet_write<<<nb, 1024, 0, c->cs>>>(c->v, c->dev, gated);
-  count_launch(c, 3);
+  count_launch(c, 2);
 }
 
 void launch_flux_out(hc_ctx* c, int gated, int record) {

@@ -78,6 +78,10 @@ struct hc_dev {
   unsigned int depth_done;   // blocks finished in depth_update (last-block reduction)
   unsigned int pass_done;    // blocks finished in an entrainment pass
   unsigned int misc_done;
+  // arrival counters of the launches whose last block finishes the step
+  // (last_to_arrive): the wet list's count, the grain records' count and
+  // assignment, slide_3's flag count; each is zero between launches
+  unsigned int wet_arrive, alloc_arrive, assign_arrive, flag_arrive;
   unsigned long long body_kernels;  // kernels run inside conditional graph nodes
   int wet_count;          // length of hc_view::wet
   int do_drain;           // this iteration moved the baseflow threshold
@@ -277,7 +281,10 @@ inline void count_launch(hc_ctx* c, int n) {
 // Every thread of the block calls it; blockDim a multiple of 32, <= 1024.
 __device__ __forceinline__ double block_sum(double v) {
   __shared__ double ws[32];
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  // a warp whose values are all +0 sums to +0: no FP64 adds (sums of
+  // sparse terms, like the ledger's border fluxes, are mostly such warps)
+  if (__ballot_sync(0xffffffffu, __double_as_longlong(v) != 0))
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
   const int t = threadIdx.x + threadIdx.y * blockDim.x;
   const int nw = (blockDim.x * blockDim.y) >> 5;
   __syncthreads();  // ws may still be read by a previous call
@@ -287,6 +294,51 @@ __device__ __forceinline__ double block_sum(double v) {
   if (t == 0)
     for (int w = 0; w < nw; w++) s += ws[w];
   return s;
+}
+
+// Called once by every block of a launch (all its threads), after the
+// block's own writes: true in every thread of the block that arrives last,
+// which then sees every block's writes (read them through volatile or
+// __ldcg: L1 is not coherent); the counter is back at zero afterwards.
+__device__ __forceinline__ bool last_to_arrive(unsigned int* counter) {
+  __shared__ bool last;
+  __syncthreads();
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    __threadfence();
+    last = atomicAdd(counter, 1u) == gridDim.x * gridDim.y - 1;
+    if (last) *counter = 0;
+  }
+  __syncthreads();
+  if (last) __threadfence();
+  return last;
+}
+
+// Exclusive prefix sums, in place, of the per-block counts sums[0..n)
+// written by the blocks of the same launch, by one block of 1024 threads;
+// returns the total (in every thread).
+__device__ __forceinline__ int scan_block_counts(int32_t* sums, int n) {
+  __shared__ int buf[1024];
+  __shared__ int carry;
+  volatile int32_t* vs = sums;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (int base = 0; base < n; base += 1024) {
+    const int k = base + threadIdx.x;
+    const int v = (k < n) ? vs[k] : 0;
+    buf[threadIdx.x] = v;
+    __syncthreads();
+    for (int off = 1; off < 1024; off <<= 1) {
+      const int t = (threadIdx.x >= (unsigned)off) ? buf[threadIdx.x - off] : 0;
+      __syncthreads();
+      buf[threadIdx.x] += t;
+      __syncthreads();
+    }
+    if (k < n) vs[k] = carry + buf[threadIdx.x] - v;
+    __syncthreads();
+    if (threadIdx.x == 1023) carry += buf[1023];
+    __syncthreads();
+  }
+  return carry;
 }
 
 // Deterministic grid-wide sum: each block stores its block_sum in part[b];
@@ -574,6 +626,43 @@ HC_DEV double ddiv_by(double a, const hc_divisor& d) {
 }
 
 HC_DEV double ddiv_rn(double a, double b) { return ddiv_by(a, ddiv_prep(b)); }
+
+// RN(a * b), the IEEE product, on the integer pipes: the 106-bit product of
+// the significands from one 64 x 64 multiply (low and high halves), rounded
+// at its 53rd bit with the round bit and the bits below it.  A zero times a
+// finite number gives the signed zero here; other operands that are zero,
+// subnormal, infinite or NaN, and products outside the normal range, take
+// the hardware multiplication (out of line: its FP64 instruction issues only
+// where it runs).
+static __device__ __noinline__ double dmul_hw(double a, double b) { return __dmul_rn(a, b); }
+
+HC_DEV double imul_rn(double a, double b) {
+  const unsigned long long A = (unsigned long long)__double_as_longlong(a);
+  const unsigned long long B = (unsigned long long)__double_as_longlong(b);
+  const unsigned long long M52 = (1ull << 52) - 1, H52 = 1ull << 52;
+  const unsigned long long sgn = (A ^ B) & 0x8000000000000000ull;
+  const int ea = (int)(A >> 52) & 0x7ff, eb = (int)(B >> 52) & 0x7ff;
+  if (ea == 0 || eb == 0 || ea == 0x7ff || eb == 0x7ff) {
+    if ((((A << 1) == 0) && eb != 0x7ff) || (((B << 1) == 0) && ea != 0x7ff))
+      return __longlong_as_double((long long)sgn);
+    return dmul_hw(a, b);
+  }
+  const unsigned long long ma = (A & M52) | H52, mb = (B & M52) | H52;
+  const unsigned long long lo = ma * mb, hi = __umul64hi(ma, mb);  // in [2^104, 2^106)
+  const int top = (int)(hi >> 41) & 1;                              // bit 105
+  const int sh = 52 + top;
+  unsigned long long sig = (hi << (64 - sh)) | (lo >> sh);
+  const unsigned long long rem = lo & ((1ull << sh) - 1), half = 1ull << (sh - 1);
+  int er = ea + eb - 1023 + top;
+  if (er < 1) return dmul_hw(a, b);  // a subnormal (or zero) product
+  if (rem > half || (rem == half && (sig & 1))) sig++;
+  if (sig == (H52 << 1)) {
+    sig = H52;
+    er++;
+  }
+  if (er > 2046) return dmul_hw(a, b);  // overflow
+  return __longlong_as_double((long long)(sgn | ((unsigned long long)er << 52) | (sig & M52)));
+}
 
 // hc_divisor for a divisor fixed for the run, V exact (floor(2^116/mb))
 hc_divisor host_divisor(double b);

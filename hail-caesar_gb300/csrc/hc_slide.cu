@@ -193,8 +193,11 @@ __global__ void k_slide_probe(const hc_view c, const hc_dev* d, uint8_t* flag, d
   flag[o.pos(x, y)] = f;
 }
 
-__global__ void k_flag_count(const uint8_t* flag, size_t n, int32_t* block_sums, const hc_dev* d,
-                             int gated) {
+// Per-block counts of the flags; the block that finishes last scans them
+// (exclusive, in place) and stores the total.
+__global__ void __launch_bounds__(1024) k_flag_count(const uint8_t* flag, size_t n,
+                                                     int32_t* block_sums, int32_t* total,
+                                                     hc_dev* d, int gated) {
   __shared__ int ws[32];
   if (gated && !(d->it_active && d->rest_active && d->do_slide)) return;
   const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -207,32 +210,9 @@ __global__ void k_flag_count(const uint8_t* flag, size_t n, int32_t* block_sums,
     for (int k = 0; k < (int)blockDim.x / 32; k++) s += ws[k];
     block_sums[blockIdx.x] = s;
   }
-}
-
-__global__ void k_flag_scan(int32_t* block_sums, int nblocks, int32_t* total, const hc_dev* d,
-                            int gated) {
-  __shared__ int buf[1024];
-  __shared__ int carry;
-  if (gated && !(d->it_active && d->rest_active && d->do_slide)) return;
-  if (threadIdx.x == 0) carry = 0;
-  __syncthreads();
-  for (int base = 0; base < nblocks; base += 1024) {
-    int k = base + threadIdx.x;
-    int v = (k < nblocks) ? block_sums[k] : 0;
-    buf[threadIdx.x] = v;
-    __syncthreads();
-    for (int off = 1; off < 1024; off <<= 1) {
-      int t = (threadIdx.x >= (unsigned)off) ? buf[threadIdx.x - off] : 0;
-      __syncthreads();
-      buf[threadIdx.x] += t;
-      __syncthreads();
-    }
-    if (k < nblocks) block_sums[k] = carry + buf[threadIdx.x] - v;
-    __syncthreads();
-    if (threadIdx.x == 1023) carry += buf[1023];
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) *total = carry;
+  if (!last_to_arrive(&d->flag_arrive)) return;
+  const int t = scan_block_counts(block_sums, (int)gridDim.x);
+  if (threadIdx.x == 0) *total = t;
 }
 
 __global__ void k_flag_compact(const uint8_t* flag, size_t n, const int32_t* block_sums,
@@ -799,9 +779,7 @@ static void slide_sweep(hc_ctx* c, double factor, int gated) {
   count_launch(c, 1);
   const size_t n = c->v.N2;
   const int nblocks = (int)((n + 1023) / 1024);
-  k_flag_count<<<nblocks, 1024, 0, c->cs>>>(s.flag, n, s.block_sums, c->dev, gated);
-  count_launch(c, 1);
-  k_flag_scan<<<1, 1024, 0, c->cs>>>(s.block_sums, nblocks, s.count, c->dev, gated);
+  k_flag_count<<<nblocks, 1024, 0, c->cs>>>(s.flag, n, s.block_sums, s.count, c->dev, gated);
   count_launch(c, 1);
   k_flag_compact<<<nblocks, 1024, 0, c->cs>>>(s.flag, n, s.block_sums, s.list, c->dev, gated);
   count_launch(c, 1);
@@ -837,9 +815,8 @@ hc_status run_global_landsliding(hc_ctx* c, int* sweeps) {
     inc++;
     cudaMemsetAsync(s.flag, 0, n, c->s);
     k_gslide_probe<<<g, b, 0, c->s>>>(c->v, s.flag, slide_factor(c));
-    k_flag_count<<<nblocks, 1024, 0, c->s>>>(s.flag, n, s.block_sums, c->dev, 0);
-    k_flag_scan<<<1, 1024, 0, c->s>>>(s.block_sums, nblocks, s.count, c->dev, 0);
-    count_launch(c, 3);
+    k_flag_count<<<nblocks, 1024, 0, c->s>>>(s.flag, n, s.block_sums, s.count, c->dev, 0);
+    count_launch(c, 2);
     cudaError_t e = cudaMemcpyAsync(&h_count, s.count, 4, cudaMemcpyDeviceToHost, c->s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->s);
     if (e != cudaSuccess) return hc_cuda(c, e, "global_landsliding");

@@ -246,9 +246,12 @@ def catchment_case(n=2000, DX=20.0, seed=2, hours=72, lateral=True, hydro_only=F
 
 
 def flow_case(n=8192, DX=5.0, seed=3, hours=2, rain_mmh=30.0, jmax=None, relief=150.0,
-              fill=False):
+              fill=False, grid_rain=False):
     """Flow-only bandwidth case: fractal DEM at `relief` m, uniform rain
-    `rain_mmh` for `hours` h, erosion off."""
+    `rain_mmh` for `hours` h, erosion off.  grid_rain: the rain reaches every
+    cell (the distributed TOPMODEL runoff grid, spatially_complex_rainfall)
+    instead of the drainage network's input points, so the whole grid is
+    wet."""
     imax = n
     jmax = n if jmax is None else jmax
     z = fractal_dem(imax, jmax, relief, seed, fill=fill)
@@ -259,6 +262,8 @@ def flow_case(n=8192, DX=5.0, seed=3, hours=2, rain_mmh=30.0, jmax=None, relief=
     p.hydro_only = 1
     p.M = 0.005
     p.edgeslope = 0.005
+    if grid_rain:
+        p.spatially_complex_rainfall = 1
     rows = int(p.maxcycle * 60 / p.rain_data_time_step) + 100
     rain = np.zeros((rows, 1), dtype=np.float32)
     rain[: hours] = rain_mmh

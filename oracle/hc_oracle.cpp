@@ -86,6 +86,9 @@ struct hco_model {
   double time_1 = 1, baseflow = 0, sediQ = 0, globalsediq = 0, tempbmax = 0;
   double creep_time = 1, creep_time2 = 1;
   int grain_array_tot = 1;
+  // a record beyond the grain arrays' N2/LIMIT rows was asked for (the
+  // reference's arrays would overflow); hco_iterate stops
+  bool grain_full = false;
   int totalinputpoints = 0;
   std::vector<double> sum_grain, jv, jo, j_mean, old_j_mean, new_j_mean;
   // runoffGrid (LSDRainfallRunoff.cpp:120-133), per cell, for the
@@ -531,7 +534,12 @@ static void sort_active(hco_model* m, unsigned x, unsigned y) {  // :3874-3947
 }
 
 static void addGS(hco_model* m, unsigned x, unsigned y) {  // :3949-3983
-  HCO_PRAGMA(omp critical(hco_addGS)) {
+  // rows 0 .. N2/LIMIT - 1 exist; past the second last, the cell gets the
+  // last row as scratch (no write outside the arrays) and the run stops
+  HCO_PRAGMA(omp critical(hco_addGS)) if ((size_t)m->grain_array_tot + 2 >= m->grain.size() / 11) {
+    m->grain_full = true;
+    m->IDX(x, y) = (int32_t)(m->grain.size() / 11) - 1;
+  } else {
     const double active = m->p.active;
     m->grain_array_tot++;
     const int r = m->grain_array_tot;
@@ -1583,6 +1591,8 @@ extern "C" void hco_prepare(hco_model* m) {
 extern "C" long hco_iterate(hco_model* m, long n, int flags, hco_step_record* rec) {
   long it = 0;
   const hc_params& p = m->p;
+  // the main loop has ended (:1838): nothing runs, as in hc_run
+  if (m->counter > 0 && !(m->cycle / 60 < p.maxcycle)) return 0;
   do {
     m->previous = m->cycle;                       // set_loop_cycle
     m->iod = std::abs(m->waterinput - m->waterOut);  // set_inputoutput_diff
@@ -1644,6 +1654,7 @@ extern "C" long hco_iterate(hco_model* m, long n, int flags, hco_step_record* re
     }
     m->vin_it = m->vout_it = m->vlost_it = m->vmask_it = 0;
     it++;
+    if (m->grain_full) break;
     if (n >= 0 && it >= n) break;
   } while (m->cycle / 60 < p.maxcycle);
   return it;
@@ -1686,7 +1697,8 @@ extern "C" double hco_get_scalar(hco_model* m, const char* name) {
   S("waterinput", m->waterinput) S("waterOut", m->waterOut) S("counter", m->counter)
   S("erode_call", m->erode_call) S("erode_mult", m->erode_mult)
   S("lateralcounter", m->lateralcounter) S("time_1", m->time_1) S("baseflow", m->baseflow)
-  S("grain_array_tot", m->grain_array_tot) S("sediQ", m->sediQ)
+  S("grain_array_tot", m->grain_array_tot) S("grain_full", m->grain_full ? 1.0 : 0.0)
+  S("sediQ", m->sediQ)
   S("globalsediq", m->globalsediq) S("tempbmax", m->tempbmax)
   S("totalinputpoints", m->totalinputpoints) S("temptot", m->temptot)
   S("mannings", m->mannings) S("j_mean1", m->j_mean.size() > 1 ? m->j_mean[1] : 0)

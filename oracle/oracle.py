@@ -151,6 +151,8 @@ class Oracle:
         cap = n if n >= 0 else 10_000_000
         rec = np.zeros((cap, len(STEP_FIELDS)), dtype=np.float64)
         done = self.lib.hco_iterate(self.h, n, flags, rec.ctypes.data)
+        if self.scalar("grain_full"):
+            raise RuntimeError("grain records beyond the N2/LIMIT rows the reference allocates")
         return rec[:done]
 
     def load_from(self, model):
