@@ -1023,13 +1023,11 @@ extern "C" hc_status hc_creep(hc_ctx* c, double time) {
 // ------------------------------------------------------------------ hc_run
 static void launch_iteration(hc_ctx* c, int flags) {
   launch_control(c);
-  if (!c->v.p.hydro_only) launch_drain_snapshot(c);
   launch_inputs(c);
   launch_flow_route(c, 1);
   launch_depth_update(c, 1);
   launch_scan_area(c, 1);
   if (!c->v.p.hydro_only) {
-    launch_erode_begin(c, 1, -1);
     for (int k = 0; k < HC_ERODE_PASSES; k++) launch_erode_pass(c, HC_ERODE_PASSES);
     launch_erode_finish(c, 1);
     if (flags & HC_RUN_LATERAL) launch_lateral_check(c);
@@ -1092,7 +1090,6 @@ static hc_status capture_iteration(hc_ctx* c, int flags) {
   H.has = 1;
   launch_control(c);
   H.has = 0;  // no other launch sets the iteration's conditions
-  if (sed) launch_drain_snapshot(c);
   if (c->v.adj_sh) launch_adj_save(c);
   launch_inputs(c);
   launch_flow_route(c, 1);
@@ -1100,10 +1097,7 @@ static hc_status capture_iteration(hc_ctx* c, int flags) {
   HC_TRY(capture_if(c, H.scan, [&] { launch_scan_area(c, 1); }));
   if (sed) {
     const hc_iter_handles h = H;
-    HC_TRY(capture_if(c, h.erode, [&] {
-      launch_erode_begin(c, 1, -1);
-      launch_erode_pass(c, HC_ERODE_PASSES, h.retry2, 1);
-    }));
+    HC_TRY(capture_if(c, h.erode, [&] { launch_erode_pass(c, HC_ERODE_PASSES, h.retry2, 1); }));
     HC_TRY(capture_if(c, h.retry2, [&] { launch_erode_pass(c, HC_ERODE_PASSES, h.retry3, 1); }));
     HC_TRY(capture_if(c, h.retry3, [&] { launch_erode_pass(c, HC_ERODE_PASSES, h.retry4, 1); }));
     HC_TRY(capture_if(c, h.retry4, [&] { launch_erode_pass(c, HC_ERODE_PASSES); }));
@@ -1545,7 +1539,6 @@ extern "C" hc_status hc_profile_iteration(hc_ctx* c, int32_t flags, double* ms) 
   for (int k = 0; k < 10; k++) HC_CU(cudaEventCreate(&ev[k]), "profile");
   cudaEventRecord(ev[0], c->s);
   launch_control(c);
-  if (!c->v.p.hydro_only) launch_drain_snapshot(c);
   launch_inputs(c);
   cudaEventRecord(ev[1], c->s);
   launch_flow_route(c, 1);
@@ -1556,7 +1549,6 @@ extern "C" hc_status hc_profile_iteration(hc_ctx* c, int32_t flags, double* ms) 
   cudaEventRecord(ev[4], c->s);
   const bool sed = !c->v.p.hydro_only;
   if (sed) {
-    launch_erode_begin(c, 1, -1);
     HC_TRY(pull(c));
     for (int guard = 0; hd->erode_retry && hd->it_active && guard < 100000; guard++) {
       launch_erode_pass(c, 0);

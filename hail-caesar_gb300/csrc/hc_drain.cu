@@ -26,7 +26,7 @@
 // exact sort where that declines).
 //
 // The elevations are those at the start of the iteration that moved the
-// threshold (k_drain_snapshot copies them before the iteration's erosion).
+// threshold (k_depth_update copies them before the iteration's erosion).
 
 #include "hc_internal.cuh"
 
@@ -127,15 +127,6 @@ __global__ void k_sel_pick(const hc_view c, int shift, unsigned long long paddin
   a->prefix |= (unsigned long long)digit << shift;
   a->mask |= 255ull << shift;
   for (int d = 0; d < 256; d++) a->hist[d] = 0;
-}
-
-// elevations at the start of the iteration (erosion runs change elev later
-// in it); hydro-only runs never change elev
-__global__ void k_drain_snapshot(const hc_view c, const hc_dev* d) {
-  if (!(d->it_active && d->do_drain)) return;
-  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < c.N2;
-       k += (size_t)gridDim.x * blockDim.x)
-    c.drain_snap[k] = c.elev[k];
 }
 
 // sorted position of every cell the sweep reaches (1 .. imax*jmax); 0 = not
@@ -607,11 +598,6 @@ __global__ void k_points_finish(const hc_view c, hc_dev* d) {
 }
 
 }  // namespace
-
-void launch_drain_snapshot(hc_ctx* c) {
-  k_drain_snapshot<<<152 * 4, 256, 0, c->cs>>>(c->v, c->dev);
-  count_launch(c, 1);
-}
 
 // The drainage area for the elevations `el` (device), then the input points.
 // `sort_order` is called, and its order used, only when the sort's order

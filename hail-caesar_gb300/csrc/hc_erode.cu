@@ -1,7 +1,8 @@
 // erode(mult) :4211-4845 ("erodedepo"), with call_erosion :2277-2294.
 //
 // Structure on the device:
-//   k_erode_begin    time_step *= 1.5 (:4219), open the retry loop
+//   k_erode_begin    time_step *= 1.5 (:4219), open the retry loop (a direct
+//                    call; an iteration's k_control does this itself)
 //   k_entrain_tau, k_entrain  the entrainment pass (:4236-4548): shear stress
 //                    per cell, then the transport of the cells with tau > 0;
 //                    its last block evaluates the retry test (:4550-4565)
@@ -41,8 +42,13 @@ __device__ __forceinline__ size_t EX(const hc_view& c, int x, int y) {
   return (size_t)x * (c.jmax + 1) + y;
 }
 
-// blocks of 128 threads of the transport kernel (grid-stride over its list)
-constexpr unsigned kEntrainBlocks = 152 * 8;
+// blocks of 128 threads of the transport kernel (grid-stride over its
+// list): 1216 on large grids, fewer on small ones, whose lists are short and
+// whose idle blocks would only cost dispatch (ensembles of small members run
+// many such launches side by side)
+static unsigned entrain_blocks(size_t N2) {
+  return (unsigned)std::min<size_t>(152 * 8, std::max<size_t>(16, N2 / 1024));
+}
 
 __global__ void k_erode_begin(const hc_view c, hc_dev* d, int gated, double mult_override) {
   if (gated) {
@@ -674,8 +680,14 @@ __global__ void __launch_bounds__(256) k_apply_gather(const hc_view c, hc_dev* d
 // longer chain to the warp walkers: the rows it holds go back to memory and
 // the rest of the chain is listed as a resume point (bit 31: the row before
 // it is part of the chain).
-constexpr unsigned kWalkBlocks = 152 * 8;            // blocks of 128 threads
-constexpr unsigned kWarpChains = kWalkBlocks * 4;    // warps in flight
+// Blocks of 128 threads of the chain walkers, sized like entrain_blocks; a
+// pass with no more chains than the launch has warps leaves them all to the
+// warp walkers (both launches have the same grid, so both kernels see the
+// same limit: gridDim.x * 4).
+static unsigned walk_blocks(size_t N2) {
+  return (unsigned)std::min<size_t>(152 * 8, std::max<size_t>(16, N2 / 2048));
+}
+__device__ __forceinline__ unsigned warps_in_flight() { return gridDim.x * (blockDim.x >> 5); }
 constexpr int kHandOff = 32;
 constexpr uint32_t kResumeU = 0x80000000u;
 
@@ -764,7 +776,7 @@ __device__ __forceinline__ unsigned take_chain(unsigned* counter, bool need) {
 __global__ void __launch_bounds__(128) k_apply_xchains_t(const hc_view c, hc_dev* d) {
   __shared__ StagedRow slots[128];
   if (!(d->it_active && d->rest_active && d->do_erode) || d->erode_retry) return;
-  if (d->xchains <= kWarpChains) return;  // few chains: the warp walker takes them
+  if (d->xchains <= warps_in_flight()) return;  // few chains: the warp walker takes them
   StagedRow* st = &slots[threadIdx.x];
   const unsigned nch = d->xchains;
   const double mult = d->mult, ts = d->s.time_step;
@@ -856,7 +868,7 @@ __global__ void __launch_bounds__(128) k_apply_xchains_t(const hc_view c, hc_dev
 __global__ void __launch_bounds__(128) k_apply_ychains_t(const hc_view c, hc_dev* d) {
   __shared__ StagedRow slots[128];
   if (!(d->it_active && d->rest_active && d->do_erode) || d->erode_retry) return;
-  if (d->ychains <= kWarpChains) return;
+  if (d->ychains <= warps_in_flight()) return;
   StagedRow* st = &slots[threadIdx.x];
   const unsigned nch = d->ychains;
   const double mult = d->mult, ts = d->s.time_step;
@@ -1142,7 +1154,7 @@ __global__ void __launch_bounds__(128) k_apply_xchains_w(const hc_view c, hc_dev
   if (!(d->it_active && d->rest_active && d->do_erode) || d->erode_retry) return;
   // few chains: all of them from their starts; many: the long ones the
   // thread walker handed over
-  const bool few = d->xchains <= kWarpChains;
+  const bool few = d->xchains <= warps_in_flight();
   const unsigned nch = few ? d->xchains : d->xresume;
   const uint32_t* list = c.chains + (few ? 0 : 2 * c.N2);
   const double mult = d->mult, ts = d->s.time_step;
@@ -1218,7 +1230,7 @@ __global__ void __launch_bounds__(128) k_apply_xchains_w(const hc_view c, hc_dev
 // q-1, q, q+1 held in U, C, D
 __global__ void __launch_bounds__(128) k_apply_ychains_w(const hc_view c, hc_dev* d) {
   if (!(d->it_active && d->rest_active && d->do_erode) || d->erode_retry) return;
-  const bool few = d->ychains <= kWarpChains;
+  const bool few = d->ychains <= warps_in_flight();
   const unsigned nch = few ? d->ychains : d->yresume;
   const uint32_t* list = c.chains + (few ? 1 : 3) * c.N2;
   const double mult = d->mult, ts = d->s.time_step;
@@ -1471,7 +1483,8 @@ void launch_erode_pass(hc_ctx* c, int max_passes, cudaGraphConditionalHandle nex
   dim3 g((c->v.jmax - 1 + b.x - 1) / b.x, (c->v.imax + b.y - 1) / b.y);
   if (g.x < 1) g.x = 1;
   k_entrain_tau<<<g, b, 0, c->cs>>>(c->v, c->dev);
-  k_entrain<<<kEntrainBlocks, 128, 0, c->cs>>>(c->v, c->dev, max_passes, next, has_next);
+  k_entrain<<<entrain_blocks(c->v.N2), 128, 0, c->cs>>>(c->v, c->dev, max_passes, next,
+                                                          has_next);
   count_launch(c, 2);
   size_t nwords = c->v.N2 / 4 + 1;
   int nb = (int)((c->v.N2 + 255) / 256);
@@ -1492,10 +1505,11 @@ void launch_erode_finish(hc_ctx* c, int gated) {
   dim3 g((c->v.jmax - 2 + 31) / 32, (c->v.imax + 7) / 8);
   k_apply_pre<<<g, b, 0, c->cs>>>(c->v, c->dev);
   k_apply_gather<<<g, b, 0, c->cs>>>(c->v, c->dev);
-  k_apply_xchains_t<<<kWalkBlocks, 128, 0, c->cs>>>(c->v, c->dev);
-  k_apply_xchains_w<<<kWalkBlocks, 128, 0, c->cs>>>(c->v, c->dev);
-  k_apply_ychains_t<<<kWalkBlocks, 128, 0, c->cs>>>(c->v, c->dev);
-  k_apply_ychains_w<<<kWalkBlocks, 128, 0, c->cs>>>(c->v, c->dev);
+  const unsigned wb = walk_blocks(c->v.N2);
+  k_apply_xchains_t<<<wb, 128, 0, c->cs>>>(c->v, c->dev);
+  k_apply_xchains_w<<<wb, 128, 0, c->cs>>>(c->v, c->dev);
+  k_apply_ychains_t<<<wb, 128, 0, c->cs>>>(c->v, c->dev);
+  k_apply_ychains_w<<<wb, 128, 0, c->cs>>>(c->v, c->dev);
   count_launch(c, 6);
   k_edge_out<<<1, 1024, 0, c->cs>>>(c->v, c->dev, s.contrib, nullptr, gated);
   count_launch(c, 1);

@@ -241,7 +241,8 @@ __global__ void k_control(const hc_view c, hc_dev* d, hc_iter_handles hh) {
     }
     // The drainage area and the input-point list are recomputed before the
     // next iteration (the host sorts the elevations, hc_drain.cu does the
-    // rest), from the elevations as they are now (k_drain_snapshot); the
+    // rest), from the elevations as they are now (k_depth_update copies
+    // them before the iteration's erosion); the
     // reference, too, applies the new list from the next iteration on.
     d->do_drain = recalc;
     if (recalc) d->pause |= HC_PAUSE_DRAINAGE;
@@ -256,10 +257,18 @@ __global__ void k_control(const hc_view c, hc_dev* d, hc_iter_handles hh) {
   d->do_scan = ((long long)s.counter % p.scan_area_interval_iter) == 0;
   d->do_erode = !p.hydro_only && s.counter >= s.erode_call;
   d->erode_retry = d->do_erode;
+  if (d->do_erode) {
+    // erode()'s start (:4219; k_erode_begin for a direct call): the
+    // kernels between here and the erosion block read flow_timestep, set
+    // above, not time_step
+    s.time_step = s.time_step * 1.5;
+    d->mult = s.erode_mult;
+    d->tempbmax_bits = 0;
+  }
   d->do_slide = !p.hydro_only && ((long long)s.counter % p.in_channel_landslide_iter_interval) == 0;
   if (hh.has) {
-    // kernels inside the bodies enabled here: scan 3, erosion 6 + 7, slide_3 4
-    d->body_kernels += (d->do_scan ? 3 : 0) + (d->do_erode && !p.hydro_only ? 13 : 0) +
+    // kernels inside the bodies enabled here: scan 3, erosion 5 + 7, slide_3 4
+    d->body_kernels += (d->do_scan ? 3 : 0) + (d->do_erode && !p.hydro_only ? 12 : 0) +
                        (d->do_slide ? 4 : 0);
     cudaGraphSetConditional(hh.scan, d->do_scan ? 1u : 0u);
     if (!p.hydro_only) {
@@ -381,7 +390,18 @@ __device__ __forceinline__ int decide_gt(float a, float b) {
 // the reference's.
 // The face past the hflow gate: hflow (> hflow_threshold) and dA = a1 - a0
 // (the surface difference) as the gate formed them.
-template <bool kSusp, bool kVel>
+// The face update's divisions: inline, or (kCall) through one out-of-line
+// copy, which keeps the kernel's code small (its instruction fetches stall
+// the warps) at the cost of a call per division; a launch-shape choice of
+// the face-compacted kernel.
+static __device__ __noinline__ double ddiv_rn_call(double a, double b) { return ddiv_rn(a, b); }
+template <bool kCall>
+__device__ __forceinline__ double fdiv(double a, double b) {
+  if (kCall) return ddiv_rn_call(a, b);
+  return ddiv_rn(a, b);
+}
+
+template <bool kSusp, bool kVel, bool kCall = false>
 __device__ __forceinline__ void inertial_face_core(double& q, double& qs, double& vel_out,
                                                    int& vdir, double hflow, double dA, double h0,
                                                    double h1, double v0, double v1, double c0,
@@ -400,7 +420,7 @@ __device__ __forceinline__ void inertial_face_core(double& q, double& qs, double
   // q = 0: (0 - ghd*slope) / (1 + (ghd*nn*0)/h^3) = (0 - ghd*slope) / 1
   if (!deq0(q)) {
     const double aq = __longlong_as_double(dbits(q) & 0x7fffffffffffffffLL);  // fabs
-    qn = ddiv_rn(qn, 1 + ddiv_rn(ghd * nn * aq, icube_rn(hflow)));
+    qn = fdiv<kCall>(qn, 1 + fdiv<kCall>(ghd * nn * aq, icube_rn(hflow)));
   }
   const float hf = approx_abs_f(hflow);
   const float dtf = approx_abs_f(dt);
@@ -412,7 +432,7 @@ __device__ __forceinline__ void inertial_face_core(double& q, double& qs, double
   if (!deq0(qn)) {
     float fr;
     if (kVel) {
-      qoh = ddiv_rn(qn, hflow);
+      qoh = fdiv<kCall>(qn, hflow);
       qoh_valid = true;
       fr = approx_abs_f(qoh) / sqrtf(9.81f * hf);
     } else {
@@ -420,7 +440,7 @@ __device__ __forceinline__ void inertial_face_core(double& q, double& qs, double
     }
     int t = decide_gt(fr, c.flf);
     if (t == 0) {
-      if (!qoh_valid) qoh = ddiv_rn(qn, hflow);
+      if (!qoh_valid) qoh = fdiv<kCall>(qn, hflow);
       t = froude_exceeds(qoh, hflow, p.froude_limit) ? 1 : -1;
     }
     if (t > 0) {
@@ -451,7 +471,7 @@ __device__ __forceinline__ void inertial_face_core(double& q, double& qs, double
   if (kSusp) {
     // qs = q * (V/h) of the giving cell; V = 0 gives 0 * q (a signed zero)
     // (one product for both signs: h1 > 0 here, as h0 above)
-    if (qpos || qneg) qs = qn * (qpos ? c0 : (deq0(v1) ? v1 : ddiv_rn(v1, h1)));
+    if (qpos || qneg) qs = qn * (qpos ? c0 : (deq0(v1) ? v1 : fdiv<kCall>(v1, h1)));
     // qs*dt > V*DX/4 (giving cell) caps the sediment flux
     if (dgt0(qs)) {
       int t = decide_gt(approx_abs_f(qs) * dtf, approx_f(v0) * c.DXf * 0.25f);
@@ -466,7 +486,7 @@ __device__ __forceinline__ void inertial_face_core(double& q, double& qs, double
   }
   if (kVel) {
     // (0 - q)/hflow = -(q/hflow) exactly: division rounds symmetrically
-    if ((qpos || qneg) && !qoh_valid) qoh = ddiv_rn(qn, hflow);
+    if ((qpos || qneg) && !qoh_valid) qoh = fdiv<kCall>(qn, hflow);
     if (qpos) {
       vel_out = qoh;
       vdir = 1;
@@ -592,7 +612,7 @@ __global__ void __launch_bounds__(256, MINB) k_flow_route(const hc_view c,
 // k_flow_route, so the results are the same bit for bit.
 constexpr int kFaceQ = 96;  // queue entries per warp: < 32 carried + 64 new
 
-template <bool kSed>
+template <bool kSed, bool kCall>
 __device__ __forceinline__ void face_work(const hc_view& c, const hc_dev* __restrict__ d,
                                           uint32_t f, double hflow, double dA, double dt) {
   const size_t W = c.W, N2 = c.N2;
@@ -606,7 +626,7 @@ __device__ __forceinline__ void face_work(const hc_view& c, const hc_dev* __rest
   const bool susp = kSed && p.isSuspended[1] != 0;
   const double h0 = c.h[cell], h1 = c.h[nb];
   const double v0 = susp ? c.vs[cell] : 0.0;
-  const double c0 = (susp && !deq0(v0)) ? ddiv_rn(v0, h0) : v0;
+  const double c0 = (susp && !deq0(v0)) ? fdiv<kCall>(v0, h0) : v0;
   double* qa = yface ? c.qy : c.qx;
   double* qsa = yface ? c.qys : c.qxs;
   double q = qa[cell], qs = kSed ? qsa[cell] : 0.0, vel = 0;
@@ -614,10 +634,10 @@ __device__ __forceinline__ void face_work(const hc_view& c, const hc_dev* __rest
   const int es = yface ? ((j == c.jmax) ? 1 : ((j <= 2) ? -1 : 0))
                        : ((i == c.imax) ? 1 : ((i <= 2) ? -1 : 0));
   if (susp)
-    inertial_face_core<true, kSed>(q, qs, vel, vdir, hflow, dA, h0, h1, v0, c.vs[nb], c0, nn,
+    inertial_face_core<true, kSed, kCall>(q, qs, vel, vdir, hflow, dA, h0, h1, v0, c.vs[nb], c0, nn,
                                    dt, es, c);
   else
-    inertial_face_core<false, kSed>(q, qs, vel, vdir, hflow, dA, h0, h1, v0, 0.0, c0, nn, dt,
+    inertial_face_core<false, kSed, kCall>(q, qs, vel, vdir, hflow, dA, h0, h1, v0, 0.0, c0, nn, dt,
                                     es, c);
   qa[cell] = q;
   if (kSed) {
@@ -628,7 +648,7 @@ __device__ __forceinline__ void face_work(const hc_view& c, const hc_dev* __rest
   }
 }
 
-template <bool kSed, int MINB>
+template <bool kSed, int MINB, bool kCall = false>
 __global__ void __launch_bounds__(256, MINB) k_flow_route_q(const hc_view c,
                                                             const hc_dev* __restrict__ d,
                                                             int gated) {
@@ -709,10 +729,10 @@ __global__ void __launch_bounds__(256, MINB) k_flow_route_q(const hc_view c,
       const uint32_t f = Q[qn + lane];
       const double hf = HF[qn + lane], da = DA[qn + lane];
       __syncwarp();  // the entries are read before the next cells' are written
-      face_work<kSed>(c, d, f, hf, da, dt);
+      face_work<kSed, kCall>(c, d, f, hf, da, dt);
     }
   }
-  if (lane < qn) face_work<kSed>(c, d, Q[lane], HF[lane], DA[lane], dt);
+  if (lane < qn) face_work<kSed, kCall>(c, d, Q[lane], HF[lane], DA[lane], dt);
 }
 
 // ---------------------------------------------------------------------------
@@ -776,6 +796,13 @@ __global__ void __launch_bounds__(256, 6) k_depth_update(const hc_view c, hc_dev
   }
   // no flux enters a no-data cell, so this is empty in practice (its order
   // of addition is not fixed)
+  // the elevations the drainage recomputation after this iteration starts
+  // from (flow and depth_update leave them unchanged; erosion comes later);
+  // only erosion runs keep the copy (hydro-only elevations never change)
+  if (gated && d->do_drain && c.drain_snap)
+    for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < c.N2;
+         k += (size_t)gridDim.x * blockDim.x)
+      c.drain_snap[k] = c.elev[k];
   if (!deq0(lost)) atomicAdd(&d->vlost_step, lost);
   if (nonfinite) {
     d->err_code = 301;  // a NaN water depth: the run cannot continue
@@ -1033,9 +1060,12 @@ void launch_inputs(hc_ctx* c) {
     count_launch(c, 1);
     return;
   }
-  // grid-stride over the current list (its length lives on the device)
+  // grid-stride over the current list (its length lives on the device):
+  // four blocks per SM on large grids, fewer on small ones, whose lists are
+  // short (ensembles run many small members' launches side by side)
   int n = c->v.cin_cap;
-  int blocks = std::min((n + 255) / 256, std::min(152 * 4, c->v.vpart_cap));
+  const int cap = std::min(c->sms * 4, std::max(c->sms, (int)(c->v.N2 / 4096)));
+  int blocks = std::min((n + 255) / 256, std::min(cap, c->v.vpart_cap));
   if (blocks < 1) blocks = 1;
   k_inputs<<<blocks, 256, 0, c->cs>>>(c->v, c->dev);
   count_launch(c, 1);
@@ -1058,13 +1088,22 @@ static int list_blocks(const hc_ctx* c) {
 // blocks per SM x waves; one wave: every block resident at once).
 const FlowShape kFlowShapes[kFlowShapeCount] = {
     {4, 0, 0}, {3, 1, 0}, {4, 1, 0}, {5, 1, 0}, {6, 1, 0}, {3, 4, 0}, {4, 4, 0}, {5, 4, 0},
-    {6, 4, 0}, {3, 1, 1}, {4, 1, 1}, {5, 1, 1}, {3, 4, 1}, {4, 4, 1}, {5, 4, 1}};
+    {6, 4, 0}, {3, 1, 1}, {4, 1, 1}, {5, 1, 1}, {3, 4, 1}, {4, 4, 1}, {5, 4, 1},
+    {3, 1, 2}, {4, 1, 2}, {5, 1, 2}};
 
 template <bool kSed>
 static void flow_launch(hc_ctx* c, int gated, int shape) {
   const FlowShape f = kFlowShapes[shape];
   int blocks = f.waves ? c->sms * f.minb * f.waves : list_blocks(c);
   blocks = std::max(1, std::min(blocks, (int)((c->v.N2 + 255) / 256)));
+  if (f.compact == 2) {  // divisions through one out-of-line copy
+    switch (f.minb) {
+      case 3: k_flow_route_q<kSed, 3, true><<<blocks, 256, 0, c->cs>>>(c->v, c->dev, gated); break;
+      case 5: k_flow_route_q<kSed, 5, true><<<blocks, 256, 0, c->cs>>>(c->v, c->dev, gated); break;
+      default: k_flow_route_q<kSed, 4, true><<<blocks, 256, 0, c->cs>>>(c->v, c->dev, gated); break;
+    }
+    return;
+  }
   if (f.compact) {
     switch (f.minb) {
       case 3: k_flow_route_q<kSed, 3><<<blocks, 256, 0, c->cs>>>(c->v, c->dev, gated); break;

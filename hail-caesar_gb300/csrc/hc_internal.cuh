@@ -217,6 +217,8 @@ struct hc_iter_handles {
   int has;  // 0 outside graph capture: nothing to set
 };
 
+constexpr int kMaxFlowShapes = 24;  // launch shapes of k_flow_route the tuner can time
+
 struct hc_ctx {
   hc_view v;
   cudaStream_t s;         // the context's stream
@@ -243,7 +245,7 @@ struct hc_ctx {
   int flow_shape;          // launch shape of k_flow_route (kFlowShapes), autotuned
   bool flow_pinned;        // the caller fixed flow_shape (hc_set_launch_shape)
   int64_t tuned_key;       // the shape class flow_shape was chosen for (-1: none)
-  double tune_ms[16];      // the autotuner's times per shape (ms per launch)
+  double tune_ms[kMaxFlowShapes];  // the autotuner's times per shape (ms per launch)
   // called after every recomputation of the input points (adjoint replays)
   void (*points_hook)(hc_ctx*, void*);
   void* points_hook_arg;
@@ -627,43 +629,6 @@ HC_DEV double ddiv_by(double a, const hc_divisor& d) {
 
 HC_DEV double ddiv_rn(double a, double b) { return ddiv_by(a, ddiv_prep(b)); }
 
-// RN(a * b), the IEEE product, on the integer pipes: the 106-bit product of
-// the significands from one 64 x 64 multiply (low and high halves), rounded
-// at its 53rd bit with the round bit and the bits below it.  A zero times a
-// finite number gives the signed zero here; other operands that are zero,
-// subnormal, infinite or NaN, and products outside the normal range, take
-// the hardware multiplication (out of line: its FP64 instruction issues only
-// where it runs).
-static __device__ __noinline__ double dmul_hw(double a, double b) { return __dmul_rn(a, b); }
-
-HC_DEV double imul_rn(double a, double b) {
-  const unsigned long long A = (unsigned long long)__double_as_longlong(a);
-  const unsigned long long B = (unsigned long long)__double_as_longlong(b);
-  const unsigned long long M52 = (1ull << 52) - 1, H52 = 1ull << 52;
-  const unsigned long long sgn = (A ^ B) & 0x8000000000000000ull;
-  const int ea = (int)(A >> 52) & 0x7ff, eb = (int)(B >> 52) & 0x7ff;
-  if (ea == 0 || eb == 0 || ea == 0x7ff || eb == 0x7ff) {
-    if ((((A << 1) == 0) && eb != 0x7ff) || (((B << 1) == 0) && ea != 0x7ff))
-      return __longlong_as_double((long long)sgn);
-    return dmul_hw(a, b);
-  }
-  const unsigned long long ma = (A & M52) | H52, mb = (B & M52) | H52;
-  const unsigned long long lo = ma * mb, hi = __umul64hi(ma, mb);  // in [2^104, 2^106)
-  const int top = (int)(hi >> 41) & 1;                              // bit 105
-  const int sh = 52 + top;
-  unsigned long long sig = (hi << (64 - sh)) | (lo >> sh);
-  const unsigned long long rem = lo & ((1ull << sh) - 1), half = 1ull << (sh - 1);
-  int er = ea + eb - 1023 + top;
-  if (er < 1) return dmul_hw(a, b);  // a subnormal (or zero) product
-  if (rem > half || (rem == half && (sig & 1))) sig++;
-  if (sig == (H52 << 1)) {
-    sig = H52;
-    er++;
-  }
-  if (er > 2046) return dmul_hw(a, b);  // overflow
-  return __longlong_as_double((long long)(sgn | ((unsigned long long)er << 52) | (sig & M52)));
-}
-
 // hc_divisor for a divisor fixed for the run, V exact (floor(2^116/mb))
 hc_divisor host_divisor(double b);
 
@@ -770,9 +735,11 @@ void launch_flux_out(hc_ctx* c, int gated, int record);
 struct FlowShape {
   int minb;     // blocks of 256 per multiprocessor (register budget)
   int waves;    // grid = SMs x minb x waves; 0: the wet-list default grid
-  int compact;  // 1: the face-compacted kernel (k_flow_route_q)
+  int compact;  // 1: the face-compacted kernel (k_flow_route_q); 2: the same
+                // with its divisions through one out-of-line copy
 };
-constexpr int kFlowShapeCount = 15;
+constexpr int kFlowShapeCount = 18;
+static_assert(kFlowShapeCount <= kMaxFlowShapes, "hc_ctx::tune_ms holds every shape");
 extern const FlowShape kFlowShapes[kFlowShapeCount];
 void launch_flow_route_shape(hc_ctx* c, int gated, int shape);
 hc_status autotune(hc_ctx* c, bool force);
@@ -810,7 +777,6 @@ cudaError_t device_drainage_order(hc_ctx* c, const double* el, uint32_t* order, 
 cudaError_t device_sort_values(struct hc_sort_work* w, const double* v, size_t n, uint32_t* perm,
                                cudaStream_t s, bool* fallback, int64_t* launches);
 void host_sort_exact(std::pair<double, double>* a, size_t n, int threads);
-void launch_drain_snapshot(hc_ctx* c);
 void launch_adj_save(hc_ctx* c);         // adjoint replay: state before the iteration
 hc_status ctx_pull(hc_ctx* c);   // control block device -> host mirror
 hc_status ctx_push(hc_ctx* c);   // host mirror -> device

@@ -239,8 +239,8 @@ class Model:
         """(launch shape in use, [ms per launch of each shape of the last
         tuning]) of k_flow_route; force=True times the shapes now."""
         shape = C.c_int32()
-        ms = (C.c_double * 15)()
-        self._check(self.lib.hc_autotune(self.h, 1 if force else 0, C.byref(shape), ms, 15),
+        ms = (C.c_double * 18)()
+        self._check(self.lib.hc_autotune(self.h, 1 if force else 0, C.byref(shape), ms, 18),
                     "autotune")
         return shape.value, list(ms)
 

@@ -402,7 +402,7 @@ hc_status hc_test_bounded_waits(hc_ctx* ctx, int32_t spins, int32_t extra_arriva
  * them now; *shape (optional) receives the shape in use, ms (optional, n
  * doubles) the last timings per shape in ms per launch. */
 hc_status hc_autotune(hc_ctx* ctx, int32_t force, int32_t* shape, double* ms, int32_t n);
-/* Fixes k_flow_route's launch shape (0 .. 14; every shape computes the same
+/* Fixes k_flow_route's launch shape (0 .. 17; every shape computes the same
  * results), or -1: back to the autotuner. */
 hc_status hc_set_launch_shape(hc_ctx* ctx, int32_t shape);
 

@@ -183,38 +183,6 @@ __global__ void k_check_sqrt(unsigned long long n, unsigned long long seed, int 
   }
 }
 
-// the integer-pipe product against the hardware's; modes as for the
-// division, and 7: products at the edges of the normal range
-__global__ void k_check_mul(unsigned long long n, unsigned long long seed, int mode,
-                            unsigned long long* bad, double* first) {
-  for (unsigned long long k = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; k < n;
-       k += (unsigned long long)gridDim.x * blockDim.x) {
-    const unsigned long long key = k + seed * 0x100000000ull;
-    double a, b;
-    if (mode == 7) {
-      const unsigned long long r1 = mix(key), r2 = mix(key ^ 0x5151ull), r3 = mix(key * 3 + 1);
-      const int eb = 1 + (int)(r2 >> 53) % 2046;
-      const int t = (int)(r3 % 8);
-      const int target = (t < 4) ? (t - 1) : (2044 + (t - 4));  // -1..2, 2044..2047
-      int ea = target - eb + 1023;
-      if (ea < 1) ea = 1;
-      if (ea > 2046) ea = 2046;
-      a = mk(r3 >> 63, ea, r1);
-      b = mk((r3 >> 62) & 1, eb, r2);
-    } else {
-      pair(mode, key, a, b);
-    }
-    const double x = imul_rn(a, b), y = __dmul_rn(a, b);
-    const bool same = __double_as_longlong(x) == __double_as_longlong(y) || (disnan(x) && disnan(y));
-    if (!same && atomicAdd(bad, 1ull) == 0) {
-      first[0] = a;
-      first[1] = b;
-      first[2] = x;
-      first[3] = y;
-    }
-  }
-}
-
 // throughput: each thread divides independent operands kIter times
 template <bool kInt>
 __global__ void k_time(const double* in, double* out, int iters) {
@@ -272,22 +240,6 @@ extern "C" int arith_check_conv(unsigned long long n, unsigned long long seed,
   cudaMemset(d_bad, 0, 8);
   cudaMemset(d_first, 0, 32);
   k_check_conv<<<152 * 16, 256>>>(n, seed, d_bad, d_first);
-  cudaMemcpy(bad, d_bad, 8, cudaMemcpyDeviceToHost);
-  cudaMemcpy(first, d_first, 32, cudaMemcpyDeviceToHost);
-  const cudaError_t e = cudaGetLastError();
-  cudaFree(d_bad);
-  cudaFree(d_first);
-  return e == cudaSuccess ? 0 : 2;
-}
-
-extern "C" int arith_check_mul(unsigned long long n, unsigned long long seed, int mode,
-                               unsigned long long* bad, double* first) {
-  unsigned long long* d_bad;
-  double* d_first;
-  if (cudaMalloc(&d_bad, 8) != cudaSuccess || cudaMalloc(&d_first, 32) != cudaSuccess) return 1;
-  cudaMemset(d_bad, 0, 8);
-  cudaMemset(d_first, 0, 32);
-  k_check_mul<<<152 * 16, 256>>>(n, seed, mode, d_bad, d_first);
   cudaMemcpy(bad, d_bad, 8, cudaMemcpyDeviceToHost);
   cudaMemcpy(first, d_first, 32, cudaMemcpyDeviceToHost);
   const cudaError_t e = cudaGetLastError();

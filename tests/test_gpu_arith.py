@@ -1,6 +1,6 @@
 """The integer-pipe IEEE division of the kernels (ddiv_rn in
 hc_internal.cuh) against the hardware's division, bit for bit (and the
-product, cube, square root and float conversions likewise): 2^30
+cube, square root and float conversions likewise): 2^30
 quotients per input family (arbitrary bit patterns, normal operands, edge
 significands, near-integer quotients, edges of the normal range, the
 model's magnitudes, signed zero and subnormal dividends); and the
@@ -35,8 +35,6 @@ def arith(tmp_path_factory):
                                      C.POINTER(C.c_double)]
     lib.arith_check_sqrt.argtypes = [C.c_uint64, C.c_uint64, C.c_int, C.POINTER(C.c_uint64),
                                      C.POINTER(C.c_double)]
-    lib.arith_check_mul.argtypes = [C.c_uint64, C.c_uint64, C.c_int, C.POINTER(C.c_uint64),
-                                    C.POINTER(C.c_double)]
     lib.arith_time.argtypes = [C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float)]
     return lib
 
@@ -86,19 +84,6 @@ def test_sqrt_on_integer_pipe(arith, mode):
     assert arith.arith_check_sqrt(1 << 30, 11 + mode, mode, C.byref(bad), first) == 0
     assert bad.value == 0, "%d mismatches; first x=%r got %r want %r" % (
         bad.value, first[0], first[1], first[2])
-
-
-@pytest.mark.parametrize("mode", [0, 1, 2, 3, 5, 6, 7])
-def test_product_on_integer_pipe(arith, mode):
-    """imul_rn against the hardware's IEEE product, bit for bit, 2^30 pairs
-    per family (arbitrary bit patterns, normal operands, edge significands,
-    products of near-integers, the model's magnitudes, zero and subnormal
-    operands, products at the edges of the normal range)."""
-    bad = C.c_uint64(0)
-    first = (C.c_double * 4)()
-    assert arith.arith_check_mul(1 << 30, 23 + mode, mode, C.byref(bad), first) == 0
-    assert bad.value == 0, "%d mismatches; first a=%r b=%r got %r want %r" % (
-        bad.value, first[0], first[1], first[2], first[3])
 
 
 def test_float_conversions_on_integer_pipe(arith):

@@ -9,7 +9,7 @@ from helpers import assert_bitwise
 
 pytestmark = pytest.mark.gpu
 
-SHAPES = 15
+SHAPES = 18
 FIELDS = ("water_depth", "qx", "qy", "qxs", "qys", "Vsusptot", "elev", "vel_dir", "index")
 
 
