@@ -80,6 +80,10 @@ static __device__ __noinline__ bool adj_froude_exceeds(double qn, double hflow, 
   return dgt(ddiv_rn(fabs(ddiv_rn(qn, hflow)), isqrt_rn(kG * hflow)), fl);
 }
 static __device__ __noinline__ double adj_sqrt_ghf(double hflow) { return isqrt_rn(kG * hflow); }
+// the face's divisions through one out-of-line copy: inlined at each of its
+// call sites, the integer-pipe division made the code large enough that
+// instruction fetch stalled the warps (as in the forward kernel)
+static __device__ __noinline__ double adj_div(double a, double b) { return ddiv_rn(a, b); }
 
 // One face (:3096-3191), as the device evaluates it, with derivatives.
 // The value and the branch decisions are the forward kernel's (exact FP64
@@ -104,7 +108,7 @@ __device__ DQ face_dq(double q, double hflow, double dA, bool e0max, H0 h0f, H1 
   if (es == 1) slope = p.edgeslope, ds0 = ds1 = 0;
   if (es == -1) slope = zero_minus(p.edgeslope), ds0 = ds1 = 0;
   const double ghd = kG * hflow * dt;
-  const double rhf = ddiv_rn(1.0, hflow);
+  const double rhf = adj_div(1.0, hflow);
   // qn and its derivatives with respect to q, hflow, slope, nn
   double qn, d_q, d_hf, d_s, d_nn;
   if (deq0(q)) {
@@ -116,10 +120,10 @@ __device__ DQ face_dq(double q, double hflow, double dA, bool e0max, H0 h0f, H1 
   } else {
     const double aq = __longlong_as_double(dbits(q) & 0x7fffffffffffffffLL);  // fabs
     const double c3 = icube_rn(hflow);
-    const double F = ddiv_rn(ghd * nn * aq, c3);
+    const double F = adj_div(ghd * nn * aq, c3);
     const double D = 1 + F, N = q - (ghd * slope);
-    qn = ddiv_rn(N, D);
-    const double rD = ddiv_rn(1.0, D), rc3 = ddiv_rn(1.0, c3);
+    qn = adj_div(N, D);
+    const double rD = adj_div(1.0, D), rc3 = adj_div(1.0, c3);
     const double dF_q = ghd * nn * (dgt0(q) ? 1.0 : -1.0) * rc3;
     const double dF_hf = -2 * F * rhf;
     const double dF_nn = ghd * aq * rc3;
