@@ -182,11 +182,11 @@ def log(msg):
 #       --profile-skip 20  under  ncu --clock-control none -k regex:k_flow_route
 #       -c 1 --metrics dram__bytes_read.sum,dram__bytes_write.sum,
 #       sm__inst_executed_pipe_fp64.sum,sm__pipe_fp64_cycles_active.sum
-FLOW_CAPTURE = {"dram_bytes_per_wet_cell": 115.0, "fp64_warp_inst_per_wet_cell": 1.048,
-                "source": "ncu capture of k_flow_route_q (face-compacted), catchment "
-                          "1400x1400, 500-iteration spin-up + 25 iterations, 1,663,494 wet "
-                          "cells: 191.3 MB DRAM, 1.743 M FP64 warp instructions; scaled by "
-                          "this launch's wet cells"}
+FLOW_CAPTURE = {"dram_bytes_per_wet_cell": 121.9, "fp64_warp_inst_per_wet_cell": 1.001,
+                "source": "ncu capture of k_flow_route_q<1,5,1> (face-compacted, out-of-line "
+                          "divisions), catchment 1400x1400, 500-iteration spin-up + 25 "
+                          "iterations, 1,663,494 wet cells: 202.7 MB DRAM, 1.665 M FP64 warp "
+                          "instructions; scaled by this launch's wet cells"}
 FP64_LANES_PER_CLK_SM = 2  # this GPU's FP64 pipe: a warp instruction takes 16 cycles
 
 
