@@ -293,8 +293,9 @@ extern "C" hc_status hc_create(const hc_params* p, size_t max_bytes, hc_ctx** ou
   A(v.drain_frac, 9 * N2) A(v.drain_multi, N2)
   A(v.drain_aux, 1)
   if (sed) {
-    A(v.sflux, 40 * N2) A(v.sdirty, N2) A(v.grain, 11 * N2) A(v.strata, 90 * N2) A(v.alloc_key, N2)
-    A(v.erodetot, N2) A(v.erodetot3, N2) A(v.pre, 11 * N2) A(v.chains, 4 * N2)
+    A(v.sflux, 40 * N2) A(v.sdirty, N2) A(v.grain, kGrainStride * N2)
+    A(v.strata, kStrataStride * N2) A(v.alloc_key, N2)
+    A(v.erodetot, N2) A(v.erodetot3, N2) A(v.pre, kGrainStride * N2) A(v.chains, 4 * N2)
     A(v.drain_snap, N2) A(v.ent_list, N2) A(v.ent_qs, 2 * N2)
   } else {
     A(v.erodetot, N2)
@@ -338,8 +339,8 @@ extern "C" hc_status hc_create(const hc_params* p, size_t max_bytes, hc_ctx** ou
   if (sed) {
     cudaMemsetAsync(v.sflux, 0, 40 * N2 * 8, s);
     cudaMemsetAsync(v.sdirty, 0, N2, s);
-    cudaMemsetAsync(v.grain, 0, 11 * N2 * 8, s);
-    cudaMemsetAsync(v.strata, 0, 90 * N2 * 8, s);
+    cudaMemsetAsync(v.grain, 0, kGrainStride * N2 * 8, s);
+    cudaMemsetAsync(v.strata, 0, kStrataStride * N2 * 8, s);
     cudaMemsetAsync(v.erodetot3, 0, N2 * 8, s);
     k_fill_u64<<<4096, 256, 0, s>>>(v.alloc_key, N2, ~0ull);
   }
@@ -506,23 +507,25 @@ extern "C" hc_status hc_upload(hc_ctx* c, hc_field f, const void* host, size_t n
       const int64_t nrec = (int64_t)N2 / std::max(1, v.p.LIMIT);
       const double* h = (const double*)host;
       if (f == HC_F_GRAIN) {
-        std::vector<double> planes(11 * N2, 0.0);
+        std::vector<double> slots(kGrainStride * N2, 0.0);
         for (size_t cell = 0; cell < N2; cell++) {
           const int r = idx[cell];
           if (r < 0 || r >= nrec) continue;
-          for (int n = 0; n < 11; n++) planes[(size_t)n * N2 + cell] = h[(size_t)r * 11 + n];
+          for (int n = 0; n < 11; n++) slots[cell * kGrainStride + n] = h[(size_t)r * 11 + n];
         }
-        HC_CU(cudaMemcpy(v.grain, planes.data(), 11 * N2 * 8, cudaMemcpyHostToDevice), "upload");
+        HC_CU(cudaMemcpy(v.grain, slots.data(), slots.size() * 8, cudaMemcpyHostToDevice),
+              "upload");
       } else {
-        std::vector<double> planes(90 * N2, 0.0);
+        std::vector<double> slots(kStrataStride * N2, 0.0);
         for (size_t cell = 0; cell < N2; cell++) {
           const int r = idx[cell];
           if (r < 0 || r >= nrec) continue;
           for (int z = 0; z < 10; z++)
             for (int n = 0; n < 9; n++)
-              planes[((size_t)z * 9 + n) * N2 + cell] = h[((size_t)r * 10 + z) * 11 + n];
+              slots[cell * kStrataStride + (size_t)z * 9 + n] = h[((size_t)r * 10 + z) * 11 + n];
         }
-        HC_CU(cudaMemcpy(v.strata, planes.data(), 90 * N2 * 8, cudaMemcpyHostToDevice), "upload");
+        HC_CU(cudaMemcpy(v.strata, slots.data(), slots.size() * 8, cudaMemcpyHostToDevice),
+              "upload");
       }
       break;
     }
@@ -598,22 +601,24 @@ extern "C" hc_status hc_download(hc_ctx* c, hc_field f, void* host, size_t nbyte
       double* h = (double*)host;
       std::memset(h, 0, nbytes);
       if (f == HC_F_GRAIN) {
-        std::vector<double> planes(11 * N2);
-        HC_CU(cudaMemcpy(planes.data(), v.grain, 11 * N2 * 8, cudaMemcpyDeviceToHost), "download");
+        std::vector<double> slots(kGrainStride * N2);
+        HC_CU(cudaMemcpy(slots.data(), v.grain, slots.size() * 8, cudaMemcpyDeviceToHost),
+              "download");
         for (size_t cell = 0; cell < N2; cell++) {
           const int r = idx[cell];
           if (r < 0 || r >= nrec) continue;
-          for (int n = 0; n < 11; n++) h[(size_t)r * 11 + n] = planes[(size_t)n * N2 + cell];
+          for (int n = 0; n < 11; n++) h[(size_t)r * 11 + n] = slots[cell * kGrainStride + n];
         }
       } else {
-        std::vector<double> planes(90 * N2);
-        HC_CU(cudaMemcpy(planes.data(), v.strata, 90 * N2 * 8, cudaMemcpyDeviceToHost), "download");
+        std::vector<double> slots(kStrataStride * N2);
+        HC_CU(cudaMemcpy(slots.data(), v.strata, slots.size() * 8, cudaMemcpyDeviceToHost),
+              "download");
         for (size_t cell = 0; cell < N2; cell++) {
           const int r = idx[cell];
           if (r < 0 || r >= nrec) continue;
           for (int z = 0; z < 10; z++)
             for (int n = 0; n < 9; n++)
-              h[((size_t)r * 10 + z) * 11 + n] = planes[((size_t)z * 9 + n) * N2 + cell];
+              h[((size_t)r * 10 + z) * 11 + n] = slots[cell * kStrataStride + (size_t)z * 9 + n];
         }
       }
       break;

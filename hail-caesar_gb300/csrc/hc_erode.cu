@@ -474,7 +474,7 @@ __device__ __forceinline__ bool apply_active(const hc_view& c, size_t cell, int 
 // settled suspended load Vpdrop, plane 10 = erodetot.  The new Vsusptot is
 // written directly (nothing else in the pass touches it).
 __device__ __forceinline__ double& PRE(const hc_view& c, int k, size_t cell) {
-  return c.pre[(size_t)k * c.N2 + cell];
+  return c.pre[cell * kGrainStride + k];  // a cell's 11 terms side by side, like its record
 }
 
 __global__ void __launch_bounds__(256) k_apply_pre(const hc_view c, hc_dev* d) {

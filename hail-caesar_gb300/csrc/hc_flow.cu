@@ -118,7 +118,7 @@ __global__ void k_control(const hc_view c, hc_dev* d, hc_iter_handles hh) {
             if (p.isSuspended[tn - 4]) {
               c.vs[cell] += amt;
             } else {
-              c.grain[(size_t)(tn - 4) * c.N2 + cell] += amt;
+              grain_at(c, cell, tn - 4) += amt;
               c.elev[cell] += amt;
             }
           }

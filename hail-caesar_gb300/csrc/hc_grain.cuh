@@ -2,16 +2,15 @@
 // sort_active :3874-3947, sand_fraction :3985-4009, d50 :4038-4075,
 // slide_GS :4077-4171, mean_ws_elev :4011-4036.
 //
-// A cell's record lives in its own slot (plane n at offset n*N2 + cell);
-// index[cell] == -9999 means "no record" exactly as in the reference.
+// A cell's record lives in its own slot (grain_at, strata_at in
+// hc_internal.cuh); index[cell] == -9999 means "no record" exactly as in the
+// reference.
 #pragma once
 #include "hc_internal.cuh"
 
-HC_DEV double& GRN(const hc_view& c, size_t cell, int n) {
-  return c.grain[(size_t)n * c.N2 + cell];
-}
+HC_DEV double& GRN(const hc_view& c, size_t cell, int n) { return grain_at(c, cell, n); }
 HC_DEV double& STR(const hc_view& c, size_t cell, int z, int n) {
-  return c.strata[((size_t)z * HC_ST_N + n) * c.N2 + cell];
+  return strata_at(c, cell, z, n);
 }
 
 // addGS for contexts that run in the reference's serial order (one thread):

@@ -145,8 +145,8 @@ struct hc_view {
   double *vd;        // 4 * N2
   double *sflux;     // 4 dirs * 10 fractions * N2 ; dir order su, sr, sd, sl
   uint8_t *sdirty;   // N2: 1 where the cell's sflux entries may be nonzero
-  double *grain;     // 11 * N2
-  double *strata;    // 10 * 9 * N2
+  double *grain;     // 12 * N2: a cell's fractions side by side (grain_at)
+  double *strata;    // 90 * N2: a cell's 10 layers x 9 fractions side by side (strata_at)
   int32_t *index;
   uint8_t *mask;
   uint8_t *border;   // N2: 1 where a listed cell has an unlisted 4-neighbour (wet-list border)
@@ -175,7 +175,7 @@ struct hc_view {
 
   // scratch
   double *erodetot, *erodetot3;  // N2 each
-  double *pre;                   // 11 * N2: per-cell apply-pass terms (see hc_erode.cu)
+  double *pre;                   // 12 * N2: per-cell apply-pass terms, side by side (PRE)
   uint32_t *chains;              // 4 * N2: apply-pass chain starts (x pass, y pass), then
                                  // the resume points of long chains (x, y)
   // drainage area (hc_drain.cu): sweep position, sum of drops, higher
@@ -700,20 +700,34 @@ HC_DEV void atomic_max_pos(unsigned long long* a, double v) {
   atomicMax(a, (unsigned long long)__double_as_longlong(v));
 }
 
+// A cell's grain record lives in its own slot, its fractions side by side:
+// the grain row (fractions 0..HC_G) in 12 doubles (96 bytes, three 32-byte
+// sectors), the strata (10 layers x HC_ST_N fractions) in 90.  Every kernel
+// reads and writes a record whole, and the cells it visits are gathered
+// (wet lists, chains), so a record costs three sectors instead of one per
+// fraction.
+constexpr size_t kGrainStride = 12;
+constexpr size_t kStrataStride = 10 * HC_ST_N;
+HC_DEV double& grain_at(const hc_view& c, size_t cell, int n) {
+  return c.grain[cell * kGrainStride + n];
+}
+HC_DEV double& strata_at(const hc_view& c, size_t cell, int z, int n) {
+  return c.strata[cell * kStrataStride + (size_t)z * HC_ST_N + n];
+}
+
 // addGS :3949-3983 for a record held in the cell's own slot (the caller
 // assigns the reference's row number).  sort_active on a fresh record is a
 // no-op whenever dprop[1..9] sums to about 1; callers that need it run it.
 HC_DEV void grain_record_init(const hc_view& c, size_t cell, double elev, double bedrock) {
   const hc_params& p = c.p;
   const double active = p.active;
-  const size_t N2 = c.N2;
-  c.grain[cell] = 0;
-  for (int n = 1; n <= HC_G - 1; n++) c.grain[(size_t)n * N2 + cell] = active * p.dprop[n];
-  c.grain[(size_t)HC_G * N2 + cell] = 0;
+  grain_at(c, cell, 0) = 0;
+  for (int n = 1; n <= HC_G - 1; n++) grain_at(c, cell, n) = active * p.dprop[n];
+  grain_at(c, cell, HC_G) = 0;
   for (int z = 0; z <= 9; z++) {
     bool below = elev - (active * (z + 1)) < (bedrock - active);
     for (int n2 = 0; n2 <= HC_G - 2; n2++)
-      c.strata[((size_t)z * HC_ST_N + n2) * N2 + cell] = below ? 0.0 : (active)*p.dprop[n2 + 1];
+      strata_at(c, cell, z, n2) = below ? 0.0 : (active)*p.dprop[n2 + 1];
   }
 }
 
