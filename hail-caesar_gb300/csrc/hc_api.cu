@@ -1540,8 +1540,10 @@ extern "C" hc_status hc_profile_iteration(hc_ctx* c, int32_t flags, double* ms) 
   hd->budget = 1;
   hd->flags = flags;
   HC_TRY(push(c));
-  cudaEvent_t ev[10];
-  for (int k = 0; k < 10; k++) HC_CU(cudaEventCreate(&ev[k]), "profile");
+  // ev[10]: the start of the lateral3 phase, after the host has read the
+  // control block (the read is not device work of any phase)
+  cudaEvent_t ev[11];
+  for (int k = 0; k < 11; k++) HC_CU(cudaEventCreate(&ev[k]), "profile");
   cudaEventRecord(ev[0], c->s);
   launch_control(c);
   launch_inputs(c);
@@ -1553,12 +1555,30 @@ extern "C" hc_status hc_profile_iteration(hc_ctx* c, int32_t flags, double* ms) 
   launch_scan_area(c, 1);
   cudaEventRecord(ev[4], c->s);
   const bool sed = !c->v.p.hydro_only;
+  // the entrainment passes' device time only: the host reads the retry test
+  // between passes (pass_ms sums the passes' own event pairs)
+  double pass_ms = 0;
   if (sed) {
     HC_TRY(pull(c));
+    cudaEvent_t p0, p1;
+    HC_CU(cudaEventCreate(&p0), "profile");
+    HC_CU(cudaEventCreate(&p1), "profile");
     for (int guard = 0; hd->erode_retry && hd->it_active && guard < 100000; guard++) {
+      cudaEventRecord(p0, c->s);
       launch_erode_pass(c, 0);
-      HC_TRY(pull(c));
+      cudaEventRecord(p1, c->s);
+      const hc_status st = pull(c);
+      if (st != HC_OK) {
+        cudaEventDestroy(p0);
+        cudaEventDestroy(p1);
+        return st;
+      }
+      float t = 0;
+      cudaEventElapsedTime(&t, p0, p1);
+      pass_ms += t;
     }
+    cudaEventDestroy(p0);
+    cudaEventDestroy(p1);
   }
   cudaEventRecord(ev[5], c->s);
   if (sed) {
@@ -1567,6 +1587,7 @@ extern "C" hc_status hc_profile_iteration(hc_ctx* c, int32_t flags, double* ms) 
   }
   cudaEventRecord(ev[6], c->s);
   HC_TRY(pull(c));
+  cudaEventRecord(ev[10], c->s);
   if (hd->pause & HC_PAUSE_LATERAL) {
     HC_TRY(run_lateral(c));
     HC_TRY(pull(c));
@@ -1583,10 +1604,10 @@ extern "C" hc_status hc_profile_iteration(hc_ctx* c, int32_t flags, double* ms) 
   HC_CU(cudaEventSynchronize(ev[9]), "profile");
   for (int k = 0; k < 9; k++) {
     float t = 0;
-    cudaEventElapsedTime(&t, ev[k], ev[k + 1]);
-    ms[k] = t;
+    cudaEventElapsedTime(&t, k == 6 ? ev[10] : ev[k], ev[k + 1]);
+    ms[k] = (k == 4) ? pass_ms : t;
   }
-  for (int k = 0; k < 10; k++) cudaEventDestroy(ev[k]);
+  for (int k = 0; k < 11; k++) cudaEventDestroy(ev[k]);
   HC_TRY(pull(c));
   HC_TRY(host_steps(c, flags));
   hd->pause &= HC_PAUSE_FINISHED;

@@ -428,7 +428,8 @@ hc_status hc_get_counters(hc_ctx* ctx, int64_t* launches, int64_t* h2d_bytes,
  * hc_run's sequence phase by phase, without the graph, timing each phase with
  * CUDA events: ms[0..8] = control+inputs, flow_route, depth_update,
  * scan_area, entrainment passes, apply and lateral passes with the edge
- * output, lateral3, water_flux_out, slide_3. */
+ * output, lateral3, water_flux_out, slide_3 (device time; the host's reads
+ * of the control block between passes are in no phase). */
 hc_status hc_profile_iteration(hc_ctx* ctx, int32_t flags, double* ms);
 
 #ifdef __cplusplus
