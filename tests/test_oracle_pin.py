@@ -137,3 +137,17 @@ def test_oracle_matches_live_reference(oracle_mod, kind):
     for k in ("elev", "water_depth", "qx", "qy", "index", "grain", "strata", "edge", "Vsusptot"):
         if k in st:
             assert_bitwise(o.field(k), st[k], k)
+
+
+def test_oracle_stops_at_the_end_of_the_run(oracle_mod):
+    """The main loop ends at maxcycle (:1838): once it has, iterate runs
+    nothing, as hc_run returns no iterations; the grain arrays keep the
+    reference's N2/LIMIT rows and a run that would need more raises instead
+    of writing past them."""
+    case = synth.reach_case(imax=40, jmax=16, DX=10.0, hours=1)
+    o = oracle_mod.Oracle(case)
+    rec = o.iterate(-1)
+    assert len(rec) > 0 and rec[-1][1] / 60 >= case.params.maxcycle
+    assert len(o.iterate(1)) == 0
+    assert len(o.iterate(50)) == 0
+    assert o.scalar("grain_full") == 0
