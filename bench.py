@@ -369,7 +369,11 @@ def amortized_window(model, case, flags, stream, max_steps):
             "lateral3_calls": st["lateral"][0] - st0["lateral"][0],
             "drainage_recomputations": st["drainage"][0] - st0["drainage"][0],
             "host_ms": round(sum(st[k][1] - st0[k][1] for k in st
-                                 if k not in ("drainage_sweep", "wet_cell_steps")), 3)}
+                                 if k not in ("drainage_sweep", "wet_cell_steps")), 3),
+            # wall time of each kind of host-driven work in the window (the
+            # drainage kinds nest: sort, sweep and levels are parts of it)
+            "host_work_ms": {k: round(st[k][1] - st0[k][1], 3) for k in st
+                             if k != "wet_cell_steps" and st[k][1] - st0[k][1] > 0}}
 
 
 def run_ensemble_bench(args, rank):
