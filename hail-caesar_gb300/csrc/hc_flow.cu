@@ -665,13 +665,19 @@ __global__ void __launch_bounds__(256, MINB) k_flow_route_q(const hc_view c,
   const size_t W = c.W;
   const int warps = gridDim.x * (blockDim.x >> 5);
   int qn = 0;  // the same on every lane
-  for (int base = (blockIdx.x * (blockDim.x >> 5) + warp) * 32; base < n; base += warps * 32) {
+  // the list entry of the warp's next turn is fetched a turn ahead (its
+  // cell's loads then need not wait for it)
+  int base = (blockIdx.x * (blockDim.x >> 5) + warp) * 32;
+  uint32_t next = (base + lane < n) ? (uint32_t)c.wet[base + lane] : 0u;
+  for (; base < n; base += warps * 32) {
     const int k = base + lane;
     bool fx = false, fy = false;
     double hx = 0, hy = 0, ax = 0, ay = 0;
     uint32_t cell = 0;
+    const uint32_t mine = next;
+    if (k + warps * 32 < n) next = (uint32_t)c.wet[k + warps * 32];
     if (k < n) {
-      cell = (uint32_t)c.wet[k];
+      cell = mine;
       const double e0 = c.elev[cell];
       if (dkey(e0) > kNoDataKey) {  // e > -9999
         const double h0 = c.h[cell];
@@ -757,13 +763,21 @@ __global__ void __launch_bounds__(256, 6) k_depth_update(const hc_view c, hc_dev
   // not updated), so the water crossing it appears or vanishes.  The same
   // expression as the update, over those faces only.
   double edge = 0;
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nw; k += gridDim.x * blockDim.x) {
-    const size_t cell = (size_t)c.wet[k];
-    if (c.border[cell]) {  // k_wet_write marks the listed cells on the border
-      const uint8_t mu = c.mask[cell - W], md = c.mask[cell + W], ml = c.mask[cell - 1],
-                    mr = c.mask[cell + 1];
-      const double ux1 = md ? 0.0 : c.qx[cell + W], ux0 = mu ? 0.0 : c.qx[cell];
-      const double uy1 = mr ? 0.0 : c.qy[cell + 1], uy0 = ml ? 0.0 : c.qy[cell];
+  // The discharges, fluxes, mask, border and elevations are not written by
+  // this kernel: they are read through the read-only path (__ldg).  The next
+  // list entry is fetched a turn ahead, so that its cell's loads do not wait
+  // for the index behind them.
+  const int stride = gridDim.x * blockDim.x;
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  int next = (k < nw) ? __ldg(c.wet + k) : 0;
+  for (; k < nw; k += stride) {
+    const size_t cell = (size_t)next;
+    if (k + stride < nw) next = __ldg(c.wet + k + stride);
+    if (__ldg(c.border + cell)) {  // k_wet_write marks the listed cells on the border
+      const uint8_t mu = __ldg(c.mask + cell - W), md = __ldg(c.mask + cell + W),
+                    ml = __ldg(c.mask + cell - 1), mr = __ldg(c.mask + cell + 1);
+      const double ux1 = md ? 0.0 : __ldg(c.qx + cell + W), ux0 = mu ? 0.0 : __ldg(c.qx + cell);
+      const double uy1 = mr ? 0.0 : __ldg(c.qy + cell + 1), uy0 = ml ? 0.0 : __ldg(c.qy + cell);
       edge += ddiv_by(dt * (ux1 - ux0 + uy1 - uy0), c.dxd);
     }
     // Where the four fluxes are zero (either sign) the update adds a signed
@@ -772,20 +786,22 @@ __global__ void __launch_bounds__(256, 6) k_depth_update(const hc_view c, hc_dev
     constexpr long long kNegZero = (long long)0x8000000000000000ULL;
     double h = c.h[cell];
     {
-      const double a = c.qx[cell + W], b = c.qx[cell], e = c.qy[cell + 1], f = c.qy[cell];
+      const double a = __ldg(c.qx + cell + W), b = __ldg(c.qx + cell),
+                   e = __ldg(c.qy + cell + 1), f = __ldg(c.qy + cell);
       if (((dbits(a) | dbits(b) | dbits(e) | dbits(f)) << 1) != 0 || dbits(h) == kNegZero)
         h += ddiv_by(dt * (a - b + e - f), c.dxd);
     }
     // hydro-only runs keep Vsusptot at zero (no sediment source exists)
     if (susp) {
-      const double a = c.qxs[cell + W], b = c.qxs[cell], e = c.qys[cell + 1], f = c.qys[cell];
+      const double a = __ldg(c.qxs + cell + W), b = __ldg(c.qxs + cell),
+                   e = __ldg(c.qys + cell + 1), f = __ldg(c.qys + cell);
       const double v = c.vs[cell];
       if (((dbits(a) | dbits(b) | dbits(e) | dbits(f)) << 1) != 0 || dbits(v) == kNegZero)
         c.vs[cell] = v + ddiv_by(dt * (a - b + e - f), c.dxd);
     }
     nonfinite |= disnan(h);
     if (dgt0(h)) {
-      if (dbits(c.elev[cell]) == kNoDataBits) {
+      if (dbits(__ldg(c.elev + cell)) == kNoDataBits) {
         lost += h;
         h = 0;
       } else {
