@@ -400,7 +400,7 @@ __global__ void __launch_bounds__(32) k_slide_replay(const hc_view c, hc_dev* d,
       }
       pend += __shfl_sync(kFull, added, 0);
     }
-    // lane 0's moves and pushes are visible to the warp's next round
+    // lane 0's moves and pushes are visible to the warp's next turn
     __syncwarp();
   }
   if (lane == 0) d->s.grain_array_tot = d->grain_tot;
