@@ -457,9 +457,14 @@ __global__ void __launch_bounds__(256) k_adj_gather(const hc_view c, AdjBufs b, 
     }
   }
   // per zone: warp sums, then block sums, then one atomic per zone and block
+  // (input points are few: a warp without one of the zone's sums to +0 with
+  // no FP64 work)
   for (int z = 0; z <= c.p.rfnum && z <= HC_MAX_RF; z++) {
-    double v = (myrf == z) ? mine : 0.0;
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    double v = 0.0;
+    if (__ballot_sync(0xffffffffu, myrf == z)) {
+      v = (myrf == z) ? mine : 0.0;
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    }
     if (lane == 0) sj[warp][z] = v;
   }
   __syncthreads();
