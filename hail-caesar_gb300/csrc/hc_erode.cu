@@ -42,6 +42,17 @@ __device__ __forceinline__ size_t EX(const hc_view& c, int x, int y) {
   return (size_t)x * (c.jmax + 1) + y;
 }
 
+// The Einstein transport of one fraction (:4398-4405) and the bedrock
+// rescaling's division, out of line: the fraction loop is unrolled, and with
+// their integer-pipe divisions and cube inlined nine times over the
+// transport kernel's code would be several times larger.
+static __device__ __noinline__ double einstein_td(double mts, double einA, hc_divisor Bd,
+                                                  hc_divisor einSd, hc_divisor dxd) {
+  const double x = ddiv_by(einA, Bd);
+  return ddiv_by(ddiv_by(mts * (40 * icube_rn(ddiv_rn(1.0, x))), einSd), dxd);
+}
+static __device__ __noinline__ double ddiv_rn_entrain(double a, double b) { return ddiv_rn(a, b); }
+
 // blocks of 128 threads of the transport kernel (grid-stride over its
 // list): 1216 on large grids, fewer on small ones, whose lists are short and
 // whose idle blocks would only cost dispatch (ensembles of small members run
@@ -224,10 +235,7 @@ __device__ double entrain_cell(const hc_view& c, hc_dev* d, size_t cell, double 
       td = ddiv_by(mts * ((Fi * (U_star * U_star * U_star)) / ((2.65 - 1) * kG)) * Wi_star,
                    c.dxd);
     }
-    if (p.einstein) {
-      const double x = ddiv_by(c.einA[n], Bd);
-      td = ddiv_by(ddiv_by(mts * (40 * icube_rn(ddiv_rn(1.0, x))), c.einSd[n]), c.dxd);
-    }
+    if (p.einstein) td = einstein_td(mts, c.einA[n], Bd, c.einSd[n], c.dxd);
     if (dgt(td, GRN(c, cell, n))) td = GRN(c, cell, n);
     if (p.isSuspended[n] && n == 1) {
       if (dgt((td + c.vs[cell]) / h, p.Csuspmax)) td = (h * p.Csuspmax) - c.vs[cell];
@@ -245,7 +253,7 @@ __device__ double entrain_cell(const hc_view& c, hc_dev* d, size_t cell, double 
       if (!dgt(e0, bed)) {
         temp_dist[n] = 0;
       } else {
-        temp_dist[n] = elevdiff * ddiv_rn(temp_dist[n], temptot3);
+        temp_dist[n] = elevdiff * ddiv_rn_entrain(temp_dist[n], temptot3);
         if (dlt0(temp_dist[n])) temp_dist[n] = 0;
       }
       temptot1 += temp_dist[n];
