@@ -151,3 +151,16 @@ def test_oracle_stops_at_the_end_of_the_run(oracle_mod):
     assert len(o.iterate(1)) == 0
     assert len(o.iterate(50)) == 0
     assert o.scalar("grain_full") == 0
+
+
+def test_oracle_refuses_to_overflow_the_grain_rows(oracle_mod):
+    """A run asking for more grain records than the N2/LIMIT rows the
+    reference allocates stops with an error (the reference's arrays would
+    be overrun) instead of writing past them."""
+    case = synth.reach_case(imax=40, jmax=16, DX=10.0, hours=2)
+    p = case.params
+    p.LIMIT = (p.imax + 2) * (p.jmax + 2) // 4  # four rows
+    o = oracle_mod.Oracle(case)
+    with pytest.raises(RuntimeError, match="grain records"):
+        o.iterate(-1)
+    assert o.scalar("grain_full") == 1
